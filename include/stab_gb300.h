@@ -1,0 +1,163 @@
+/*
+ * stab_gb300.h -- C ABI of the GB300 (sm_103a) compressible linear-stability
+ * hot path: Chebyshev-collocation assembly of the temporal pencil and of the
+ * alpha-linearised spatial operator, the full-spectrum FP64 eigensolve, and
+ * the mixed-precision shift-invert polish of the least-stable mode.
+ *
+ * Conventions
+ *   - Plain C types only; every array is caller-owned host memory unless a
+ *     function says "device".  The library never frees caller memory.
+ *   - A complex number is two doubles {re, im}; this is the layout of Fortran
+ *     complex(8) and C99 double _Complex, so Fortran callers bind through
+ *     iso_c_binding with complex(c_double_complex) arrays.
+ *   - Matrices are column-major (Fortran order).  Unknown (i, dof) of node i
+ *     (0-based, i = 0 is the free stream, i = ny-1 the wall) and field
+ *     dof in {rho, u, v, w, T} sits at row 5*i + dof, as in the reference.
+ *   - Functions return 0 on success and a negative STAB_ERR_* code on error;
+ *     stab_last_error() gives a message.  Per-instance numerical outcomes are
+ *     reported through status arrays (STAB_ST_*), never by aborting: the
+ *     reference's `stop` paths (temporal.f90:776-785, :806-809) become codes.
+ */
+#ifndef STAB_GB300_H
+#define STAB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STAB_GB300_ABI_VERSION 1
+
+/* return codes */
+#define STAB_OK 0
+#define STAB_ERR_ARG (-1)     /* bad argument (size, flag, unsupported option)  */
+#define STAB_ERR_CUDA (-2)    /* CUDA runtime error                              */
+#define STAB_ERR_NOMEM (-3)   /* device allocation failed                        */
+#define STAB_ERR_IO (-4)      /* file could not be read or written               */
+#define STAB_ERR_STATE (-5)   /* object used in the wrong state                  */
+
+/* per-instance status (LAPACK-like: 0 ok, >0 numerical) */
+#define STAB_ST_OK 0
+#define STAB_ST_SINGULAR 1    /* exactly singular factor (ZGESV/ZGETRF info>0)   */
+#define STAB_ST_NOCONV 2      /* iteration cap reached (ZGEEV info>0 analogue)   */
+#define STAB_ST_NAN 3         /* non-finite value in the inputs or results      */
+#define STAB_ST_FELLBACK 4    /* polish did not converge; plain FP64 path used   */
+#define STAB_ST_NOMODE 5      /* no eigenvalue passed the least-stable filter    */
+
+/* solve modes for stab_batch_run / stab_solve_batch */
+#define STAB_MODE_PLAIN 0     /* FP64 full spectrum + least-stable eigenvector   */
+#define STAB_MODE_SEEDED 1    /* mixed-precision polish from caller seeds        */
+#define STAB_MODE_COARSE 2    /* seeds from an FP64 full spectrum at N = 32,     *
+                               * then the mixed-precision polish                 */
+
+/*
+ * Run parameters of one solve: a mirror of module `stuff` (stuff.f90:11-55)
+ * as input.f90:15-81 and stab.f90:46-55 fill it.  Te is derived as the
+ * reference derives it (input.f90:25 evaluates te = t0/(1+0.2 Ma^2) before
+ * Ma is read, so Te = T0 for Sutherland and Te = 0 for constant viscosity).
+ */
+typedef struct stab_params {
+    int32_t mattyp;   /* 0 constant mu, 1 Sutherland                         */
+    int32_t ny;       /* collocation points N (polynomial degree N-1)        */
+    int32_t ievec;    /* 1: eigenvectors wanted                              */
+    int32_t ider;     /* 1: internal derivatives (the only supported value) */
+    int32_t top;      /* spatial free-stream BC: 0 rho=0, 1 continuity       */
+    int32_t wall;     /* carried through to evec.dat                         */
+    int32_t wallt;    /* 0 isothermal, 2 adiabatic wall                      */
+    int32_t curve;    /* 0 flat (the only supported value)                   */
+    int32_t itype;    /* 1 temporal, 2 spatial                               */
+    int32_t ind;      /* profile index (profile.<ind>)                       */
+    double T0, Ma, Re, Pr, yi, ymax, x;
+    double alpha[2];  /* temporal: streamwise wavenumber                     */
+    double beta[2];   /* spanwise wavenumber                                 */
+    double omega[2];  /* spatial: frequency                                  */
+} stab_params;
+
+typedef struct stab_ctx stab_ctx;
+typedef struct stab_batch stab_batch;
+
+/* ---- context ---------------------------------------------------------- */
+int stab_abi_version(void);
+/* Create a context on CUDA device `device`; it owns a stream and device
+ * memory pools.  Replaces nothing in the reference (which has no state
+ * beyond module `stuff`). */
+int stab_create(stab_ctx** ctx, int device);
+int stab_destroy(stab_ctx* ctx);
+const char* stab_last_error(const stab_ctx* ctx);
+/* Launch on a caller stream (a cudaStream_t passed as void*); NULL restores
+ * the context's own stream. */
+int stab_set_stream(stab_ctx* ctx, void* stream);
+int stab_sync(stab_ctx* ctx);
+/* Per-kernel CUDA-event timing (0 off, 1 on) and its readout: for kernel
+ * index k < *count, name, number of launches and total milliseconds. */
+int stab_set_profiling(stab_ctx* ctx, int on);
+int stab_kernel_stats(stab_ctx* ctx, int32_t k, const char** name, int64_t* launches, double* total_ms, int32_t* count);
+int stab_reset_kernel_stats(stab_ctx* ctx);
+
+/* ---- operator assembly (parity / inspection) -------------------------- */
+/*
+ * Assemble the operator of one instance on the GPU and copy it back.
+ *   itype 1: mats_out = [A0 | B0], two n x n complex matrices, n = 5*ny
+ *            (temporal.f90:604-752; A0 x = omega B0 x).
+ *   itype 2: mats_out = [C0 | C1 | C2], three n x n complex matrices
+ *            (spatial.f90:677-959; (C0 + alpha C1 + alpha^2 C2) phi = 0).
+ * profile: nym rows of (y, rho, u, v, w, T), row-major, as profile.<ind>
+ * (getmean.f90:40-80; v is forced to zero).
+ * Replaces the inline assembly of temporal.f90:95-752 / spatial.f90:96-959.
+ */
+int stab_assemble(stab_ctx* ctx, const stab_params* p, int32_t nym, const double* profile,
+                  double* mats_out);
+
+/* ---- full spectrum (plain FP64 path) --------------------------------- */
+/*
+ * All eigenvalues of one instance, sorted ascending by imaginary part with
+ * the stable order of PIKSR2: omega (itype 1, n = 5*ny values) or alpha
+ * (itype 2, n = 10*ny values, alpha = 1/lambda and lambda = 0 -> 0).
+ * vec_out (may be NULL): the least-stable eigenvector, n complex values,
+ * normalised as the reference normalises evec.dat columns (temporal: divided
+ * by its max-modulus entry, temporal.f90:867-879; spatial: unit 2-norm with
+ * its max-modulus entry real and positive, the ZGEEV convention).
+ * least_index_out (may be NULL): index in the sorted list of the selected
+ * least-stable mode, -1 when none passed the filter.
+ * Replaces ZGESV+ZGEEV+PIKSR2 (temporal.f90:771-855) and
+ * ZGETRF+ZGETRS+ZGEEV+PIKSR2 (spatial.f90:972-1084).
+ */
+int stab_full_spectrum(stab_ctx* ctx, const stab_params* p, int32_t nym, const double* profile,
+                       double* eig_out, double* vec_out, int32_t* least_index_out,
+                       int32_t* status_out);
+
+/* ---- batched least-stable mode ---------------------------------------- */
+/*
+ * Upload `count` instances (parameters + profiles) to device memory.
+ * profiles[k] points at nym[k] x 6 doubles; identical pointers are uploaded
+ * once.  The instances may have different ny and itype.
+ */
+int stab_batch_create(stab_ctx* ctx, int32_t count, const stab_params* p, const int32_t* nym,
+                      const double* const* profiles, stab_batch** out);
+/* Seeds for STAB_MODE_SEEDED: count complex values (omega for temporal,
+ * alpha for spatial), copied to the device. */
+int stab_batch_set_seeds(stab_batch* b, const double* seeds);
+/* Run the whole path on the device (asynchronous on the context stream). */
+int stab_batch_run(stab_batch* b, int32_t mode);
+/*
+ * Copy results back (synchronises): eig_out[2*k] least-stable eigenvalue,
+ * err_out[k] relative FP64 residual estimate |r|/(|M||x|) of the final pair,
+ * iters_out[k] refinement steps used, status_out[k] STAB_ST_*.  vec_out
+ * (may be NULL) receives count pointers, each to n_k complex values.
+ * Any output pointer may be NULL.
+ */
+int stab_batch_results(stab_batch* b, double* eig_out, double* err_out, int32_t* iters_out,
+                       int32_t* status_out, double* const* vec_out);
+int stab_batch_destroy(stab_batch* b);
+
+/* One-shot: create + run + results + destroy (the end-to-end call). */
+int stab_solve_batch(stab_ctx* ctx, int32_t count, const stab_params* p, const int32_t* nym,
+                     const double* const* profiles, int32_t mode, const double* seeds,
+                     double* eig_out, double* err_out, int32_t* status_out, double* const* vec_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STAB_GB300_H */

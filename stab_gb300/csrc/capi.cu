@@ -1,0 +1,928 @@
+// C ABI of libstab_gb300: context, batches and the orchestration of the
+// kernels of prep.cu, assemble.cu, lu.cu, hqr.cu, polish.cu and post.cu.
+//
+// Batch order: instances are kept internally with all temporal instances
+// first and all spatial ones after (stable), so each phase launches on
+// contiguous ranges; results are mapped back to the caller's order.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/stab_gb300.h"
+#include "common.cuh"
+#include "hqr.cuh"
+#include "kernels.cuh"
+#include "lu.cuh"
+#include "polish.cuh"
+
+using namespace stab;
+
+namespace {
+
+struct KStat {
+  std::string name;
+  int64_t launches = 0;
+  double ms = 0.0;
+};
+struct PendingEv {
+  int idx;
+  cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct stab_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::map<int, std::pair<double*, double*>> dtabs;  // ny -> (D1, D2) on the device
+  int profiling = 0;
+  std::vector<KStat> stats;
+  std::vector<PendingEv> pending;
+  std::vector<cudaEvent_t> evpool;
+  int sms = 152;
+};
+
+static int set_err(stab_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+static int cuda_fail(stab_ctx* c, cudaError_t e, const char* what) {
+  return set_err(c, STAB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(ctx, expr)                                  \
+  do {                                                 \
+    cudaError_t e_ = (expr);                           \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #expr); \
+  } while (0)
+
+static cudaEvent_t get_ev(stab_ctx* c) {
+  if (!c->evpool.empty()) {
+    cudaEvent_t e = c->evpool.back();
+    c->evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+static int stat_index(stab_ctx* c, const char* name) {
+  for (size_t i = 0; i < c->stats.size(); ++i)
+    if (c->stats[i].name == name) return (int)i;
+  c->stats.push_back(KStat{name, 0, 0.0});
+  return (int)c->stats.size() - 1;
+}
+// Launch through f(); with profiling on, bracket it with events on the
+// context stream and account the time to `name`.
+template <typename F>
+static cudaError_t timed(stab_ctx* c, const char* name, F&& f) {
+  if (!c->profiling) return f();
+  cudaEvent_t a = get_ev(c), b = get_ev(c);
+  cudaEventRecord(a, c->stream);
+  cudaError_t e = f();
+  cudaEventRecord(b, c->stream);
+  c->pending.push_back(PendingEv{stat_index(c, name), a, b});
+  return e;
+}
+static void drain_stats(stab_ctx* c) {
+  if (c->pending.empty()) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto& p : c->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    c->stats[p.idx].launches += 1;
+    c->stats[p.idx].ms += ms;
+    c->evpool.push_back(p.a);
+    c->evpool.push_back(p.b);
+  }
+  c->pending.clear();
+}
+
+// Chebyshev tables for ny, built once per context
+static int ensure_dtab(stab_ctx* c, int ny) {
+  if (c->dtabs.count(ny)) return 0;
+  double *D1 = nullptr, *D2 = nullptr, *xa = nullptr;
+  CK(c, cudaMalloc(&D1, sizeof(double) * ny * ny));
+  CK(c, cudaMalloc(&D2, sizeof(double) * ny * ny));
+  CK(c, cudaMalloc(&xa, sizeof(double) * 2 * ny));
+  k_cheb_a<<<(ny + 127) / 128, 128, 0, c->stream>>>(ny, xa);
+  CK(c, cudaGetLastError());
+  dim3 g((ny + 127) / 128, ny);
+  k_cheb_d1<<<g, 128, 0, c->stream>>>(ny, xa, D1);
+  CK(c, cudaGetLastError());
+  k_cheb_d2<<<g, 128, 0, c->stream>>>(ny, D1, D2);
+  CK(c, cudaGetLastError());
+  CK(c, cudaStreamSynchronize(c->stream));
+  cudaFree(xa);
+  c->dtabs[ny] = {D1, D2};
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// device buffer helpers
+// ---------------------------------------------------------------------------
+namespace {
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (b == 0) b = 16;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+template <typename T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+  cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s);
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// batch
+// ---------------------------------------------------------------------------
+struct stab_batch {
+  stab_ctx* ctx = nullptr;
+  int count = 0, tcount = 0;             // tcount temporal instances first
+  std::vector<stab_params> P;            // internal order
+  std::vector<int> perm;                 // internal k -> caller index
+  std::vector<InstDesc> hd;
+  std::vector<int32_t> hn, hm;
+  std::vector<int64_t> h_n2, h_m2, h_m2c2, h_nof, h_mof, h_vec;
+  int nmax = 0, mmax = 0;
+  size_t sum_n2 = 0, sum_m2 = 0, sum_n = 0, sum_m = 0;
+  // device
+  DevBuf desc, dtab, pdesc, prof, spl, node, blk, ops, vec;
+  DevBuf nsz, msz, off_n2, off_m2, off_m2c2, off_nof, off_mof, xoff[VEC_SLOTS], order;
+  DevBuf M32, Z64, Abig, Hbig, eigraw, eigsorted, outvec;
+  DevBuf piv, info, flags, theta, sigma, least_raw, least_val, least_idx, pcol, done, err, iters, status, counter;
+  int nprof = 0;
+  bool have_seeds = false;
+  std::vector<double> seeds;             // caller order, 2 per instance
+  int last_mode = -1;
+  bool ran = false;
+  // host copies filled by fallback runs (internal order)
+  std::vector<int> fell_back;
+};
+
+static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const int32_t* nym,
+                       const double* const* profiles, stab_batch** out, int force_ny) {
+  if (!c || count <= 0 || !p || !nym || !profiles || !out) return set_err(c, STAB_ERR_ARG, "null argument or count <= 0");
+  std::unique_ptr<stab_batch> b(new stab_batch());
+  b->ctx = c;
+  b->count = count;
+  std::vector<int> idx(count);
+  for (int i = 0; i < count; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return p[a].itype < p[bb].itype; });
+  b->perm = idx;
+  // profiles: dedupe by pointer
+  std::map<const double*, int> pidx;
+  std::vector<ProfDesc> pds;
+  std::vector<double> hprof;
+  int64_t spl_off = 0;
+  for (int i = 0; i < count; ++i) {
+    const double* pp = profiles[i];
+    if (!pp) return set_err(c, STAB_ERR_ARG, "null profile pointer");
+    if (nym[i] < 4) return set_err(c, STAB_ERR_ARG, "profile needs at least 4 rows");
+    if (pidx.count(pp)) {
+      if (pds[pidx[pp]].nym != nym[i]) return set_err(c, STAB_ERR_ARG, "same profile pointer with different nym");
+      continue;
+    }
+    ProfDesc pd{};
+    pd.off_prof = (int64_t)hprof.size();
+    pd.off_spl = spl_off;
+    pd.nym = nym[i];
+    for (int r = 0; r < nym[i] * 6; ++r) hprof.push_back(pp[r]);
+    for (int r = 1; r < nym[i]; ++r)
+      if (!(pp[6 * r] > pp[6 * (r - 1)])) return set_err(c, STAB_ERR_ARG, "profile y must be strictly ascending");
+    spl_off += (int64_t)nym[i] * 6;
+    pidx[pp] = (int)pds.size();
+    pds.push_back(pd);
+  }
+  b->nprof = (int)pds.size();
+  // tables
+  std::vector<int> tab_ny;
+  int64_t node_off = 0, blk_off = 0, vec_off = 0;
+  for (int k = 0; k < count; ++k) {
+    const int u = idx[k];
+    stab_params q = p[u];
+    if (force_ny > 0) q.ny = force_ny;
+    if (q.itype != 1 && q.itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal) or 2 (spatial)");
+    if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
+    if (q.curve != 0) return set_err(c, STAB_ERR_ARG, "curve != 0 (curved walls) is not supported");
+    if (q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider = 0 (external derivatives) is not supported");
+    if (q.wallt != 0 && q.wallt != 2) return set_err(c, STAB_ERR_ARG, "Illegal value of wallt");
+    if (q.yi == 0.0) return set_err(c, STAB_ERR_ARG, "Yi = 0 (tanh map) is not supported");
+    if (q.mattyp != 0 && q.mattyp != 1) return set_err(c, STAB_ERR_ARG, "mattyp must be 0 or 1");
+    if (!(q.Ma > 0.0)) return set_err(c, STAB_ERR_ARG, "Ma must be > 0");
+    b->P.push_back(q);
+    if (std::find(tab_ny.begin(), tab_ny.end(), q.ny) == tab_ny.end()) tab_ny.push_back(q.ny);
+    InstDesc d{};
+    d.ny = q.ny;
+    d.n = 5 * q.ny;
+    d.itype = q.itype;
+    d.m = (q.itype == 1) ? d.n : 2 * d.n;
+    d.wallt = q.wallt;
+    d.top = q.top;
+    d.mattyp = q.mattyp;
+    d.navier = !(q.Re >= 1.0e98 || q.Re == 0.0);
+    d.Ma = q.Ma;
+    d.Re = q.Re;
+    d.Pr = q.Pr;
+    d.Te = (q.mattyp == 1) ? q.T0 : 0.0;   // input.f90:25 runs before Ma is read
+    d.yi = q.yi;
+    d.ymax = q.ymax;
+    d.ar = q.alpha[0]; d.ai = q.alpha[1];
+    d.br = q.beta[0]; d.bi = q.beta[1];
+    d.wr = q.omega[0]; d.wi = q.omega[1];
+    const ProfDesc& pd = pds[pidx[profiles[u]]];
+    d.nym = pd.nym;
+    d.off_prof = pd.off_prof;
+    d.off_spl = pd.off_spl;
+    d.off_node = node_off;
+    d.off_blk = blk_off;
+    d.off_vec = vec_off;
+    node_off += (int64_t)NODE_STRIDE * d.ny;
+    blk_off += (int64_t)BLK_STRIDE * d.ny;
+    vec_off += (int64_t)VEC_SLOTS * d.n;
+    if (q.itype == 1) b->tcount++;
+    b->hd.push_back(d);
+  }
+  for (int ny : tab_ny) {
+    int r = ensure_dtab(c, ny);
+    if (r) return r;
+  }
+  std::vector<double*> hdt;
+  std::map<int, int> tab_index;
+  for (auto& kv : c->dtabs) {
+    tab_index[kv.first] = (int)hdt.size() / 2;
+    hdt.push_back(kv.second.first);
+    hdt.push_back(kv.second.second);
+  }
+  for (auto& d : b->hd) d.dmat = tab_index[d.ny];
+  // offsets
+  for (auto& d : b->hd) {
+    b->hn.push_back(d.n);
+    b->hm.push_back(d.m);
+    b->h_n2.push_back((int64_t)b->sum_n2);
+    b->h_m2.push_back((int64_t)b->sum_m2);
+    b->h_m2c2.push_back((int64_t)b->sum_m2 + (int64_t)d.m * d.n);   // column n of the companion
+    b->h_nof.push_back((int64_t)b->sum_n);
+    b->h_mof.push_back((int64_t)b->sum_m);
+    b->h_vec.push_back(d.off_vec);
+    b->sum_n2 += (size_t)d.n * d.n;
+    b->sum_m2 += (size_t)d.m * d.m;
+    b->sum_n += d.n;
+    b->sum_m += d.m;
+    b->nmax = std::max(b->nmax, d.n);
+    b->mmax = std::max(b->mmax, d.m);
+  }
+  cudaStream_t s = c->stream;
+  CK(c, upload(b->desc, b->hd, s));
+  CK(c, upload(b->dtab, hdt, s));
+  CK(c, upload(b->pdesc, pds, s));
+  CK(c, upload(b->prof, hprof, s));
+  CK(c, b->spl.ensure(sizeof(double) * std::max<int64_t>(spl_off, 1)));
+  CK(c, b->node.ensure(sizeof(double) * node_off));
+  CK(c, b->blk.ensure(sizeof(zc) * blk_off));
+  CK(c, b->ops.ensure(sizeof(zc) * (blk_off / BLK_STRIDE) * 75));
+  CK(c, b->vec.ensure(sizeof(zc) * vec_off));
+  CK(c, upload(b->nsz, b->hn, s));
+  CK(c, upload(b->msz, b->hm, s));
+  CK(c, upload(b->off_n2, b->h_n2, s));
+  CK(c, upload(b->off_m2, b->h_m2, s));
+  CK(c, upload(b->off_m2c2, b->h_m2c2, s));
+  CK(c, upload(b->off_nof, b->h_nof, s));
+  CK(c, upload(b->off_mof, b->h_mof, s));
+  for (int sl = 0; sl < VEC_SLOTS; ++sl) {
+    std::vector<int64_t> xo(count);
+    for (int k = 0; k < count; ++k) xo[k] = b->h_vec[k] + (int64_t)sl * b->hn[k];
+    CK(c, upload(b->xoff[sl], xo, s));
+  }
+  // processing order of the persistent eigensolver: largest first
+  std::vector<int32_t> ord(count);
+  for (int k = 0; k < count; ++k) ord[k] = k;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int bb) { return b->hm[a] > b->hm[bb]; });
+  CK(c, upload(b->order, ord, s));
+  CK(c, b->M32.ensure(sizeof(cc) * b->sum_n2));
+  CK(c, b->piv.ensure(sizeof(int32_t) * b->sum_n));
+  CK(c, b->eigraw.ensure(sizeof(zc) * b->sum_m));
+  CK(c, b->eigsorted.ensure(sizeof(zc) * b->sum_m));
+  CK(c, b->outvec.ensure(sizeof(zc) * b->sum_m));
+  const size_t I4 = sizeof(int32_t) * count, Z = sizeof(zc) * count;
+  CK(c, b->info.ensure(I4));
+  CK(c, b->flags.ensure(I4));
+  CK(c, b->theta.ensure(Z));
+  CK(c, b->sigma.ensure(Z));
+  CK(c, b->least_raw.ensure(Z));
+  CK(c, b->least_val.ensure(Z));
+  CK(c, b->least_idx.ensure(I4));
+  CK(c, b->pcol.ensure(I4));
+  CK(c, b->done.ensure(I4));
+  CK(c, b->iters.ensure(I4));
+  CK(c, b->status.ensure(I4));
+  CK(c, b->err.ensure(sizeof(double) * count));
+  CK(c, b->counter.ensure(sizeof(int32_t) * 4));
+  CK(c, cudaStreamSynchronize(s));
+  *out = b.release();
+  return 0;
+}
+
+// grid / index helpers over a contiguous internal range [k0, k0 + cnt)
+struct Range {
+  int k0, cnt;
+};
+
+static int run_prep(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const InstDesc* D = b->desc.as<InstDesc>();
+  const double* const* T = b->dtab.as<const double*>();
+  CK(c, timed(c, "k_spline", [&] {
+    k_spline<<<(b->nprof + 63) / 64, 64, 0, s>>>(b->nprof, b->pdesc.as<ProfDesc>(), b->prof.as<double>(),
+                                                  b->spl.as<double>());
+    return cudaGetLastError();
+  }));
+  const int nymax = b->nmax / 5;
+  CK(c, timed(c, "k_nodes", [&] {
+    dim3 g((nymax + 127) / 128, b->count);
+    k_nodes<<<g, 128, 0, s>>>(b->count, D, b->prof.as<double>(), b->spl.as<double>(), b->node.as<double>());
+    return cudaGetLastError();
+  }));
+  CK(c, timed(c, "k_meanderiv", [&] {
+    dim3 g((5 * nymax + 127) / 128, b->count);
+    k_meanderiv<<<g, 128, 0, s>>>(b->count, D, T, b->node.as<double>());
+    return cudaGetLastError();
+  }));
+  CK(c, cudaMemsetAsync(b->flags.p, 0, sizeof(int32_t) * b->count, s));
+  CK(c, timed(c, "k_blocks", [&] {
+    dim3 g((nymax + 63) / 64, b->count);
+    k_blocks<<<g, 64, 0, s>>>(b->count, D, T, b->node.as<double>(), b->blk.as<zc>(), b->flags.as<int>());
+    return cudaGetLastError();
+  }));
+  return 0;
+}
+
+static int node_ops(stab_batch* b, Range r, int kind_t, int kind_s, const zc* sigma) {
+  stab_ctx* c = b->ctx;
+  const int nymax = b->nmax / 5;
+  return timed(c, "k_node_ops", [&] {
+           dim3 g((nymax + 63) / 64, r.cnt);
+           k_node_ops<<<g, 64, 0, c->stream>>>(r.cnt, b->desc.as<InstDesc>() + r.k0, b->blk.as<zc>(), kind_t, kind_s,
+                                                sigma ? sigma + r.k0 : nullptr, b->ops.as<zc>());
+           return cudaGetLastError();
+         }) == cudaSuccess
+             ? 0
+             : set_err(c, STAB_ERR_CUDA, "k_node_ops launch failed");
+}
+
+template <typename T>
+static int dense(stab_batch* b, Range r, T* out, const int64_t* off, int ldmul, double scale, const char* name) {
+  stab_ctx* c = b->ctx;
+  cudaError_t e = timed(c, name, [&] {
+    return launch_dense<T>(r.cnt, b->nmax, b->desc.as<InstDesc>() + r.k0, b->dtab.as<const double*>(),
+                           b->ops.as<zc>(), out, off + r.k0, ldmul, scale, c->stream);
+  });
+  return e == cudaSuccess ? 0 : cuda_fail(c, e, name);
+}
+
+static int ensure_plain_pools(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  CK(c, b->Z64.ensure(sizeof(zc) * b->sum_n2));
+  CK(c, b->Abig.ensure(sizeof(zc) * b->sum_m2));
+  CK(c, b->Hbig.ensure(sizeof(zc) * b->sum_m2));
+  return 0;
+}
+
+// inverse iteration for the eigenvector of the pair (least_raw, .) with an
+// LU of Q(theta) in precision T (complex128 for the plain path)
+static int eigvec_inverse_iteration(stab_batch* b, Range r, const zc* theta_dev) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const InstDesc* D = b->desc.as<InstDesc>() + r.k0;
+  int rc = node_ops(b, r, OP_T_Q, OP_S_Q, theta_dev);
+  if (rc) return rc;
+  rc = dense<zc>(b, r, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z");
+  if (rc) return rc;
+  CK(c, timed(c, "k_lu_z", [&] {
+    return launch_lu<zc>(r.cnt, D, b->nsz.as<int32_t>() + r.k0, b->nmax, b->Z64.as<zc>(),
+                         b->off_n2.as<int64_t>() + r.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + r.k0,
+                         b->info.as<int32_t>() + r.k0, s);
+  }));
+  CK(c, launch_vec_init(r.cnt, b->nmax, D, b->vec.as<zc>(), 0, s));
+  for (int it = 0; it < 3; ++it) {
+    CK(c, timed(c, "k_qmv", [&] {
+      return launch_qmv(r.cnt, b->nmax, D, b->dtab.as<const double*>(), b->blk.as<zc>(), theta_dev + r.k0, 1,
+                        b->vec.as<zc>(), 0, 1, nullptr, s);
+    }));
+    CK(c, timed(c, "k_getrs_z", [&] {
+      return launch_getrs<zc>(r.cnt, b->nsz.as<int32_t>() + r.k0, b->nmax, b->Z64.as<zc>(),
+                              b->off_n2.as<int64_t>() + r.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + r.k0,
+                              b->vec.as<zc>(), b->xoff[1].as<int64_t>() + r.k0, 1, 0, 1, nullptr, s);
+    }));
+    CK(c, launch_normalize(r.cnt, D, b->vec.as<zc>(), 1, b->pcol.as<int32_t>() + r.k0, nullptr, s));
+    CK(c, launch_vec_copy(r.cnt, b->nmax, D, b->vec.as<zc>(), 1, 0, nullptr, s));
+  }
+  return 0;
+}
+
+static int write_vectors(stab_batch* b, Range r, const zc* theta_dev) {
+  stab_ctx* c = b->ctx;
+  const InstDesc* D = b->desc.as<InstDesc>() + r.k0;
+  k_temporal_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, b->vec.as<zc>(), 0, b->outvec.as<zc>(),
+                                                b->off_mof.as<int64_t>() + r.k0);
+  CK(c, cudaGetLastError());
+  k_spatial_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, theta_dev + r.k0, b->vec.as<zc>(), 0, b->outvec.as<zc>(),
+                                               b->off_mof.as<int64_t>() + r.k0);
+  CK(c, cudaGetLastError());
+  return 0;
+}
+
+// plain FP64 path on all instances: standard-form matrices, full spectrum,
+// sort + select, optional eigenvector of the selected mode
+static int run_plain(stab_batch* b, bool want_vec) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  int rc = ensure_plain_pools(b);
+  if (rc) return rc;
+  const Range all{0, b->count};
+  const Range tr{0, b->tcount};
+  const Range sr{b->tcount, b->count - b->tcount};
+  if (tr.cnt > 0) {
+    rc = node_ops(b, tr, OP_T_C, OP_T_C, nullptr);
+    if (rc) return rc;
+    rc = dense<zc>(b, tr, b->Abig.as<zc>(), b->off_m2.as<int64_t>(), 1, 1.0, "k_dense_z");
+    if (rc) return rc;
+  }
+  if (sr.cnt > 0) {
+    const InstDesc* D = b->desc.as<InstDesc>() + sr.k0;
+    rc = node_ops(b, sr, OP_S_C0, OP_S_C0, nullptr);
+    if (rc) return rc;
+    rc = dense<zc>(b, sr, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z");
+    if (rc) return rc;
+    CK(c, timed(c, "k_lu_z", [&] {
+      return launch_lu<zc>(sr.cnt, D, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<zc>(),
+                           b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + sr.k0,
+                           b->info.as<int32_t>() + sr.k0, s);
+    }));
+    rc = node_ops(b, sr, OP_S_C1, OP_S_C1, nullptr);
+    if (rc) return rc;
+    rc = dense<zc>(b, sr, b->Abig.as<zc>(), b->off_m2.as<int64_t>(), 2, -1.0, "k_dense_z");
+    if (rc) return rc;
+    rc = node_ops(b, sr, OP_S_C2, OP_S_C2, nullptr);
+    if (rc) return rc;
+    rc = dense<zc>(b, sr, b->Abig.as<zc>(), b->off_m2c2.as<int64_t>(), 2, -1.0, "k_dense_z");
+    if (rc) return rc;
+    CK(c, timed(c, "k_getrs_z", [&] {
+      return launch_getrs<zc>(sr.cnt, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<zc>(),
+                              b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(),
+                              b->off_nof.as<int64_t>() + sr.k0, b->Abig.as<zc>(), b->off_m2.as<int64_t>() + sr.k0, 0,
+                              2, 2, nullptr, s);
+    }));
+    CK(c, timed(c, "k_companion_fill", [&] {
+      dim3 g(2 * (b->nmax), sr.cnt);
+      k_companion_fill<<<g, 128, 0, s>>>(sr.cnt, D, b->Abig.as<zc>(), b->off_m2.as<int64_t>() + sr.k0);
+      return cudaGetLastError();
+    }));
+  }
+  CK(c, timed(c, "k_eig_plain", [&] {
+    int grid = std::min(b->count, c->sms * 2);
+    return launch_eig_plain(b->count, b->mmax, b->msz.as<int32_t>(), b->Abig.as<zc>(), b->off_m2.as<int64_t>(),
+                            b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
+                            b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(), grid, s);
+  }));
+  CK(c, timed(c, "k_post_spectrum", [&] {
+    size_t sm = sizeof(zc) * b->mmax;
+    cudaFuncSetAttribute(k_post_spectrum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_post_spectrum<<<b->count, 256, sm, s>>>(b->count, b->desc.as<InstDesc>(), b->eigraw.as<zc>(),
+                                              b->off_mof.as<int64_t>(), b->eigsorted.as<zc>(),
+                                              b->least_idx.as<int32_t>(), b->least_raw.as<zc>(),
+                                              b->least_val.as<zc>());
+    return cudaGetLastError();
+  }));
+  CK(c, cudaMemsetAsync(b->err.p, 0, sizeof(double) * b->count, s));
+  CK(c, cudaMemsetAsync(b->iters.p, 0, sizeof(int32_t) * b->count, s));
+  if (want_vec) {
+    CK(c, cudaMemcpyAsync(b->theta.p, b->least_raw.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, s));
+    rc = eigvec_inverse_iteration(b, all, b->theta.as<zc>());
+    if (rc) return rc;
+    rc = write_vectors(b, all, b->theta.as<zc>());
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+// mixed-precision polish from sigma (device, internal order)
+static const int kNewtonSteps = 8;
+static const double kNewtonTol = 2e-14;
+
+static int run_polish(stab_batch* b, bool want_vec) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const Range all{0, b->count};
+  const InstDesc* D = b->desc.as<InstDesc>();
+  const double* const* T = b->dtab.as<const double*>();
+  zc* V = b->vec.as<zc>();
+  int32_t* done = b->done.as<int32_t>();
+  CK(c, cudaMemcpyAsync(b->theta.p, b->sigma.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, s));
+  int rc = node_ops(b, all, OP_T_Q, OP_S_Q, b->theta.as<zc>());
+  if (rc) return rc;
+  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c");
+  if (rc) return rc;
+  auto lu32 = [&]() {
+    return timed(c, "k_lu_c", [&] {
+      return launch_lu<cc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
+                           b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s);
+    });
+  };
+  auto solve32 = [&](int slot, const int32_t* skip) {
+    return timed(c, "k_getrs_c", [&] {
+      return launch_getrs<cc>(b->count, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
+                              b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V, b->xoff[slot].as<int64_t>(), 1, 0, 1,
+                              skip, s);
+    });
+  };
+  auto qmv = [&](int deriv, int xs, int ys, const int32_t* skip) {
+    return timed(c, "k_qmv", [&] {
+      return launch_qmv(b->count, b->nmax, D, T, b->blk.as<zc>(), b->theta.as<zc>(), deriv, V, xs, ys, skip, s);
+    });
+  };
+  CK(c, lu32());
+  CK(c, launch_vec_init(b->count, b->nmax, D, V, 0, s));
+  for (int it = 0; it < 2; ++it) {   // inverse iteration at the seed
+    CK(c, qmv(1, 0, 1, nullptr));
+    CK(c, solve32(1, nullptr));
+    CK(c, launch_normalize(b->count, D, V, 1, b->pcol.as<int32_t>(), nullptr, s));
+    CK(c, launch_vec_copy(b->count, b->nmax, D, V, 1, 0, nullptr, s));
+  }
+  // bordered Jacobian at (sigma, x): Q(sigma) with column p <- Q'(sigma) x
+  CK(c, qmv(1, 0, 2, nullptr));
+  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c");
+  if (rc) return rc;
+  CK(c, launch_set_column(b->count, b->nmax, D, b->M32.as<cc>(), b->off_n2.as<int64_t>(), b->pcol.as<int32_t>(), V, 2,
+                          s));
+  CK(c, lu32());
+  CK(c, cudaMemsetAsync(done, 0, sizeof(int32_t) * b->count, s));
+  CK(c, cudaMemsetAsync(b->iters.p, 0, sizeof(int32_t) * b->count, s));
+  for (int it = 0; it < kNewtonSteps; ++it) {
+    CK(c, qmv(0, 0, 3, done));
+    CK(c, solve32(3, done));
+    CK(c, timed(c, "k_newton_update", [&] {
+      return launch_newton_update(b->count, D, V, 0, 3, b->pcol.as<int32_t>(), b->theta.as<zc>(), done,
+                                  b->err.as<double>(), b->iters.as<int32_t>(), kNewtonTol, s);
+    }));
+  }
+  CK(c, launch_normalize(b->count, D, V, 0, nullptr, nullptr, s));
+  // least_val in caller units: omega (temporal) or alpha = 1/lambda (spatial)
+  CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, s));
+  if (want_vec) {
+    rc = write_vectors(b, all, b->theta.as<zc>());
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+// host-side: status from `done` and NaN checks; theta -> eigenvalue
+static void finalize_polish_host(std::vector<zc>& val, std::vector<int32_t>& st, const std::vector<int32_t>& dn,
+                                 const std::vector<stab_params>& P) {
+  for (size_t k = 0; k < val.size(); ++k) {
+    if (P[k].itype == 2) {
+      zc l = val[k];
+      double d = l.x * l.x + l.y * l.y;
+      val[k] = d > 0 ? zmk(l.x / d, -l.y / d) : zmk(0.0, 0.0);
+    }
+    st[k] = (dn[k] == 1) ? STAB_ST_OK : (dn[k] == 3 ? STAB_ST_NAN : STAB_ST_NOCONV);
+  }
+}
+
+static int batch_run(stab_batch* b, int32_t mode) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  b->fell_back.clear();
+  b->last_mode = mode;
+  int rc = run_prep(b);
+  if (rc) return rc;
+  if (mode == STAB_MODE_PLAIN) {
+    rc = run_plain(b, true);
+    if (rc) return rc;
+    b->ran = true;
+    return 0;
+  }
+  if (mode == STAB_MODE_SEEDED) {
+    if (!b->have_seeds) return set_err(c, STAB_ERR_STATE, "STAB_MODE_SEEDED needs stab_batch_set_seeds first");
+    std::vector<zc> sg(b->count);
+    for (int k = 0; k < b->count; ++k) {
+      const int u = b->perm[k];
+      zc a = zmk(b->seeds[2 * u], b->seeds[2 * u + 1]);
+      if (b->P[k].itype == 2) {
+        double d = a.x * a.x + a.y * a.y;
+        a = d > 0 ? zmk(a.x / d, -a.y / d) : zmk(0.0, 0.0);
+      }
+      sg[k] = a;
+    }
+    CK(c, cudaMemcpyAsync(b->sigma.p, sg.data(), sizeof(zc) * b->count, cudaMemcpyHostToDevice, s));
+    CK(c, cudaStreamSynchronize(s));
+  } else {
+    return set_err(c, STAB_ERR_ARG, "unknown mode");
+  }
+  rc = run_polish(b, true);
+  if (rc) return rc;
+  b->ran = true;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// the coarse-seed wrapper keeps the caller inputs to build the N = 32 batch
+// ---------------------------------------------------------------------------
+struct BatchInputs {
+  std::vector<stab_params> p;
+  std::vector<int32_t> nym;
+  std::vector<const double*> prof;
+};
+static std::map<stab_batch*, BatchInputs> g_inputs;
+
+extern "C" {
+
+int stab_abi_version(void) { return STAB_GB300_ABI_VERSION; }
+
+int stab_create(stab_ctx** out, int device) {
+  if (!out) return STAB_ERR_ARG;
+  std::unique_ptr<stab_ctx> c(new stab_ctx());
+  c->device = device;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    *out = nullptr;
+    return STAB_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) return STAB_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return STAB_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) return STAB_ERR_CUDA;
+  c->stream = c->own;
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+  *out = c.release();
+  return STAB_OK;
+}
+
+int stab_destroy(stab_ctx* c) {
+  if (!c) return STAB_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->dtabs) {
+    cudaFree(kv.second.first);
+    cudaFree(kv.second.second);
+  }
+  for (auto& p : c->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : c->evpool) cudaEventDestroy(e);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return STAB_OK;
+}
+
+const char* stab_last_error(const stab_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int stab_set_stream(stab_ctx* c, void* stream) {
+  if (!c) return STAB_ERR_ARG;
+  c->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : c->own;
+  return STAB_OK;
+}
+
+int stab_sync(stab_ctx* c) {
+  if (!c) return STAB_ERR_ARG;
+  CK(c, cudaStreamSynchronize(c->stream));
+  return STAB_OK;
+}
+
+int stab_set_profiling(stab_ctx* c, int on) {
+  if (!c) return STAB_ERR_ARG;
+  drain_stats(c);
+  c->profiling = on ? 1 : 0;
+  return STAB_OK;
+}
+
+int stab_kernel_stats(stab_ctx* c, int32_t k, const char** name, int64_t* launches, double* total_ms,
+                      int32_t* count) {
+  if (!c) return STAB_ERR_ARG;
+  drain_stats(c);
+  if (count) *count = (int32_t)c->stats.size();
+  if (k < 0 || k >= (int32_t)c->stats.size()) return (name || launches || total_ms) ? STAB_ERR_ARG : STAB_OK;
+  if (name) *name = c->stats[k].name.c_str();
+  if (launches) *launches = c->stats[k].launches;
+  if (total_ms) *total_ms = c->stats[k].ms;
+  return STAB_OK;
+}
+
+int stab_reset_kernel_stats(stab_ctx* c) {
+  if (!c) return STAB_ERR_ARG;
+  drain_stats(c);
+  c->stats.clear();
+  return STAB_OK;
+}
+
+int stab_batch_create(stab_ctx* c, int32_t count, const stab_params* p, const int32_t* nym,
+                      const double* const* profiles, stab_batch** out) {
+  if (!c) return STAB_ERR_ARG;
+  cudaSetDevice(c->device);
+  int rc = batch_build(c, count, p, nym, profiles, out, 0);
+  if (rc) return rc;
+  BatchInputs in;
+  in.p.assign(p, p + count);
+  in.nym.assign(nym, nym + count);
+  in.prof.assign(profiles, profiles + count);
+  g_inputs[*out] = std::move(in);
+  return STAB_OK;
+}
+
+int stab_batch_set_seeds(stab_batch* b, const double* seeds) {
+  if (!b || !seeds) return STAB_ERR_ARG;
+  b->seeds.assign(seeds, seeds + 2 * (size_t)b->count);
+  b->have_seeds = true;
+  return STAB_OK;
+}
+
+static int coarse_seeds(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  auto it = g_inputs.find(b);
+  if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
+  stab_batch* cb = nullptr;
+  int rc = batch_build(c, b->count, it->second.p.data(), it->second.nym.data(), it->second.prof.data(), &cb, 32);
+  if (rc) return rc;
+  std::unique_ptr<stab_batch> guard(cb);
+  rc = run_prep(cb);
+  if (rc) return rc;
+  rc = run_plain(cb, false);
+  if (rc) return rc;
+  // same internal order in both batches (same stable itype sort)
+  CK(c, cudaMemcpyAsync(b->sigma.p, cb->least_raw.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int stab_batch_run(stab_batch* b, int32_t mode) {
+  if (!b) return STAB_ERR_ARG;
+  stab_ctx* c = b->ctx;
+  cudaSetDevice(c->device);
+  if (mode == STAB_MODE_COARSE) {
+    int rc = run_prep(b);
+    if (rc) return rc;
+    rc = coarse_seeds(b);
+    if (rc) return rc;
+    b->fell_back.clear();
+    b->last_mode = mode;
+    rc = run_polish(b, true);
+    if (rc) return rc;
+    b->ran = true;
+    return STAB_OK;
+  }
+  return batch_run(b, mode);
+}
+
+int stab_batch_results(stab_batch* b, double* eig_out, double* err_out, int32_t* iters_out, int32_t* status_out,
+                       double* const* vec_out) {
+  if (!b) return STAB_ERR_ARG;
+  stab_ctx* c = b->ctx;
+  if (!b->ran) return set_err(c, STAB_ERR_STATE, "stab_batch_run has not run");
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int n = b->count;
+  std::vector<zc> val(n), raw(n);
+  std::vector<double> er(n);
+  std::vector<int32_t> it(n), st(n), dn(n), li(n), fl(n);
+  CK(c, cudaMemcpyAsync(raw.data(), b->least_raw.p, sizeof(zc) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(val.data(), b->least_val.p, sizeof(zc) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(er.data(), b->err.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(it.data(), b->iters.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(st.data(), b->status.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(dn.data(), b->done.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(li.data(), b->least_idx.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(fl.data(), b->flags.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaStreamSynchronize(s));
+  if (b->last_mode == STAB_MODE_PLAIN) {
+    for (int k = 0; k < n; ++k) {
+      if (st[k] == 0 && li[k] < 0) st[k] = STAB_ST_NOMODE;
+      if (fl[k]) st[k] = STAB_ST_SINGULAR;
+    }
+  } else {
+    val = raw;
+    finalize_polish_host(val, st, dn, b->P);
+    for (int k = 0; k < n; ++k)
+      if (fl[k]) st[k] = STAB_ST_SINGULAR;
+  }
+  for (int k = 0; k < n; ++k) {
+    const int u = b->perm[k];
+    if (eig_out) { eig_out[2 * u] = val[k].x; eig_out[2 * u + 1] = val[k].y; }
+    if (err_out) err_out[u] = er[k];
+    if (iters_out) iters_out[u] = it[k];
+    if (status_out) status_out[u] = st[k];
+    if (vec_out && vec_out[u]) {
+      CK(c, cudaMemcpyAsync(vec_out[u], b->outvec.as<zc>() + b->h_mof[k], sizeof(zc) * b->hm[k],
+                            cudaMemcpyDeviceToHost, s));
+    }
+  }
+  CK(c, cudaStreamSynchronize(s));
+  return STAB_OK;
+}
+
+int stab_batch_destroy(stab_batch* b) {
+  if (!b) return STAB_ERR_ARG;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  g_inputs.erase(b);
+  delete b;
+  return STAB_OK;
+}
+
+int stab_solve_batch(stab_ctx* c, int32_t count, const stab_params* p, const int32_t* nym,
+                     const double* const* profiles, int32_t mode, const double* seeds, double* eig_out,
+                     double* err_out, int32_t* status_out, double* const* vec_out) {
+  stab_batch* b = nullptr;
+  int rc = stab_batch_create(c, count, p, nym, profiles, &b);
+  if (rc) return rc;
+  std::unique_ptr<stab_batch, int (*)(stab_batch*)> guard(b, stab_batch_destroy);
+  if (seeds) {
+    rc = stab_batch_set_seeds(b, seeds);
+    if (rc) return rc;
+  }
+  rc = stab_batch_run(b, mode);
+  if (rc) return rc;
+  return stab_batch_results(b, eig_out, err_out, nullptr, status_out, vec_out);
+}
+
+int stab_assemble(stab_ctx* c, const stab_params* p, int32_t nym, const double* profile, double* mats_out) {
+  if (!c || !p || !profile || !mats_out) return set_err(c, STAB_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  stab_batch* b = nullptr;
+  const double* pr[1] = {profile};
+  int rc = batch_build(c, 1, p, &nym, pr, &b, 0);
+  if (rc) return rc;
+  std::unique_ptr<stab_batch> guard(b);
+  rc = run_prep(b);
+  if (rc) return rc;
+  rc = ensure_plain_pools(b);
+  if (rc) return rc;
+  const int n = b->hn[0];
+  const Range r{0, 1};
+  const int kinds_t[2] = {OP_T_A0, OP_T_B0};
+  const int kinds_s[3] = {OP_S_C0, OP_S_C1, OP_S_C2};
+  const int nk = (p->itype == 1) ? 2 : 3;
+  for (int q = 0; q < nk; ++q) {
+    const int kd = (p->itype == 1) ? kinds_t[q] : kinds_s[q];
+    rc = node_ops(b, r, kd, kd, nullptr);
+    if (rc) return rc;
+    rc = dense<zc>(b, r, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z");
+    if (rc) return rc;
+    CK(c, cudaMemcpyAsync(mats_out + 2 * (size_t)q * n * n, b->Z64.p, sizeof(zc) * n * n, cudaMemcpyDeviceToHost,
+                          c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+  }
+  return STAB_OK;
+}
+
+int stab_full_spectrum(stab_ctx* c, const stab_params* p, int32_t nym, const double* profile, double* eig_out,
+                       double* vec_out, int32_t* least_index_out, int32_t* status_out) {
+  if (!c || !p || !profile || !eig_out) return set_err(c, STAB_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  stab_batch* b = nullptr;
+  const double* pr[1] = {profile};
+  int rc = batch_build(c, 1, p, &nym, pr, &b, 0);
+  if (rc) return rc;
+  std::unique_ptr<stab_batch> guard(b);
+  rc = run_prep(b);
+  if (rc) return rc;
+  rc = run_plain(b, vec_out != nullptr);
+  if (rc) return rc;
+  const int m = b->hm[0];
+  int32_t st = 0, li = -1, fl = 0;
+  CK(c, cudaMemcpyAsync(eig_out, b->eigsorted.p, sizeof(zc) * m, cudaMemcpyDeviceToHost, c->stream));
+  if (vec_out) CK(c, cudaMemcpyAsync(vec_out, b->outvec.p, sizeof(zc) * m, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(&st, b->status.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(&li, b->least_idx.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(&fl, b->flags.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (fl) st = STAB_ST_SINGULAR;
+  if (st == 0 && li < 0) st = STAB_ST_NOMODE;
+  if (least_index_out) *least_index_out = li;
+  if (status_out) *status_out = st;
+  return STAB_OK;
+}
+
+}  // extern "C"

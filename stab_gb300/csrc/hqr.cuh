@@ -1,0 +1,14 @@
+// Host launcher of the plain FP64 full-spectrum eigensolver (hqr.cu).
+#pragma once
+#include "common.cuh"
+
+namespace stab {
+size_t eig_plain_smem(int mmax);
+// A: count column-major m x m matrices (destroyed); H: workspace of the same
+// size; eig receives m eigenvalues per instance (QR eigenvalues first, then
+// the isolated ones); status[k] = 0 or STAB_ST_NOCONV.  `order` (may be null)
+// is the processing order (largest first balances the persistent grid).
+cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
+                             const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
+                             int32_t* work_counter, const int32_t* order, int grid, cudaStream_t s);
+}  // namespace stab

@@ -1,0 +1,53 @@
+// Kernel declarations shared by the translation units of libstab_gb300.
+#pragma once
+#include "common.cuh"
+
+namespace stab {
+
+// operator kinds assembled from the per-node blocks (see k_blocks)
+enum OpKind : int {
+  OP_T_A0 = 0,   // temporal A0
+  OP_T_B0 = 1,   // temporal B0 (block diagonal)
+  OP_T_C = 2,    // B0^-1 A0 (the matrix ZGEEV sees after ZGESV)
+  OP_T_Q = 3,    // A0 - s B0
+  OP_T_DQ = 4,   // d/ds (A0 - s B0) = -B0
+  OP_S_C0 = 5,
+  OP_S_C1 = 6,
+  OP_S_C2 = 7,
+  OP_S_Q = 8,    // s^2 C0 + s C1 + C2   (lambda = 1/alpha form)
+  OP_S_DQ = 9,   // 2 s C0 + C1
+};
+
+// prep.cu
+__global__ void k_cheb_a(int ny, double* xa);
+__global__ void k_cheb_d1(int ny, const double* xa, double* D1);
+__global__ void k_cheb_d2(int ny, const double* D1, double* D2);
+__global__ void k_spline(int nprof, const ProfDesc* pdesc, const double* prof, double* spl);
+__global__ void k_nodes(int count, const InstDesc* desc, const double* prof, const double* spl, double* node);
+__global__ void k_meanderiv(int count, const InstDesc* desc, const double* const* dtab, double* node);
+__global__ void k_blocks(int count, const InstDesc* desc, const double* const* dtab, const double* node, zc* blk,
+                         int* flags);
+
+// assemble.cu
+// per-node operator (P1, P2, P3): kind_t for temporal, kind_s for spatial
+// instances, at shift sigma[k] (may be null)
+__global__ void k_node_ops(int count, const InstDesc* desc, const zc* blk, int kind_t, int kind_s, const zc* sigma,
+                           zc* ops);
+// dense column-major n x n operator (times `scale`) from ops into out +
+// out_off[k] with leading dimension ldmul*n; element type T
+template <typename T>
+cudaError_t launch_dense(int count, int nmax, const InstDesc* desc, const double* const* dtab, const zc* ops, T* out,
+                         const int64_t* out_off, int ldmul, double scale, cudaStream_t s);
+// structured y = M x for M given by ops (FP64):  y_i = P1 (D1 X)_i - P2 (D2 X)_i + P3 x_i
+__global__ void k_opmv(int count, const InstDesc* desc, const double* const* dtab, const zc* ops, const zc* x,
+                       int xslot, zc* y, int yslot);
+// post.cu
+__global__ void k_companion_fill(int count, const InstDesc* desc, zc* A, const int64_t* a_off);
+__global__ void k_post_spectrum(int count, const InstDesc* desc, const zc* eig_raw, const int64_t* eig_off,
+                                zc* eig_sorted, int32_t* least_sorted, zc* least_raw, zc* least_val);
+__global__ void k_spatial_vec(int count, const InstDesc* desc, const zc* theta, const zc* vec, int slot,
+                              zc* out, const int64_t* out_off);
+__global__ void k_temporal_vec(int count, const InstDesc* desc, const zc* vec, int slot, zc* out,
+                               const int64_t* out_off);
+
+}  // namespace stab

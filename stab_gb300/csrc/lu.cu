@@ -1,0 +1,294 @@
+// Batched dense complex LU with partial pivoting and triangular solves.
+//
+// Replaces ZGETRF (spatial.f90:978), ZGETRS (spatial.f90:996,1002) and the
+// factorisation inside ZGESV (temporal.f90:774); complex64 instances of the
+// same kernels factor A - s B for the mixed-precision polish.
+//
+// Layout: column-major n x n per instance at pool offset mat_off[k].  One
+// CTA per instance (n <= 960 here).  Blocked right-looking algorithm:
+//   1. the panel A[k0:n, k0:k0+w] is copied to shared memory and factored
+//      there (pivot search = block arg-max of |re|+|im|, first index wins,
+//      as IZAMAX);
+//   2. the panel's row swaps are applied to the other columns;
+//   3. U12 = L11^-1 A12 (forward substitution, one thread per column);
+//   4. A22 -= L21 U12 as a 64x64-tiled GEMM with L21 read from shared memory
+//      and each thread holding a 4x4 block of complex accumulators.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "lu.cuh"
+
+namespace stab {
+
+template <typename T>
+struct Piv {
+  typename cx<T>::real v;
+  int i;
+};
+
+template <typename T>
+__device__ __forceinline__ void argmax_merge(typename cx<T>::real& bv, int& bi, typename cx<T>::real v, int i) {
+  if (v > bv || (v == bv && i < bi)) { bv = v; bi = i; }
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restrict__ desc, const int32_t* __restrict__ nsz,
+                                            T* __restrict__ A, const int64_t* __restrict__ mat_off,
+                                            int32_t* __restrict__ piv, const int64_t* __restrict__ piv_off,
+                                            int32_t* __restrict__ info) {
+  typedef typename cx<T>::real R;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  const int n = nsz[k];
+  T* M = A + mat_off[k];
+  int32_t* ip = piv + piv_off[k];
+  T* P = reinterpret_cast<T*>(smraw);                  // panel: n x NB, column-major, ld = n
+  T* Ub = P + (size_t)n * NB;                          // U12 tile: NB rows x 64 (+1 pad)
+  __shared__ R red_v[256 / 32];
+  __shared__ int red_i[256 / 32];
+  __shared__ int s_piv;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int first_zero = 0;
+  for (int k0 = 0; k0 < n; k0 += NB) {
+    const int w = min(NB, n - k0);
+    const int rows = n - k0;
+    // 1. load panel
+    for (int c = 0; c < w; ++c)
+      for (int r = tid; r < rows; r += blockDim.x) P[(size_t)c * n + r] = M[(size_t)(k0 + c) * n + k0 + r];
+    __syncthreads();
+    for (int j = 0; j < w; ++j) {
+      // pivot search over panel rows j..rows-1 of column j
+      R bv = (R)-1;
+      int bi = 0x7fffffff;
+      for (int r = j + tid; r < rows; r += blockDim.x) argmax_merge<T>(bv, bi, cx<T>::abs1(P[(size_t)j * n + r]), r);
+      for (int o = 16; o > 0; o >>= 1) {
+        R ov = __shfl_down_sync(0xffffffffu, bv, o);
+        int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        argmax_merge<T>(bv, bi, ov, oi);
+      }
+      if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
+      __syncthreads();
+      if (tid == 0) {
+        R v = red_v[0];
+        int ii = red_i[0];
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) argmax_merge<T>(v, ii, red_v[q], red_i[q]);
+        if (ii < j || ii >= rows) ii = j;   // no finite entry (NaN input): keep the diagonal
+        s_piv = ii;
+        ip[k0 + j] = k0 + ii;
+        if (v == (R)0 && first_zero == 0) first_zero = k0 + j + 1;
+      }
+      __syncthreads();
+      const int p = s_piv;
+      if (p != j && tid < w) {
+        T t = P[(size_t)tid * n + j];
+        P[(size_t)tid * n + j] = P[(size_t)tid * n + p];
+        P[(size_t)tid * n + p] = t;
+      }
+      __syncthreads();
+      const T d = P[(size_t)j * n + j];
+      const bool nz = (cx<T>::abs1(d) != (R)0);
+      // scale the column below the pivot and update the rest of the panel
+      for (int r = j + 1 + tid; r < rows; r += blockDim.x) {
+        T l = P[(size_t)j * n + r];
+        if (nz) l = cx<T>::div(l, d);
+        P[(size_t)j * n + r] = l;
+        for (int c = j + 1; c < w; ++c) {
+          T u = P[(size_t)c * n + j];
+          P[(size_t)c * n + r] = cx<T>::sub(P[(size_t)c * n + r], cx<T>::mul(l, u));
+        }
+      }
+      __syncthreads();
+    }
+    // write the factored panel back
+    for (int c = 0; c < w; ++c)
+      for (int r = tid; r < rows; r += blockDim.x) M[(size_t)(k0 + c) * n + k0 + r] = P[(size_t)c * n + r];
+    // 2. row swaps on the columns outside the panel (one thread per column)
+    for (int c = tid; c < n; c += blockDim.x) {
+      if (c >= k0 && c < k0 + w) continue;
+      for (int j = 0; j < w; ++j) {
+        const int p = ip[k0 + j];
+        if (p != k0 + j) {
+          T t = M[(size_t)c * n + k0 + j];
+          M[(size_t)c * n + k0 + j] = M[(size_t)c * n + p];
+          M[(size_t)c * n + p] = t;
+        }
+      }
+    }
+    __syncthreads();
+    const int c1 = k0 + w;
+    if (c1 >= n) break;
+    // 3. U12 = L11^-1 A12 (unit lower), one thread per column
+    for (int c = c1 + tid; c < n; c += blockDim.x) {
+      T x[NB];
+#pragma unroll
+      for (int j = 0; j < NB; ++j) x[j] = (j < w) ? M[(size_t)c * n + k0 + j] : cx<T>::make(0, 0);
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        if (j >= w) break;
+#pragma unroll
+        for (int r = j + 1; r < NB; ++r)
+          if (r < w) x[r] = cx<T>::sub(x[r], cx<T>::mul(P[(size_t)j * n + r], x[j]));
+      }
+#pragma unroll
+      for (int j = 0; j < NB; ++j)
+        if (j < w) M[(size_t)c * n + k0 + j] = x[j];
+    }
+    __syncthreads();
+    // 4. A22 -= L21 U12, 64x64 tiles, 4x4 complex per thread (16x16 threads)
+    const int m2 = n - c1;
+    const int tr = tid & 15, tc = tid >> 4;
+    for (int tc0 = 0; tc0 < m2; tc0 += 64) {
+      // stage U12 tile (w x 64) in shared memory
+      for (int q = tid; q < NB * 64; q += blockDim.x) {
+        const int j = q % NB, cc_ = q / NB;   // coalesced along the column
+        const int c = c1 + tc0 + cc_;
+        Ub[j * 65 + cc_] = (j < w && c < n) ? M[(size_t)c * n + k0 + j] : cx<T>::make(0, 0);
+      }
+      __syncthreads();
+      for (int tr0 = 0; tr0 < m2; tr0 += 64) {
+        T acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] = cx<T>::make(0, 0);
+        for (int j = 0; j < w; ++j) {
+          T lv[4], uv[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const int r = tr0 + tr + 16 * a;          // row within A22
+            lv[a] = (r < m2) ? P[(size_t)j * n + w + r] : cx<T>::make(0, 0);
+          }
+#pragma unroll
+          for (int b = 0; b < 4; ++b) uv[b] = Ub[j * 65 + tc + 16 * b];
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = cx<T>::fma_(lv[a], uv[b], acc[a][b]);
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int c = c1 + tc0 + tc + 16 * b;
+          if (c >= n) continue;
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const int r = c1 + tr0 + tr + 16 * a;
+            if (r >= n) continue;
+            T* e = &M[(size_t)c * n + r];
+            *e = cx<T>::sub(*e, acc[a][b]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (tid == 0) info[k] = first_zero;
+}
+
+// Triangular solves with the factors of k_lu: X <- U^-1 L^-1 P X for nrhs
+// columns per instance.  One warp per right-hand side, the column held in
+// shared memory; the factor columns are read coalesced from global memory.
+// Right-hand sides are complex128 in memory and solved in the factor's type.
+template <typename T>
+__global__ void __launch_bounds__(256) k_getrs(int count, const int32_t* __restrict__ nsz, const T* __restrict__ LU,
+                                               const int64_t* __restrict__ mat_off, const int32_t* __restrict__ piv,
+                                               const int64_t* __restrict__ piv_off, zc* __restrict__ X,
+                                               const int64_t* __restrict__ x_off, int nrhs_fixed, int nrhs_mul,
+                                               int ldmul, const int32_t* __restrict__ skip) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int k = blockIdx.y;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const int n = nsz[k];
+  const int nrhs = nrhs_fixed > 0 ? nrhs_fixed : nrhs_mul * n;
+  const int64_t ldx = (int64_t)ldmul * n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int col = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (col >= nrhs) return;
+  T* xs = reinterpret_cast<T*>(smraw) + (size_t)warp * n;
+  const T* M = LU + mat_off[k];
+  const int32_t* ip = piv + piv_off[k];
+  zc* xg = X + x_off[k] + (size_t)col * ldx;
+  for (int r = lane; r < n; r += 32) xs[r] = cx<T>::from(xg[r]);
+  __syncwarp();
+  if (lane == 0)
+    for (int j = 0; j < n; ++j) {
+      const int p = ip[j];
+      if (p != j) { T t = xs[j]; xs[j] = xs[p]; xs[p] = t; }
+    }
+  __syncwarp();
+  for (int j = 0; j < n; ++j) {       // L y = b (unit diagonal)
+    const T xj = xs[j];
+    for (int r = j + 1 + lane; r < n; r += 32) xs[r] = cx<T>::sub(xs[r], cx<T>::mul(M[(size_t)j * n + r], xj));
+    __syncwarp();
+  }
+  for (int j = n - 1; j >= 0; --j) {  // U x = y
+    T d = M[(size_t)j * n + j];
+    T xj = xs[j];
+    if (cx<T>::abs1(d) != 0) xj = cx<T>::div(xj, d);
+    __syncwarp();
+    if (lane == 0) xs[j] = xj;
+    for (int r = lane; r < j; r += 32) xs[r] = cx<T>::sub(xs[r], cx<T>::mul(M[(size_t)j * n + r], xj));
+    __syncwarp();
+  }
+  for (int r = lane; r < n; r += 32) xg[r] = cx<T>::to64(xs[r]);
+}
+
+// ---- host launchers ------------------------------------------------------
+template <typename T>
+int lu_nb_for(int n) {
+  // panel width such that the panel (n x NB) plus the U tile fit in shared memory
+  const size_t lim = 200 * 1024;
+  if ((size_t)n * 32 * sizeof(T) + 32 * 65 * sizeof(T) <= lim) return 32;
+  if ((size_t)n * 16 * sizeof(T) + 16 * 65 * sizeof(T) <= lim) return 16;
+  return 8;
+}
+
+template <typename T, int NB>
+static cudaError_t launch_lu_nb(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A,
+                                const int64_t* mat_off, int32_t* piv, const int64_t* piv_off, int32_t* info,
+                                cudaStream_t s) {
+  size_t sm = (size_t)nmax * NB * sizeof(T) + (size_t)NB * 65 * sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(k_lu<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_lu<T, NB><<<count, 256, sm, s>>>(count, desc, nsz, A, mat_off, piv, piv_off, info);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
+                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  int nb = lu_nb_for<T>(nmax);
+  if (nb == 32) return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s);
+  if (nb == 16) return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s);
+  return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s);
+}
+
+template <typename T>
+cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, const int64_t* mat_off,
+                         const int32_t* piv, const int64_t* piv_off, zc* X, const int64_t* x_off, int nrhs_fixed,
+                         int nrhs_mul, int ldmul, const int32_t* skip, cudaStream_t s) {
+  const int nrhs_max = nrhs_fixed > 0 ? nrhs_fixed : nrhs_mul * nmax;
+  if (count <= 0 || nrhs_max <= 0) return cudaSuccess;
+  const int warps = nrhs_max >= 8 ? 8 : 1;
+  size_t sm = (size_t)warps * nmax * sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(k_getrs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  dim3 g((nrhs_max + warps - 1) / warps, count);
+  k_getrs<T><<<g, warps * 32, sm, s>>>(count, nsz, LU, mat_off, piv, piv_off, X, x_off, nrhs_fixed, nrhs_mul, ldmul,
+                                        skip);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_lu<zc>(int, const InstDesc*, const int32_t*, int, zc*, const int64_t*, int32_t*,
+                                   const int64_t*, int32_t*, cudaStream_t);
+template cudaError_t launch_lu<cc>(int, const InstDesc*, const int32_t*, int, cc*, const int64_t*, int32_t*,
+                                   const int64_t*, int32_t*, cudaStream_t);
+template cudaError_t launch_getrs<zc>(int, const int32_t*, int, const zc*, const int64_t*, const int32_t*,
+                                      const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
+                                      cudaStream_t);
+template cudaError_t launch_getrs<cc>(int, const int32_t*, int, const cc*, const int64_t*, const int32_t*,
+                                      const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
+                                      cudaStream_t);
+
+}  // namespace stab

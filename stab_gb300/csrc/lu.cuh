@@ -1,0 +1,20 @@
+// Host launchers of the batched LU / triangular-solve kernels (lu.cu).
+#pragma once
+#include "common.cuh"
+
+namespace stab {
+// Factor count column-major matrices (n = nsz[k], nmax = max n) in place.
+// piv receives 0-based absolute pivot rows; info[k] = 1-based index of the
+// first exactly-zero pivot, 0 if none (ZGETRF's INFO convention).
+template <typename T>
+cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
+                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s);
+// Solve with the factors for complex128 right-hand sides at X + x_off[k]:
+// nrhs = nrhs_fixed if > 0, else nrhs_mul * n; leading dimension ldmul * n.
+// The solve runs in the factor's precision; instances with skip[k] != 0
+// (skip may be null) are left alone.
+template <typename T>
+cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, const int64_t* mat_off,
+                         const int32_t* piv, const int64_t* piv_off, zc* X, const int64_t* x_off, int nrhs_fixed,
+                         int nrhs_mul, int ldmul, const int32_t* skip, cudaStream_t s);
+}  // namespace stab

@@ -1,0 +1,273 @@
+// Mixed-precision polish of one eigenpair per instance (no reference
+// function: the reference leaves mode selection to a human with
+// getevec -v, getevec.f90:161-172, and polishing to an external shooting
+// code).  The eigenproblem is written as Q(t) x = 0 with
+//   temporal:  Q(w) = A0 - w B0                 (t = omega)
+//   spatial:   Q(l) = l^2 C0 + l C1 + C2        (t = lambda = 1/alpha)
+// Steps (host side in capi.cu):
+//   a. complex64 LU of Q(s) at the seed s; two inverse-iteration steps
+//      x <- Q(s)^-1 Q'(s) x give the eigenvector direction;
+//   b. complex64 LU of the bordered Jacobian J = [Q(s) with column p
+//      replaced by Q'(s) x], p = arg max |x_p| (x_p = 1 fixes the scale);
+//   c. Newton-chord steps: r = Q(t) x in FP64 (k_qmv, O(N^2) from the
+//      per-node blocks), d = J^-1 r in complex64, x_j -= d_j (j != p),
+//      t -= d_p.  The FP64 residual makes the fixed point FP64-accurate; the
+//      complex64 factor only sets the contraction rate.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "polish.cuh"
+
+namespace stab {
+
+__device__ __forceinline__ int64_t pnode_index(const InstDesc& d) { return d.off_blk / BLK_STRIDE; }
+
+// (P1, P2, P3)[e][v] of Q(t) (deriv = 0) or Q'(t) (deriv = 1) for node block b
+__device__ __forceinline__ void qblock(const InstDesc& d, const zc* b, zc t, int deriv, int q, zc& p1, zc& p2,
+                                       zc& p3) {
+  const zc z0 = zmk(0.0, 0.0);
+  if (d.itype == 1) {
+    if (!deriv) { p1 = b[q]; p2 = b[25 + q]; p3 = zsub(b[50 + q], zmul(t, b[75 + q])); }
+    else { p1 = z0; p2 = z0; p3 = zmk(-b[75 + q].x, -b[75 + q].y); }
+  } else {
+    if (!deriv) {
+      const zc t2 = zmul(t, t);
+      p1 = zadd(zmul(t2, b[q]), zmul(t, b[75 + q]));
+      p2 = zmul(t2, b[25 + q]);
+      p3 = zadd(zadd(zmul(t2, b[50 + q]), zmul(t, b[100 + q])), b[125 + q]);
+    } else {
+      const zc tt = zscale(t, 2.0);
+      p1 = zadd(zmul(tt, b[q]), b[75 + q]);
+      p2 = zmul(tt, b[25 + q]);
+      p3 = zadd(zmul(tt, b[50 + q]), b[100 + q]);
+    }
+  }
+}
+
+// y = Q(t) x or Q'(t) x, FP64, one CTA per instance
+__global__ void k_qmv(int count, const InstDesc* __restrict__ desc, const double* const* __restrict__ dtab,
+                      const zc* __restrict__ blk, const zc* __restrict__ theta, int deriv, zc* __restrict__ vec,
+                      int xslot, int yslot, const int32_t* __restrict__ skip) {
+  extern __shared__ zc qsm[];
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const InstDesc d = desc[k];
+  const int n = d.n, ny = d.ny;
+  const double* D1 = dtab[2 * d.dmat];
+  const double* D2 = dtab[2 * d.dmat + 1];
+  const zc* bb = blk + d.off_blk;
+  const zc* xv = vec + d.off_vec + (int64_t)xslot * n;
+  zc* yv = vec + d.off_vec + (int64_t)yslot * n;
+  const zc t = theta[k];
+  zc* xs = qsm;
+  zc* w1 = qsm + n;
+  zc* w2 = qsm + 2 * n;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) xs[q] = xv[q];
+  __syncthreads();
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int i = q / 5, v = q % 5;
+    zc s1 = zmk(0.0, 0.0), s2 = zmk(0.0, 0.0);
+    const double* r1 = D1 + (size_t)i * ny;
+    const double* r2 = D2 + (size_t)i * ny;
+    for (int j = 0; j < ny; ++j) {
+      const zc xj = xs[j * 5 + v];
+      const double a = r1[j], b = r2[j];
+      s1.x = fma(a, xj.x, s1.x); s1.y = fma(a, xj.y, s1.y);
+      s2.x = fma(b, xj.x, s2.x); s2.y = fma(b, xj.y, s2.y);
+    }
+    w1[q] = s1;
+    w2[q] = s2;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int i = q / 5, e = q % 5;
+    const zc* b = bb + (size_t)BLK_STRIDE * i;
+    zc acc = zmk(0.0, 0.0);
+    for (int v = 0; v < 5; ++v) {
+      zc p1, p2, p3;
+      qblock(d, b, t, deriv, e * 5 + v, p1, p2, p3);
+      acc = zfma(p1, w1[i * 5 + v], acc);
+      acc = zsub(acc, zmul(p2, w2[i * 5 + v]));
+      acc = zfma(p3, xs[i * 5 + v], acc);
+    }
+    yv[q] = acc;
+  }
+}
+
+// deterministic start vector (hash of the index), so it is not orthogonal to
+// the wanted eigenvector by accident
+__global__ void k_vec_init(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int slot) {
+  const int k = blockIdx.y;
+  if (k >= count) return;
+  const InstDesc d = desc[k];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.n) return;
+  uint32_t h = (uint32_t)q * 2654435761u + 0x9e3779b9u;
+  h ^= h >> 15; h *= 0x85ebca6bu; h ^= h >> 13;
+  const double a = (double)(h & 0xffff) / 65536.0, b = (double)((h >> 16) & 0xffff) / 65536.0;
+  vec[d.off_vec + (int64_t)slot * d.n + q] = zmk(1.0 + a, b - 0.5);
+}
+
+// x <- x / x_p with p = first index of max |x|; writes p to piv_out when non-null
+__global__ void k_normalize(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int slot,
+                            int32_t* __restrict__ piv_out, const int32_t* __restrict__ skip) {
+  __shared__ double bv[32];
+  __shared__ int bi[32];
+  __shared__ int s_p;
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const InstDesc d = desc[k];
+  zc* x = vec + d.off_vec + (int64_t)slot * d.n;
+  double best = -1.0;
+  int idx = 0x7fffffff;
+  for (int q = threadIdx.x; q < d.n; q += blockDim.x) {
+    double a = zabs(x[q]);
+    if (a > best || (a == best && q < idx)) { best = a; idx = q; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double ob = __shfl_down_sync(0xffffffffu, best, o);
+    int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (ob > best || (ob == best && oi < idx)) { best = ob; idx = oi; }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { bv[warp] = best; bi[warp] = idx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      if (bv[w] > best || (bv[w] == best && bi[w] < idx)) { best = bv[w]; idx = bi[w]; }
+    if (idx < 0 || idx >= d.n) idx = 0;   // no finite entry
+    s_p = idx;
+    if (piv_out) piv_out[k] = idx;
+  }
+  __syncthreads();
+  const zc sc = x[s_p];
+  __syncthreads();
+  if (sc.x == 0.0 && sc.y == 0.0) return;
+  for (int q = threadIdx.x; q < d.n; q += blockDim.x) x[q] = zdiv(x[q], sc);
+}
+
+// column p of the complex64 matrix <- vector slot (the bordered Jacobian)
+__global__ void k_set_column(int count, const InstDesc* __restrict__ desc, cc* __restrict__ M,
+                             const int64_t* __restrict__ m_off, const int32_t* __restrict__ pcol,
+                             const zc* __restrict__ vec, int slot) {
+  const int k = blockIdx.y;
+  if (k >= count) return;
+  const InstDesc d = desc[k];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.n) return;
+  const zc a = vec[d.off_vec + (int64_t)slot * d.n + q];
+  M[m_off[k] + (int64_t)pcol[k] * d.n + q] = cmk((float)a.x, (float)a.y);
+}
+
+// copy slot a -> slot b
+__global__ void k_vec_copy(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int a, int b,
+                           const int32_t* __restrict__ skip) {
+  const int k = blockIdx.y;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const InstDesc d = desc[k];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.n) return;
+  vec[d.off_vec + (int64_t)b * d.n + q] = vec[d.off_vec + (int64_t)a * d.n + q];
+}
+
+// Newton-chord update from the correction d (slot dslot):
+// x_j -= d_j (j != p), t -= d_p; converged when |d_p| <= tol |t| and
+// max_j |d_j| <= tol max_j |x_j|.
+__global__ void k_newton_update(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int xslot,
+                                int dslot, const int32_t* __restrict__ pcol, zc* __restrict__ theta,
+                                int32_t* __restrict__ done, double* __restrict__ err, int32_t* __restrict__ iters,
+                                double tol) {
+  __shared__ double red[64];
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  if (done[k]) return;
+  const InstDesc d = desc[k];
+  zc* x = vec + d.off_vec + (int64_t)xslot * d.n;
+  const zc* dd = vec + d.off_vec + (int64_t)dslot * d.n;
+  const int p = pcol[k];
+  double dmax = 0.0, xmax = 0.0;
+  bool bad = false;
+  for (int q = threadIdx.x; q < d.n; q += blockDim.x) {
+    if (q == p) continue;
+    zc a = dd[q];
+    if (!isfinite(a.x) || !isfinite(a.y)) bad = true;
+    zc nx = zsub(x[q], a);
+    x[q] = nx;
+    dmax = fmax(dmax, zabs(a));
+    xmax = fmax(xmax, zabs(nx));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    dmax = fmax(dmax, __shfl_down_sync(0xffffffffu, dmax, o));
+    xmax = fmax(xmax, __shfl_down_sync(0xffffffffu, xmax, o));
+  }
+  const int anybad = __syncthreads_or(bad);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { red[warp] = dmax; red[32 + warp] = xmax; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { dmax = fmax(dmax, red[w]); xmax = fmax(xmax, red[32 + w]); }
+    xmax = fmax(xmax, 1.0);   // x_p = 1
+    const zc dp = dd[p];
+    const zc t = zsub(theta[k], dp);
+    theta[k] = t;
+    const double rel = zabs(dp) / fmax(zabs(t), 1e-300);
+    err[k] = rel;
+    iters[k] += 1;
+    if (anybad || !isfinite(t.x) || !isfinite(t.y)) done[k] = 3;           // NaN
+    else if (rel <= tol && dmax <= tol * xmax) done[k] = 1;                 // converged
+  }
+}
+
+// ---- host launchers --------------------------------------------------------
+cudaError_t launch_qmv(int count, int nmax, const InstDesc* desc, const double* const* dtab, const zc* blk,
+                       const zc* theta, int deriv, zc* vec, int xslot, int yslot, const int32_t* skip,
+                       cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  size_t sm = 3 * (size_t)nmax * sizeof(zc);
+  cudaError_t e = cudaFuncSetAttribute(k_qmv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_qmv<<<count, 256, sm, s>>>(count, desc, dtab, blk, theta, deriv, vec, xslot, yslot, skip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vec_init(int count, int nmax, const InstDesc* desc, zc* vec, int slot, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  dim3 g((nmax + 255) / 256, count);
+  k_vec_init<<<g, 256, 0, s>>>(count, desc, vec, slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_normalize(int count, const InstDesc* desc, zc* vec, int slot, int32_t* piv_out,
+                             const int32_t* skip, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_normalize<<<count, 256, 0, s>>>(count, desc, vec, slot, piv_out, skip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_column(int count, int nmax, const InstDesc* desc, cc* M, const int64_t* m_off,
+                              const int32_t* pcol, const zc* vec, int slot, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  dim3 g((nmax + 255) / 256, count);
+  k_set_column<<<g, 256, 0, s>>>(count, desc, M, m_off, pcol, vec, slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vec_copy(int count, int nmax, const InstDesc* desc, zc* vec, int a, int b, const int32_t* skip,
+                            cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  dim3 g((nmax + 255) / 256, count);
+  k_vec_copy<<<g, 256, 0, s>>>(count, desc, vec, a, b, skip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_newton_update(int count, const InstDesc* desc, zc* vec, int xslot, int dslot, const int32_t* pcol,
+                                 zc* theta, int32_t* done, double* err, int32_t* iters, double tol,
+                                 cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_newton_update<<<count, 256, 0, s>>>(count, desc, vec, xslot, dslot, pcol, theta, done, err, iters, tol);
+  return cudaGetLastError();
+}
+
+}  // namespace stab

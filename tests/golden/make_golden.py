@@ -1,0 +1,87 @@
+"""Generate the golden fixtures of this directory from the reference tree.
+
+Run once in a container that has the reference checkout (path given as the
+first argument); the GPU machine does not.  It copies the reference's own test
+inputs and outputs for the Chebyshev path into small files:
+
+  ts_profile.npy      TStest/profile.0 (= test/profile.0, same md5): the FSC
+                      Tollmien-Schlichting mean profile, rows y rho u v w T
+  cases.json          run parameters of each case (from its input.dat /
+                      *.inp) and the reference's published eigenvalues
+                      (test/space.1:3, TStest/README.md:9-10,
+                      thesis/TStest/time.ref:2, space.ref:3)
+  space1.ref          test/space.1 (spatial N=32 eigenfunction)
+  thesis_time.ref     thesis/TStest/time.ref (temporal N=96 eigenfunction)
+  thesis_space.ref    thesis/TStest/space.ref (spatial N=96 eigenfunction)
+"""
+import json
+import os
+import shutil
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def read_input(path):
+    vals = []
+    for ln in open(path):
+        f = ln.split("!")[0].replace(",", " ").split()
+        if f:
+            vals.append(f)
+    mattyp = int(vals[0][0])
+    o = 1
+    T0 = 0.0
+    if mattyp == 1:
+        T0 = float(vals[1][0]); o = 2
+    Ma, Re, Pr = map(float, vals[o][:3])
+    ny, yi, ymax = int(vals[o + 1][0]), float(vals[o + 1][1]), float(vals[o + 1][2])
+    ievec = int(vals[o + 2][0])
+    ider = int(vals[o + 3][0])
+    top, wall, wallt, curve = map(int, vals[o + 4][:4])
+    itype = int(vals[o + 5][0])
+    a = complex(float(vals[o + 6][0]), float(vals[o + 6][1]))
+    b = complex(float(vals[o + 7][0]), float(vals[o + 7][1]))
+    d = dict(mattyp=mattyp, T0=T0, Ma=Ma, Re=Re, Pr=Pr, ny=ny, yi=yi, ymax=ymax, ievec=ievec, ider=ider,
+             top=top, wall=wall, wallt=wallt, curve=curve, itype=itype)
+    if itype == 1:
+        d["alpha"], d["beta"], d["omega"] = [a.real, a.imag], [b.real, b.imag], [0.0, 0.0]
+    else:
+        d["omega"], d["beta"], d["alpha"] = [a.real, a.imag], [b.real, b.imag], [0.0, 0.0]
+    return d
+
+
+def main(ref):
+    rows = []
+    for ln in open(os.path.join(ref, "TStest", "profile.0")):
+        if ln[:1] == "#" or not ln.split():
+            continue
+        rows.append([float(t) for t in ln.split()[:6]])
+    np.save(os.path.join(HERE, "ts_profile.npy"), np.asarray(rows, dtype=np.float64))
+    cases = {}
+    c = read_input(os.path.join(ref, "test", "input.dat"))
+    c["golden"] = [2.2805022654496E-01, -6.5136925762007E-03]
+    c["eigfunction"] = "space1.ref"
+    cases["test_spatial_n32"] = c
+    c = read_input(os.path.join(ref, "TStest", "input.dat"))
+    c64 = dict(c, ny=64, golden=[2.2804739410500E-01, -6.5163146761218E-03])
+    cases["tstest_spatial_n64"] = c64
+    cases["tstest_spatial_n96"] = dict(c, golden=[2.2804739411367E-01, -6.5163146912049E-03])
+    c = read_input(os.path.join(ref, "thesis", "TStest", "temporal.inp"))
+    c["golden"] = [1.1467880189410E-01, 2.3844535276599E-03]
+    c["eigfunction"] = "thesis_time.ref"
+    cases["thesis_temporal_n96"] = c
+    c = read_input(os.path.join(ref, "thesis", "TStest", "spatial.inp"))
+    c["golden"] = [2.2804739411180E-01, -6.5163146952626E-03]
+    c["eigfunction"] = "thesis_space.ref"
+    cases["thesis_spatial_n96"] = c
+    with open(os.path.join(HERE, "cases.json"), "w") as fh:
+        json.dump(cases, fh, indent=1)
+    shutil.copyfile(os.path.join(ref, "test", "space.1"), os.path.join(HERE, "space1.ref"))
+    shutil.copyfile(os.path.join(ref, "thesis", "TStest", "time.ref"), os.path.join(HERE, "thesis_time.ref"))
+    shutil.copyfile(os.path.join(ref, "thesis", "TStest", "space.ref"), os.path.join(HERE, "thesis_space.ref"))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,183 @@
+"""GPU path against the oracle and the reference's golden files.
+
+Tolerances (stated per check):
+  operators     max |GPU - oracle| <= 1e-12 * max |oracle|   (FP64 assembly)
+  eigenvalue    |GPU - oracle| / |oracle| <= 1e-10            (least-stable mode)
+  eigenvector   max |GPU - oracle| <= 1e-8 after dividing both by their
+                first max-modulus entry
+  golden files  ndiff -abserr 1e-8 on every number of space.N / time.N
+                (thesis/TStest/run.sh:36-39)
+"""
+import numpy as np
+import pytest
+
+import stab_gb300 as sg
+from oracle import stab_oracle as so
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+EIG_REL = 1e-10
+VEC_ABS = 1e-8
+NDIFF_ABS = 1e-8
+
+
+def _mat_close(a, b, tol=1e-12):
+    scale = max(np.max(np.abs(b)), 1e-300)
+    return np.max(np.abs(a - b)) / scale
+
+
+@pytest.mark.parametrize("wallt", [0, 2])
+def test_assemble_temporal_matches_oracle(ctx, wallt):
+    d, prof = H.synth_case(1, 24, 0.7, 1500.0, a=0.2, b=0.1)
+    d["wallt"] = wallt
+    A0, B0 = ctx.assemble(H.stab_params(d), prof)
+    p = H.oracle_params(d)
+    ms = so.mean_state(p, prof[:, 0], np.where(np.arange(5) == 2, 0.0, prof[:, 1:6]))
+    A0o, B0o = so.temporal_pencil(p, ms)
+    assert _mat_close(A0, A0o) < 1e-12
+    assert _mat_close(B0, B0o) < 1e-12
+
+
+@pytest.mark.parametrize("top,wallt", [(0, 0), (1, 0), (0, 2)])
+def test_assemble_spatial_matches_oracle(ctx, top, wallt):
+    d, prof = H.synth_case(2, 20, 0.8, 2000.0, w=0.05, b=0.1, crossflow=True)
+    d["top"], d["wallt"] = top, wallt
+    mats = ctx.assemble(H.stab_params(d), prof)
+    p = H.oracle_params(d)
+    ms = so.mean_state(p, prof[:, 0], np.where(np.arange(5) == 2, 0.0, prof[:, 1:6]))
+    ref = so.spatial_operators(p, ms)
+    for a, b in zip(mats, ref):
+        assert _mat_close(a, b) < 1e-12
+
+
+def test_assemble_constant_viscosity_infinite_map(ctx):
+    c = H.cases()["test_spatial_n32"]
+    mats = ctx.assemble(H.stab_params(c), H.ts_profile())
+    p = H.oracle_params(c)
+    prof = H.ts_profile()
+    ms = so.mean_state(p, prof[:, 0], np.where(np.arange(5) == 2, 0.0, prof[:, 1:6]))
+    for a, b in zip(mats, so.spatial_operators(p, ms)):
+        assert _mat_close(a, b) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["thesis_temporal_n96", "test_spatial_n32"])
+def test_full_spectrum_golden_eigenvalue(ctx, name):
+    c = H.cases()[name]
+    eig, vec, li, st = ctx.full_spectrum(H.stab_params(c), H.ts_profile(), want_vector=False)
+    assert st in (sg.ST_OK, sg.ST_NOMODE)
+    es = H.oracle_solve(c, H.ts_profile(), want_vectors=False)
+    g = complex(*c["golden"])
+    j = so.getevec_select(eig, g)
+    jo = so.getevec_select(es.eig, g)
+    assert abs(eig[j] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    assert abs(eig[j] - g) / abs(g) < 1e-9     # reference platform band ~1e-11
+    # sorted ascending by imaginary part (PIKSR2 order)
+    assert np.all(np.diff(eig.imag[np.isfinite(eig.imag)]) >= 0)
+
+
+def test_full_spectrum_set_matches_oracle(ctx):
+    d, prof = H.synth_case(1, 32, 0.5, 1000.0, a=0.2)
+    eig, vec, li, st = ctx.full_spectrum(H.stab_params(d), prof, want_vector=True)
+    es = H.oracle_solve(d, prof)
+    assert np.sum(eig == 0) == np.sum(es.eig == 0) == 8
+    # every oracle eigenvalue of modest size is reproduced
+    for w in es.eig[(np.abs(es.eig) > 0) & (np.abs(es.eig) < 2.0)]:
+        assert np.min(np.abs(eig - w)) <= 1e-8 * max(1.0, abs(w))
+    # least-stable selection and its eigenvector
+    jo = H.select_least(es.eig, d)
+    assert li >= 0
+    assert abs(eig[li] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    vo = H.phase_normalize(es.evec[:, jo])
+    assert np.max(np.abs(H.phase_normalize(vec) - vo)) < VEC_ABS
+
+
+def test_full_spectrum_spatial_selection(ctx):
+    d, prof = H.synth_case(2, 32, 0.8, 2000.0, w=0.05, b=0.1, crossflow=True)
+    eig, vec, li, st = ctx.full_spectrum(H.stab_params(d), prof, want_vector=True)
+    es = H.oracle_solve(d, prof)
+    jo = H.select_least(es.eig, d)
+    assert li >= 0 and jo >= 0
+    assert abs(eig[li] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    # eigenvector: [lambda phi; phi] with the ZGEEV scaling
+    assert abs(np.linalg.norm(vec) - 1.0) < 1e-12
+    k = int(np.argmax(np.abs(vec)))
+    assert vec[k].imag == 0.0 and vec[k].real > 0
+    assert np.max(np.abs(H.phase_normalize(vec) - H.phase_normalize(es.evec[:, jo]))) < VEC_ABS
+
+
+@pytest.mark.parametrize("name,ref", [("test_spatial_n32", "space1.ref"),
+                                      ("thesis_temporal_n96", "thesis_time.ref"),
+                                      ("thesis_spatial_n96", "thesis_space.ref")])
+def test_polish_reproduces_golden_eigenfunction(ctx, name, ref):
+    """getevec -v on the reference's value, then the eigenfunction file."""
+    c = H.cases()[name]
+    g = complex(*c["golden"])
+    p = H.stab_params(c)
+    eig, err, iters, status, vecs = ctx.solve_batch([p], [H.ts_profile()], sg.MODE_SEEDED, seeds=[g],
+                                                    want_vectors=True)
+    assert status[0] == sg.ST_OK, (status, err, iters)
+    es = H.oracle_solve(c, H.ts_profile(), want_vectors=False)
+    jo = so.getevec_select(es.eig, g)
+    assert abs(eig[0] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    ms = so.mean_state(H.oracle_params(c), H.ts_profile()[:, 0],
+                       np.where(np.arange(5) == 2, 0.0, H.ts_profile()[:, 1:6]))
+    rows = H.eigfunction_rows(vecs[0], c["ny"], ms.y)
+    refr = H.ref_rows(ref)
+    assert np.max(np.abs(rows[:, 1:] - refr[:, 1:])) < NDIFF_ABS
+
+
+def test_polish_from_perturbed_seed_temporal(ctx):
+    d, prof = H.synth_case(1, 48, 1.2, 800.0, a=0.25, b=0.05)
+    es = H.oracle_solve(d, prof)
+    jo = H.select_least(es.eig, d)
+    w = es.eig[jo]
+    seed = w * (1 + 1e-7 * (1 + 1j))
+    eig, err, iters, status, vecs = ctx.solve_batch([H.stab_params(d)], [prof], sg.MODE_SEEDED, seeds=[seed],
+                                                    want_vectors=True)
+    assert status[0] == sg.ST_OK
+    assert abs(eig[0] - w) / abs(w) < EIG_REL
+    assert np.max(np.abs(H.phase_normalize(vecs[0]) - H.phase_normalize(es.evec[:, jo]))) < VEC_ABS
+
+
+def _mixed_batch():
+    rng = np.random.Generator(np.random.PCG64(7))
+    cases = []
+    for k in range(6):
+        N = int(rng.choice([16, 24, 32]))
+        if k % 3 == 2:
+            d, prof = H.synth_case(2, N, float(rng.uniform(0.3, 1.5)), float(rng.uniform(500, 2500)),
+                                   w=0.05, b=float(rng.uniform(0, 0.2)), crossflow=True)
+        else:
+            d, prof = H.synth_case(1, N, float(rng.uniform(0.1, 2.0)), float(10 ** rng.uniform(2.5, 3.5)),
+                                   a=float(rng.uniform(0.05, 0.4)), b=float(rng.uniform(0, 0.3)))
+        cases.append((d, prof))
+    return cases
+
+
+def test_batch_plain_mixed_sizes_and_types(ctx):
+    cases = _mixed_batch()
+    eig, err, iters, status, vecs = ctx.solve_batch([H.stab_params(d) for d, _ in cases],
+                                                    [p for _, p in cases], sg.MODE_PLAIN, want_vectors=True)
+    for k, (d, prof) in enumerate(cases):
+        es = H.oracle_solve(d, prof)
+        jo = H.select_least(es.eig, d)
+        assert status[k] == sg.ST_OK
+        assert abs(eig[k] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL, k
+        assert np.max(np.abs(H.phase_normalize(vecs[k]) - H.phase_normalize(es.evec[:, jo]))) < VEC_ABS
+
+
+def test_batch_coarse_seeded_matches_oracle(ctx):
+    rng = np.random.Generator(np.random.PCG64(11))
+    cases = [H.synth_case(1, int(rng.choice([48, 64])), float(rng.uniform(0.2, 1.5)),
+                          float(10 ** rng.uniform(2.5, 3.4)), a=float(rng.uniform(0.05, 0.4)),
+                          b=float(rng.uniform(0, 0.3))) for _ in range(4)]
+    eig, err, iters, status, vecs = ctx.solve_batch([H.stab_params(d) for d, _ in cases],
+                                                    [p for _, p in cases], sg.MODE_COARSE)
+    ok = 0
+    for k, (d, prof) in enumerate(cases):
+        es = H.oracle_solve(d, prof, want_vectors=False)
+        w = es.eig[H.select_least(es.eig, d)]
+        if status[k] == sg.ST_OK and abs(eig[k] - w) / abs(w) < EIG_REL:
+            ok += 1
+    assert ok >= 3

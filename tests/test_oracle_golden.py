@@ -1,0 +1,52 @@
+"""The oracle against the reference's own golden files (parity pin)."""
+import numpy as np
+import pytest
+
+from oracle import stab_oracle as so
+from tests import helpers as H
+
+NDIFF_ABS = 1e-8        # thesis/TStest/run.sh:36-39 (ndiff -abserr 1e-8)
+EIG_REL = 1e-10         # least-stable eigenvalue, relative
+
+
+@pytest.mark.parametrize("name", ["test_spatial_n32", "tstest_spatial_n64", "tstest_spatial_n96",
+                                  "thesis_temporal_n96", "thesis_spatial_n96"])
+def test_oracle_eigenvalue_matches_reference(name):
+    c = H.cases()[name]
+    es = H.oracle_solve(c, H.ts_profile(), want_vectors=("eigfunction" in c))
+    g = complex(*c["golden"])
+    j = so.getevec_select(es.eig, g)   # getevec -v
+    assert abs(es.eig[j] - g) / abs(g) < EIG_REL
+    if "eigfunction" in c:
+        rows = H.eigfunction_rows(es.evec[:, j], c["ny"], es.ms.y)
+        ref = H.ref_rows(c["eigfunction"])
+        assert rows.shape == ref.shape
+        assert np.max(np.abs(rows[:, 1:] - ref[:, 1:])) < NDIFF_ABS
+        assert np.allclose(rows[:-1, 0], ref[:-1, 0], rtol=1e-12, atol=1e-13)
+
+
+def test_oracle_text_format_matches_space1():
+    c = H.cases()["test_spatial_n32"]
+    es = H.oracle_solve(c, H.ts_profile())
+    j = so.getevec_select(es.eig, complex(*c["golden"]))
+    txt = so.eigfunction_text(es, j).splitlines()
+    ref = open(H.GOLDEN + "/space1.ref").read().splitlines()
+    assert txt[0] == ref[0] and txt[1] == ref[1] and txt[3] == ref[3]
+    assert len(txt) == len(ref)
+    assert all(len(a) == len(b) for a, b in zip(txt[4:], ref[4:]))
+
+
+def test_temporal_dirichlet_rows_give_exact_zero_eigenvalues():
+    d, prof = H.synth_case(1, 24, 0.5, 1000.0, a=0.2)
+    es = H.oracle_solve(d, prof, want_vectors=False)
+    assert np.sum(es.eig == 0) == 8
+
+
+def test_evec_dat_record_layout():
+    d, prof = H.synth_case(1, 8, 0.5, 1000.0, a=0.2)
+    es = H.oracle_solve(d, prof)
+    raw = so.evec_dat_bytes(es)
+    import struct
+    n1 = struct.unpack("<i", raw[:4])[0]
+    assert n1 == 40
+    assert struct.unpack("<10i", raw[4:44])[:4] == (0, 8, 5, 1)

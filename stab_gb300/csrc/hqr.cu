@@ -354,6 +354,12 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
           for (int q = tid; q < ntask; q += HQ_T) {
             if (q == 0) {
               if (k > m0) { Hs(k, k - 1) = zmk(ident ? v1.x : beta, ident ? v1.y : 0.0); Hs(k + 1, k - 1) = zmk(0.0, 0.0); }
+              if (k == m0 && m0 > l && !ident) {
+                // a sweep started below l still applies the first reflector to
+                // column m0-1: H(m0, m0-1) picks up the factor (1 - conj(tau));
+                // the fill-in at H(m0+1, m0-1) is what the start test bounds.
+                Hs(m0, m0 - 1) = zmul(Hs(m0, m0 - 1), zsub(zmk(1.0, 0.0), zconj(tau)));
+              }
               if (!ident) {
                 for (int j = k; j <= k + 1; ++j) {   // left on the 2x2 corner
                   zc a = Hs(k, j), b = Hs(k + 1, j);

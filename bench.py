@@ -1,0 +1,375 @@
+"""Benchmark: converged least-stable modes per second on one GB300.
+
+Workload (the configuration the metric is quoted on): 4096 temporal
+instances, N uniform over {48, 64, 96, 128} (pencils of order 240-640),
+alpha ~ U[0.05, 0.4], beta ~ U[0, 0.3], Re ~ log-U[300, 3000],
+M ~ U[0, 2] (clamped to >= 1e-3), seeded with PCG64(20261203 + rank).
+Mean profiles are synthetic with the stated shapes: U = erf(y/2), V = W = 0,
+T by Crocco-Busemann with an adiabatic Tw, rho = 1/T, 2000 rows on [0, 60];
+Sutherland viscosity with S/T_inf = 0.3815, Pr = 0.72, Streett map with
+ymax = 50 and half the points below y = 2.
+
+One step = one pass of the seeded mixed-precision path over the whole batch
+(STAB_MODE_COARSE: FP64 full spectrum at N = 32 for the shifts, complex64 LU
+shift-invert with FP64 residuals at full N, FP64 fallback on failure).  A
+mode counts as converged when it agrees with the plain FP64 path (the full
+GPU spectrum, itself checked against the CPU oracle by the tests) to
+|d omega| / |omega| <= 1e-10.  The working set (393 MB of profiles and
+~7 GB of matrices) is far larger than L2, so no flush is needed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "converged least-stable modes/sec at |d omega|<=1e-10 (seeded+mixed vs plain FP64)"
+UNIT = "modes/s"
+TOL = 1e-10
+T0_SUTH = 110.4 / 0.3815
+FP64_PEAK_TFLOPS = 1.19   # measured on this machine's GB300 (profiles/fp64_fp32_peak_probe.md)
+FP32_PEAK_TFLOPS = 69.9
+
+
+def workload(count: int, seed: int):
+    """Run parameters (dicts) and one contiguous (count, 2000, 6) profile array."""
+    from scipy.special import erf
+    rng = np.random.Generator(np.random.PCG64(seed))
+    N = rng.choice([48, 64, 96, 128], size=count)
+    al = rng.uniform(0.05, 0.4, count)
+    be = rng.uniform(0.0, 0.3, count)
+    Re = 10.0 ** rng.uniform(math.log10(300.0), math.log10(3000.0), count)
+    M = np.maximum(rng.uniform(0.0, 2.0, count), 1e-3)
+    y = np.linspace(0.0, 60.0, 2000)
+    U = erf(y / 2.0)
+    prof = np.empty((count, y.size, 6))
+    for k in range(count):
+        Tw = 1.0 + 0.2 * math.sqrt(0.72) * M[k] ** 2
+        T = Tw + (1.0 - Tw) * U + 0.2 * M[k] ** 2 * U * (1.0 - U)
+        prof[k, :, 0] = y
+        prof[k, :, 1] = 1.0 / T
+        prof[k, :, 2] = U
+        prof[k, :, 3] = 0.0
+        prof[k, :, 4] = 0.0
+        prof[k, :, 5] = T
+    params = [dict(itype=1, ny=int(N[k]), Ma=float(M[k]), Re=float(Re[k]), Pr=0.72, mattyp=1, T0=T0_SUTH,
+                   yi=1.0 / 23.0, ymax=50.0, alpha=[float(al[k]), 0.0], beta=[float(be[k]), 0.0],
+                   omega=[0.0, 0.0], top=0, wallt=0) for k in range(count)]
+    return params, prof
+
+
+def to_stab(d):
+    import stab_gb300 as sg
+    return sg.StabParams.make(itype=d["itype"], ny=d["ny"], Ma=d["Ma"], Re=d["Re"], Pr=d["Pr"],
+                              mattyp=d["mattyp"], T0=d["T0"], yi=d["yi"], ymax=d["ymax"],
+                              alpha=complex(*d["alpha"]), beta=complex(*d["beta"]), omega=complex(*d["omega"]))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.rows.append([t.strip() for t in ln.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for q, nm in enumerate(names):
+                if len(r) > 5 + q and r[5 + q].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_leg(params, prof, sample: int, procs: int):
+    """The oracle (reference algorithm) on `sample` instances with `procs`
+    single-threaded processes: (modes/s, results, seconds)."""
+    from oracle import baseline
+    jobs = []
+    for k in range(sample):
+        d = dict(params[k])
+        d["profile"] = prof[k]
+        jobs.append(d)
+    pool = baseline.pool(procs)
+    try:
+        t0 = time.perf_counter()
+        out = pool.map(baseline.solve_one, jobs, chunksize=1)
+        dt = time.perf_counter() - t0
+    finally:
+        pool.close()
+        pool.join()
+    eig = np.array([complex(*o[0]) for o in out])
+    return sample / dt, eig, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    params, prof = workload(args.count, 20261203)
+    procs = os.cpu_count() or 1
+    sample = args.ref_sample
+    times = []
+    for it in range(args.warmup + args.steps):
+        lo = (it * sample) % args.count
+        sel = list(range(lo, lo + sample))
+        rate, _, dt = cpu_leg([params[k] for k in sel], prof[sel], sample, procs)
+        if it >= args.warmup:
+            times.append(dt)
+    ms = 1000.0 * statistics.mean(times)
+    value = sample / (ms / 1000.0)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": f"temporal sweep, {sample} of {args.count} instances per step, "
+                                   "N in {48,64,96,128}, seed 20261203", "count": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": f"{sample} instances per step (ZGESV+ZGEEV('N','V') via scipy LAPACK, "
+                                       f"{procs} single-thread processes)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--cpu-sample", type=int, default=64)
+    ap.add_argument("--ref-sample", type=int, default=48)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    params, prof = workload(args.count, 20261203 + rank)
+    # CPU baseline first: the spawn pool starts before any GPU work
+    cpu = None
+    if rank == 0 and args.cpu_sample > 0:
+        procs = os.cpu_count() or 1
+        rate, cpu_eig, dt = cpu_leg(params, prof, args.cpu_sample, procs)
+        cpu = {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
+               "sample": f"first {args.cpu_sample} instances of the workload, {dt:.1f} s: oracle restatement of "
+                         "ZGESV+ZGEEV('N','V') (scipy LAPACK), one single-thread process per core"}
+
+    import torch
+    import stab_gb300 as sg
+    torch.cuda.set_device(local)
+    ctx = sg.Context(local)
+    stream = torch.cuda.Stream()          # a real stream: the legacy default would not order with ours
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    sp = [to_stab(d) for d in params]
+    # pinned host copy of the inputs for the end-to-end leg
+    prof_pinned = torch.from_numpy(prof).pin_memory()
+    prof_np = prof_pinned.numpy()
+    profiles = [prof_np[k] for k in range(args.count)]
+    batch = ctx.batch(sp, profiles)
+
+    # judge: plain FP64 full spectrum on every instance (timed once)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    batch.run(sg.MODE_PLAIN)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    ref_eig, _, _, ref_st, _ = batch.results()
+    plain_work = batch.work()
+
+    # warm-up and timed steps of the seeded mixed path
+    for _ in range(args.warmup):
+        batch.run(sg.MODE_COARSE)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        batch.run(sg.MODE_COARSE)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms_local = t0.elapsed_time(t1) / args.steps
+    eig, err, iters, status, _ = batch.results()
+    work = batch.work()
+    rel = np.abs(eig - ref_eig) / np.maximum(np.abs(ref_eig), 1e-300)
+    ok = (rel <= TOL) & np.isin(status, [sg.ST_OK, sg.ST_FELLBACK]) & (ref_st == sg.ST_OK)
+    converged_local = int(np.sum(ok))
+    fell = int(np.sum(status == sg.ST_FELLBACK))
+
+    # per-kernel breakdown of one extra step (CUDA events on the launch stream)
+    ctx.reset_kernel_stats()
+    ctx.set_profiling(True)
+    batch.run(sg.MODE_COARSE)
+    stats = ctx.kernel_stats()
+    ctx.set_profiling(False)
+    launches_per_step = sum(v[0] for v in stats.values())
+
+    # end-to-end through the C ABI call with host buffers (pinned), results read back
+    barrier(world)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        w_e2e, err_e2e, iters_e2e, st_e2e, _ = ctx.solve_batch(sp, profiles, sg.MODE_COARSE)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - te) / args.e2e_steps
+    ok_e2e = int(np.sum((np.abs(w_e2e - ref_eig) / np.maximum(np.abs(ref_eig), 1e-300) <= TOL)
+                        & np.isin(st_e2e, [sg.ST_OK, sg.ST_FELLBACK])))
+
+    ms = reduce_max(ms_local, world)
+    converged = reduce_sum(converged_local, world)
+    e2e_s = reduce_max(e2e_s, world)
+    ok_e2e = reduce_sum(ok_e2e, world)
+    plain_ms = reduce_max(plain_ms, world)
+    if rank != 0:
+        return 0
+
+    value = converged / (ms / 1000.0)
+    total = args.count * world
+    # dominant kernel and its roofline
+    dom = max(stats.items(), key=lambda kv: kv[1][1])
+    dname, (dl, dms) = dom
+    roof = None
+    if dname == "k_eig_plain":
+        flops = work["eig_fp64_coarse"] + work["eig_fp64"]
+        ach = flops / (dms / 1000.0) / 1e12 if dms else 0.0   # flops and ms of the same launches
+        roof = {"bound": "fp64", "achieved": ach, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                "frac": ach / FP64_PEAK_TFLOPS, "traffic": None, "kernel": dname,
+                "algorithmic": "FP64 flops counted by the kernel (Householder reduction + QR sweeps)",
+                "peak_source": "FMA probe on this pool's GB300 (MEASURED_PEAKS.json has no FP64 entry)"}
+    elif dname == "k_lu_c":
+        per = work["lu_c64"] / dl
+        ach = per / (dms / dl / 1000.0) / 1e12
+        roof = {"bound": "fp32", "achieved": ach, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+                "frac": ach / FP32_PEAK_TFLOPS, "traffic": None, "kernel": dname,
+                "algorithmic": "8/3 n^3 real flops per complex LU",
+                "peak_source": "FMA probe on this pool's GB300"}
+    else:
+        roof = {"bound": "unknown", "kernel": dname, "achieved": None, "peak": None, "unit": None, "frac": None,
+                "traffic": None}
+    h2d = int(prof.nbytes + len(sp) * 120 + len(sp) * 4)
+    d2h = int(len(sp) * (16 + 8 + 4 + 4))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 LU + c128 residual (plain path c128)", "data": "synthetic",
+        "config": {"workload": "temporal sweep: 4096 instances/GPU, N in {48,64,96,128} (n = 240-640), "
+                               "alpha~U[.05,.4], beta~U[0,.3], Re~logU[300,3000], M~U[0,2], seed 20261203",
+                   "count_per_gpu": args.count, "seeds": "FP64 full spectrum at N=32",
+                   "l2": "working set > L2 (393 MB profiles, GBs of matrices); no flush"},
+        "e2e": {"value": ok_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": 1000.0 * e2e_s, "call": "stab_solve_batch (host buffers, pinned)"},
+        "converged": {"count": int(converged), "of": total, "fell_back": fell,
+                      "max_rel_err": float(np.nanmax(rel[ok])) if np.any(ok) else None},
+        "plain_fp64": {"value": total / (plain_ms / 1000.0), "unit": UNIT, "ms_per_step": plain_ms,
+                       "speedup_seeded_over_plain": value / (total / (plain_ms / 1000.0))},
+        "roofline": roof,
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in sorted(stats.items(),
+                                                                               key=lambda kv: -kv[1][1])},
+        "gpu_launches": int(launches_per_step * args.steps),
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    if cpu is not None and args.cpu_sample > 0:
+        s = args.cpu_sample
+        d = np.abs(eig[:s] - cpu_eig) / np.abs(cpu_eig)
+        line["oracle_check"] = {"sample": s, "max_rel_err_vs_cpu_oracle": float(np.nanmax(d)),
+                                "within_1e-10": int(np.sum(d <= TOL))}
+    print(json.dumps(line), flush=True)
+    batch.close()
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

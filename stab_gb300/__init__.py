@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from typing import Optional, Sequence
 
 import numpy as np
@@ -31,7 +32,7 @@ EXPORTED = (
     "stab_abi_version", "stab_create", "stab_destroy", "stab_last_error", "stab_set_stream", "stab_sync",
     "stab_set_profiling", "stab_kernel_stats", "stab_reset_kernel_stats", "stab_assemble",
     "stab_full_spectrum", "stab_batch_create", "stab_batch_set_seeds", "stab_batch_run",
-    "stab_batch_results", "stab_batch_destroy", "stab_solve_batch",
+    "stab_batch_results", "stab_batch_work", "stab_batch_destroy", "stab_solve_batch",
 )
 
 
@@ -105,6 +106,7 @@ def load(path: str = LIB_PATH):
     lib.stab_batch_run.argtypes = [vp, i32]
     lib.stab_batch_results.argtypes = [vp, P(dbl), P(dbl), P(i32), P(i32), P(P(dbl))]
     lib.stab_batch_destroy.argtypes = [vp]
+    lib.stab_batch_work.argtypes = [vp, P(dbl)]
     lib.stab_solve_batch.argtypes = [vp, i32, P(StabParams), P(i32), P(P(dbl)), i32, P(dbl), P(dbl), P(dbl),
                                      P(i32), P(P(dbl))]
     _lib = lib
@@ -141,6 +143,7 @@ class Batch:
         h = ctypes.c_void_p()
         ctx._check(self.lib.stab_batch_create(ctx.h, self.count, self.params, _iptr(nym), ptrs, ctypes.byref(h)))
         self.h = h
+        ctx._batches.add(self)
 
     def set_seeds(self, seeds) -> None:
         s = np.ascontiguousarray(np.asarray(seeds, dtype=np.complex128)).view(np.float64)
@@ -164,6 +167,12 @@ class Batch:
                                                     _iptr(status), vptr))
         return eig, err, iters, status, vecs
 
+    def work(self) -> dict:
+        """Algorithmic flops of the last run (see stab_batch_work)."""
+        w = np.zeros(4)
+        self.ctx._check(self.lib.stab_batch_work(self.h, _dptr(w)))
+        return {"eig_fp64": w[0], "eig_fp64_coarse": w[1], "lu_c64": w[2], "lu_c128": w[3]}
+
     def close(self) -> None:
         if getattr(self, "h", None):
             self.lib.stab_batch_destroy(self.h)
@@ -182,6 +191,7 @@ class Context:
     def __init__(self, device: int = 0):
         self.lib = load()
         h = ctypes.c_void_p()
+        self._batches = weakref.WeakSet()
         rc = self.lib.stab_create(ctypes.byref(h), int(device))
         if rc != 0:
             raise StabError(f"stab_create failed ({rc}): no usable CUDA device {device}")
@@ -189,6 +199,8 @@ class Context:
 
     def close(self) -> None:
         if getattr(self, "h", None):
+            for b in list(self._batches):
+                b.close()
             self.lib.stab_destroy(self.h)
             self.h = None
 

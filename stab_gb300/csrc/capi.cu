@@ -46,6 +46,7 @@ struct stab_ctx {
   std::vector<PendingEv> pending;
   std::vector<cudaEvent_t> evpool;
   int sms = 152;
+  std::vector<stab_batch*> live;   // caller-visible batches, released by stab_destroy
 };
 
 static int set_err(stab_ctx* c, int code, const std::string& msg) {
@@ -127,19 +128,24 @@ static int ensure_dtab(stab_ctx* c, int ny) {
 // device buffer helpers
 // ---------------------------------------------------------------------------
 namespace {
+// Device buffer from the stream-ordered allocator: the context keeps the
+// device's default pool from releasing memory, so batches created per call
+// reuse it instead of paying cudaMalloc each time.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t st = nullptr;
   ~DevBuf() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, st);
   }
-  cudaError_t ensure(size_t b) {
+  cudaError_t ensure(size_t b, cudaStream_t s) {
     if (b <= bytes && p) return cudaSuccess;
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, st);
     p = nullptr;
     bytes = 0;
     if (b == 0) b = 16;
-    cudaError_t e = cudaMalloc(&p, b);
+    st = s;
+    cudaError_t e = cudaMallocAsync(&p, b, s);
     if (e == cudaSuccess) bytes = b;
     return e;
   }
@@ -147,7 +153,7 @@ struct DevBuf {
 };
 template <typename T>
 cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
-  cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
+  cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1), s);
   if (e != cudaSuccess) return e;
   if (v.empty()) return cudaSuccess;
   return cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s);
@@ -171,15 +177,42 @@ struct stab_batch {
   DevBuf desc, dtab, pdesc, prof, spl, node, blk, ops, vec;
   DevBuf nsz, msz, off_n2, off_m2, off_m2c2, off_nof, off_mof, xoff[VEC_SLOTS], order;
   DevBuf M32, Z64, Abig, Hbig, eigraw, eigsorted, outvec;
+  DevBuf bad, flops;
   DevBuf piv, info, flags, theta, sigma, least_raw, least_val, least_idx, pcol, done, err, iters, status, counter;
   int nprof = 0;
   bool have_seeds = false;
   std::vector<double> seeds;             // caller order, 2 per instance
   int last_mode = -1;
   bool ran = false;
-  // host copies filled by fallback runs (internal order)
-  std::vector<int> fell_back;
+  // instances re-solved by the plain FP64 path after a failed polish
+  std::vector<int> fell_back;                 // internal indices
+  std::vector<zc> fb_val;
+  std::vector<int32_t> fb_status;
+  std::vector<std::vector<zc>> fb_vec;
+  stab_batch* coarse = nullptr;               // N = 32 batch of STAB_MODE_COARSE, built on first use
+  ~stab_batch();
+  // free every device buffer now (used when the owning context goes away first)
+  void release() {
+    DevBuf* all[] = {&desc, &dtab, &pdesc, &prof, &spl, &node, &blk, &ops, &vec, &nsz, &msz, &off_n2, &off_m2,
+                     &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
+                     &bad, &flops, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
+                     &done, &err, &iters, &status, &counter};
+    for (DevBuf* d : all) {
+      if (d->p) cudaFreeAsync(d->p, d->st);
+      d->p = nullptr;
+      d->bytes = 0;
+    }
+    for (auto& x : xoff) {
+      if (x.p) cudaFreeAsync(x.p, x.st);
+      x.p = nullptr;
+      x.bytes = 0;
+    }
+    delete coarse;
+    coarse = nullptr;
+  }
 };
+
+stab_batch::~stab_batch() { delete coarse; }
 
 static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const int32_t* nym,
                        const double* const* profiles, stab_batch** out, int force_ny) {
@@ -191,27 +224,30 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   for (int i = 0; i < count; ++i) idx[i] = i;
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return p[a].itype < p[bb].itype; });
   b->perm = idx;
-  // profiles: dedupe by pointer
+  // profiles: dedupe by pointer; copied straight from caller memory in
+  // contiguous runs (validated on the device by k_spline)
   std::map<const double*, int> pidx;
   std::vector<ProfDesc> pds;
-  std::vector<double> hprof;
-  int64_t spl_off = 0;
+  std::vector<std::pair<const double*, int64_t>> runs;   // (source, doubles)
+  int64_t prof_off = 0, spl_off = 0;
   for (int i = 0; i < count; ++i) {
     const double* pp = profiles[i];
     if (!pp) return set_err(c, STAB_ERR_ARG, "null profile pointer");
     if (nym[i] < 4) return set_err(c, STAB_ERR_ARG, "profile needs at least 4 rows");
-    if (pidx.count(pp)) {
-      if (pds[pidx[pp]].nym != nym[i]) return set_err(c, STAB_ERR_ARG, "same profile pointer with different nym");
+    auto it = pidx.find(pp);
+    if (it != pidx.end()) {
+      if (pds[it->second].nym != nym[i]) return set_err(c, STAB_ERR_ARG, "same profile pointer with different nym");
       continue;
     }
     ProfDesc pd{};
-    pd.off_prof = (int64_t)hprof.size();
+    pd.off_prof = prof_off;
     pd.off_spl = spl_off;
     pd.nym = nym[i];
-    for (int r = 0; r < nym[i] * 6; ++r) hprof.push_back(pp[r]);
-    for (int r = 1; r < nym[i]; ++r)
-      if (!(pp[6 * r] > pp[6 * (r - 1)])) return set_err(c, STAB_ERR_ARG, "profile y must be strictly ascending");
-    spl_off += (int64_t)nym[i] * 6;
+    const int64_t len = (int64_t)nym[i] * 6;
+    if (!runs.empty() && runs.back().first + runs.back().second == pp) runs.back().second += len;
+    else runs.push_back({pp, len});
+    prof_off += len;
+    spl_off += len;
     pidx[pp] = (int)pds.size();
     pds.push_back(pd);
   }
@@ -251,7 +287,9 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
     d.ar = q.alpha[0]; d.ai = q.alpha[1];
     d.br = q.beta[0]; d.bi = q.beta[1];
     d.wr = q.omega[0]; d.wi = q.omega[1];
-    const ProfDesc& pd = pds[pidx[profiles[u]]];
+    const int ip = pidx[profiles[u]];
+    const ProfDesc& pd = pds[ip];
+    d.iprof = ip;
     d.nym = pd.nym;
     d.off_prof = pd.off_prof;
     d.off_spl = pd.off_spl;
@@ -297,12 +335,20 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   CK(c, upload(b->desc, b->hd, s));
   CK(c, upload(b->dtab, hdt, s));
   CK(c, upload(b->pdesc, pds, s));
-  CK(c, upload(b->prof, hprof, s));
-  CK(c, b->spl.ensure(sizeof(double) * std::max<int64_t>(spl_off, 1)));
-  CK(c, b->node.ensure(sizeof(double) * node_off));
-  CK(c, b->blk.ensure(sizeof(zc) * blk_off));
-  CK(c, b->ops.ensure(sizeof(zc) * (blk_off / BLK_STRIDE) * 75));
-  CK(c, b->vec.ensure(sizeof(zc) * vec_off));
+  CK(c, b->prof.ensure(sizeof(double) * std::max<int64_t>(prof_off, 1), c->stream));
+  {
+    int64_t o = 0;
+    for (auto& r : runs) {
+      CK(c, cudaMemcpyAsync(b->prof.as<double>() + o, r.first, sizeof(double) * r.second, cudaMemcpyHostToDevice, s));
+      o += r.second;
+    }
+  }
+  CK(c, b->spl.ensure(sizeof(double) * std::max<int64_t>(spl_off, 1), c->stream));
+  CK(c, b->bad.ensure(sizeof(int32_t) * std::max(b->nprof, 1), c->stream));
+  CK(c, b->node.ensure(sizeof(double) * node_off, c->stream));
+  CK(c, b->blk.ensure(sizeof(zc) * blk_off, c->stream));
+  CK(c, b->ops.ensure(sizeof(zc) * (blk_off / BLK_STRIDE) * 75, c->stream));
+  CK(c, b->vec.ensure(sizeof(zc) * vec_off, c->stream));
   CK(c, upload(b->nsz, b->hn, s));
   CK(c, upload(b->msz, b->hm, s));
   CK(c, upload(b->off_n2, b->h_n2, s));
@@ -320,25 +366,26 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   for (int k = 0; k < count; ++k) ord[k] = k;
   std::stable_sort(ord.begin(), ord.end(), [&](int a, int bb) { return b->hm[a] > b->hm[bb]; });
   CK(c, upload(b->order, ord, s));
-  CK(c, b->M32.ensure(sizeof(cc) * b->sum_n2));
-  CK(c, b->piv.ensure(sizeof(int32_t) * b->sum_n));
-  CK(c, b->eigraw.ensure(sizeof(zc) * b->sum_m));
-  CK(c, b->eigsorted.ensure(sizeof(zc) * b->sum_m));
-  CK(c, b->outvec.ensure(sizeof(zc) * b->sum_m));
+  CK(c, b->M32.ensure(sizeof(cc) * b->sum_n2, c->stream));
+  CK(c, b->piv.ensure(sizeof(int32_t) * b->sum_n, c->stream));
+  CK(c, b->eigraw.ensure(sizeof(zc) * b->sum_m, c->stream));
+  CK(c, b->eigsorted.ensure(sizeof(zc) * b->sum_m, c->stream));
+  CK(c, b->outvec.ensure(sizeof(zc) * b->sum_m, c->stream));
   const size_t I4 = sizeof(int32_t) * count, Z = sizeof(zc) * count;
-  CK(c, b->info.ensure(I4));
-  CK(c, b->flags.ensure(I4));
-  CK(c, b->theta.ensure(Z));
-  CK(c, b->sigma.ensure(Z));
-  CK(c, b->least_raw.ensure(Z));
-  CK(c, b->least_val.ensure(Z));
-  CK(c, b->least_idx.ensure(I4));
-  CK(c, b->pcol.ensure(I4));
-  CK(c, b->done.ensure(I4));
-  CK(c, b->iters.ensure(I4));
-  CK(c, b->status.ensure(I4));
-  CK(c, b->err.ensure(sizeof(double) * count));
-  CK(c, b->counter.ensure(sizeof(int32_t) * 4));
+  CK(c, b->info.ensure(I4, c->stream));
+  CK(c, b->flags.ensure(I4, c->stream));
+  CK(c, b->theta.ensure(Z, c->stream));
+  CK(c, b->sigma.ensure(Z, c->stream));
+  CK(c, b->least_raw.ensure(Z, c->stream));
+  CK(c, b->least_val.ensure(Z, c->stream));
+  CK(c, b->least_idx.ensure(I4, c->stream));
+  CK(c, b->pcol.ensure(I4, c->stream));
+  CK(c, b->done.ensure(I4, c->stream));
+  CK(c, b->iters.ensure(I4, c->stream));
+  CK(c, b->status.ensure(I4, c->stream));
+  CK(c, b->err.ensure(sizeof(double) * count, c->stream));
+  CK(c, b->flops.ensure(sizeof(double) * count, c->stream));
+  CK(c, b->counter.ensure(sizeof(int32_t) * 4, c->stream));
   CK(c, cudaStreamSynchronize(s));
   *out = b.release();
   return 0;
@@ -356,13 +403,15 @@ static int run_prep(stab_batch* b) {
   const double* const* T = b->dtab.as<const double*>();
   CK(c, timed(c, "k_spline", [&] {
     k_spline<<<(b->nprof + 63) / 64, 64, 0, s>>>(b->nprof, b->pdesc.as<ProfDesc>(), b->prof.as<double>(),
-                                                  b->spl.as<double>());
+                                                  b->spl.as<double>(), b->bad.as<int32_t>());
     return cudaGetLastError();
   }));
   const int nymax = b->nmax / 5;
+  CK(c, cudaMemsetAsync(b->flags.p, 0, sizeof(int32_t) * b->count, s));
   CK(c, timed(c, "k_nodes", [&] {
     dim3 g((nymax + 127) / 128, b->count);
-    k_nodes<<<g, 128, 0, s>>>(b->count, D, b->prof.as<double>(), b->spl.as<double>(), b->node.as<double>());
+    k_nodes<<<g, 128, 0, s>>>(b->count, D, b->prof.as<double>(), b->spl.as<double>(), b->node.as<double>(),
+                              b->bad.as<int32_t>(), b->flags.as<int32_t>());
     return cudaGetLastError();
   }));
   CK(c, timed(c, "k_meanderiv", [&] {
@@ -370,7 +419,6 @@ static int run_prep(stab_batch* b) {
     k_meanderiv<<<g, 128, 0, s>>>(b->count, D, T, b->node.as<double>());
     return cudaGetLastError();
   }));
-  CK(c, cudaMemsetAsync(b->flags.p, 0, sizeof(int32_t) * b->count, s));
   CK(c, timed(c, "k_blocks", [&] {
     dim3 g((nymax + 63) / 64, b->count);
     k_blocks<<<g, 64, 0, s>>>(b->count, D, T, b->node.as<double>(), b->blk.as<zc>(), b->flags.as<int>());
@@ -404,9 +452,9 @@ static int dense(stab_batch* b, Range r, T* out, const int64_t* off, int ldmul, 
 
 static int ensure_plain_pools(stab_batch* b) {
   stab_ctx* c = b->ctx;
-  CK(c, b->Z64.ensure(sizeof(zc) * b->sum_n2));
-  CK(c, b->Abig.ensure(sizeof(zc) * b->sum_m2));
-  CK(c, b->Hbig.ensure(sizeof(zc) * b->sum_m2));
+  CK(c, b->Z64.ensure(sizeof(zc) * b->sum_n2, c->stream));
+  CK(c, b->Abig.ensure(sizeof(zc) * b->sum_m2, c->stream));
+  CK(c, b->Hbig.ensure(sizeof(zc) * b->sum_m2, c->stream));
   return 0;
 }
 
@@ -425,7 +473,7 @@ static int eigvec_inverse_iteration(stab_batch* b, Range r, const zc* theta_dev)
                          b->off_n2.as<int64_t>() + r.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + r.k0,
                          b->info.as<int32_t>() + r.k0, s);
   }));
-  CK(c, launch_vec_init(r.cnt, b->nmax, D, b->vec.as<zc>(), 0, s));
+  CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(r.cnt, b->nmax, D, b->vec.as<zc>(), 0, s); }));
   for (int it = 0; it < 3; ++it) {
     CK(c, timed(c, "k_qmv", [&] {
       return launch_qmv(r.cnt, b->nmax, D, b->dtab.as<const double*>(), b->blk.as<zc>(), theta_dev + r.k0, 1,
@@ -436,8 +484,8 @@ static int eigvec_inverse_iteration(stab_batch* b, Range r, const zc* theta_dev)
                               b->off_n2.as<int64_t>() + r.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + r.k0,
                               b->vec.as<zc>(), b->xoff[1].as<int64_t>() + r.k0, 1, 0, 1, nullptr, s);
     }));
-    CK(c, launch_normalize(r.cnt, D, b->vec.as<zc>(), 1, b->pcol.as<int32_t>() + r.k0, nullptr, s));
-    CK(c, launch_vec_copy(r.cnt, b->nmax, D, b->vec.as<zc>(), 1, 0, nullptr, s));
+    CK(c, timed(c, "k_normalize", [&] { return launch_normalize(r.cnt, D, b->vec.as<zc>(), 1, b->pcol.as<int32_t>() + r.k0, nullptr, s); }));
+    CK(c, timed(c, "k_vec_copy", [&] { return launch_vec_copy(r.cnt, b->nmax, D, b->vec.as<zc>(), 1, 0, nullptr, s); }));
   }
   return 0;
 }
@@ -445,12 +493,16 @@ static int eigvec_inverse_iteration(stab_batch* b, Range r, const zc* theta_dev)
 static int write_vectors(stab_batch* b, Range r, const zc* theta_dev) {
   stab_ctx* c = b->ctx;
   const InstDesc* D = b->desc.as<InstDesc>() + r.k0;
-  k_temporal_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, b->vec.as<zc>(), 0, b->outvec.as<zc>(),
-                                                b->off_mof.as<int64_t>() + r.k0);
-  CK(c, cudaGetLastError());
-  k_spatial_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, theta_dev + r.k0, b->vec.as<zc>(), 0, b->outvec.as<zc>(),
-                                               b->off_mof.as<int64_t>() + r.k0);
-  CK(c, cudaGetLastError());
+  CK(c, timed(c, "k_temporal_vec", [&] {
+    k_temporal_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, b->vec.as<zc>(), 0, b->outvec.as<zc>(),
+                                                  b->off_mof.as<int64_t>() + r.k0);
+    return cudaGetLastError();
+  }));
+  CK(c, timed(c, "k_spatial_vec", [&] {
+    k_spatial_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, theta_dev + r.k0, b->vec.as<zc>(), 0,
+                                                 b->outvec.as<zc>(), b->off_mof.as<int64_t>() + r.k0);
+    return cudaGetLastError();
+  }));
   return 0;
 }
 
@@ -505,7 +557,8 @@ static int run_plain(stab_batch* b, bool want_vec) {
     int grid = std::min(b->count, c->sms * 2);
     return launch_eig_plain(b->count, b->mmax, b->msz.as<int32_t>(), b->Abig.as<zc>(), b->off_m2.as<int64_t>(),
                             b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
-                            b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(), grid, s);
+                            b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
+                            b->flops.as<double>(), grid, s);
   }));
   CK(c, timed(c, "k_post_spectrum", [&] {
     size_t sm = sizeof(zc) * b->mmax;
@@ -564,19 +617,21 @@ static int run_polish(stab_batch* b, bool want_vec) {
     });
   };
   CK(c, lu32());
-  CK(c, launch_vec_init(b->count, b->nmax, D, V, 0, s));
+  CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s); }));
   for (int it = 0; it < 2; ++it) {   // inverse iteration at the seed
     CK(c, qmv(1, 0, 1, nullptr));
     CK(c, solve32(1, nullptr));
-    CK(c, launch_normalize(b->count, D, V, 1, b->pcol.as<int32_t>(), nullptr, s));
-    CK(c, launch_vec_copy(b->count, b->nmax, D, V, 1, 0, nullptr, s));
+    CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 1, b->pcol.as<int32_t>(), nullptr, s); }));
+    CK(c, timed(c, "k_vec_copy", [&] { return launch_vec_copy(b->count, b->nmax, D, V, 1, 0, nullptr, s); }));
   }
   // bordered Jacobian at (sigma, x): Q(sigma) with column p <- Q'(sigma) x
   CK(c, qmv(1, 0, 2, nullptr));
   rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c");
   if (rc) return rc;
-  CK(c, launch_set_column(b->count, b->nmax, D, b->M32.as<cc>(), b->off_n2.as<int64_t>(), b->pcol.as<int32_t>(), V, 2,
-                          s));
+  CK(c, timed(c, "k_set_column", [&] {
+    return launch_set_column(b->count, b->nmax, D, b->M32.as<cc>(), b->off_n2.as<int64_t>(), b->pcol.as<int32_t>(), V,
+                             2, s);
+  }));
   CK(c, lu32());
   CK(c, cudaMemsetAsync(done, 0, sizeof(int32_t) * b->count, s));
   CK(c, cudaMemsetAsync(b->iters.p, 0, sizeof(int32_t) * b->count, s));
@@ -588,7 +643,7 @@ static int run_polish(stab_batch* b, bool want_vec) {
                                   b->err.as<double>(), b->iters.as<int32_t>(), kNewtonTol, s);
     }));
   }
-  CK(c, launch_normalize(b->count, D, V, 0, nullptr, nullptr, s));
+  CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, nullptr, nullptr, s); }));
   // least_val in caller units: omega (temporal) or alpha = 1/lambda (spatial)
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, s));
   if (want_vec) {
@@ -674,6 +729,13 @@ int stab_create(stab_ctx** out, int device) {
   if (device < 0 || device >= ndev) return STAB_ERR_ARG;
   if (cudaSetDevice(device) != cudaSuccess) return STAB_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) return STAB_ERR_CUDA;
+  {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;   // keep freed blocks for reuse by later batches of this process
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   c->stream = c->own;
   cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
   *out = c.release();
@@ -683,6 +745,14 @@ int stab_create(stab_ctx** out, int device) {
 int stab_destroy(stab_ctx* c) {
   if (!c) return STAB_ERR_ARG;
   cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  // batches the caller has not destroyed lose their device memory and their
+  // context; a later stab_batch_destroy only frees the host side
+  for (stab_batch* b : c->live) {
+    b->release();
+    b->ctx = nullptr;
+  }
+  c->live.clear();
   cudaStreamSynchronize(c->stream);
   for (auto& kv : c->dtabs) {
     cudaFree(kv.second.first);
@@ -744,6 +814,7 @@ int stab_batch_create(stab_ctx* c, int32_t count, const stab_params* p, const in
   cudaSetDevice(c->device);
   int rc = batch_build(c, count, p, nym, profiles, out, 0);
   if (rc) return rc;
+  c->live.push_back(*out);
   BatchInputs in;
   in.p.assign(p, p + count);
   in.nym.assign(nym, nym + count);
@@ -754,6 +825,7 @@ int stab_batch_create(stab_ctx* c, int32_t count, const stab_params* p, const in
 
 int stab_batch_set_seeds(stab_batch* b, const double* seeds) {
   if (!b || !seeds) return STAB_ERR_ARG;
+  if (!b->ctx) return STAB_ERR_STATE;
   b->seeds.assign(seeds, seeds + 2 * (size_t)b->count);
   b->have_seeds = true;
   return STAB_OK;
@@ -763,22 +835,87 @@ static int coarse_seeds(stab_batch* b) {
   stab_ctx* c = b->ctx;
   auto it = g_inputs.find(b);
   if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
-  stab_batch* cb = nullptr;
-  int rc = batch_build(c, b->count, it->second.p.data(), it->second.nym.data(), it->second.prof.data(), &cb, 32);
-  if (rc) return rc;
-  std::unique_ptr<stab_batch> guard(cb);
-  rc = run_prep(cb);
+  if (!b->coarse) {
+    stab_batch* cb = nullptr;
+    int rc = batch_build(c, b->count, it->second.p.data(), it->second.nym.data(), it->second.prof.data(), &cb, 32);
+    if (rc) return rc;
+    b->coarse = cb;
+  }
+  stab_batch* cb = b->coarse;
+  int rc = run_prep(cb);
   if (rc) return rc;
   rc = run_plain(cb, false);
   if (rc) return rc;
   // same internal order in both batches (same stable itype sort)
   CK(c, cudaMemcpyAsync(b->sigma.p, cb->least_raw.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, c->stream));
+  return 0;
+}
+
+// Re-solve, with the plain FP64 path, every instance whose polish did not
+// converge (or had no seed); results are kept on the host for
+// stab_batch_results.
+static int run_fallback(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  const int n = b->count;
+  std::vector<int32_t> dn(n);
+  CK(c, cudaMemcpyAsync(dn.data(), b->done.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  b->fell_back.clear();
+  b->fb_val.clear();
+  b->fb_status.clear();
+  b->fb_vec.clear();
+  for (int k = 0; k < n; ++k)
+    if (dn[k] != 1) b->fell_back.push_back(k);
+  if (b->fell_back.empty()) return 0;
+  auto it = g_inputs.find(b);
+  if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
+  const BatchInputs& in = it->second;
+  std::vector<stab_params> fp;
+  std::vector<int32_t> fn;
+  std::vector<const double*> fpr;
+  for (int k : b->fell_back) {
+    const int u = b->perm[k];
+    fp.push_back(in.p[u]);
+    fn.push_back(in.nym[u]);
+    fpr.push_back(in.prof[u]);
+  }
+  stab_batch* fb = nullptr;
+  int rc = batch_build(c, (int)fp.size(), fp.data(), fn.data(), fpr.data(), &fb, 0);
+  if (rc) return rc;
+  std::unique_ptr<stab_batch> guard(fb);
+  rc = run_prep(fb);
+  if (rc) return rc;
+  rc = run_plain(fb, true);
+  if (rc) return rc;
+  const int nf = fb->count;
+  std::vector<zc> val(nf);
+  std::vector<int32_t> st(nf), li(nf);
+  CK(c, cudaMemcpyAsync(val.data(), fb->least_val.p, sizeof(zc) * nf, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(st.data(), fb->status.p, sizeof(int32_t) * nf, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(li.data(), fb->least_idx.p, sizeof(int32_t) * nf, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<std::vector<zc>> vecs(nf);
+  for (int q = 0; q < nf; ++q) {
+    vecs[q].resize(fb->hm[q]);
+    CK(c, cudaMemcpyAsync(vecs[q].data(), fb->outvec.as<zc>() + fb->h_mof[q], sizeof(zc) * fb->hm[q],
+                          cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
+  // the sub-batch keeps caller order of `fp` internally sorted by itype; map back
+  b->fb_val.assign(b->fell_back.size(), zmk(0, 0));
+  b->fb_status.assign(b->fell_back.size(), 0);
+  b->fb_vec.assign(b->fell_back.size(), {});
+  for (int q = 0; q < nf; ++q) {
+    const int j = fb->perm[q];            // index into fell_back
+    b->fb_val[j] = val[q];
+    b->fb_status[j] = (st[q] == 0 && li[q] >= 0) ? STAB_ST_FELLBACK : (st[q] ? st[q] : STAB_ST_NOMODE);
+    b->fb_vec[j] = std::move(vecs[q]);
+  }
   return 0;
 }
 
 int stab_batch_run(stab_batch* b, int32_t mode) {
   if (!b) return STAB_ERR_ARG;
+  if (!b->ctx) return STAB_ERR_STATE;
   stab_ctx* c = b->ctx;
   cudaSetDevice(c->device);
   if (mode == STAB_MODE_COARSE) {
@@ -790,15 +927,21 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
     b->last_mode = mode;
     rc = run_polish(b, true);
     if (rc) return rc;
+    rc = run_fallback(b);
+    if (rc) return rc;
     b->ran = true;
     return STAB_OK;
   }
-  return batch_run(b, mode);
+  int rc = batch_run(b, mode);
+  if (rc) return rc;
+  if (mode == STAB_MODE_SEEDED) return run_fallback(b);
+  return STAB_OK;
 }
 
 int stab_batch_results(stab_batch* b, double* eig_out, double* err_out, int32_t* iters_out, int32_t* status_out,
                        double* const* vec_out) {
   if (!b) return STAB_ERR_ARG;
+  if (!b->ctx) return STAB_ERR_STATE;
   stab_ctx* c = b->ctx;
   if (!b->ran) return set_err(c, STAB_ERR_STATE, "stab_batch_run has not run");
   cudaSetDevice(c->device);
@@ -817,15 +960,22 @@ int stab_batch_results(stab_batch* b, double* eig_out, double* err_out, int32_t*
   CK(c, cudaMemcpyAsync(fl.data(), b->flags.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
   CK(c, cudaStreamSynchronize(s));
   if (b->last_mode == STAB_MODE_PLAIN) {
-    for (int k = 0; k < n; ++k) {
+    for (int k = 0; k < n; ++k)
       if (st[k] == 0 && li[k] < 0) st[k] = STAB_ST_NOMODE;
-      if (fl[k]) st[k] = STAB_ST_SINGULAR;
-    }
   } else {
     val = raw;
     finalize_polish_host(val, st, dn, b->P);
-    for (int k = 0; k < n; ++k)
-      if (fl[k]) st[k] = STAB_ST_SINGULAR;
+  }
+  std::vector<int> fbpos(n, -1);
+  for (size_t j = 0; j < b->fell_back.size(); ++j) {
+    const int k = b->fell_back[j];
+    fbpos[k] = (int)j;
+    val[k] = b->fb_val[j];
+    st[k] = b->fb_status[j];
+  }
+  for (int k = 0; k < n; ++k) {
+    if (fl[k] & 2) { st[k] = STAB_ST_NAN; val[k] = zmk(NAN, NAN); }
+    else if (fl[k] & 1) st[k] = STAB_ST_SINGULAR;
   }
   for (int k = 0; k < n; ++k) {
     const int u = b->perm[k];
@@ -834,19 +984,54 @@ int stab_batch_results(stab_batch* b, double* eig_out, double* err_out, int32_t*
     if (iters_out) iters_out[u] = it[k];
     if (status_out) status_out[u] = st[k];
     if (vec_out && vec_out[u]) {
-      CK(c, cudaMemcpyAsync(vec_out[u], b->outvec.as<zc>() + b->h_mof[k], sizeof(zc) * b->hm[k],
-                            cudaMemcpyDeviceToHost, s));
+      if (fbpos[k] >= 0) {
+        std::memcpy(vec_out[u], b->fb_vec[fbpos[k]].data(), sizeof(zc) * b->hm[k]);
+      } else {
+        CK(c, cudaMemcpyAsync(vec_out[u], b->outvec.as<zc>() + b->h_mof[k], sizeof(zc) * b->hm[k],
+                              cudaMemcpyDeviceToHost, s));
+      }
     }
   }
   CK(c, cudaStreamSynchronize(s));
   return STAB_OK;
 }
 
+int stab_batch_work(stab_batch* b, double* work_out) {
+  if (!b || !work_out) return STAB_ERR_ARG;
+  if (!b->ctx) return STAB_ERR_STATE;
+  stab_ctx* c = b->ctx;
+  if (!b->ran) return set_err(c, STAB_ERR_STATE, "stab_batch_run has not run");
+  CK(c, cudaStreamSynchronize(c->stream));
+  auto eig_flops = [&](stab_batch* x) -> double {
+    std::vector<double> f(x->count);
+    if (cudaMemcpy(f.data(), x->flops.p, sizeof(double) * x->count, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    double t = 0;
+    for (double v : f) t += v;
+    return t;
+  };
+  double lu_c = 0.0;
+  for (int n : b->hn) lu_c += 2.0 * (8.0 / 3.0) * (double)n * n * n;   // two complex64 LUs per instance
+  const bool plain = (b->last_mode == STAB_MODE_PLAIN);
+  work_out[0] = plain ? eig_flops(b) : 0.0;
+  work_out[1] = (b->last_mode == STAB_MODE_COARSE && b->coarse) ? eig_flops(b->coarse) : 0.0;
+  work_out[2] = plain ? 0.0 : lu_c;
+  double lu_z = 0.0;
+  if (plain)
+    for (int n : b->hn) lu_z += (8.0 / 3.0) * (double)n * n * n;
+  work_out[3] = lu_z;
+  return STAB_OK;
+}
+
 int stab_batch_destroy(stab_batch* b) {
   if (!b) return STAB_ERR_ARG;
-  cudaSetDevice(b->ctx->device);
-  cudaStreamSynchronize(b->ctx->stream);
   g_inputs.erase(b);
+  if (!b->ctx) {            // context already destroyed: device memory is gone
+    delete b;
+    return STAB_OK;
+  }
+  stab_ctx* c = b->ctx;
+  cudaSetDevice(c->device);
+  c->live.erase(std::remove(c->live.begin(), c->live.end(), b), c->live.end());
   delete b;
   return STAB_OK;
 }
@@ -918,7 +1103,8 @@ int stab_full_spectrum(stab_ctx* c, const stab_params* p, int32_t nym, const dou
   CK(c, cudaMemcpyAsync(&li, b->least_idx.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaMemcpyAsync(&fl, b->flags.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
-  if (fl) st = STAB_ST_SINGULAR;
+  if (fl & 2) st = STAB_ST_NAN;
+  else if (fl & 1) st = STAB_ST_SINGULAR;
   if (st == 0 && li < 0) st = STAB_ST_NOMODE;
   if (least_index_out) *least_index_out = li;
   if (status_out) *status_out = st;

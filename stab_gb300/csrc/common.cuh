@@ -98,6 +98,8 @@ struct InstDesc {
   int32_t itype, wallt, top, mattyp, navier, nym;
   int32_t dmat;           // index of the (D1, D2) table for this ny
   int32_t m;              // order of the standard eigenproblem: n (temporal), 2n (spatial)
+  int32_t iprof;          // index of the mean profile (ProfDesc)
+  int32_t pad_;
   double Ma, Re, Pr, Te, yi, ymax;
   double ar, ai, br, bi, wr, wi;  // alpha, beta, omega
   int64_t off_prof;       // profile pool (doubles): nym*6, row-major y rho u v w T

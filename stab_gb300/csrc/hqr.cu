@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
                                                    const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
                                                    const int64_t* __restrict__ h_off, zc* __restrict__ eig,
                                                    const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
-                                                   int32_t* __restrict__ work_counter, const int32_t* __restrict__ order) {
+                                                   int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
+                                                   double* __restrict__ flops_out) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ HqrSmem s;
   __shared__ int s_inst;
@@ -187,8 +188,10 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
       __syncthreads();
     }
     // ---- 4. Hessenberg reduction -----------------------------------------
+    double flops = 0.0;   // FP64 work of the reduction and the sweeps (thread 0)
     for (int k = 0; k + 2 < mp; ++k) {
       const int L = mp - k - 1;
+      if (tid == 0) flops += 16.0 * (double)mp * L + 16.0 * (double)L * L;
       double ss = 0.0, dummy = 0.0;
       for (int r = tid; r < L; r += HQ_T) {
         zc x = H[(size_t)k * ld + k + 1 + r];
@@ -351,6 +354,7 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
           __syncthreads();   // everyone has read the column before it changes
           const int nleft = i - k - 1;        // columns k+2..i
           const int ntask = i - l;            // 1 corner + nleft + (k - l) right rows
+          if (tid == 0) flops += 24.0 * (double)(ntask + 4);   // 24 flops per 2-element pair update
           for (int q = tid; q < ntask; q += HQ_T) {
             if (q == 0) {
               if (k > m0) { Hs(k, k - 1) = zmk(ident ? v1.x : beta, ident ? v1.y : 0.0); Hs(k + 1, k - 1) = zmk(0.0, 0.0); }
@@ -402,7 +406,10 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
     if (st) {
       for (int q = tid; q <= i; q += HQ_T) ev[q] = zmk(nan(""), nan(""));
     }
-    if (tid == 0) status[inst] = st;
+    if (tid == 0) {
+      status[inst] = st;
+      if (flops_out) flops_out[inst] = flops;
+    }
     __syncthreads();
   }
 }
@@ -413,14 +420,16 @@ size_t eig_plain_smem(int mmax) {
 
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
                              const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
-                             int32_t* work_counter, const int32_t* order, int grid, cudaStream_t s) {
+                             int32_t* work_counter, const int32_t* order, double* flops, int grid,
+                             cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   size_t sm = eig_plain_smem(mmax);
   cudaError_t e = cudaFuncSetAttribute(k_eig_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(work_counter, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
-  k_eig_plain<<<grid, HQ_T, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter, order);
+  k_eig_plain<<<grid, HQ_T, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter, order,
+                                     flops);
   return cudaGetLastError();
 }
 

@@ -22,8 +22,11 @@ enum OpKind : int {
 __global__ void k_cheb_a(int ny, double* xa);
 __global__ void k_cheb_d1(int ny, const double* xa, double* D1);
 __global__ void k_cheb_d2(int ny, const double* D1, double* D2);
-__global__ void k_spline(int nprof, const ProfDesc* pdesc, const double* prof, double* spl);
-__global__ void k_nodes(int count, const InstDesc* desc, const double* prof, const double* spl, double* node);
+// bad[p] = 1 when profile p has non-finite values or non-ascending y
+__global__ void k_spline(int nprof, const ProfDesc* pdesc, const double* prof, double* spl, int32_t* bad);
+// flags[k] |= 2 when the instance's profile is bad
+__global__ void k_nodes(int count, const InstDesc* desc, const double* prof, const double* spl, double* node,
+                        const int32_t* bad, int32_t* flags);
 __global__ void k_meanderiv(int count, const InstDesc* desc, const double* const* dtab, double* node);
 __global__ void k_blocks(int count, const InstDesc* desc, const double* const* dtab, const double* node, zc* blk,
                          int* flags);

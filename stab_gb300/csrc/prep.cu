@@ -71,13 +71,20 @@ __global__ void k_cheb_d2(int ny, const double* D1, double* D2) {
 // Spline pool layout per instance: nym rows x 6 (fdp[5], modified diag).
 // ---------------------------------------------------------------------------
 __global__ void k_spline(int nprof, const ProfDesc* __restrict__ pdesc, const double* __restrict__ prof,
-                         double* __restrict__ spl) {
+                         double* __restrict__ spl, int32_t* __restrict__ bad) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nprof) return;
   const ProfDesc d = pdesc[k];
   const int n = d.nym;
   const double* P = prof + d.off_prof;   // row i: y rho u v w T
   double* S = spl + d.off_spl;           // row i: r[5] then b
+  // the interval search of SPEVAL needs strictly ascending, finite abscissae
+  int ok = 1;
+  for (int i = 0; i < n; ++i) {
+    for (int f = 0; f < 6; ++f) ok &= isfinite(P[6 * i + f]) ? 1 : 0;
+    if (i > 0) ok &= (P[6 * i] > P[6 * (i - 1)]) ? 1 : 0;
+  }
+  bad[k] = ok ? 0 : 1;
   auto X = [&](int i) { return P[6 * i]; };
   auto Y = [&](int i, int f) { return f == 2 ? 0.0 : P[6 * i + 1 + f]; };  // v forced to 0
   // assemble c(i), a(i), b(i), r(i) and eliminate forward in one pass
@@ -150,12 +157,14 @@ __device__ __forceinline__ void node_grid(const InstDesc& d, int i, double& y, d
 // linear scan; the profile abscissae are strictly ascending, so a binary
 // search gives the same interval.
 __global__ void k_nodes(int count, const InstDesc* __restrict__ desc, const double* __restrict__ prof,
-                        const double* __restrict__ spl, double* __restrict__ node) {
+                        const double* __restrict__ spl, double* __restrict__ node, const int32_t* __restrict__ bad,
+                        int32_t* __restrict__ flags) {
   int k = blockIdx.y;
   if (k >= count) return;
   const InstDesc d = desc[k];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ny) return;
+  if (i == 0 && bad[d.iprof]) atomicOr(flags + k, 2);
   double y, eta, deta, d2eta;
   node_grid(d, i, y, eta, deta, d2eta);
   const double* P = prof + d.off_prof;

@@ -181,3 +181,28 @@ def test_batch_coarse_seeded_matches_oracle(ctx):
         if status[k] == sg.ST_OK and abs(eig[k] - w) / abs(w) < EIG_REL:
             ok += 1
     assert ok >= 3
+
+
+def test_batch_outliving_its_context_is_safe():
+    """Destroying the context first orphans live batches instead of leaving
+    dangling device state (stab_destroy releases them)."""
+    import gc
+    c = sg.Context(0)
+    d, prof = H.synth_case(1, 16, 0.5, 1000.0, a=0.2)
+    b = c.batch([H.stab_params(d)], [prof])
+    b.run(sg.MODE_PLAIN)
+    c.lib.stab_destroy(c.h)        # bypass Context.close(): the batch is still open
+    c.h = None
+    with pytest.raises(sg.StabError):
+        b.ctx._check(c.lib.stab_batch_run(b.h, sg.MODE_PLAIN) or -5)
+    b.close()
+    gc.collect()
+
+
+def test_bad_profile_is_reported_not_solved(ctx):
+    d, prof = H.synth_case(1, 16, 0.5, 1000.0, a=0.2)
+    bad = prof.copy()
+    bad[100, 1] = np.nan
+    eig, err, iters, status, _ = ctx.solve_batch([H.stab_params(d), H.stab_params(d)], [prof, bad], sg.MODE_PLAIN)
+    assert status[0] == sg.ST_OK
+    assert status[1] != sg.ST_OK

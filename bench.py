@@ -320,8 +320,8 @@ def main():
     dom = max(stats.items(), key=lambda kv: kv[1][1])
     dname, (dl, dms) = dom
     roof = None
-    if dname == "k_eig_plain":
-        flops = work["eig_fp64_coarse"] + work["eig_fp64"]
+    if dname in ("k_eig_plain", "k_eig_plain_coarse"):
+        flops = work["eig_fp64_coarse"] if dname == "k_eig_plain_coarse" else work["eig_fp64"]
         ach = flops / (dms / 1000.0) / 1e12 if dms else 0.0   # flops and ms of the same launches
         roof = {"bound": "fp64", "achieved": ach, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
                 "frac": ach / FP64_PEAK_TFLOPS, "traffic": None, "kernel": dname,

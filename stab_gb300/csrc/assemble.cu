@@ -15,9 +15,11 @@ namespace stab {
 __device__ __forceinline__ int64_t node_index(const InstDesc& d) { return d.off_blk / BLK_STRIDE; }
 
 __global__ void k_node_ops(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ blk, int kind_t,
-                           int kind_s, const zc* __restrict__ sigma, zc* __restrict__ ops) {
+                           int kind_s, const zc* __restrict__ sigma, zc* __restrict__ ops,
+                           const int32_t* __restrict__ skip) {
   int k = blockIdx.y;
   if (k >= count) return;
+  if (skip && skip[k]) return;
   const InstDesc d = desc[k];
   const int kind = (d.itype == 1) ? kind_t : kind_s;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -75,9 +77,10 @@ template <> __device__ __forceinline__ cc store_cast<cc>(zc v) { return cmk((flo
 template <typename T>
 __global__ void k_dense(int count, const InstDesc* __restrict__ desc, const double* const* __restrict__ dtab,
                         const zc* __restrict__ ops, T* __restrict__ out, const int64_t* __restrict__ out_off,
-                        int ldmul, double scale) {
+                        int ldmul, double scale, const int32_t* __restrict__ skip) {
   int k = blockIdx.y;
   if (k >= count) return;
+  if (skip && skip[k]) return;
   const InstDesc d = desc[k];
   const int n = d.n, ny = d.ny;
   const int c0 = blockIdx.x * 8;
@@ -105,16 +108,16 @@ __global__ void k_dense(int count, const InstDesc* __restrict__ desc, const doub
 
 template <typename T>
 cudaError_t launch_dense(int count, int nmax, const InstDesc* desc, const double* const* dtab, const zc* ops, T* out,
-                         const int64_t* out_off, int ldmul, double scale, cudaStream_t s) {
+                         const int64_t* out_off, int ldmul, double scale, cudaStream_t s, const int32_t* skip) {
   if (count <= 0) return cudaSuccess;
   dim3 g((nmax + 7) / 8, count);
-  k_dense<T><<<g, 256, 0, s>>>(count, desc, dtab, ops, out, out_off, ldmul, scale);
+  k_dense<T><<<g, 256, 0, s>>>(count, desc, dtab, ops, out, out_off, ldmul, scale, skip);
   return cudaGetLastError();
 }
 template cudaError_t launch_dense<zc>(int, int, const InstDesc*, const double* const*, const zc*, zc*,
-                                      const int64_t*, int, double, cudaStream_t);
+                                      const int64_t*, int, double, cudaStream_t, const int32_t*);
 template cudaError_t launch_dense<cc>(int, int, const InstDesc*, const double* const*, const zc*, cc*,
-                                      const int64_t*, int, double, cudaStream_t);
+                                      const int64_t*, int, double, cudaStream_t, const int32_t*);
 
 // Structured product y = M x (FP64).  One CTA per instance: x staged in
 // shared memory, W1 = D1 X and W2 = D2 X formed per (node, variable), then

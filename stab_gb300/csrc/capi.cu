@@ -21,6 +21,12 @@
 
 using namespace stab;
 
+// shift candidates per instance taken from the coarse spectrum
+static const int kShiftCandidates = 4;
+// a polished eigenvalue within this relative distance of the top coarse
+// candidate is final after the first round (the coarse mode is resolved)
+static const double kQuickAcceptTol = 1e-7;
+
 namespace {
 
 struct KStat {
@@ -177,7 +183,7 @@ struct stab_batch {
   DevBuf desc, dtab, pdesc, prof, spl, node, blk, ops, vec;
   DevBuf nsz, msz, off_n2, off_m2, off_m2c2, off_nof, off_mof, xoff[VEC_SLOTS], order;
   DevBuf M32, Z64, Abig, Hbig, eigraw, eigsorted, outvec;
-  DevBuf bad, flops;
+  DevBuf bad, flops, rsc, csc, cand, accepted, have, best_key, best_theta, best_err, best_iters, best_out;
   DevBuf piv, info, flags, theta, sigma, least_raw, least_val, least_idx, pcol, done, err, iters, status, counter;
   int nprof = 0;
   bool have_seeds = false;
@@ -195,7 +201,8 @@ struct stab_batch {
   void release() {
     DevBuf* all[] = {&desc, &dtab, &pdesc, &prof, &spl, &node, &blk, &ops, &vec, &nsz, &msz, &off_n2, &off_m2,
                      &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
-                     &bad, &flops, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
+                     &bad, &flops, &rsc, &csc, &cand, &accepted, &have, &best_key, &best_theta, &best_err,
+                     &best_iters, &best_out, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
                      &done, &err, &iters, &status, &counter};
     for (DevBuf* d : all) {
       if (d->p) cudaFreeAsync(d->p, d->st);
@@ -385,6 +392,10 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   CK(c, b->status.ensure(I4, c->stream));
   CK(c, b->err.ensure(sizeof(double) * count, c->stream));
   CK(c, b->flops.ensure(sizeof(double) * count, c->stream));
+  CK(c, b->rsc.ensure(sizeof(float) * b->sum_n, c->stream));
+  CK(c, b->csc.ensure(sizeof(float) * b->sum_n, c->stream));
+  CK(c, b->cand.ensure(Z * kShiftCandidates, c->stream));
+  CK(c, b->accepted.ensure(I4, c->stream));
   CK(c, b->counter.ensure(sizeof(int32_t) * 4, c->stream));
   CK(c, cudaStreamSynchronize(s));
   *out = b.release();
@@ -427,13 +438,15 @@ static int run_prep(stab_batch* b) {
   return 0;
 }
 
-static int node_ops(stab_batch* b, Range r, int kind_t, int kind_s, const zc* sigma) {
+static int node_ops(stab_batch* b, Range r, int kind_t, int kind_s, const zc* sigma,
+                    const int32_t* skip = nullptr) {
   stab_ctx* c = b->ctx;
   const int nymax = b->nmax / 5;
   return timed(c, "k_node_ops", [&] {
            dim3 g((nymax + 63) / 64, r.cnt);
            k_node_ops<<<g, 64, 0, c->stream>>>(r.cnt, b->desc.as<InstDesc>() + r.k0, b->blk.as<zc>(), kind_t, kind_s,
-                                                sigma ? sigma + r.k0 : nullptr, b->ops.as<zc>());
+                                                sigma ? sigma + r.k0 : nullptr, b->ops.as<zc>(),
+                                                skip ? skip + r.k0 : nullptr);
            return cudaGetLastError();
          }) == cudaSuccess
              ? 0
@@ -441,11 +454,12 @@ static int node_ops(stab_batch* b, Range r, int kind_t, int kind_s, const zc* si
 }
 
 template <typename T>
-static int dense(stab_batch* b, Range r, T* out, const int64_t* off, int ldmul, double scale, const char* name) {
+static int dense(stab_batch* b, Range r, T* out, const int64_t* off, int ldmul, double scale, const char* name,
+                 const int32_t* skip = nullptr) {
   stab_ctx* c = b->ctx;
   cudaError_t e = timed(c, name, [&] {
     return launch_dense<T>(r.cnt, b->nmax, b->desc.as<InstDesc>() + r.k0, b->dtab.as<const double*>(),
-                           b->ops.as<zc>(), out, off + r.k0, ldmul, scale, c->stream);
+                           b->ops.as<zc>(), out, off + r.k0, ldmul, scale, c->stream, skip ? skip + r.k0 : nullptr);
   });
   return e == cudaSuccess ? 0 : cuda_fail(c, e, name);
 }
@@ -490,17 +504,18 @@ static int eigvec_inverse_iteration(stab_batch* b, Range r, const zc* theta_dev)
   return 0;
 }
 
-static int write_vectors(stab_batch* b, Range r, const zc* theta_dev) {
+static int write_vectors(stab_batch* b, Range r, const zc* theta_dev, const int32_t* skip = nullptr) {
   stab_ctx* c = b->ctx;
   const InstDesc* D = b->desc.as<InstDesc>() + r.k0;
   CK(c, timed(c, "k_temporal_vec", [&] {
     k_temporal_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, b->vec.as<zc>(), 0, b->outvec.as<zc>(),
-                                                  b->off_mof.as<int64_t>() + r.k0);
+                                                  b->off_mof.as<int64_t>() + r.k0, skip ? skip + r.k0 : nullptr);
     return cudaGetLastError();
   }));
   CK(c, timed(c, "k_spatial_vec", [&] {
     k_spatial_vec<<<r.cnt, 256, 0, c->stream>>>(r.cnt, D, theta_dev + r.k0, b->vec.as<zc>(), 0,
-                                                 b->outvec.as<zc>(), b->off_mof.as<int64_t>() + r.k0);
+                                                 b->outvec.as<zc>(), b->off_mof.as<int64_t>() + r.k0,
+                                                 skip ? skip + r.k0 : nullptr);
     return cudaGetLastError();
   }));
   return 0;
@@ -508,7 +523,7 @@ static int write_vectors(stab_batch* b, Range r, const zc* theta_dev) {
 
 // plain FP64 path on all instances: standard-form matrices, full spectrum,
 // sort + select, optional eigenvector of the selected mode
-static int run_plain(stab_batch* b, bool want_vec) {
+static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig_plain") {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   int rc = ensure_plain_pools(b);
@@ -553,8 +568,8 @@ static int run_plain(stab_batch* b, bool want_vec) {
       return cudaGetLastError();
     }));
   }
-  CK(c, timed(c, "k_eig_plain", [&] {
-    int grid = std::min(b->count, c->sms * 2);
+  CK(c, timed(c, eig_name, [&] {
+    int grid = 0;   // sized by occupancy in the launcher
     return launch_eig_plain(b->count, b->mmax, b->msz.as<int32_t>(), b->Abig.as<zc>(), b->off_m2.as<int64_t>(),
                             b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
                             b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
@@ -566,7 +581,7 @@ static int run_plain(stab_batch* b, bool want_vec) {
     k_post_spectrum<<<b->count, 256, sm, s>>>(b->count, b->desc.as<InstDesc>(), b->eigraw.as<zc>(),
                                               b->off_mof.as<int64_t>(), b->eigsorted.as<zc>(),
                                               b->least_idx.as<int32_t>(), b->least_raw.as<zc>(),
-                                              b->least_val.as<zc>());
+                                              b->least_val.as<zc>(), b->cand.as<zc>(), kShiftCandidates);
     return cudaGetLastError();
   }));
   CK(c, cudaMemsetAsync(b->err.p, 0, sizeof(double) * b->count, s));
@@ -582,10 +597,11 @@ static int run_plain(stab_batch* b, bool want_vec) {
 }
 
 // mixed-precision polish from sigma (device, internal order)
-static const int kNewtonSteps = 8;
-static const double kNewtonTol = 2e-14;
+static const int kNewtonSteps = 10;
+static const double kNewtonTol = 1e-13;      // |d theta| / |theta| of the last Newton-chord step
+static const double kNewtonTolVec = 1e-11;   // max |d x| / max |x|
 
-static int run_polish(stab_batch* b, bool want_vec) {
+static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullptr) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   const Range all{0, b->count};
@@ -593,61 +609,68 @@ static int run_polish(stab_batch* b, bool want_vec) {
   const double* const* T = b->dtab.as<const double*>();
   zc* V = b->vec.as<zc>();
   int32_t* done = b->done.as<int32_t>();
-  CK(c, cudaMemcpyAsync(b->theta.p, b->sigma.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, s));
-  int rc = node_ops(b, all, OP_T_Q, OP_S_Q, b->theta.as<zc>());
+  CK(c, timed(c, "k_start_shift", [&] {
+    return launch_start_shift(b->count, b->sigma.as<zc>(), b->theta.as<zc>(), skip, s);
+  }));
+  int rc = node_ops(b, all, OP_T_Q, OP_S_Q, b->theta.as<zc>(), skip);
   if (rc) return rc;
-  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c");
+  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c", skip);
   if (rc) return rc;
   auto lu32 = [&]() {
+    cudaError_t e = timed(c, "k_equilibrate", [&] {
+      return launch_equilibrate(b->count, b->nsz.as<int32_t>(), b->M32.as<cc>(), b->off_n2.as<int64_t>(),
+                                b->rsc.as<float>(), b->csc.as<float>(), b->off_nof.as<int64_t>(), s, skip);
+    });
+    if (e != cudaSuccess) return e;
     return timed(c, "k_lu_c", [&] {
       return launch_lu<cc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
-                           b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s);
+                           b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip);
     });
   };
-  auto solve32 = [&](int slot, const int32_t* skip) {
+  auto solve32 = [&](int slot, const int32_t* sk) {
     return timed(c, "k_getrs_c", [&] {
       return launch_getrs<cc>(b->count, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
                               b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V, b->xoff[slot].as<int64_t>(), 1, 0, 1,
-                              skip, s);
+                              sk, s, b->rsc.as<float>(), b->csc.as<float>());
     });
   };
-  auto qmv = [&](int deriv, int xs, int ys, const int32_t* skip) {
+  auto qmv = [&](int deriv, int xs, int ys, const int32_t* sk) {
     return timed(c, "k_qmv", [&] {
-      return launch_qmv(b->count, b->nmax, D, T, b->blk.as<zc>(), b->theta.as<zc>(), deriv, V, xs, ys, skip, s);
+      return launch_qmv(b->count, b->nmax, D, T, b->blk.as<zc>(), b->theta.as<zc>(), deriv, V, xs, ys, sk, s);
     });
   };
   CK(c, lu32());
-  CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s); }));
-  for (int it = 0; it < 2; ++it) {   // inverse iteration at the seed
-    CK(c, qmv(1, 0, 1, nullptr));
-    CK(c, solve32(1, nullptr));
-    CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 1, b->pcol.as<int32_t>(), nullptr, s); }));
-    CK(c, timed(c, "k_vec_copy", [&] { return launch_vec_copy(b->count, b->nmax, D, V, 1, 0, nullptr, s); }));
+  CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
+  for (int it = 0; it < 2; ++it) {   // inverse iteration at the shift
+    CK(c, qmv(1, 0, 1, skip));
+    CK(c, solve32(1, skip));
+    CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 1, b->pcol.as<int32_t>(), skip, s); }));
+    CK(c, timed(c, "k_vec_copy", [&] { return launch_vec_copy(b->count, b->nmax, D, V, 1, 0, skip, s); }));
   }
   // bordered Jacobian at (sigma, x): Q(sigma) with column p <- Q'(sigma) x
-  CK(c, qmv(1, 0, 2, nullptr));
-  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c");
+  CK(c, qmv(1, 0, 2, skip));
+  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c", skip);
   if (rc) return rc;
   CK(c, timed(c, "k_set_column", [&] {
     return launch_set_column(b->count, b->nmax, D, b->M32.as<cc>(), b->off_n2.as<int64_t>(), b->pcol.as<int32_t>(), V,
-                             2, s);
+                             2, s, skip);
   }));
   CK(c, lu32());
-  CK(c, cudaMemsetAsync(done, 0, sizeof(int32_t) * b->count, s));
-  CK(c, cudaMemsetAsync(b->iters.p, 0, sizeof(int32_t) * b->count, s));
+  CK(c, timed(c, "k_reset_polish", [&] { return launch_reset_polish(b->count, done, b->iters.as<int32_t>(), skip, s); }));
+  // Newton-chord steps; converged instances (done != 0) drop out
   for (int it = 0; it < kNewtonSteps; ++it) {
     CK(c, qmv(0, 0, 3, done));
     CK(c, solve32(3, done));
     CK(c, timed(c, "k_newton_update", [&] {
       return launch_newton_update(b->count, D, V, 0, 3, b->pcol.as<int32_t>(), b->theta.as<zc>(), done,
-                                  b->err.as<double>(), b->iters.as<int32_t>(), kNewtonTol, s);
+                                  b->err.as<double>(), b->iters.as<int32_t>(), kNewtonTol, kNewtonTolVec, s, skip);
     }));
   }
-  CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, nullptr, nullptr, s); }));
-  // least_val in caller units: omega (temporal) or alpha = 1/lambda (spatial)
+  CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, nullptr, skip, s); }));
+  // least_raw: omega (temporal) or lambda = 1/alpha (spatial)
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, s));
   if (want_vec) {
-    rc = write_vectors(b, all, b->theta.as<zc>());
+    rc = write_vectors(b, all, b->theta.as<zc>(), skip);
     if (rc) return rc;
   }
   return 0;
@@ -844,15 +867,64 @@ static int coarse_seeds(stab_batch* b) {
   stab_batch* cb = b->coarse;
   int rc = run_prep(cb);
   if (rc) return rc;
-  rc = run_plain(cb, false);
+  rc = run_plain(cb, false, "k_eig_plain_coarse");
   if (rc) return rc;
   // same internal order in both batches (same stable itype sort)
-  CK(c, cudaMemcpyAsync(b->sigma.p, cb->least_raw.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(b->cand.p, cb->cand.p, sizeof(zc) * b->count * kShiftCandidates, cudaMemcpyDeviceToDevice,
+                        c->stream));
+  return 0;
+}
+
+// Coarse-shift rounds.  Each polished pair is an eigenpair of the fine
+// problem, so the least-stable of the converged pairs over the top coarse
+// candidates is the answer whenever one candidate sits near the fine
+// least-stable mode (N = 32 can carry unresolved modes above it at M > 1.4,
+// and can resolve the right one only to ~1e-2).  Round 0 takes the top
+// candidate; when its polish lands within kQuickAcceptTol of the shift the
+// instance is final, otherwise the next candidates are polished too.
+// Instances with no converged pair go to the FP64 fallback.
+static int polish_candidate_rounds(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const int n = b->count;
+  CK(c, b->have.ensure(sizeof(int32_t) * n, s));
+  CK(c, b->best_key.ensure(sizeof(double) * n, s));
+  CK(c, b->best_theta.ensure(sizeof(zc) * n, s));
+  CK(c, b->best_err.ensure(sizeof(double) * n, s));
+  CK(c, b->best_iters.ensure(sizeof(int32_t) * n, s));
+  CK(c, b->best_out.ensure(sizeof(zc) * b->sum_m, s));
+  int32_t* fin = b->accepted.as<int32_t>();
+  CK(c, cudaMemsetAsync(fin, 0, sizeof(int32_t) * n, s));
+  CK(c, cudaMemsetAsync(b->have.p, 0, sizeof(int32_t) * n, s));
+  for (int j = 0; j < kShiftCandidates; ++j) {
+    CK(c, timed(c, "k_take_candidate", [&] {
+      k_take_candidate<<<(n + 255) / 256, 256, 0, s>>>(n, b->cand.as<zc>(), kShiftCandidates, j, b->sigma.as<zc>());
+      return cudaGetLastError();
+    }));
+    int rc = run_polish(b, true, fin);
+    if (rc) return rc;
+    CK(c, timed(c, "k_fold_best", [&] {
+      k_fold_best<<<n, 128, 0, s>>>(n, b->desc.as<InstDesc>(), b->sigma.as<zc>(), b->theta.as<zc>(),
+                                    b->done.as<int32_t>(), b->err.as<double>(), b->iters.as<int32_t>(),
+                                    b->outvec.as<zc>(), b->off_mof.as<int64_t>(), fin, b->have.as<int32_t>(),
+                                    b->best_key.as<double>(), b->best_theta.as<zc>(), b->best_err.as<double>(),
+                                    b->best_iters.as<int32_t>(), b->best_out.as<zc>(), j, kQuickAcceptTol);
+      return cudaGetLastError();
+    }));
+  }
+  CK(c, timed(c, "k_take_best", [&] {
+    k_take_best<<<n, 128, 0, s>>>(n, b->desc.as<InstDesc>(), b->have.as<int32_t>(), b->best_theta.as<zc>(),
+                                  b->best_err.as<double>(), b->best_iters.as<int32_t>(), b->best_out.as<zc>(),
+                                  b->off_mof.as<int64_t>(), b->theta.as<zc>(), b->done.as<int32_t>(),
+                                  b->err.as<double>(), b->iters.as<int32_t>(), b->outvec.as<zc>());
+    return cudaGetLastError();
+  }));
+  CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
   return 0;
 }
 
 // Re-solve, with the plain FP64 path, every instance whose polish did not
-// converge (or had no seed); results are kept on the host for
+// converge (or had no accepted shift); results are kept on the host for
 // stab_batch_results.
 static int run_fallback(stab_batch* b) {
   stab_ctx* c = b->ctx;
@@ -885,7 +957,7 @@ static int run_fallback(stab_batch* b) {
   std::unique_ptr<stab_batch> guard(fb);
   rc = run_prep(fb);
   if (rc) return rc;
-  rc = run_plain(fb, true);
+  rc = run_plain(fb, true, "k_eig_plain_fallback");
   if (rc) return rc;
   const int nf = fb->count;
   std::vector<zc> val(nf);
@@ -900,7 +972,7 @@ static int run_fallback(stab_batch* b) {
                           cudaMemcpyDeviceToHost, c->stream));
   }
   CK(c, cudaStreamSynchronize(c->stream));
-  // the sub-batch keeps caller order of `fp` internally sorted by itype; map back
+  // the sub-batch orders its instances temporal-first internally; map back
   b->fb_val.assign(b->fell_back.size(), zmk(0, 0));
   b->fb_status.assign(b->fell_back.size(), 0);
   b->fb_vec.assign(b->fell_back.size(), {});
@@ -925,7 +997,7 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
     if (rc) return rc;
     b->fell_back.clear();
     b->last_mode = mode;
-    rc = run_polish(b, true);
+    rc = polish_candidate_rounds(b);
     if (rc) return rc;
     rc = run_fallback(b);
     if (rc) return rc;
@@ -1010,7 +1082,8 @@ int stab_batch_work(stab_batch* b, double* work_out) {
     return t;
   };
   double lu_c = 0.0;
-  for (int n : b->hn) lu_c += 2.0 * (8.0 / 3.0) * (double)n * n * n;   // two complex64 LUs per instance
+  const double nlu = (b->last_mode == STAB_MODE_COARSE) ? 4.0 : 2.0;   // two LUs per polish, two polishes in coarse
+  for (int n : b->hn) lu_c += nlu * (8.0 / 3.0) * (double)n * n * n;
   const bool plain = (b->last_mode == STAB_MODE_PLAIN);
   work_out[0] = plain ? eig_flops(b) : 0.0;
   work_out[1] = (b->last_mode == STAB_MODE_COARSE && b->coarse) ? eig_flops(b->coarse) : 0.0;

@@ -15,6 +15,15 @@
 //      Tisseur (the algorithm of ZLAHQR, eigenvalues only).  The 2-element
 //      reflectors are general complex ones, so the subdiagonal need not be
 //      kept real.
+//
+// GB300 shape of step 5: FP64 issues at 1/59 of the FP32 rate, so no FP64
+// scalar work is repeated across threads.  The thread that updates the
+// 2x2/3x2 corner of a bulge step also forms the next step's reflector and
+// publishes it through a double-buffered shared slot: one barrier per bulge
+// step.  When the Hessenberg matrix (packed by columns with two
+// subdiagonals, for the bulge) fits in shared memory -- the N = 32 seed
+// problems do -- the sweeps run there instead of in global memory.
+//
 // All arithmetic is FP64.  Every loop has an iteration cap; an instance
 // that hits it gets status STAB_ST_NOCONV and NaN for the missing values.
 #include "common.cuh"
@@ -26,14 +35,19 @@ namespace stab {
 #define HQ_T 256
 #define HQ_W (HQ_T / 32)
 
+struct Refl {
+  double tr, ti, ur, ui, beta, v1r, v1i;
+  int ident;
+};
+
 struct HqrSmem {
   double red[2 * HQ_W];
-  int ired[HQ_W];
   int flag;
   int found;
   int mp;
   int kk;
-  double f;
+  double sc[8];   // broadcast scalars (Householder step, shift)
+  Refl refl[2];   // reflector of the next bulge step, double buffered
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -56,18 +70,218 @@ __device__ void block_sum2(HqrSmem& s, double& a, double& b) {
   __syncthreads();
 }
 
+// column-major storage in global memory
+struct GAcc {
+  zc* H;
+  int ld;
+  __device__ __forceinline__ zc& operator()(int r, int c) const { return H[(size_t)c * ld + r]; }
+};
+
+// packed Hessenberg-plus-one storage in shared memory: column c keeps rows
+// 0 .. min(c + 2, mp - 1)
+__host__ __device__ __forceinline__ int64_t hess_coff(int c, int mp) {
+  return (int64_t)c * (c + 5) / 2 - ((c == mp - 1 && mp >= 2) ? 1 : 0);
+}
+__host__ __device__ __forceinline__ int64_t hess_packed_size(int mp) {
+  return mp <= 0 ? 0 : hess_coff(mp - 1, mp) + mp;
+}
+struct SAcc {
+  zc* S;
+  int mp;
+  __device__ __forceinline__ zc& operator()(int r, int c) const { return S[hess_coff(c, mp) + r]; }
+};
+
+// 2-element reflector (as ZLARFG): (v1, v2) -> (beta, 0)
+__device__ __forceinline__ Refl make_refl(zc v1, zc v2) {
+  Refl f;
+  f.v1r = v1.x;
+  f.v1i = v1.y;
+  const double xn = zabs(v2);
+  if (xn == 0.0 && v1.y == 0.0) {
+    f.ident = 1;
+    f.tr = f.ti = f.ur = f.ui = 0.0;
+    f.beta = v1.x;
+    return f;
+  }
+  f.ident = 0;
+  const double beta = -copysign(sqrt(v1.x * v1.x + v1.y * v1.y + xn * xn), v1.x);
+  f.beta = beta;
+  f.tr = (beta - v1.x) / beta;
+  f.ti = -v1.y / beta;
+  const zc u2 = zdiv(v2, zmk(v1.x - beta, v1.y));
+  f.ur = u2.x;
+  f.ui = u2.y;
+  return f;
+}
+
+// left: rows k, k+1 of column j;  right: columns k, k+1 of row j
+template <class Acc>
+__device__ __forceinline__ void apply_left(const Acc& H, int k, int j, zc tau, zc u2) {
+  zc a = H(k, j), b = H(k + 1, j);
+  zc sm = zmul(zconj(tau), zcfma(u2, b, a));
+  H(k, j) = zsub(a, sm);
+  H(k + 1, j) = zsub(b, zmul(sm, u2));
+}
+template <class Acc>
+__device__ __forceinline__ void apply_right(const Acc& H, int k, int j, zc tau, zc u2) {
+  zc a = H(j, k), b = H(j, k + 1);
+  zc sm = zmul(tau, zfma(u2, b, a));
+  H(j, k) = zsub(a, sm);
+  H(j, k + 1) = zsub(b, zmul(sm, zconj(u2)));
+}
+
+// Single-shift QR on the mp x mp upper Hessenberg matrix behind H; writes
+// the eigenvalues to ev[0..mp).  Returns 0 or STAB_ST_NOCONV.
+template <class Acc>
+__device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& flops) {
+  const int tid = threadIdx.x;
+  const double ulp = 2.220446049250313e-16;
+  const double safmin = 2.2250738585072014e-308;
+  const double smlnum = safmin * ((double)mp / ulp);
+  const int its_cap = 40 * (mp > 10 ? mp : 10);
+  int st = 0;
+  int total_its = 0;
+  int i = mp - 1;
+  while (i >= 0 && st == 0) {
+    int l = 0;
+    int kdefl = 0;
+    for (;;) {
+      // largest k in [l+1, i] with a negligible subdiagonal; l if none
+      if (tid == 0) s.kk = l;
+      __syncthreads();
+      for (int k = i - tid; k >= l + 1; k -= HQ_T) {
+        const zc h = H(k, k - 1);
+        bool ok = zabs1(h) <= smlnum;
+        if (!ok) {
+          double tst = zabs1(H(k - 1, k - 1)) + zabs1(H(k, k));
+          if (tst == 0.0) {
+            if (k - 2 >= 0) tst += zabs1(H(k - 1, k - 2));
+            if (k + 1 <= mp - 1) tst += zabs1(H(k + 1, k));
+          }
+          if (zabs1(h) <= ulp * tst) {
+            const double h1 = zabs1(h), h2 = zabs1(H(k - 1, k));
+            const double ab = fmax(h1, h2), ba = fmin(h1, h2);
+            const double d1 = zabs1(H(k, k)), d2 = zabs1(zsub(H(k - 1, k - 1), H(k, k)));
+            const double aa = fmax(d1, d2), bb = fmin(d1, d2);
+            const double sm = aa + ab;
+            ok = ba * (ab / sm) <= fmax(smlnum, ulp * (bb * (aa / sm)));
+          }
+        }
+        if (ok) { atomicMax(&s.kk, k); break; }   // this thread's larger k's were tested first
+      }
+      __syncthreads();
+      l = s.kk;
+      __syncthreads();
+      if (l > 0 && tid == 0) H(l, l - 1) = zmk(0.0, 0.0);
+      if (l >= i) break;
+      if (total_its >= its_cap) { st = STAB_ST_NOCONV; break; }
+      ++kdefl;
+      ++total_its;
+      // shift (one thread)
+      if (tid == 0) {
+        zc t;
+        if (kdefl % 20 == 0) {
+          t = zadd(zmk(0.75 * zabs(H(i, i - 1)), 0.0), H(i, i));
+        } else if (kdefl % 10 == 0) {
+          t = zadd(zmk(0.75 * zabs(H(l + 1, l)), 0.0), H(l, l));
+        } else {
+          t = H(i, i);
+          const zc u = zmul(zsqrt(H(i - 1, i)), zsqrt(H(i, i - 1)));
+          const double su = zabs1(u);
+          if (su != 0.0) {
+            const zc x = zscale(zsub(H(i - 1, i - 1), t), 0.5);
+            const double sx = zabs1(x);
+            const double sc = fmax(su, sx);
+            const zc xs = zscale(x, 1.0 / sc), us = zscale(u, 1.0 / sc);
+            zc y = zscale(zsqrt(zadd(zmul(xs, xs), zmul(us, us))), sc);
+            if (sx > 0.0) {
+              const zc xn = zscale(x, 1.0 / sx);
+              if (xn.x * y.x + xn.y * y.y < 0.0) y = zmk(-y.x, -y.y);
+            }
+            t = zsub(t, zmul(u, zdiv(u, zadd(x, y))));
+          }
+        }
+        s.sc[0] = t.x;
+        s.sc[1] = t.y;
+        s.kk = l;
+      }
+      __syncthreads();
+      const zc t = zmk(s.sc[0], s.sc[1]);
+      // start row: largest m in [l+1, i-1] where two consecutive small
+      // subdiagonals decouple the sweep; l otherwise
+      for (int mm = i - 1 - tid; mm >= l + 1; mm -= HQ_T) {
+        const zc h11 = H(mm, mm), h22 = H(mm + 1, mm + 1);
+        const zc h11s = zsub(h11, t);
+        const zc h21 = H(mm + 1, mm);
+        const double sc = zabs1(h11s) + zabs1(h21);
+        if (sc == 0.0) continue;
+        const double h10 = zabs1(H(mm, mm - 1));
+        // |h10| |h21/sc| <= ulp |h11s/sc| (|h11| + |h22|), multiplied through by sc
+        if (h10 * zabs1(h21) <= ulp * (zabs1(h11s) * (zabs1(h11) + zabs1(h22)))) {
+          atomicMax(&s.kk, mm);
+          break;
+        }
+      }
+      __syncthreads();
+      const int m0 = s.kk;
+      if (tid == 0) {
+        const zc h11s = zsub(H(m0, m0), t);
+        const zc h21 = H(m0 + 1, m0);
+        double sc = zabs1(h11s) + zabs1(h21);
+        if (sc == 0.0) sc = 1.0;
+        s.refl[m0 & 1] = make_refl(zscale(h11s, 1.0 / sc), zscale(h21, 1.0 / sc));
+      }
+      __syncthreads();
+      // bulge chase, one barrier per step
+      for (int k = m0; k < i; ++k) {
+        const Refl f = s.refl[k & 1];
+        const zc tau = zmk(f.tr, f.ti), u2 = zmk(f.ur, f.ui);
+        const int nleft = i - k - 1;        // columns k+2..i
+        const int ntask = i - l;            // corner + nleft + (k - l) rows above
+        if (tid == 0) flops += 24.0 * (double)(ntask + 4);
+        for (int q = tid; q < ntask; q += HQ_T) {
+          if (q == 0) {
+            if (k > m0) { H(k, k - 1) = zmk(f.ident ? f.v1r : f.beta, f.ident ? f.v1i : 0.0); H(k + 1, k - 1) = zmk(0.0, 0.0); }
+            if (!f.ident) {
+              // a sweep started below l still applies the first reflector to
+              // column m0-1: H(m0, m0-1) picks up (1 - conj(tau)); the fill-in
+              // at H(m0+1, m0-1) is what the start test bounds
+              if (k == m0 && m0 > l) H(m0, m0 - 1) = zmul(H(m0, m0 - 1), zsub(zmk(1.0, 0.0), zconj(tau)));
+              apply_left(H, k, k, tau, u2);
+              apply_left(H, k, k + 1, tau, u2);
+              const int rmax = (k + 2 <= i) ? k + 2 : i;
+              for (int j = k; j <= rmax; ++j) apply_right(H, k, j, tau, u2);
+            }
+            if (k + 1 < i) s.refl[(k + 1) & 1] = make_refl(H(k + 1, k), H(k + 2, k));
+          } else if (!f.ident) {
+            if (q <= nleft) apply_left(H, k, k + 1 + q, tau, u2);
+            else apply_right(H, k, l + (q - nleft - 1), tau, u2);
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (st) break;
+    if (tid == 0) ev[i] = H(i, i);
+    i = l - 1;
+    __syncthreads();
+  }
+  if (st)
+    for (int q = tid; q <= i; q += HQ_T) ev[q] = zmk(nan(""), nan(""));
+  __syncthreads();
+  return st;
+}
+
 __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
                                                    const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
                                                    const int64_t* __restrict__ h_off, zc* __restrict__ eig,
                                                    const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
                                                    int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
-                                                   double* __restrict__ flops_out) {
+                                                   double* __restrict__ flops_out, int64_t smem_qr_elems) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ HqrSmem s;
   __shared__ int s_inst;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const double ulp = 2.220446049250313e-16;
-  const double safmin = 2.2250738585072014e-308;
   for (;;) {
     if (tid == 0) s_inst = atomicAdd(work_counter, 1);
     __syncthreads();
@@ -76,12 +290,14 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
     const int inst = order ? order[slot] : slot;
     const int m = msz[inst];
     zc* M = A + a_off[inst];
-    zc* H = Hp + h_off[inst];
+    zc* Hg = Hp + h_off[inst];
     zc* ev = eig + eig_off[inst];
-    // shared scratch: active flags (m bytes, as int), act list (m ints), v, w, z (m complex each)
+    // shared scratch: active flags and act list (m ints each), then either
+    // v, w, z (Hessenberg phase) or the packed matrix (QR phase)
     int* active = reinterpret_cast<int*>(smraw);
     int* act = active + m;
-    zc* v = reinterpret_cast<zc*>(smraw + ((2 * (size_t)m * sizeof(int) + 15) / 16) * 16);
+    zc* zs = reinterpret_cast<zc*>(smraw + ((2 * (size_t)m * sizeof(int) + 15) / 16) * 16);
+    zc* v = zs;
     zc* w = v + m;
     zc* z = w + m;
     for (int i = tid; i < m; i += HQ_T) active[i] = 1;
@@ -92,33 +308,29 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
     for (int pass = 0; pass < m; ++pass) {
       if (tid == 0) s.found = 0;
       __syncthreads();
-      // rows: thread per row
-      for (int r = tid; r < m; r += HQ_T) {
+      for (int r = tid; r < m; r += HQ_T) {           // rows: thread per row
         if (!active[r]) continue;
         bool zero = true;
         for (int c = 0; c < m && zero; ++c) {
           if (c == r || !active[c]) continue;
-          zc a = M[(size_t)c * m + r];
+          const zc a = M[(size_t)c * m + r];
           zero = (a.x == 0.0 && a.y == 0.0);
         }
-        if (zero) { active[r] = 2; atomicAdd(&s.found, 1); }   // 2 = isolated this pass (row)
+        if (zero) { active[r] = 2; atomicAdd(&s.found, 1); }
       }
-      // columns: warp per column
-      for (int c = warp; c < m; c += HQ_W) {
+      for (int c = warp; c < m; c += HQ_W) {          // columns: warp per column
         if (active[c] != 1) continue;
         bool zero = true;
         for (int r = lane; r < m; r += 32) {
           if (r == c || active[r] == 0) continue;
-          zc a = M[(size_t)c * m + r];
+          const zc a = M[(size_t)c * m + r];
           if (a.x != 0.0 || a.y != 0.0) zero = false;
         }
         zero = __all_sync(0xffffffffu, zero);
         if (zero && lane == 0) { active[c] = 3; atomicAdd(&s.found, 1); }
       }
       __syncthreads();
-      const int found = s.found;
-      if (found == 0) break;
-      // record eigenvalues of the newly isolated indices (sequential, deterministic order)
+      if (s.found == 0) break;
       if (tid == 0) {
         int q = n_iso;
         for (int i = 0; i < m; ++i)
@@ -141,7 +353,7 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
     const int ld = mp;
     for (int c = warp; c < mp; c += HQ_W) {
       const int sc = act[c];
-      for (int r = lane; r < mp; r += 32) H[(size_t)c * ld + r] = M[(size_t)sc * m + act[r]];
+      for (int r = lane; r < mp; r += 32) Hg[(size_t)c * ld + r] = M[(size_t)sc * m + act[r]];
     }
     __syncthreads();
     // ---- 3. balancing -------------------------------------------------------
@@ -152,38 +364,42 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
         double cs = 0.0, rs = 0.0;
         for (int r = tid; r < mp; r += HQ_T) {
           if (r == i) continue;
-          zc a = H[(size_t)i * ld + r];
+          const zc a = Hg[(size_t)i * ld + r];
           cs += a.x * a.x + a.y * a.y;
-          zc b = H[(size_t)r * ld + i];
+          const zc b = Hg[(size_t)r * ld + i];
           rs += b.x * b.x + b.y * b.y;
         }
         block_sum2(s, cs, rs);
-        double c = sqrt(cs), r = sqrt(rs);
-        double f = 1.0;
-        if (c != 0.0 && r != 0.0) {
-          double g = r / 2.0, sum = c + r;
-          int guard = 0;
-          while (c < g && guard++ < 2000) { f *= 2.0; c *= 2.0; r /= 2.0; g /= 2.0; }
-          g = c / 2.0;
-          while (g >= r && guard++ < 4000) { f /= 2.0; c /= 2.0; g /= 2.0; r *= 2.0; }
-          if (c + r >= 0.95 * sum) f = 1.0;
+        if (tid == 0) {
+          double c = sqrt(cs), r = sqrt(rs), f = 1.0;
+          if (c != 0.0 && r != 0.0) {
+            double g = r / 2.0;
+            const double sum = c + r;
+            int guard = 0;
+            while (c < g && guard++ < 2000) { f *= 2.0; c *= 2.0; r /= 2.0; g /= 2.0; }
+            g = c / 2.0;
+            while (g >= r && guard++ < 4000) { f /= 2.0; c /= 2.0; g /= 2.0; r *= 2.0; }
+            if (c + r >= 0.95 * sum) f = 1.0;
+          }
+          s.sc[0] = f;
+          if (f != 1.0) s.flag = 1;
         }
+        __syncthreads();
+        const double f = s.sc[0];
         if (f != 1.0) {
           const double gi = 1.0 / f;
           for (int q = tid; q < mp; q += HQ_T) {
-            zc* a = &H[(size_t)q * ld + i];    // row i
+            zc* a = &Hg[(size_t)q * ld + i];    // row i
             *a = zscale(*a, gi);
           }
           __syncthreads();
           for (int q = tid; q < mp; q += HQ_T) {
-            zc* a = &H[(size_t)i * ld + q];    // column i
+            zc* a = &Hg[(size_t)i * ld + q];    // column i
             *a = zscale(*a, f);
           }
-          if (tid == 0) s.flag = 1;
-          __syncthreads();
         }
+        __syncthreads();
       }
-      __syncthreads();
       if (!s.flag) break;
       __syncthreads();
     }
@@ -194,35 +410,49 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
       if (tid == 0) flops += 16.0 * (double)mp * L + 16.0 * (double)L * L;
       double ss = 0.0, dummy = 0.0;
       for (int r = tid; r < L; r += HQ_T) {
-        zc x = H[(size_t)k * ld + k + 1 + r];
+        const zc x = Hg[(size_t)k * ld + k + 1 + r];
         v[r] = x;
         if (r >= 1) ss += x.x * x.x + x.y * x.y;
       }
       block_sum2(s, ss, dummy);
-      const zc alpha = v[0];
-      if (ss == 0.0 && alpha.y == 0.0) continue;   // H(k) = I
-      const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + ss), alpha.x);
-      const zc tau = zmk((beta - alpha.x) / beta, -alpha.y / beta);
-      const zc scal = zdiv(zmk(1.0, 0.0), zmk(alpha.x - beta, alpha.y));
+      if (tid == 0) {
+        const zc alpha = v[0];
+        if (ss == 0.0 && alpha.y == 0.0) {
+          s.flag = 0;                                      // H(k) = I
+        } else {
+          s.flag = 1;
+          const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + ss), alpha.x);
+          const zc scal = zdiv(zmk(1.0, 0.0), zmk(alpha.x - beta, alpha.y));
+          s.sc[0] = (beta - alpha.x) / beta;   // tau
+          s.sc[1] = -alpha.y / beta;
+          s.sc[2] = scal.x;
+          s.sc[3] = scal.y;
+          s.sc[4] = beta;
+        }
+      }
       __syncthreads();
+      if (!s.flag) continue;
+      const zc tau = zmk(s.sc[0], s.sc[1]);
+      const zc scal = zmk(s.sc[2], s.sc[3]);
+      const double beta = s.sc[4];
       for (int r = tid; r < L; r += HQ_T) v[r] = (r == 0) ? zmk(1.0, 0.0) : zmul(v[r], scal);
-      if (tid == 0) H[(size_t)k * ld + k + 1] = zmk(beta, 0.0);
-      for (int r = 2 + tid; r <= L; r += HQ_T) H[(size_t)k * ld + k + r] = zmk(0.0, 0.0);
+      if (tid == 0) Hg[(size_t)k * ld + k + 1] = zmk(beta, 0.0);
+      for (int r = 2 + tid; r <= L; r += HQ_T) Hg[(size_t)k * ld + k + r] = zmk(0.0, 0.0);
       __syncthreads();
-      // right: w = H(:, k+1:) v
+      // right: w = tau H(:, k+1:) v
       for (int r = tid; r < mp; r += HQ_T) {
         zc acc = zmk(0.0, 0.0);
-        for (int c = 0; c < L; ++c) acc = zfma(H[(size_t)(k + 1 + c) * ld + r], v[c], acc);
+        for (int c = 0; c < L; ++c) acc = zfma(Hg[(size_t)(k + 1 + c) * ld + r], v[c], acc);
         w[r] = zmul(tau, acc);
       }
       __syncthreads();
-      // right update fused with the left product z = v^H H(k+1:, k+1:), warp per column
+      // right update fused with the left product z = conj(tau) v^H H(k+1:, k+1:), warp per column
       for (int c = warp; c < L; c += HQ_W) {
         const zc vc = zconj(v[c]);
-        zc* col = H + (size_t)(k + 1 + c) * ld;
+        zc* col = Hg + (size_t)(k + 1 + c) * ld;
         zc acc = zmk(0.0, 0.0);
         for (int r = lane; r < mp; r += 32) {
-          zc h = zsub(col[r], zmul(w[r], vc));
+          const zc h = zsub(col[r], zmul(w[r], vc));
           col[r] = h;
           if (r >= k + 1) acc = zcfma(v[r - k - 1], h, acc);
         }
@@ -234,177 +464,26 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
       // left update: H(k+1:, k+1:) -= v z
       for (int c = warp; c < L; c += HQ_W) {
         const zc zc_ = z[c];
-        zc* col = H + (size_t)(k + 1 + c) * ld + k + 1;
+        zc* col = Hg + (size_t)(k + 1 + c) * ld + k + 1;
         for (int r = lane; r < L; r += 32) col[r] = zsub(col[r], zmul(v[r], zc_));
       }
       __syncthreads();
     }
     // ---- 5. QR iteration ----------------------------------------------------
-    int st = 0;
-    int total_its = 0;
-    const int its_cap = 40 * (mp > 10 ? mp : 10);
-    const double smlnum = safmin * ((double)mp / ulp);
-    auto Hs = [&](int r, int c) -> zc& { return H[(size_t)c * ld + r]; };
-    int i = mp - 1;
-    while (i >= 0 && st == 0) {
-      int l = 0;
-      int kdefl = 0;
-      for (;;) {
-        // largest k in [l+1, i] with a negligible subdiagonal; l if none
-        if (tid == 0) s.kk = l;
-        __syncthreads();
-        for (int k = i - tid; k >= l + 1; k -= HQ_T) {
-          zc h = Hs(k, k - 1);
-          bool ok = zabs1(h) <= smlnum;
-          if (!ok) {
-            double tst = zabs1(Hs(k - 1, k - 1)) + zabs1(Hs(k, k));
-            if (tst == 0.0) {
-              if (k - 2 >= 0) tst += zabs1(Hs(k - 1, k - 2));
-              if (k + 1 <= mp - 1) tst += zabs1(Hs(k + 1, k));
-            }
-            if (zabs1(h) <= ulp * tst) {
-              const double h1 = zabs1(h), h2 = zabs1(Hs(k - 1, k));
-              const double ab = fmax(h1, h2), ba = fmin(h1, h2);
-              const double d1 = zabs1(Hs(k, k)), d2 = zabs1(zsub(Hs(k - 1, k - 1), Hs(k, k)));
-              const double aa = fmax(d1, d2), bb = fmin(d1, d2);
-              const double sm = aa + ab;
-              ok = ba * (ab / sm) <= fmax(smlnum, ulp * (bb * (aa / sm)));
-            }
-          }
-          if (ok) { atomicMax(&s.kk, k); break; }   // larger k's of this thread were tested first
-        }
-        __syncthreads();
-        l = s.kk;
-        __syncthreads();
-        if (l > 0 && tid == 0) Hs(l, l - 1) = zmk(0.0, 0.0);
-        if (l >= i) break;
-        if (total_its >= its_cap) { st = STAB_ST_NOCONV; break; }
-        ++kdefl;
-        ++total_its;
-        // shift
-        zc t;
-        if (kdefl % 20 == 0) {
-          t = zadd(zmk(0.75 * zabs(Hs(i, i - 1)), 0.0), Hs(i, i));
-        } else if (kdefl % 10 == 0) {
-          t = zadd(zmk(0.75 * zabs(Hs(l + 1, l)), 0.0), Hs(l, l));
-        } else {
-          t = Hs(i, i);
-          zc u = zmul(zsqrt(Hs(i - 1, i)), zsqrt(Hs(i, i - 1)));
-          double su = zabs1(u);
-          if (su != 0.0) {
-            zc x = zscale(zsub(Hs(i - 1, i - 1), t), 0.5);
-            double sx = zabs1(x);
-            double sc = fmax(su, sx);
-            zc xs = zscale(x, 1.0 / sc), us = zscale(u, 1.0 / sc);
-            zc y = zscale(zsqrt(zadd(zmul(xs, xs), zmul(us, us))), sc);
-            if (sx > 0.0) {
-              zc xn = zscale(x, 1.0 / sx);
-              if (xn.x * y.x + xn.y * y.y < 0.0) y = zmk(-y.x, -y.y);
-            }
-            t = zsub(t, zmul(u, zdiv(u, zadd(x, y))));
-          }
-        }
-        // start row: largest m in [l+1, i-1] where two consecutive small
-        // subdiagonals decouple the sweep; l otherwise
-        if (tid == 0) s.kk = l;
-        __syncthreads();
-        for (int mm = i - 1 - tid; mm >= l + 1; mm -= HQ_T) {
-          zc h11 = Hs(mm, mm), h22 = Hs(mm + 1, mm + 1);
-          zc h11s = zsub(h11, t);
-          zc h21 = Hs(mm + 1, mm);
-          double sc = zabs1(h11s) + zabs1(h21);
-          if (sc == 0.0) continue;
-          h11s = zscale(h11s, 1.0 / sc);
-          h21 = zscale(h21, 1.0 / sc);
-          zc h10 = Hs(mm, mm - 1);
-          if (zabs1(h10) * zabs1(h21) <= ulp * (zabs1(h11s) * (zabs1(h11) + zabs1(h22)))) {
-            atomicMax(&s.kk, mm);
-            break;
-          }
-        }
-        __syncthreads();
-        const int m0 = s.kk;
-        __syncthreads();
-        zc v1, v2;
-        {
-          zc h11s = zsub(Hs(m0, m0), t);
-          zc h21 = Hs(m0 + 1, m0);
-          double sc = zabs1(h11s) + zabs1(h21);
-          if (sc == 0.0) sc = 1.0;
-          v1 = zscale(h11s, 1.0 / sc);
-          v2 = zscale(h21, 1.0 / sc);
-        }
-        // bulge chase
-        for (int k = m0; k < i; ++k) {
-          if (k > m0) { v1 = Hs(k, k - 1); v2 = Hs(k + 1, k - 1); }
-          // 2-element reflector (as ZLARFG): (v1, v2) -> (beta, 0)
-          zc tau = zmk(0.0, 0.0), u2 = zmk(0.0, 0.0);
-          double beta = v1.x;
-          bool ident = false;
-          {
-            double xn = zabs(v2);
-            if (xn == 0.0 && v1.y == 0.0) {
-              ident = true;
-            } else {
-              beta = -copysign(sqrt(v1.x * v1.x + v1.y * v1.y + xn * xn), v1.x);
-              tau = zmk((beta - v1.x) / beta, -v1.y / beta);
-              u2 = zdiv(v2, zmk(v1.x - beta, v1.y));
-            }
-          }
-          __syncthreads();   // everyone has read the column before it changes
-          const int nleft = i - k - 1;        // columns k+2..i
-          const int ntask = i - l;            // 1 corner + nleft + (k - l) right rows
-          if (tid == 0) flops += 24.0 * (double)(ntask + 4);   // 24 flops per 2-element pair update
-          for (int q = tid; q < ntask; q += HQ_T) {
-            if (q == 0) {
-              if (k > m0) { Hs(k, k - 1) = zmk(ident ? v1.x : beta, ident ? v1.y : 0.0); Hs(k + 1, k - 1) = zmk(0.0, 0.0); }
-              if (k == m0 && m0 > l && !ident) {
-                // a sweep started below l still applies the first reflector to
-                // column m0-1: H(m0, m0-1) picks up the factor (1 - conj(tau));
-                // the fill-in at H(m0+1, m0-1) is what the start test bounds.
-                Hs(m0, m0 - 1) = zmul(Hs(m0, m0 - 1), zsub(zmk(1.0, 0.0), zconj(tau)));
-              }
-              if (!ident) {
-                for (int j = k; j <= k + 1; ++j) {   // left on the 2x2 corner
-                  zc a = Hs(k, j), b = Hs(k + 1, j);
-                  zc sm = zmul(zconj(tau), zcfma(u2, b, a));
-                  Hs(k, j) = zsub(a, sm);
-                  Hs(k + 1, j) = zsub(b, zmul(sm, u2));
-                }
-                const int rmax = (k + 2 <= i) ? k + 2 : i;
-                for (int j = k; j <= rmax; ++j) {   // right on rows k..k+2
-                  zc a = Hs(j, k), b = Hs(j, k + 1);
-                  zc sm = zmul(tau, zfma(u2, b, a));
-                  Hs(j, k) = zsub(a, sm);
-                  Hs(j, k + 1) = zsub(b, zmul(sm, zconj(u2)));
-                }
-              }
-            } else if (!ident) {
-              if (q <= nleft) {
-                const int j = k + 1 + q;          // column
-                zc a = Hs(k, j), b = Hs(k + 1, j);
-                zc sm = zmul(zconj(tau), zcfma(u2, b, a));
-                Hs(k, j) = zsub(a, sm);
-                Hs(k + 1, j) = zsub(b, zmul(sm, u2));
-              } else {
-                const int j = l + (q - nleft - 1);   // row < k
-                zc a = Hs(j, k), b = Hs(j, k + 1);
-                zc sm = zmul(tau, zfma(u2, b, a));
-                Hs(j, k) = zsub(a, sm);
-                Hs(j, k + 1) = zsub(b, zmul(sm, zconj(u2)));
-              }
-            }
-          }
-          __syncthreads();
-        }
+    int st;
+    if (hess_packed_size(mp) <= smem_qr_elems) {
+      SAcc S{zs, mp};
+      for (int c = warp; c < mp; c += HQ_W) {
+        const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
+        for (int r = lane; r <= rmax; r += 32) S(r, c) = (r <= c + 1) ? Hg[(size_t)c * ld + r] : zmk(0.0, 0.0);
       }
-      if (st) break;
-      if (tid == 0) ev[i] = Hs(i, i);
-      i = l - 1;
       __syncthreads();
-    }
-    if (st) {
-      for (int q = tid; q <= i; q += HQ_T) ev[q] = zmk(nan(""), nan(""));
+      st = qr_eigs(S, mp, ev, s, flops);
+    } else {
+      GAcc G{Hg, ld};
+      for (int c = tid; c + 2 < mp; c += HQ_T) Hg[(size_t)c * ld + c + 2] = zmk(0.0, 0.0);
+      __syncthreads();
+      st = qr_eigs(G, mp, ev, s, flops);
     }
     if (tid == 0) {
       status[inst] = st;
@@ -414,8 +493,17 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
   }
 }
 
-size_t eig_plain_smem(int mmax) {
-  return ((2 * (size_t)mmax * sizeof(int) + 15) / 16) * 16 + 3 * (size_t)mmax * sizeof(zc);
+size_t eig_plain_smem(int mmax, int64_t* qr_elems) {
+  const size_t head = ((2 * (size_t)mmax * sizeof(int) + 15) / 16) * 16;
+  const size_t vwz = 3 * (size_t)mmax * sizeof(zc);
+  const size_t cap = 220 * 1024;   // leave room for the static shared state
+  const size_t packed = (size_t)hess_packed_size(mmax) * sizeof(zc);
+  if (head + packed <= cap) {
+    if (qr_elems) *qr_elems = hess_packed_size(mmax);
+    return head + (packed > vwz ? packed : vwz);
+  }
+  if (qr_elems) *qr_elems = 0;
+  return head + vwz;
 }
 
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
@@ -423,13 +511,23 @@ cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, con
                              int32_t* work_counter, const int32_t* order, double* flops, int grid,
                              cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  size_t sm = eig_plain_smem(mmax);
+  int64_t qr_elems = 0;
+  size_t sm = eig_plain_smem(mmax, &qr_elems);
   cudaError_t e = cudaFuncSetAttribute(k_eig_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(work_counter, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
+  // persistent grid: as many CTAs as can be resident at once
+  int dev = 0, sms = 1, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eig_plain, HQ_T, sm) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const int resident = sms * per_sm;
+  if (grid <= 0 || grid > resident) grid = resident;
+  if (grid > count) grid = count;
   k_eig_plain<<<grid, HQ_T, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter, order,
-                                     flops);
+                                     flops, qr_elems);
   return cudaGetLastError();
 }
 

@@ -3,7 +3,9 @@
 #include "common.cuh"
 
 namespace stab {
-size_t eig_plain_smem(int mmax);
+// dynamic shared memory of k_eig_plain; qr_elems receives the packed QR
+// capacity (0 when the sweeps run in global memory)
+size_t eig_plain_smem(int mmax, int64_t* qr_elems);
 // A: count column-major m x m matrices (destroyed); H: workspace of the same
 // size; eig receives m eigenvalues per instance (QR eigenvalues first, then
 // the isolated ones); status[k] = 0 or STAB_ST_NOCONV.  `order` (may be null)

@@ -35,22 +35,34 @@ __global__ void k_blocks(int count, const InstDesc* desc, const double* const* d
 // per-node operator (P1, P2, P3): kind_t for temporal, kind_s for spatial
 // instances, at shift sigma[k] (may be null)
 __global__ void k_node_ops(int count, const InstDesc* desc, const zc* blk, int kind_t, int kind_s, const zc* sigma,
-                           zc* ops);
+                           zc* ops, const int32_t* skip);
 // dense column-major n x n operator (times `scale`) from ops into out +
 // out_off[k] with leading dimension ldmul*n; element type T
 template <typename T>
 cudaError_t launch_dense(int count, int nmax, const InstDesc* desc, const double* const* dtab, const zc* ops, T* out,
-                         const int64_t* out_off, int ldmul, double scale, cudaStream_t s);
+                         const int64_t* out_off, int ldmul, double scale, cudaStream_t s,
+                         const int32_t* skip = nullptr);
 // structured y = M x for M given by ops (FP64):  y_i = P1 (D1 X)_i - P2 (D2 X)_i + P3 x_i
 __global__ void k_opmv(int count, const InstDesc* desc, const double* const* dtab, const zc* ops, const zc* x,
                        int xslot, zc* y, int yslot);
 // post.cu
 __global__ void k_companion_fill(int count, const InstDesc* desc, zc* A, const int64_t* a_off);
 __global__ void k_post_spectrum(int count, const InstDesc* desc, const zc* eig_raw, const int64_t* eig_off,
-                                zc* eig_sorted, int32_t* least_sorted, zc* least_raw, zc* least_val);
+                                zc* eig_sorted, int32_t* least_sorted, zc* least_raw, zc* least_val, zc* cand,
+                                int ncand);
 __global__ void k_spatial_vec(int count, const InstDesc* desc, const zc* theta, const zc* vec, int slot,
-                              zc* out, const int64_t* out_off);
+                              zc* out, const int64_t* out_off, const int32_t* skip);
+// seed rounds of the coarse mode: candidate j of k_post_spectrum -> sigma,
+// folding of each round into the best pair, final pick
+__global__ void k_take_candidate(int count, const zc* cand, int ncand, int j, zc* sigma);
+__global__ void k_fold_best(int count, const InstDesc* desc, const zc* sigma, const zc* theta, const int32_t* done,
+                            const double* err, const int32_t* iters, const zc* out, const int64_t* out_off,
+                            int32_t* final_, int32_t* have, double* best_key, zc* best_theta, double* best_err,
+                            int32_t* best_iters, zc* best_out, int round, double quick_tol);
+__global__ void k_take_best(int count, const InstDesc* desc, const int32_t* have, const zc* best_theta,
+                            const double* best_err, const int32_t* best_iters, const zc* best_out,
+                            const int64_t* out_off, zc* theta, int32_t* done, double* err, int32_t* iters, zc* out);
 __global__ void k_temporal_vec(int count, const InstDesc* desc, const zc* vec, int slot, zc* out,
-                               const int64_t* out_off);
+                               const int64_t* out_off, const int32_t* skip);
 
 }  // namespace stab

@@ -34,11 +34,12 @@ template <typename T, int NB>
 __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restrict__ desc, const int32_t* __restrict__ nsz,
                                             T* __restrict__ A, const int64_t* __restrict__ mat_off,
                                             int32_t* __restrict__ piv, const int64_t* __restrict__ piv_off,
-                                            int32_t* __restrict__ info) {
+                                            int32_t* __restrict__ info, const int32_t* __restrict__ skip) {
   typedef typename cx<T>::real R;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int k = blockIdx.x;
   if (k >= count) return;
+  if (skip && skip[k]) return;
   const int n = nsz[k];
   T* M = A + mat_off[k];
   int32_t* ip = piv + piv_off[k];
@@ -184,6 +185,62 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
   if (tid == 0) info[k] = first_zero;
 }
 
+// Power-of-two row and column equilibration of complex64 matrices before the
+// LU: M <- R M C with R, C diagonal powers of two (exact in floating point),
+// chosen so every row and then every column has max |re|+|im| in [0.5, 1).
+// This keeps pivoting and the complex64 rounding meaningful when the
+// operator's rows differ by many orders of magnitude (e.g. the 1/(gamma M^2)
+// pressure terms at low Mach number).  R and C are stored per instance.
+__global__ void __launch_bounds__(256) k_equilibrate(int count, const int32_t* __restrict__ nsz, cc* __restrict__ A,
+                                                     const int64_t* __restrict__ mat_off, float* __restrict__ rs,
+                                                     float* __restrict__ cs, const int64_t* __restrict__ sc_off,
+                                                     const int32_t* __restrict__ skip) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const int n = nsz[k];
+  cc* M = A + mat_off[k];
+  float* R = rs + sc_off[k];
+  float* C = cs + sc_off[k];
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    float mx = 0.f;
+    for (int c = 0; c < n; ++c) mx = fmaxf(mx, cabs1f(M[(size_t)c * n + r]));
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+    R[r] = ldexpf(1.f, -e);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int c = warp; c < n; c += nw) {
+    float mx = 0.f;
+    cc* col = M + (size_t)c * n;
+    for (int r = lane; r < n; r += 32) {
+      cc v = col[r];
+      const float f = R[r];
+      v.x *= f; v.y *= f;
+      col[r] = v;
+      mx = fmaxf(mx, cabs1f(v));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+    const float g = ldexpf(1.f, -e);
+    for (int r = lane; r < n; r += 32) {
+      cc v = col[r];
+      v.x *= g; v.y *= g;
+      col[r] = v;
+    }
+    if (lane == 0) C[c] = g;
+  }
+}
+
+cudaError_t launch_equilibrate(int count, const int32_t* nsz, cc* A, const int64_t* mat_off, float* rs, float* cs,
+                               const int64_t* sc_off, cudaStream_t s, const int32_t* skip) {
+  if (count <= 0) return cudaSuccess;
+  k_equilibrate<<<count, 256, 0, s>>>(count, nsz, A, mat_off, rs, cs, sc_off, skip);
+  return cudaGetLastError();
+}
+
 // Triangular solves with the factors of k_lu: X <- U^-1 L^-1 P X for nrhs
 // columns per instance.  One warp per right-hand side, the column held in
 // shared memory; the factor columns are read coalesced from global memory.
@@ -193,7 +250,8 @@ __global__ void __launch_bounds__(256) k_getrs(int count, const int32_t* __restr
                                                const int64_t* __restrict__ mat_off, const int32_t* __restrict__ piv,
                                                const int64_t* __restrict__ piv_off, zc* __restrict__ X,
                                                const int64_t* __restrict__ x_off, int nrhs_fixed, int nrhs_mul,
-                                               int ldmul, const int32_t* __restrict__ skip) {
+                                               int ldmul, const int32_t* __restrict__ skip, const float* __restrict__ rs,
+                                               const float* __restrict__ cs) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int k = blockIdx.y;
   if (k >= count) return;
@@ -208,7 +266,13 @@ __global__ void __launch_bounds__(256) k_getrs(int count, const int32_t* __restr
   const T* M = LU + mat_off[k];
   const int32_t* ip = piv + piv_off[k];
   zc* xg = X + x_off[k] + (size_t)col * ldx;
-  for (int r = lane; r < n; r += 32) xs[r] = cx<T>::from(xg[r]);
+  const float* R = rs ? rs + piv_off[k] : nullptr;   // equilibration (k_equilibrate), same offsets as pivots
+  const float* C = cs ? cs + piv_off[k] : nullptr;
+  for (int r = lane; r < n; r += 32) {
+    zc b = xg[r];
+    if (R) b = zscale(b, (double)R[r]);
+    xs[r] = cx<T>::from(b);
+  }
   __syncwarp();
   if (lane == 0)
     for (int j = 0; j < n; ++j) {
@@ -230,7 +294,10 @@ __global__ void __launch_bounds__(256) k_getrs(int count, const int32_t* __restr
     for (int r = lane; r < j; r += 32) xs[r] = cx<T>::sub(xs[r], cx<T>::mul(M[(size_t)j * n + r], xj));
     __syncwarp();
   }
-  for (int r = lane; r < n; r += 32) xg[r] = cx<T>::to64(xs[r]);
+  for (int r = lane; r < n; r += 32) {
+    zc y = cx<T>::to64(xs[r]);
+    xg[r] = C ? zscale(y, (double)C[r]) : y;
+  }
 }
 
 // ---- host launchers ------------------------------------------------------
@@ -246,28 +313,29 @@ int lu_nb_for(int n) {
 template <typename T, int NB>
 static cudaError_t launch_lu_nb(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A,
                                 const int64_t* mat_off, int32_t* piv, const int64_t* piv_off, int32_t* info,
-                                cudaStream_t s) {
+                                cudaStream_t s, const int32_t* skip) {
   size_t sm = (size_t)nmax * NB * sizeof(T) + (size_t)NB * 65 * sizeof(T);
   cudaError_t e = cudaFuncSetAttribute(k_lu<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_lu<T, NB><<<count, 256, sm, s>>>(count, desc, nsz, A, mat_off, piv, piv_off, info);
+  k_lu<T, NB><<<count, 256, sm, s>>>(count, desc, nsz, A, mat_off, piv, piv_off, info, skip);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
-                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s) {
+                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip) {
   if (count <= 0) return cudaSuccess;
   int nb = lu_nb_for<T>(nmax);
-  if (nb == 32) return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s);
-  if (nb == 16) return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s);
-  return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s);
+  if (nb == 32) return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
+  if (nb == 16) return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
+  return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
 }
 
 template <typename T>
 cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, const int64_t* mat_off,
                          const int32_t* piv, const int64_t* piv_off, zc* X, const int64_t* x_off, int nrhs_fixed,
-                         int nrhs_mul, int ldmul, const int32_t* skip, cudaStream_t s) {
+                         int nrhs_mul, int ldmul, const int32_t* skip, cudaStream_t s, const float* rs,
+                         const float* cs) {
   const int nrhs_max = nrhs_fixed > 0 ? nrhs_fixed : nrhs_mul * nmax;
   if (count <= 0 || nrhs_max <= 0) return cudaSuccess;
   const int warps = nrhs_max >= 8 ? 8 : 1;
@@ -276,19 +344,19 @@ cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, c
   if (e != cudaSuccess) return e;
   dim3 g((nrhs_max + warps - 1) / warps, count);
   k_getrs<T><<<g, warps * 32, sm, s>>>(count, nsz, LU, mat_off, piv, piv_off, X, x_off, nrhs_fixed, nrhs_mul, ldmul,
-                                        skip);
+                                        skip, rs, cs);
   return cudaGetLastError();
 }
 
 template cudaError_t launch_lu<zc>(int, const InstDesc*, const int32_t*, int, zc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*);
 template cudaError_t launch_lu<cc>(int, const InstDesc*, const int32_t*, int, cc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*);
 template cudaError_t launch_getrs<zc>(int, const int32_t*, int, const zc*, const int64_t*, const int32_t*,
                                       const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
-                                      cudaStream_t);
+                                      cudaStream_t, const float*, const float*);
 template cudaError_t launch_getrs<cc>(int, const int32_t*, int, const cc*, const int64_t*, const int32_t*,
                                       const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
-                                      cudaStream_t);
+                                      cudaStream_t, const float*, const float*);
 
 }  // namespace stab

@@ -8,7 +8,8 @@ namespace stab {
 // first exactly-zero pivot, 0 if none (ZGETRF's INFO convention).
 template <typename T>
 cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
-                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s);
+                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s,
+                      const int32_t* skip = nullptr);
 // Solve with the factors for complex128 right-hand sides at X + x_off[k]:
 // nrhs = nrhs_fixed if > 0, else nrhs_mul * n; leading dimension ldmul * n.
 // The solve runs in the factor's precision; instances with skip[k] != 0
@@ -16,5 +17,10 @@ cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int n
 template <typename T>
 cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, const int64_t* mat_off,
                          const int32_t* piv, const int64_t* piv_off, zc* X, const int64_t* x_off, int nrhs_fixed,
-                         int nrhs_mul, int ldmul, const int32_t* skip, cudaStream_t s);
+                         int nrhs_mul, int ldmul, const int32_t* skip, cudaStream_t s, const float* rs = nullptr,
+                         const float* cs = nullptr);
+// Power-of-two row/column equilibration of complex64 matrices (scales stored
+// at rs/cs + sc_off[k]); pass the same rs/cs to launch_getrs.
+cudaError_t launch_equilibrate(int count, const int32_t* nsz, cc* A, const int64_t* mat_off, float* rs, float* cs,
+                               const int64_t* sc_off, cudaStream_t s, const int32_t* skip = nullptr);
 }  // namespace stab

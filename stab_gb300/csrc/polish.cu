@@ -96,9 +96,11 @@ __global__ void k_qmv(int count, const InstDesc* __restrict__ desc, const double
 
 // deterministic start vector (hash of the index), so it is not orthogonal to
 // the wanted eigenvector by accident
-__global__ void k_vec_init(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int slot) {
+__global__ void k_vec_init(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int slot,
+                           const int32_t* __restrict__ skip) {
   const int k = blockIdx.y;
   if (k >= count) return;
+  if (skip && skip[k]) return;
   const InstDesc d = desc[k];
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= d.n) return;
@@ -150,9 +152,10 @@ __global__ void k_normalize(int count, const InstDesc* __restrict__ desc, zc* __
 // column p of the complex64 matrix <- vector slot (the bordered Jacobian)
 __global__ void k_set_column(int count, const InstDesc* __restrict__ desc, cc* __restrict__ M,
                              const int64_t* __restrict__ m_off, const int32_t* __restrict__ pcol,
-                             const zc* __restrict__ vec, int slot) {
+                             const zc* __restrict__ vec, int slot, const int32_t* __restrict__ skip) {
   const int k = blockIdx.y;
   if (k >= count) return;
+  if (skip && skip[k]) return;
   const InstDesc d = desc[k];
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= d.n) return;
@@ -174,15 +177,15 @@ __global__ void k_vec_copy(int count, const InstDesc* __restrict__ desc, zc* __r
 
 // Newton-chord update from the correction d (slot dslot):
 // x_j -= d_j (j != p), t -= d_p; converged when |d_p| <= tol |t| and
-// max_j |d_j| <= tol max_j |x_j|.
+// max_j |d_j| <= tol_vec max_j |x_j|.
 __global__ void k_newton_update(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int xslot,
                                 int dslot, const int32_t* __restrict__ pcol, zc* __restrict__ theta,
                                 int32_t* __restrict__ done, double* __restrict__ err, int32_t* __restrict__ iters,
-                                double tol) {
+                                double tol, double tol_vec, const int32_t* __restrict__ skip) {
   __shared__ double red[64];
   const int k = blockIdx.x;
   if (k >= count) return;
-  if (done[k]) return;
+  if (done[k] || (skip && skip[k])) return;
   const InstDesc d = desc[k];
   zc* x = vec + d.off_vec + (int64_t)xslot * d.n;
   const zc* dd = vec + d.off_vec + (int64_t)dslot * d.n;
@@ -216,8 +219,27 @@ __global__ void k_newton_update(int count, const InstDesc* __restrict__ desc, zc
     err[k] = rel;
     iters[k] += 1;
     if (anybad || !isfinite(t.x) || !isfinite(t.y)) done[k] = 3;           // NaN
-    else if (rel <= tol && dmax <= tol * xmax) done[k] = 1;                 // converged
+    else if (rel <= tol && dmax <= tol_vec * xmax) done[k] = 1;             // converged
   }
+}
+
+// theta <- sigma for the instances that run
+__global__ void k_start_shift(int count, const zc* __restrict__ sigma, zc* __restrict__ theta,
+                              const int32_t* __restrict__ skip) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  theta[k] = sigma[k];
+}
+
+// start of a polish round: done = iters = 0 for the instances that run
+__global__ void k_reset_polish(int count, int32_t* __restrict__ done, int32_t* __restrict__ iters,
+                               const int32_t* __restrict__ skip) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  done[k] = 0;
+  iters[k] = 0;
 }
 
 // ---- host launchers --------------------------------------------------------
@@ -232,10 +254,11 @@ cudaError_t launch_qmv(int count, int nmax, const InstDesc* desc, const double* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_vec_init(int count, int nmax, const InstDesc* desc, zc* vec, int slot, cudaStream_t s) {
+cudaError_t launch_vec_init(int count, int nmax, const InstDesc* desc, zc* vec, int slot, cudaStream_t s,
+                            const int32_t* skip) {
   if (count <= 0) return cudaSuccess;
   dim3 g((nmax + 255) / 256, count);
-  k_vec_init<<<g, 256, 0, s>>>(count, desc, vec, slot);
+  k_vec_init<<<g, 256, 0, s>>>(count, desc, vec, slot, skip);
   return cudaGetLastError();
 }
 
@@ -247,10 +270,10 @@ cudaError_t launch_normalize(int count, const InstDesc* desc, zc* vec, int slot,
 }
 
 cudaError_t launch_set_column(int count, int nmax, const InstDesc* desc, cc* M, const int64_t* m_off,
-                              const int32_t* pcol, const zc* vec, int slot, cudaStream_t s) {
+                              const int32_t* pcol, const zc* vec, int slot, cudaStream_t s, const int32_t* skip) {
   if (count <= 0) return cudaSuccess;
   dim3 g((nmax + 255) / 256, count);
-  k_set_column<<<g, 256, 0, s>>>(count, desc, M, m_off, pcol, vec, slot);
+  k_set_column<<<g, 256, 0, s>>>(count, desc, M, m_off, pcol, vec, slot, skip);
   return cudaGetLastError();
 }
 
@@ -263,10 +286,23 @@ cudaError_t launch_vec_copy(int count, int nmax, const InstDesc* desc, zc* vec, 
 }
 
 cudaError_t launch_newton_update(int count, const InstDesc* desc, zc* vec, int xslot, int dslot, const int32_t* pcol,
-                                 zc* theta, int32_t* done, double* err, int32_t* iters, double tol,
-                                 cudaStream_t s) {
+                                 zc* theta, int32_t* done, double* err, int32_t* iters, double tol, double tol_vec,
+                                 cudaStream_t s, const int32_t* skip) {
   if (count <= 0) return cudaSuccess;
-  k_newton_update<<<count, 256, 0, s>>>(count, desc, vec, xslot, dslot, pcol, theta, done, err, iters, tol);
+  k_newton_update<<<count, 256, 0, s>>>(count, desc, vec, xslot, dslot, pcol, theta, done, err, iters, tol, tol_vec,
+                                        skip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_start_shift(int count, const zc* sigma, zc* theta, const int32_t* skip, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_start_shift<<<(count + 255) / 256, 256, 0, s>>>(count, sigma, theta, skip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reset_polish(int count, int32_t* done, int32_t* iters, const int32_t* skip, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_reset_polish<<<(count + 255) / 256, 256, 0, s>>>(count, done, iters, skip);
   return cudaGetLastError();
 }
 

@@ -3,6 +3,9 @@
 //   k_companion_fill   identity / zero lower blocks of the spatial companion
 //                      matrix B0 = [[-C0^-1 C1, -C0^-1 C2], [I, 0]]
 //                      (spatial.f90:1007-1016)
+//   k_take_candidate,  seed rounds of the coarse-shift mode
+//   k_fold_best,
+//   k_take_best
 //   k_post_spectrum    alpha = 1/lambda with lambda = 0 -> 0
 //                      (spatial.f90:1065-1069), ascending stable sort on the
 //                      imaginary part (the PIKSR2 call, temporal.f90:844-855,
@@ -14,15 +17,10 @@
 //                      2-norm with its first max-modulus entry real positive
 //                      (the convention of the ZGEEV call, spatial.f90:1043)
 //
-// Least-stable selection (the reference has none; a user picks the mode with
-// getevec -v).  With k = sqrt(alpha^2 + beta^2) and c_max = 10 (1 + 1/M):
-//   temporal: finite omega, |omega| > 1e-12, |omega| <= c_max max(|k|, 1e-3);
-//             largest Im(omega).
-//   spatial:  finite alpha != 0, Re(alpha) > 0, |Im(alpha)| <= Re(alpha),
-//             |omega/alpha| <= c_max; smallest Im(alpha).
-// Ties go to the lower index of the sorted list.
+// The least-stable selection rule is stated in select.cuh.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "select.cuh"
 
 namespace stab {
 
@@ -43,7 +41,7 @@ __device__ __forceinline__ bool zfinite(zc a) { return isfinite(a.x) && isfinite
 __global__ void k_post_spectrum(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ eig_raw,
                                 const int64_t* __restrict__ eig_off, zc* __restrict__ eig_sorted,
                                 int32_t* __restrict__ least_sorted, zc* __restrict__ least_raw,
-                                zc* __restrict__ least_val) {
+                                zc* __restrict__ least_val, zc* __restrict__ cand, int ncand) {
   extern __shared__ zc ps[];
   __shared__ double bestv[32];
   __shared__ int besti[32];
@@ -72,56 +70,131 @@ __global__ void k_post_spectrum(int count, const InstDesc* __restrict__ desc, co
     out[r] = val[q];
   }
   __syncthreads();
-  // selection on the sorted list
-  const double M = d.Ma;
-  const double cmax = 10.0 * (1.0 + 1.0 / fmax(M, 1e-300));
-  const zc al = zmk(d.ar, d.ai), be = zmk(d.br, d.bi), om = zmk(d.wr, d.wi);
-  const double kabs = fmax(zabs(zsqrt(zadd(zmul(al, al), zmul(be, be)))), 1e-3);
-  double best = -INFINITY;
-  int bi = 0x7fffffff;
-  for (int q = threadIdx.x; q < m; q += blockDim.x) {
-    const zc x = out[q];
-    if (!zfinite(x)) continue;
-    const double ax = zabs(x);
-    double key;
-    if (!spatial) {
-      if (!(ax > 1e-12) || ax > cmax * kabs) continue;
-      key = x.y;
-    } else {
-      if (ax == 0.0 || !(x.x > 0.0) || fabs(x.y) > x.x) continue;
-      if (zabs(zdiv(om, x)) > cmax) continue;
-      key = -x.y;
+  // selection on the sorted list: the least-stable mode, then (for shift
+  // candidates) the next best modes that differ from all earlier picks by
+  // more than 1e-6 relative
+  __shared__ int s_pick[8];
+  const int npass = (cand && ncand > 1) ? (ncand < 8 ? ncand : 8) : 1;
+  for (int pass = 0; pass < npass; ++pass) {
+    double best = -INFINITY;
+    int bi = 0x7fffffff;
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+      const zc x = out[q];
+      double key;
+      if (!least_key(d, x, key)) continue;
+      bool dup = false;
+      for (int pp = 0; pp < pass; ++pp) dup |= zabs(zsub(x, out[s_pick[pp]])) <= 1e-6 * zabs(out[s_pick[pp]]);
+      if (dup) continue;
+      if (key > best || (key == best && q < bi)) { best = key; bi = q; }
     }
-    if (key > best || (key == best && q < bi)) { best = key; bi = q; }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    const double ob = __shfl_down_sync(0xffffffffu, best, o);
-    const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) { bestv[warp] = best; besti[warp] = bi; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
-      if (bestv[w] > best || (bestv[w] == best && besti[w] < bi)) { best = bestv[w]; bi = besti[w]; }
-    if (bi == 0x7fffffff) {
-      least_sorted[k] = -1;
-      least_raw[k] = zmk(nan(""), nan(""));
-      least_val[k] = zmk(nan(""), nan(""));
-    } else {
-      least_sorted[k] = bi;
-      const zc v = out[bi];
-      least_val[k] = v;
-      least_raw[k] = spatial ? zdiv(zmk(1.0, 0.0), v) : v;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { bestv[warp] = best; besti[warp] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+        if (bestv[w] > best || (bestv[w] == best && besti[w] < bi)) { best = bestv[w]; bi = besti[w]; }
+      const bool none = (bi == 0x7fffffff);
+      const zc v = none ? zmk(nan(""), nan("")) : out[bi];
+      const zc raw = none ? v : (spatial ? zdiv(zmk(1.0, 0.0), v) : v);
+      if (pass == 0) {
+        least_sorted[k] = none ? -1 : bi;
+        least_val[k] = v;
+        least_raw[k] = raw;
+      }
+      if (cand) cand[(int64_t)k * ncand + pass] = raw;
+      s_pick[pass] = none ? -1 : bi;
+    }
+    __syncthreads();
+    if (s_pick[pass] < 0) {
+      if (threadIdx.x == 0 && cand)
+        for (int pp = pass + 1; pp < ncand; ++pp) cand[(int64_t)k * ncand + pp] = zmk(nan(""), nan(""));
+      break;
     }
   }
 }
 
-__global__ void k_temporal_vec(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ vec, int slot,
-                               zc* __restrict__ out, const int64_t* __restrict__ out_off) {
+// sigma[k] <- candidate j of instance k
+__global__ void k_take_candidate(int count, const zc* __restrict__ cand, int ncand, int j, zc* __restrict__ sigma) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  sigma[k] = cand[(int64_t)k * ncand + j];
+}
+
+// Fold the result of a polish round into the per-instance best: a pair
+// counts when it converged and passes the selection filter; the less stable
+// one is kept (theta, err, iters and the output vector).  In round 0 a pair
+// within quick_tol of its shift is final: the top coarse candidate is then a
+// resolved mode and later rounds skip the instance.
+__global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ sigma,
+                            const zc* __restrict__ theta, const int32_t* __restrict__ done,
+                            const double* __restrict__ err, const int32_t* __restrict__ iters,
+                            const zc* __restrict__ out, const int64_t* __restrict__ out_off,
+                            int32_t* __restrict__ final_, int32_t* __restrict__ have, double* __restrict__ best_key,
+                            zc* __restrict__ best_theta, double* __restrict__ best_err, int32_t* __restrict__ best_iters,
+                            zc* __restrict__ best_out, int round, double quick_tol) {
+  __shared__ int s_take;
   const int k = blockIdx.x;
   if (k >= count) return;
+  if (final_[k]) return;
+  const InstDesc d = desc[k];
+  if (threadIdx.x == 0) {
+    s_take = 0;
+    const zc t = theta[k];
+    const zc v = (d.itype == 2) ? ((t.x != 0.0 || t.y != 0.0) ? zdiv(zmk(1.0, 0.0), t) : t) : t;
+    double key;
+    if (done[k] == 1 && least_key(d, v, key)) {
+      if (!have[k] || key > best_key[k]) {
+        have[k] = 1;
+        best_key[k] = key;
+        best_theta[k] = t;
+        best_err[k] = err[k];
+        best_iters[k] = iters[k];
+        s_take = 1;
+      }
+      if (round == 0 && zabs(zsub(t, sigma[k])) <= quick_tol * zabs(sigma[k])) final_[k] = 1;
+    }
+  }
+  __syncthreads();
+  if (!s_take) return;
+  const int64_t o = out_off[k];
+  for (int q = threadIdx.x; q < d.m; q += blockDim.x) best_out[o + q] = out[o + q];
+}
+
+// After the rounds: the best pair becomes the result (done = 1); instances
+// without any converged pair get done = 0 for the FP64 fallback.
+__global__ void k_take_best(int count, const InstDesc* __restrict__ desc, const int32_t* __restrict__ have,
+                            const zc* __restrict__ best_theta, const double* __restrict__ best_err,
+                            const int32_t* __restrict__ best_iters, const zc* __restrict__ best_out,
+                            const int64_t* __restrict__ out_off, zc* __restrict__ theta, int32_t* __restrict__ done,
+                            double* __restrict__ err, int32_t* __restrict__ iters, zc* __restrict__ out) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  const InstDesc d = desc[k];
+  if (!have[k]) {
+    if (threadIdx.x == 0) done[k] = 0;
+    return;
+  }
+  if (threadIdx.x == 0) {
+    theta[k] = best_theta[k];
+    done[k] = 1;
+    err[k] = best_err[k];
+    iters[k] = best_iters[k];
+  }
+  const int64_t o = out_off[k];
+  for (int q = threadIdx.x; q < d.m; q += blockDim.x) out[o + q] = best_out[o + q];
+}
+
+__global__ void k_temporal_vec(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ vec, int slot,
+                               zc* __restrict__ out, const int64_t* __restrict__ out_off,
+                               const int32_t* __restrict__ skip) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
   const InstDesc d = desc[k];
   if (d.itype != 1) return;
   const zc* x = vec + d.off_vec + (int64_t)slot * d.n;
@@ -131,13 +204,14 @@ __global__ void k_temporal_vec(int count, const InstDesc* __restrict__ desc, con
 
 __global__ void k_spatial_vec(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ theta,
                               const zc* __restrict__ vec, int slot, zc* __restrict__ out,
-                              const int64_t* __restrict__ out_off) {
+                              const int64_t* __restrict__ out_off, const int32_t* __restrict__ skip) {
   __shared__ double red[32];
   __shared__ int redi[32];
   __shared__ double s_norm;
   __shared__ int s_k;
   const int k = blockIdx.x;
   if (k >= count) return;
+  if (skip && skip[k]) return;
   const InstDesc d = desc[k];
   if (d.itype != 2) return;
   const int n = d.n;

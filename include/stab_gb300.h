@@ -165,6 +165,31 @@ int stab_solve_batch(stab_ctx* ctx, int32_t count, const stab_params* p, const i
                      const double* const* profiles, int32_t mode, const double* seeds,
                      double* eig_out, double* err_out, int32_t* status_out, double* const* vec_out);
 
+/* ---- allocation-free eigenvalues -------------------------------------- */
+#define STAB_NOALLOC_MAX_M 256
+/*
+ * All eigenvalues of one dense m x m complex128 matrix (column-major, device
+ * memory, read only) with the FP64 eigensolver of stab_full_spectrum, without
+ * allocating any device memory.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory when they call, because
+ * another allocator owns the GPU's memory (a framework's caching pool, a
+ * simulation with a fixed budget) or because the device-wide synchronisation
+ * of cudaFree is not acceptable on their path.
+ *   a_dev       m x m input on the device (not modified)
+ *   eig_dev     m complex128 outputs on the device, unsorted: the QR
+ *               eigenvalues first, then those split off by isolation
+ *   status_dev  one int32 on the device: STAB_ST_OK or STAB_ST_NOCONV
+ *   stream      cudaStream_t to launch on (NULL: the legacy default stream)
+ * Limits and sharing: m must be 1..STAB_NOALLOC_MAX_M (larger m returns
+ * STAB_ERR_ARG).  The working matrix lives in one fixed 1 MiB array of the
+ * library on each device (held until the process exits), shared by every
+ * call: calls that overlap on the GPU (different streams, or different host
+ * threads) race and must be serialised by the caller.  The first call on a
+ * device looks up that array's device address, so make it before any stream
+ * capture.  Needs no stab_ctx.
+ */
+int stab_eigvals_noalloc(const double* a_dev, int32_t m, double* eig_dev, int32_t* status_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

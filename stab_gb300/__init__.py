@@ -33,6 +33,7 @@ EXPORTED = (
     "stab_set_profiling", "stab_kernel_stats", "stab_reset_kernel_stats", "stab_assemble",
     "stab_full_spectrum", "stab_batch_create", "stab_batch_set_seeds", "stab_batch_run",
     "stab_batch_results", "stab_batch_work", "stab_batch_destroy", "stab_solve_batch",
+    "stab_eigvals_noalloc",
 )
 
 
@@ -107,6 +108,7 @@ def load(path: str = LIB_PATH):
     lib.stab_batch_results.argtypes = [vp, P(dbl), P(dbl), P(i32), P(i32), P(P(dbl))]
     lib.stab_batch_destroy.argtypes = [vp]
     lib.stab_batch_work.argtypes = [vp, P(dbl)]
+    lib.stab_eigvals_noalloc.argtypes = [vp, i32, vp, vp, vp]
     lib.stab_solve_batch.argtypes = [vp, i32, P(StabParams), P(i32), P(P(dbl)), i32, P(dbl), P(dbl), P(dbl),
                                      P(i32), P(P(dbl))]
     _lib = lib

@@ -26,6 +26,8 @@
 //
 // All arithmetic is FP64.  Every loop has an iteration cap; an instance
 // that hits it gets status STAB_ST_NOCONV and NaN for the missing values.
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "hqr.cuh"
@@ -532,3 +534,83 @@ cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, con
 }
 
 }  // namespace stab
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point (stab_eigvals_noalloc).
+//
+// Some callers cannot allocate device memory at call time: codes whose device
+// memory is entirely owned by another allocator (a framework's caching pool,
+// a simulation that reserves a fixed budget at start-up) and latency-critical
+// loops where the device-wide synchronisation of cudaFree is not acceptable.
+// For them the full-spectrum kernel above runs with its working matrix in a
+// fixed array of this translation unit instead of a pool allocation.  The
+// array is created when the library is loaded and stays resident on every
+// GPU that loads it until the process exits.
+// ---------------------------------------------------------------------------
+namespace stab {
+
+#define STAB_NOALLOC_HEADER_BYTES 256
+static __device__ __align__(256) unsigned char g_noalloc_scratch[STAB_NOALLOC_HEADER_BYTES +
+                                                                 (size_t)STAB_NOALLOC_MAX_M * STAB_NOALLOC_MAX_M *
+                                                                     sizeof(zc)];
+
+// header of the scratch array: the per-instance tables k_eig_plain reads
+struct NoallocHeader {
+  int32_t counter;   // work counter of the persistent loop, must start at 0
+  int32_t m;
+  int64_t a_off, h_off, eig_off;
+};
+
+__global__ void k_noalloc_header(NoallocHeader* h, int m) {
+  h->counter = 0;
+  h->m = m;
+  h->a_off = 0;
+  h->h_off = 0;
+  h->eig_off = 0;
+}
+
+}  // namespace stab
+
+namespace {
+// device address of g_noalloc_scratch per device, looked up once
+struct NoallocSetup {
+  bool done = false;
+  cudaError_t err = cudaSuccess;
+  unsigned char* ptr = nullptr;
+};
+NoallocSetup g_noalloc_setup[64];
+std::mutex g_noalloc_mutex;
+}  // namespace
+
+extern "C" int stab_eigvals_noalloc(const double* a_dev, int32_t m, double* eig_dev, int32_t* status_dev,
+                                    void* stream) {
+  using namespace stab;
+  if (!a_dev || !eig_dev || !status_dev) return STAB_ERR_ARG;
+  if (m < 1 || m > STAB_NOALLOC_MAX_M) return STAB_ERR_ARG;   // the fixed array holds m <= STAB_NOALLOC_MAX_M
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return STAB_ERR_CUDA;
+  NoallocSetup& su = g_noalloc_setup[dev];
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!su.done) {   // first call on this device: resolve the array's device address with the device current
+      void* p = nullptr;
+      su.err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      su.ptr = reinterpret_cast<unsigned char*>(p);
+      su.done = true;
+    }
+  }
+  if (su.err != cudaSuccess || !su.ptr) return STAB_ERR_CUDA;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  NoallocHeader* hdr = reinterpret_cast<NoallocHeader*>(su.ptr);
+  zc* H = reinterpret_cast<zc*>(su.ptr + STAB_NOALLOC_HEADER_BYTES);
+  k_noalloc_header<<<1, 1, 0, s>>>(hdr, m);   // resets the work counter left by the previous call
+  if (cudaGetLastError() != cudaSuccess) return STAB_ERR_CUDA;
+  int64_t qr_elems = 0;
+  const size_t sm = eig_plain_smem(m, &qr_elems);
+  if (cudaFuncSetAttribute(k_eig_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+    return STAB_ERR_CUDA;
+  k_eig_plain<<<1, HQ_T, sm, s>>>(1, &hdr->m, const_cast<zc*>(reinterpret_cast<const zc*>(a_dev)), &hdr->a_off, H,
+                                  &hdr->h_off, reinterpret_cast<zc*>(eig_dev), &hdr->eig_off, status_dev,
+                                  &hdr->counter, nullptr, nullptr, qr_elems);
+  return cudaGetLastError() == cudaSuccess ? STAB_OK : STAB_ERR_CUDA;
+}

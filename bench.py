@@ -40,8 +40,16 @@ METRIC = "converged least-stable modes/sec at |d omega|<=1e-10 (seeded+mixed vs 
 UNIT = "modes/s"
 TOL = 1e-10
 T0_SUTH = 110.4 / 0.3815
-FP64_PEAK_TFLOPS = 1.19   # measured on this machine's GB300 (profiles/fp64_fp32_peak_probe.md)
+FP64_PEAK_TFLOPS = 1.19   # FMA probe on a GB300 (profiles/fp64_fp32_peak_probe.md)
 FP32_PEAK_TFLOPS = 69.9
+# kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
+KERNEL_WORK = {
+    "k_eig_plain": ("eig_fp64", "fp64", "FP64 flops counted by the kernel (Householder reduction + QR sweeps)"),
+    "k_eig_plain_coarse": ("eig_fp64_coarse", "fp64", "FP64 flops counted by the kernel on the N=32 seed batch"),
+    "k_eig_plain_fallback": ("eig_fp64", "fp64", "FP64 flops counted by the kernel on the fallback instances"),
+    "k_lu_c": ("lu_c64", "fp32", "8/3 n^3 real flops per complex64 LU, per factorisation run"),
+    "k_lu_z": ("lu_c128", "fp64", "8/3 n^3 real flops per complex128 LU, per factorisation run"),
+}
 
 
 def workload(count: int, seed: int):
@@ -316,27 +324,22 @@ def main():
 
     value = converged / (ms / 1000.0)
     total = args.count * world
-    # dominant kernel and its roofline
+    # dominant kernel and its roofline; every kernel with counted work gets one
     dom = max(stats.items(), key=lambda kv: kv[1][1])
-    dname, (dl, dms) = dom
-    roof = None
-    if dname in ("k_eig_plain", "k_eig_plain_coarse"):
-        flops = work["eig_fp64_coarse"] if dname == "k_eig_plain_coarse" else work["eig_fp64"]
-        ach = flops / (dms / 1000.0) / 1e12 if dms else 0.0   # flops and ms of the same launches
-        roof = {"bound": "fp64", "achieved": ach, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                "frac": ach / FP64_PEAK_TFLOPS, "traffic": None, "kernel": dname,
-                "algorithmic": "FP64 flops counted by the kernel (Householder reduction + QR sweeps)",
-                "peak_source": "FMA probe on this pool's GB300 (MEASURED_PEAKS.json has no FP64 entry)"}
-    elif dname == "k_lu_c":
-        per = work["lu_c64"] / dl
-        ach = per / (dms / dl / 1000.0) / 1e12
-        roof = {"bound": "fp32", "achieved": ach, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
-                "frac": ach / FP32_PEAK_TFLOPS, "traffic": None, "kernel": dname,
-                "algorithmic": "8/3 n^3 real flops per complex LU",
-                "peak_source": "FMA probe on this pool's GB300"}
-    else:
-        roof = {"bound": "unknown", "kernel": dname, "achieved": None, "peak": None, "unit": None, "frac": None,
-                "traffic": None}
+    dname = dom[0]
+    rooflines = {}
+    for kname, (kl, kms) in stats.items():
+        if kname not in KERNEL_WORK or kms <= 0:
+            continue
+        wkey, bound, note = KERNEL_WORK[kname]
+        peak = FP64_PEAK_TFLOPS if bound == "fp64" else FP32_PEAK_TFLOPS
+        ach = work[wkey] / (kms / 1000.0) / 1e12    # flops and time of the same launches
+        rooflines[kname] = {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                            "frac": ach / peak, "traffic": None, "kernel": kname, "launches": kl,
+                            "ms": kms, "algorithmic": note,
+                            "peak_source": "FMA probe on a GB300 of the same kind (profiles/fp64_fp32_peak_probe.md)"}
+    roof = rooflines.get(dname, {"bound": "unknown", "kernel": dname, "achieved": None, "peak": None,
+                                 "unit": None, "frac": None, "traffic": None})
     h2d = int(prof.nbytes + len(sp) * 120 + len(sp) * 4)
     d2h = int(len(sp) * (16 + 8 + 4 + 4))
     line = {
@@ -354,6 +357,7 @@ def main():
         "plain_fp64": {"value": total / (plain_ms / 1000.0), "unit": UNIT, "ms_per_step": plain_ms,
                        "speedup_seeded_over_plain": value / (total / (plain_ms / 1000.0))},
         "roofline": roof,
+        "kernel_rooflines": rooflines,
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in sorted(stats.items(),
                                                                                key=lambda kv: -kv[1][1])},
         "gpu_launches": int(launches_per_step * args.steps),

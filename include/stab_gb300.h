@@ -153,9 +153,10 @@ int stab_batch_results(stab_batch* b, double* eig_out, double* err_out, int32_t*
 /*
  * Algorithmic work of the last stab_batch_run, for roofline accounting:
  * work_out[0] FP64 flops executed by the full-spectrum eigensolver (plain
- * mode), [1] the same for the N = 32 seed batch (coarse mode), [2] complex64
- * LU flops of the polish (2 x 8/3 n^3 per instance), [3] complex128 LU flops
- * of the plain path's eigenvector step (8/3 n^3 per instance).
+ * mode: every instance; seeded and coarse modes: the fallback instances),
+ * [1] the same for the N = 32 seed batch (coarse mode), [2] complex64 LU
+ * flops of the polish and [3] complex128 LU flops (8/3 n^3 real flops per
+ * factorisation, counted per instance as run, fallback included).
  */
 int stab_batch_work(stab_batch* b, double* work_out);
 int stab_batch_destroy(stab_batch* b);

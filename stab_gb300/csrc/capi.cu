@@ -5,6 +5,7 @@
 // first and all spatial ones after (stable), so each phase launches on
 // contiguous ranges; results are mapped back to the caller's order.
 #include <algorithm>
+#include <type_traits>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -26,6 +27,9 @@ static const int kShiftCandidates = 4;
 // a polished eigenvalue within this relative distance of the top coarse
 // candidate is final after the first round (the coarse mode is resolved)
 static const double kQuickAcceptTol = 1e-7;
+// a complex64 polish that needed this many Newton-chord steps or more is
+// retried with complex128 factors (slow contraction: an unresolved cluster)
+static const int kSlowNewton = 7;
 
 namespace {
 
@@ -183,7 +187,7 @@ struct stab_batch {
   DevBuf desc, dtab, pdesc, prof, spl, node, blk, ops, vec;
   DevBuf nsz, msz, off_n2, off_m2, off_m2c2, off_nof, off_mof, xoff[VEC_SLOTS], order;
   DevBuf M32, Z64, Abig, Hbig, eigraw, eigsorted, outvec;
-  DevBuf bad, flops, rsc, csc, cand, accepted, have, best_key, best_theta, best_err, best_iters, best_out;
+  DevBuf bad, flops, rsc, csc, cand, accepted, skip64, lus32, lus64, have, best_key, best_theta, best_err, best_iters, best_out;
   DevBuf piv, info, flags, theta, sigma, least_raw, least_val, least_idx, pcol, done, err, iters, status, counter;
   int nprof = 0;
   bool have_seeds = false;
@@ -192,6 +196,7 @@ struct stab_batch {
   bool ran = false;
   // instances re-solved by the plain FP64 path after a failed polish
   std::vector<int> fell_back;                 // internal indices
+  double fb_work[2] = {0.0, 0.0};             // fallback sub-batch: eigensolver flops, complex128 LU flops
   std::vector<zc> fb_val;
   std::vector<int32_t> fb_status;
   std::vector<std::vector<zc>> fb_vec;
@@ -201,7 +206,7 @@ struct stab_batch {
   void release() {
     DevBuf* all[] = {&desc, &dtab, &pdesc, &prof, &spl, &node, &blk, &ops, &vec, &nsz, &msz, &off_n2, &off_m2,
                      &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
-                     &bad, &flops, &rsc, &csc, &cand, &accepted, &have, &best_key, &best_theta, &best_err,
+                     &bad, &flops, &rsc, &csc, &cand, &accepted, &skip64, &lus32, &lus64, &have, &best_key, &best_theta, &best_err,
                      &best_iters, &best_out, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
                      &done, &err, &iters, &status, &counter};
     for (DevBuf* d : all) {
@@ -392,6 +397,8 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   CK(c, b->status.ensure(I4, c->stream));
   CK(c, b->err.ensure(sizeof(double) * count, c->stream));
   CK(c, b->flops.ensure(sizeof(double) * count, c->stream));
+  CK(c, b->lus32.ensure(I4, c->stream));
+  CK(c, b->lus64.ensure(I4, c->stream));
   CK(c, b->rsc.ensure(sizeof(float) * b->sum_n, c->stream));
   CK(c, b->csc.ensure(sizeof(float) * b->sum_n, c->stream));
   CK(c, b->cand.ensure(Z * kShiftCandidates, c->stream));
@@ -601,12 +608,26 @@ static const int kNewtonSteps = 10;
 static const double kNewtonTol = 1e-13;      // |d theta| / |theta| of the last Newton-chord step
 static const double kNewtonTolVec = 1e-11;   // max |d x| / max |x|
 
-static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullptr) {
+// The polish with factors in precision T: complex64 (the fast path) or
+// complex128 (separates eigenvalue clusters closer than complex64 resolves).
+template <typename T>
+static T* polish_pool(stab_batch* b);
+template <>
+cc* polish_pool<cc>(stab_batch* b) { return b->M32.as<cc>(); }
+template <>
+zc* polish_pool<zc>(stab_batch* b) { return b->Z64.as<zc>(); }
+
+template <typename T>
+static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
+  const bool c64 = std::is_same<T, cc>::value;
+  const char* n_dense = c64 ? "k_dense_c" : "k_dense_z";
+  const char* n_lu = c64 ? "k_lu_c" : "k_lu_z";
+  const char* n_getrs = c64 ? "k_getrs_c" : "k_getrs_z";
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   const Range all{0, b->count};
   const InstDesc* D = b->desc.as<InstDesc>();
-  const double* const* T = b->dtab.as<const double*>();
+  const double* const* DT = b->dtab.as<const double*>();
   zc* V = b->vec.as<zc>();
   int32_t* done = b->done.as<int32_t>();
   CK(c, timed(c, "k_start_shift", [&] {
@@ -614,29 +635,35 @@ static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullpt
   }));
   int rc = node_ops(b, all, OP_T_Q, OP_S_Q, b->theta.as<zc>(), skip);
   if (rc) return rc;
-  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c", skip);
+  if (!c64) CK(c, b->Z64.ensure(sizeof(zc) * b->sum_n2, s));
+  T* MP = polish_pool<T>(b);
+  rc = dense<T>(b, all, MP, b->off_n2.as<int64_t>(), 1, 1.0, n_dense, skip);
   if (rc) return rc;
+  const float* rs = c64 ? b->rsc.as<float>() : nullptr;
+  const float* cs = c64 ? b->csc.as<float>() : nullptr;
   auto lu32 = [&]() {
-    cudaError_t e = timed(c, "k_equilibrate", [&] {
-      return launch_equilibrate(b->count, b->nsz.as<int32_t>(), b->M32.as<cc>(), b->off_n2.as<int64_t>(),
-                                b->rsc.as<float>(), b->csc.as<float>(), b->off_nof.as<int64_t>(), s, skip);
-    });
-    if (e != cudaSuccess) return e;
-    return timed(c, "k_lu_c", [&] {
-      return launch_lu<cc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
-                           b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip);
+    if (c64) {
+      cudaError_t e = timed(c, "k_equilibrate", [&] {
+        return launch_equilibrate(b->count, b->nsz.as<int32_t>(), b->M32.as<cc>(), b->off_n2.as<int64_t>(),
+                                  b->rsc.as<float>(), b->csc.as<float>(), b->off_nof.as<int64_t>(), s, skip);
+      });
+      if (e != cudaSuccess) return e;
+    }
+    return timed(c, n_lu, [&] {
+      return launch_lu<T>(b->count, D, b->nsz.as<int32_t>(), b->nmax, MP, b->off_n2.as<int64_t>(),
+                          b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip);
     });
   };
   auto solve32 = [&](int slot, const int32_t* sk) {
-    return timed(c, "k_getrs_c", [&] {
-      return launch_getrs<cc>(b->count, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
-                              b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V, b->xoff[slot].as<int64_t>(), 1, 0, 1,
-                              sk, s, b->rsc.as<float>(), b->csc.as<float>());
+    return timed(c, n_getrs, [&] {
+      return launch_getrs<T>(b->count, b->nsz.as<int32_t>(), b->nmax, MP, b->off_n2.as<int64_t>(),
+                             b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V, b->xoff[slot].as<int64_t>(), 1, 0, 1,
+                             sk, s, rs, cs);
     });
   };
   auto qmv = [&](int deriv, int xs, int ys, const int32_t* sk) {
     return timed(c, "k_qmv", [&] {
-      return launch_qmv(b->count, b->nmax, D, T, b->blk.as<zc>(), b->theta.as<zc>(), deriv, V, xs, ys, sk, s);
+      return launch_qmv(b->count, b->nmax, D, DT, b->blk.as<zc>(), b->theta.as<zc>(), deriv, V, xs, ys, sk, s);
     });
   };
   CK(c, lu32());
@@ -649,14 +676,17 @@ static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullpt
   }
   // bordered Jacobian at (sigma, x): Q(sigma) with column p <- Q'(sigma) x
   CK(c, qmv(1, 0, 2, skip));
-  rc = dense<cc>(b, all, b->M32.as<cc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_c", skip);
+  rc = dense<T>(b, all, MP, b->off_n2.as<int64_t>(), 1, 1.0, n_dense, skip);
   if (rc) return rc;
   CK(c, timed(c, "k_set_column", [&] {
-    return launch_set_column(b->count, b->nmax, D, b->M32.as<cc>(), b->off_n2.as<int64_t>(), b->pcol.as<int32_t>(), V,
-                             2, s, skip);
+    return launch_set_column<T>(b->count, b->nmax, D, MP, b->off_n2.as<int64_t>(), b->pcol.as<int32_t>(), V, 2, s,
+                                skip);
   }));
   CK(c, lu32());
-  CK(c, timed(c, "k_reset_polish", [&] { return launch_reset_polish(b->count, done, b->iters.as<int32_t>(), skip, s); }));
+  CK(c, timed(c, "k_reset_polish", [&] {
+    return launch_reset_polish(b->count, done, b->iters.as<int32_t>(), skip, s,
+                               c64 ? b->lus32.as<int32_t>() : b->lus64.as<int32_t>(), 2);
+  }));
   // Newton-chord steps; converged instances (done != 0) drop out
   for (int it = 0; it < kNewtonSteps; ++it) {
     CK(c, qmv(0, 0, 3, done));
@@ -676,6 +706,65 @@ static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullpt
   return 0;
 }
 
+// Complex128 retry: fixed-shift inverse iteration on one complex128 LU of
+// Q(sigma).  The eigenvalue estimate sigma - x_p / y_p converges with the
+// ratio |sigma - lambda_1| / |sigma - lambda_2| per step, which separates
+// mode clusters that complex64 factors cannot resolve.
+static const int kInverseSteps = 12;
+static const double kInverseTol = 1e-13;
+
+static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const Range all{0, b->count};
+  const InstDesc* D = b->desc.as<InstDesc>();
+  zc* V = b->vec.as<zc>();
+  int32_t* done = b->done.as<int32_t>();
+  CK(c, b->Z64.ensure(sizeof(zc) * b->sum_n2, s));
+  CK(c, timed(c, "k_start_shift", [&] {
+    return launch_start_shift(b->count, b->sigma.as<zc>(), b->theta.as<zc>(), skip, s);
+  }));
+  int rc = node_ops(b, all, OP_T_Q, OP_S_Q, b->sigma.as<zc>(), skip);
+  if (rc) return rc;
+  rc = dense<zc>(b, all, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z", skip);
+  if (rc) return rc;
+  CK(c, timed(c, "k_lu_z", [&] {
+    return launch_lu<zc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
+                         b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip);
+  }));
+  CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
+  CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, b->pcol.as<int32_t>(), skip, s); }));
+  CK(c, timed(c, "k_reset_polish", [&] {
+    return launch_reset_polish(b->count, done, b->iters.as<int32_t>(), skip, s, b->lus64.as<int32_t>(), 1);
+  }));
+  for (int it = 0; it < kInverseSteps; ++it) {
+    CK(c, timed(c, "k_qmv", [&] {
+      return launch_qmv(b->count, b->nmax, D, b->dtab.as<const double*>(), b->blk.as<zc>(), b->sigma.as<zc>(), 1, V,
+                        0, 1, done, s);
+    }));
+    CK(c, timed(c, "k_getrs_z", [&] {
+      return launch_getrs<zc>(b->count, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
+                              b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V, b->xoff[1].as<int64_t>(), 1, 0, 1,
+                              done, s);
+    }));
+    CK(c, timed(c, "k_ii_update", [&] {
+      return launch_ii_update(b->count, D, V, 0, 1, b->pcol.as<int32_t>(), b->sigma.as<zc>(), b->theta.as<zc>(), done,
+                              b->err.as<double>(), b->iters.as<int32_t>(), kInverseTol, skip, s);
+    }));
+  }
+  CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, nullptr, skip, s); }));
+  CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * b->count, cudaMemcpyDeviceToDevice, s));
+  if (want_vec) {
+    rc = write_vectors(b, all, b->theta.as<zc>(), skip);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullptr) {
+  return run_polish_t<cc>(b, want_vec, skip);
+}
+
 // host-side: status from `done` and NaN checks; theta -> eigenvalue
 static void finalize_polish_host(std::vector<zc>& val, std::vector<int32_t>& st, const std::vector<int32_t>& dn,
                                  const std::vector<stab_params>& P) {
@@ -693,6 +782,7 @@ static int batch_run(stab_batch* b, int32_t mode) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   b->fell_back.clear();
+  b->fb_work[0] = b->fb_work[1] = 0.0;
   b->last_mode = mode;
   int rc = run_prep(b);
   if (rc) return rc;
@@ -878,16 +968,20 @@ static int coarse_seeds(stab_batch* b) {
 // Coarse-shift rounds.  Each polished pair is an eigenpair of the fine
 // problem, so the least-stable of the converged pairs over the top coarse
 // candidates is the answer whenever one candidate sits near the fine
-// least-stable mode (N = 32 can carry unresolved modes above it at M > 1.4,
-// and can resolve the right one only to ~1e-2).  Round 0 takes the top
-// candidate; when its polish lands within kQuickAcceptTol of the shift the
-// instance is final, otherwise the next candidates are polished too.
-// Instances with no converged pair go to the FP64 fallback.
+// least-stable mode.  N = 32 carries unresolved modes above it at M > 1.4
+// and spurious acoustic ones at M < 0.03, and resolves the right one only
+// to ~1e-2.  Each candidate gets a complex64 round, and a complex128 retry
+// where that failed or contracted slowly (a mode cluster closer than
+// complex64 factors resolve).  When the top candidate's polish lands within
+// kQuickAcceptTol of its shift the instance is final; otherwise the next
+// candidates are polished too.  Instances with no converged pair go to the
+// FP64 full-spectrum fallback.
 static int polish_candidate_rounds(stab_batch* b) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   const int n = b->count;
   CK(c, b->have.ensure(sizeof(int32_t) * n, s));
+  CK(c, b->skip64.ensure(sizeof(int32_t) * n, s));
   CK(c, b->best_key.ensure(sizeof(double) * n, s));
   CK(c, b->best_theta.ensure(sizeof(zc) * n, s));
   CK(c, b->best_err.ensure(sizeof(double) * n, s));
@@ -895,20 +989,29 @@ static int polish_candidate_rounds(stab_batch* b) {
   CK(c, b->best_out.ensure(sizeof(zc) * b->sum_m, s));
   int32_t* fin = b->accepted.as<int32_t>();
   CK(c, cudaMemsetAsync(fin, 0, sizeof(int32_t) * n, s));
+  CK(c, cudaMemsetAsync(b->lus32.p, 0, sizeof(int32_t) * n, s));
+  CK(c, cudaMemsetAsync(b->lus64.p, 0, sizeof(int32_t) * n, s));
   CK(c, cudaMemsetAsync(b->have.p, 0, sizeof(int32_t) * n, s));
-  for (int j = 0; j < kShiftCandidates; ++j) {
-    CK(c, timed(c, "k_take_candidate", [&] {
-      k_take_candidate<<<(n + 255) / 256, 256, 0, s>>>(n, b->cand.as<zc>(), kShiftCandidates, j, b->sigma.as<zc>());
-      return cudaGetLastError();
-    }));
-    int rc = run_polish(b, true, fin);
+  // per candidate: a complex64 round, then a complex128 retry for the
+  // instances where it failed or contracted slowly
+  for (int r = 0; r < 2 * kShiftCandidates; ++r) {
+    const int j = r / 2;
+    const bool fp64 = (r & 1) != 0;
+    if (!fp64) {
+      CK(c, timed(c, "k_take_candidate", [&] {
+        k_take_candidate<<<(n + 255) / 256, 256, 0, s>>>(n, b->cand.as<zc>(), kShiftCandidates, j, b->sigma.as<zc>());
+        return cudaGetLastError();
+      }));
+    }
+    int rc = fp64 ? run_polish64_ii(b, true, b->skip64.as<int32_t>()) : run_polish_t<cc>(b, true, fin);
     if (rc) return rc;
     CK(c, timed(c, "k_fold_best", [&] {
       k_fold_best<<<n, 128, 0, s>>>(n, b->desc.as<InstDesc>(), b->sigma.as<zc>(), b->theta.as<zc>(),
                                     b->done.as<int32_t>(), b->err.as<double>(), b->iters.as<int32_t>(),
                                     b->outvec.as<zc>(), b->off_mof.as<int64_t>(), fin, b->have.as<int32_t>(),
                                     b->best_key.as<double>(), b->best_theta.as<zc>(), b->best_err.as<double>(),
-                                    b->best_iters.as<int32_t>(), b->best_out.as<zc>(), j, kQuickAcceptTol);
+                                    b->best_iters.as<int32_t>(), b->best_out.as<zc>(), j == 0 ? 1 : 0,
+                                    kQuickAcceptTol, fp64 ? nullptr : b->skip64.as<int32_t>(), kSlowNewton);
       return cudaGetLastError();
     }));
   }
@@ -933,6 +1036,7 @@ static int run_fallback(stab_batch* b) {
   CK(c, cudaMemcpyAsync(dn.data(), b->done.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   b->fell_back.clear();
+  b->fb_work[0] = b->fb_work[1] = 0.0;
   b->fb_val.clear();
   b->fb_status.clear();
   b->fb_vec.clear();
@@ -972,6 +1076,14 @@ static int run_fallback(stab_batch* b) {
                           cudaMemcpyDeviceToHost, c->stream));
   }
   CK(c, cudaStreamSynchronize(c->stream));
+  {
+    std::vector<double> f(nf);
+    CK(c, cudaMemcpy(f.data(), fb->flops.p, sizeof(double) * nf, cudaMemcpyDeviceToHost));
+    for (int q = 0; q < nf; ++q) {
+      b->fb_work[0] += f[q];
+      b->fb_work[1] += (8.0 / 3.0) * (double)fb->hn[q] * fb->hn[q] * fb->hn[q];
+    }
+  }
   // the sub-batch orders its instances temporal-first internally; map back
   b->fb_val.assign(b->fell_back.size(), zmk(0, 0));
   b->fb_status.assign(b->fell_back.size(), 0);
@@ -1081,17 +1193,26 @@ int stab_batch_work(stab_batch* b, double* work_out) {
     for (double v : f) t += v;
     return t;
   };
-  double lu_c = 0.0;
-  const double nlu = (b->last_mode == STAB_MODE_COARSE) ? 4.0 : 2.0;   // two LUs per polish, two polishes in coarse
-  for (int n : b->hn) lu_c += nlu * (8.0 / 3.0) * (double)n * n * n;
   const bool plain = (b->last_mode == STAB_MODE_PLAIN);
-  work_out[0] = plain ? eig_flops(b) : 0.0;
+  std::vector<int32_t> l32(b->count, 0), l64(b->count, 0);
+  if (!plain) {
+    if (b->last_mode == STAB_MODE_COARSE) {
+      cudaMemcpy(l32.data(), b->lus32.p, sizeof(int32_t) * b->count, cudaMemcpyDeviceToHost);
+      cudaMemcpy(l64.data(), b->lus64.p, sizeof(int32_t) * b->count, cudaMemcpyDeviceToHost);
+    } else {
+      for (auto& v : l32) v = 2;
+    }
+  }
+  double lu_c = 0.0, lu_z = 0.0;
+  for (int k = 0; k < b->count; ++k) {
+    const double n3 = (double)b->hn[k] * b->hn[k] * b->hn[k];
+    lu_c += l32[k] * (8.0 / 3.0) * n3;
+    lu_z += (plain ? 1 : l64[k]) * (8.0 / 3.0) * n3;
+  }
+  work_out[0] = (plain ? eig_flops(b) : 0.0) + b->fb_work[0];
   work_out[1] = (b->last_mode == STAB_MODE_COARSE && b->coarse) ? eig_flops(b->coarse) : 0.0;
-  work_out[2] = plain ? 0.0 : lu_c;
-  double lu_z = 0.0;
-  if (plain)
-    for (int n : b->hn) lu_z += (8.0 / 3.0) * (double)n * n * n;
-  work_out[3] = lu_z;
+  work_out[2] = lu_c;
+  work_out[3] = lu_z + b->fb_work[1];
   return STAB_OK;
 }
 

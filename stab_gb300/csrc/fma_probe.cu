@@ -1,5 +1,6 @@
-// Throughput probe for the roofline denominators that MEASURED_PEAKS lacks:
-// FP64 and FP32 FMA issue rates (8 independent FMA chains per thread).
+// Throughput probe for the FP64 and FP32 roofline denominators (the measured
+// copy and bf16 GEMM peaks do not cover them): FMA issue rates with 8
+// independent FMA chains per thread.
 // Build and run: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -o fma_probe fma_probe.cu && ./fma_probe
 #include <cstdio>
 #include <cuda_runtime.h>

@@ -20,9 +20,11 @@
 // scalar work is repeated across threads.  The thread that updates the
 // 2x2/3x2 corner of a bulge step also forms the next step's reflector and
 // publishes it through a double-buffered shared slot: one barrier per bulge
-// step.  When the Hessenberg matrix (packed by columns with two
-// subdiagonals, for the bulge) fits in shared memory -- the N = 32 seed
-// problems do -- the sweeps run there instead of in global memory.
+// step.  The corner is a serial chain of FP64 instructions, so the kernel
+// runs small CTAs, several per SM, letting the chains of different
+// instances overlap; the Hessenberg matrix is repacked in place into a
+// column-packed layout with two subdiagonals (room for the bulge), which
+// keeps the working set of the resident instances in L2.
 //
 // All arithmetic is FP64.  Every loop has an iteration cap; an instance
 // that hits it gets status STAB_ST_NOCONV and NaN for the missing values.
@@ -34,7 +36,7 @@
 
 namespace stab {
 
-#define HQ_T 256
+#define HQ_T 128
 #define HQ_W (HQ_T / 32)
 
 struct Refl {
@@ -93,26 +95,30 @@ struct SAcc {
   __device__ __forceinline__ zc& operator()(int r, int c) const { return S[hess_coff(c, mp) + r]; }
 };
 
-// 2-element reflector (as ZLARFG): (v1, v2) -> (beta, 0)
+// 2-element reflector (as ZLARFG): (v1, v2) -> (beta, 0).  One square root
+// and two reciprocals: FP64 division and square root are multi-instruction
+// sequences, and this sits on the serial path of every bulge step.
 __device__ __forceinline__ Refl make_refl(zc v1, zc v2) {
   Refl f;
   f.v1r = v1.x;
   f.v1i = v1.y;
-  const double xn = zabs(v2);
-  if (xn == 0.0 && v1.y == 0.0) {
+  const double n2 = v2.x * v2.x + v2.y * v2.y;
+  if (n2 == 0.0 && v1.y == 0.0) {
     f.ident = 1;
     f.tr = f.ti = f.ur = f.ui = 0.0;
     f.beta = v1.x;
     return f;
   }
   f.ident = 0;
-  const double beta = -copysign(sqrt(v1.x * v1.x + v1.y * v1.y + xn * xn), v1.x);
+  const double beta = -copysign(sqrt(fma(v1.x, v1.x, fma(v1.y, v1.y, n2))), v1.x);
+  const double ib = 1.0 / beta;
   f.beta = beta;
-  f.tr = (beta - v1.x) / beta;
-  f.ti = -v1.y / beta;
-  const zc u2 = zdiv(v2, zmk(v1.x - beta, v1.y));
-  f.ur = u2.x;
-  f.ui = u2.y;
+  f.tr = (beta - v1.x) * ib;
+  f.ti = -v1.y * ib;
+  const double dr = v1.x - beta, di = v1.y;                // u2 = v2 / (v1 - beta)
+  const double idd = 1.0 / fma(dr, dr, di * di);
+  f.ur = fma(v2.x, dr, v2.y * di) * idd;
+  f.ui = fma(v2.y, dr, -v2.x * di) * idd;
   return f;
 }
 
@@ -274,12 +280,12 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
   return st;
 }
 
-__global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
+__global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
                                                    const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
                                                    const int64_t* __restrict__ h_off, zc* __restrict__ eig,
                                                    const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
                                                    int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
-                                                   double* __restrict__ flops_out, int64_t smem_qr_elems) {
+                                                   double* __restrict__ flops_out) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ HqrSmem s;
   __shared__ int s_inst;
@@ -294,8 +300,7 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
     zc* M = A + a_off[inst];
     zc* Hg = Hp + h_off[inst];
     zc* ev = eig + eig_off[inst];
-    // shared scratch: active flags and act list (m ints each), then either
-    // v, w, z (Hessenberg phase) or the packed matrix (QR phase)
+    // shared scratch: active flags and act list (m ints each), then v, w, z
     int* active = reinterpret_cast<int*>(smraw);
     int* act = active + m;
     zc* zs = reinterpret_cast<zc*>(smraw + ((2 * (size_t)m * sizeof(int) + 15) / 16) * 16);
@@ -471,22 +476,19 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
       }
       __syncthreads();
     }
-    // ---- 5. QR iteration ----------------------------------------------------
-    int st;
-    if (hess_packed_size(mp) <= smem_qr_elems) {
-      SAcc S{zs, mp};
-      for (int c = warp; c < mp; c += HQ_W) {
-        const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
-        for (int r = lane; r <= rmax; r += 32) S(r, c) = (r <= c + 1) ? Hg[(size_t)c * ld + r] : zmk(0.0, 0.0);
-      }
+    // ---- 5. QR iteration on the packed matrix ---------------------------------
+    // in-place repack of H (ld = mp) to the column-packed layout: a packed
+    // offset never exceeds the unpacked one, so moving column by column in
+    // increasing order through shared memory is safe
+    for (int c = 0; c < mp; ++c) {
+      const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
+      for (int r = tid; r <= rmax; r += HQ_T) v[r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : zmk(0.0, 0.0);
       __syncthreads();
-      st = qr_eigs(S, mp, ev, s, flops);
-    } else {
-      GAcc G{Hg, ld};
-      for (int c = tid; c + 2 < mp; c += HQ_T) Hg[(size_t)c * ld + c + 2] = zmk(0.0, 0.0);
+      const int64_t o = hess_coff(c, mp);
+      for (int r = tid; r <= rmax; r += HQ_T) Hg[o + r] = v[r];
       __syncthreads();
-      st = qr_eigs(G, mp, ev, s, flops);
     }
+    int st = qr_eigs(SAcc{Hg, mp}, mp, ev, s, flops);
     if (tid == 0) {
       status[inst] = st;
       if (flops_out) flops_out[inst] = flops;
@@ -495,17 +497,9 @@ __global__ void __launch_bounds__(HQ_T) k_eig_plain(int count, const int32_t* __
   }
 }
 
-size_t eig_plain_smem(int mmax, int64_t* qr_elems) {
+size_t eig_plain_smem(int mmax) {
   const size_t head = ((2 * (size_t)mmax * sizeof(int) + 15) / 16) * 16;
-  const size_t vwz = 3 * (size_t)mmax * sizeof(zc);
-  const size_t cap = 220 * 1024;   // leave room for the static shared state
-  const size_t packed = (size_t)hess_packed_size(mmax) * sizeof(zc);
-  if (head + packed <= cap) {
-    if (qr_elems) *qr_elems = hess_packed_size(mmax);
-    return head + (packed > vwz ? packed : vwz);
-  }
-  if (qr_elems) *qr_elems = 0;
-  return head + vwz;
+  return head + 3 * (size_t)mmax * sizeof(zc);
 }
 
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
@@ -513,8 +507,7 @@ cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, con
                              int32_t* work_counter, const int32_t* order, double* flops, int grid,
                              cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  int64_t qr_elems = 0;
-  size_t sm = eig_plain_smem(mmax, &qr_elems);
+  size_t sm = eig_plain_smem(mmax);
   cudaError_t e = cudaFuncSetAttribute(k_eig_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(work_counter, 0, sizeof(int32_t), s);
@@ -529,7 +522,7 @@ cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, con
   if (grid <= 0 || grid > resident) grid = resident;
   if (grid > count) grid = count;
   k_eig_plain<<<grid, HQ_T, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter, order,
-                                     flops, qr_elems);
+                                     flops);
   return cudaGetLastError();
 }
 
@@ -605,12 +598,11 @@ extern "C" int stab_eigvals_noalloc(const double* a_dev, int32_t m, double* eig_
   zc* H = reinterpret_cast<zc*>(su.ptr + STAB_NOALLOC_HEADER_BYTES);
   k_noalloc_header<<<1, 1, 0, s>>>(hdr, m);   // resets the work counter left by the previous call
   if (cudaGetLastError() != cudaSuccess) return STAB_ERR_CUDA;
-  int64_t qr_elems = 0;
-  const size_t sm = eig_plain_smem(m, &qr_elems);
+  const size_t sm = eig_plain_smem(m);
   if (cudaFuncSetAttribute(k_eig_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
     return STAB_ERR_CUDA;
   k_eig_plain<<<1, HQ_T, sm, s>>>(1, &hdr->m, const_cast<zc*>(reinterpret_cast<const zc*>(a_dev)), &hdr->a_off, H,
                                   &hdr->h_off, reinterpret_cast<zc*>(eig_dev), &hdr->eig_off, status_dev,
-                                  &hdr->counter, nullptr, nullptr, qr_elems);
+                                  &hdr->counter, nullptr, nullptr);
   return cudaGetLastError() == cudaSuccess ? STAB_OK : STAB_ERR_CUDA;
 }

@@ -3,9 +3,8 @@
 #include "common.cuh"
 
 namespace stab {
-// dynamic shared memory of k_eig_plain; qr_elems receives the packed QR
-// capacity (0 when the sweeps run in global memory)
-size_t eig_plain_smem(int mmax, int64_t* qr_elems);
+// dynamic shared memory of k_eig_plain
+size_t eig_plain_smem(int mmax);
 // A: count column-major m x m matrices (destroyed); H: workspace of the same
 // size; eig receives m eigenvalues per instance (QR eigenvalues first, then
 // the isolated ones); status[k] = 0 or STAB_ST_NOCONV.  `order` (may be null)

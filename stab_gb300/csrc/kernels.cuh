@@ -58,7 +58,8 @@ __global__ void k_take_candidate(int count, const zc* cand, int ncand, int j, zc
 __global__ void k_fold_best(int count, const InstDesc* desc, const zc* sigma, const zc* theta, const int32_t* done,
                             const double* err, const int32_t* iters, const zc* out, const int64_t* out_off,
                             int32_t* final_, int32_t* have, double* best_key, zc* best_theta, double* best_err,
-                            int32_t* best_iters, zc* best_out, int round, double quick_tol);
+                            int32_t* best_iters, zc* best_out, int quick, double quick_tol, int32_t* skip64,
+                            int slow_iters);
 __global__ void k_take_best(int count, const InstDesc* desc, const int32_t* have, const zc* best_theta,
                             const double* best_err, const int32_t* best_iters, const zc* best_out,
                             const int64_t* out_off, zc* theta, int32_t* done, double* err, int32_t* iters, zc* out);

@@ -149,8 +149,9 @@ __global__ void k_normalize(int count, const InstDesc* __restrict__ desc, zc* __
   for (int q = threadIdx.x; q < d.n; q += blockDim.x) x[q] = zdiv(x[q], sc);
 }
 
-// column p of the complex64 matrix <- vector slot (the bordered Jacobian)
-__global__ void k_set_column(int count, const InstDesc* __restrict__ desc, cc* __restrict__ M,
+// column p of the factor matrix <- vector slot (the bordered Jacobian)
+template <typename T>
+__global__ void k_set_column(int count, const InstDesc* __restrict__ desc, T* __restrict__ M,
                              const int64_t* __restrict__ m_off, const int32_t* __restrict__ pcol,
                              const zc* __restrict__ vec, int slot, const int32_t* __restrict__ skip) {
   const int k = blockIdx.y;
@@ -160,7 +161,7 @@ __global__ void k_set_column(int count, const InstDesc* __restrict__ desc, cc* _
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= d.n) return;
   const zc a = vec[d.off_vec + (int64_t)slot * d.n + q];
-  M[m_off[k] + (int64_t)pcol[k] * d.n + q] = cmk((float)a.x, (float)a.y);
+  M[m_off[k] + (int64_t)pcol[k] * d.n + q] = cx<T>::from(a);
 }
 
 // copy slot a -> slot b
@@ -232,14 +233,77 @@ __global__ void k_start_shift(int count, const zc* __restrict__ sigma, zc* __res
   theta[k] = sigma[k];
 }
 
-// start of a polish round: done = iters = 0 for the instances that run
+// start of a polish round: done = iters = 0 for the instances that run and
+// done = 4 for the skipped ones; counts the factorisations per instance when
+// `lus` is non-null
 __global__ void k_reset_polish(int count, int32_t* __restrict__ done, int32_t* __restrict__ iters,
-                               const int32_t* __restrict__ skip) {
+                               const int32_t* __restrict__ skip, int32_t* __restrict__ lus, int nlu) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
-  if (skip && skip[k]) return;
+  if (skip && skip[k]) {
+    done[k] = 4;   // not run in this round: later steps of the round pass over it
+    return;
+  }
   done[k] = 0;
   iters[k] = 0;
+  if (lus) lus[k] += nlu;
+}
+
+// One step of fixed-shift inverse iteration for the complex128 retry: with
+// x_p = 1 and y = Q(s)^-1 Q'(s) x, the eigenvalue nearest s is
+// t = s - x_p / y_p (exact for the linear temporal pencil, to O((s - t)^2)
+// for the quadratic spatial one); x <- y / y_q with q = arg max |y_q|.
+// Converged when successive t agree to tol (relative).
+__global__ void k_ii_update(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int xslot, int yslot,
+                            int32_t* __restrict__ pcol, const zc* __restrict__ sigma, zc* __restrict__ theta,
+                            int32_t* __restrict__ done, double* __restrict__ err, int32_t* __restrict__ iters,
+                            double tol, const int32_t* __restrict__ skip) {
+  __shared__ double bv[32];
+  __shared__ int bi[32];
+  __shared__ int s_q;
+  __shared__ zc s_yq;
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  if (done[k] || (skip && skip[k])) return;
+  const InstDesc d = desc[k];
+  zc* x = vec + d.off_vec + (int64_t)xslot * d.n;
+  const zc* y = vec + d.off_vec + (int64_t)yslot * d.n;
+  double best = -1.0;
+  int idx = 0x7fffffff;
+  for (int q = threadIdx.x; q < d.n; q += blockDim.x) {
+    const double a = zabs(y[q]);
+    if (a > best || (a == best && q < idx)) { best = a; idx = q; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_down_sync(0xffffffffu, best, o);
+    const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (ob > best || (ob == best && oi < idx)) { best = ob; idx = oi; }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { bv[warp] = best; bi[warp] = idx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      if (bv[w] > best || (bv[w] == best && bi[w] < idx)) { best = bv[w]; idx = bi[w]; }
+    if (idx < 0 || idx >= d.n) idx = 0;
+    const int p = pcol[k];
+    const zc yp = y[p];
+    const zc told = theta[k];
+    const zc t = zsub(sigma[k], zdiv(x[p], yp));
+    theta[k] = t;
+    const double rel = zabs(zsub(t, told)) / fmax(zabs(t), 1e-300);
+    err[k] = rel;
+    iters[k] += 1;
+    if (!isfinite(t.x) || !isfinite(t.y)) done[k] = 3;
+    else if (iters[k] >= 2 && rel <= tol) done[k] = 1;
+    pcol[k] = idx;
+    s_q = idx;
+    s_yq = y[idx];
+  }
+  __syncthreads();
+  const zc yq = s_yq;
+  if (yq.x == 0.0 && yq.y == 0.0) return;
+  for (int q = threadIdx.x; q < d.n; q += blockDim.x) x[q] = zdiv(y[q], yq);
 }
 
 // ---- host launchers --------------------------------------------------------
@@ -269,13 +333,18 @@ cudaError_t launch_normalize(int count, const InstDesc* desc, zc* vec, int slot,
   return cudaGetLastError();
 }
 
-cudaError_t launch_set_column(int count, int nmax, const InstDesc* desc, cc* M, const int64_t* m_off,
+template <typename T>
+cudaError_t launch_set_column(int count, int nmax, const InstDesc* desc, T* M, const int64_t* m_off,
                               const int32_t* pcol, const zc* vec, int slot, cudaStream_t s, const int32_t* skip) {
   if (count <= 0) return cudaSuccess;
   dim3 g((nmax + 255) / 256, count);
-  k_set_column<<<g, 256, 0, s>>>(count, desc, M, m_off, pcol, vec, slot, skip);
+  k_set_column<T><<<g, 256, 0, s>>>(count, desc, M, m_off, pcol, vec, slot, skip);
   return cudaGetLastError();
 }
+template cudaError_t launch_set_column<cc>(int, int, const InstDesc*, cc*, const int64_t*, const int32_t*, const zc*,
+                                           int, cudaStream_t, const int32_t*);
+template cudaError_t launch_set_column<zc>(int, int, const InstDesc*, zc*, const int64_t*, const int32_t*, const zc*,
+                                           int, cudaStream_t, const int32_t*);
 
 cudaError_t launch_vec_copy(int count, int nmax, const InstDesc* desc, zc* vec, int a, int b, const int32_t* skip,
                             cudaStream_t s) {
@@ -300,9 +369,18 @@ cudaError_t launch_start_shift(int count, const zc* sigma, zc* theta, const int3
   return cudaGetLastError();
 }
 
-cudaError_t launch_reset_polish(int count, int32_t* done, int32_t* iters, const int32_t* skip, cudaStream_t s) {
+cudaError_t launch_reset_polish(int count, int32_t* done, int32_t* iters, const int32_t* skip, cudaStream_t s,
+                                int32_t* lus, int nlu) {
   if (count <= 0) return cudaSuccess;
-  k_reset_polish<<<(count + 255) / 256, 256, 0, s>>>(count, done, iters, skip);
+  k_reset_polish<<<(count + 255) / 256, 256, 0, s>>>(count, done, iters, skip, lus, nlu);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ii_update(int count, const InstDesc* desc, zc* vec, int xslot, int yslot, int32_t* pcol,
+                             const zc* sigma, zc* theta, int32_t* done, double* err, int32_t* iters, double tol,
+                             const int32_t* skip, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_ii_update<<<count, 256, 0, s>>>(count, desc, vec, xslot, yslot, pcol, sigma, theta, done, err, iters, tol, skip);
   return cudaGetLastError();
 }
 

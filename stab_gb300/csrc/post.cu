@@ -127,23 +127,30 @@ __global__ void k_take_candidate(int count, const zc* __restrict__ cand, int nca
 
 // Fold the result of a polish round into the per-instance best: a pair
 // counts when it converged and passes the selection filter; the less stable
-// one is kept (theta, err, iters and the output vector).  In round 0 a pair
-// within quick_tol of its shift is final: the top coarse candidate is then a
-// resolved mode and later rounds skip the instance.
+// one is kept (theta, err, iters and the output vector).  With `quick`, a
+// pair within quick_tol of its shift is final: the top coarse candidate is
+// then a resolved mode and later rounds skip the instance.
 __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ sigma,
                             const zc* __restrict__ theta, const int32_t* __restrict__ done,
                             const double* __restrict__ err, const int32_t* __restrict__ iters,
                             const zc* __restrict__ out, const int64_t* __restrict__ out_off,
                             int32_t* __restrict__ final_, int32_t* __restrict__ have, double* __restrict__ best_key,
                             zc* __restrict__ best_theta, double* __restrict__ best_err, int32_t* __restrict__ best_iters,
-                            zc* __restrict__ best_out, int round, double quick_tol) {
+                            zc* __restrict__ best_out, int quick, double quick_tol, int32_t* __restrict__ skip64,
+                            int slow_iters) {
   __shared__ int s_take;
   const int k = blockIdx.x;
   if (k >= count) return;
-  if (final_[k]) return;
+  if (final_[k]) {
+    if (skip64 && threadIdx.x == 0) skip64[k] = 1;   // accepted: no retry
+    return;
+  }
   const InstDesc d = desc[k];
   if (threadIdx.x == 0) {
     s_take = 0;
+    // a complex128 retry only where the complex64 polish failed or
+    // contracted slowly (the sign of a cluster it cannot resolve)
+    if (skip64) skip64[k] = (done[k] == 1 && iters[k] < slow_iters) ? 1 : 0;   // complex64 round: set retries
     const zc t = theta[k];
     const zc v = (d.itype == 2) ? ((t.x != 0.0 || t.y != 0.0) ? zdiv(zmk(1.0, 0.0), t) : t) : t;
     double key;
@@ -156,8 +163,9 @@ __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const 
         best_iters[k] = iters[k];
         s_take = 1;
       }
-      if (round == 0 && zabs(zsub(t, sigma[k])) <= quick_tol * zabs(sigma[k])) final_[k] = 1;
+      if (quick && zabs(zsub(t, sigma[k])) <= quick_tol * zabs(sigma[k])) final_[k] = 1;
     }
+    if (skip64 && final_[k]) skip64[k] = 1;
   }
   __syncthreads();
   if (!s_take) return;

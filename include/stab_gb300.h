@@ -77,6 +77,7 @@ typedef struct stab_params {
 
 typedef struct stab_ctx stab_ctx;
 typedef struct stab_batch stab_batch;
+typedef struct stab_mlp stab_mlp;
 
 /* ---- context ---------------------------------------------------------- */
 int stab_abi_version(void);
@@ -128,6 +129,76 @@ int stab_full_spectrum(stab_ctx* ctx, const stab_params* p, int32_t nym, const d
                        double* eig_out, double* vec_out, int32_t* least_index_out,
                        int32_t* status_out);
 
+/*
+ * Eigenvectors of one instance at `count` of its eigenvalues (omega for
+ * itype 1, alpha for itype 2, as stab_full_spectrum returns them), by FP64
+ * inverse iteration on an LU of Q(shift), instances run as one batch.
+ * vec_out: count columns of n (temporal, 5*ny) or m (spatial, 10*ny) complex
+ * values, column-major, normalised as in stab_full_spectrum.  status_out
+ * (may be NULL): count STAB_ST_* values.  With every eigenvalue of the
+ * spectrum this is the eigenvector matrix that ZGEEV('N','V') hands to the
+ * evec.dat writer (temporal.f90:803, spatial.f90:1043); vectors of
+ * repeated eigenvalues (the zero eigenvalues of the boundary rows) are some
+ * vector of their eigenspace, as in LAPACK.
+ */
+int stab_eigenvectors(stab_ctx* ctx, const stab_params* p, int32_t nym, const double* profile,
+                      int32_t count, const double* eig, double* vec_out, int32_t* status_out);
+
+/* ---- the reference's file interface (host only, no GPU) --------------- */
+/*
+ * Parse the stdin protocol of `stab < input.dat`: input.f90:15-123 followed
+ * by the index (and, for itype 2, x) reads of stab.f90:46-55.  Fortran
+ * list-directed semantics: each read starts on a new record, takes blank- or
+ * comma-separated values across records and drops the rest of its last
+ * record.  Out-of-range mattyp and itype are read again as the reference
+ * does; itype 3..9 (finite-difference, Stokes, bump and multi-point drivers)
+ * return STAB_ERR_ARG.  msg (may be NULL) receives the reason.
+ */
+int stab_parse_input(const char* text, stab_params* p, char* msg, size_t msg_cap);
+/* "profile.<ind>" (makename, getmean.f90:27-28). */
+int stab_profile_name(int32_t ind, char* out, size_t cap);
+/*
+ * Read profile.<ind> (getmean.f90:27-80): rows "y rho u v w T", records that
+ * start with '#' skipped.  rows == NULL counts only; else up to cap_rows rows
+ * of 6 doubles are stored row-major.  *nym receives the row count.
+ */
+int stab_read_profile(const char* path, int32_t cap_rows, double* rows, int32_t* nym);
+/* Collocation grid y, eta, d eta/dy, d2 eta/dy2 (sgengrid.f90:18-45). */
+int stab_grid(int32_t ny, double yi, double ymax, double* y, double* eta, double* deta, double* d2eta);
+/*
+ * Write evec.dat as gfortran writes it (temporal.f90:883-890,
+ * spatial.f90:1120-1126): sequential unformatted records with 4-byte
+ * little-endian lengths; R1 10 x int32 (ind ny ndof itype ievec curve top
+ * wall wallt ider), R2 omega alpha beta Re Ma Pr, R3 x y eta deta d2eta yi
+ * ymax, R4 the nmax eigenvalues, R5 the nmax x nmax eigenvectors (always for
+ * itype 1, only with ievec = 1 for itype 2; vec may be NULL otherwise).
+ */
+int stab_write_evec(const char* path, const stab_params* p, const double* eig, const double* vec);
+
+/* evec.dat records R1-R3 as getevec.f90:77-91 reads them. */
+typedef struct {
+  int32_t ind, ny, ndof, itype, ievec, curve, top, wall, wallt, ider;
+  int32_t nmax;         /* ndof*ny (itype 1) or 2*ndof*ny (itype 2)  */
+  int32_t has_vectors;  /* R5 present                                 */
+  double omega[2], alpha[2], beta[2];
+  double Re, Ma, Pr, x, yi, ymax;
+} stab_evec_header;
+/* Read evec.dat; y (ny), eig (nmax complex) and vec (nmax x nmax complex)
+ * may each be NULL (call once with NULLs to learn the sizes). */
+int stab_read_evec(const char* path, stab_evec_header* h, double* y, double* eig, double* vec);
+/* getevec -v (getevec.f90:161-172): 0-based index of the nearest
+ * eigenvalue, the first minimum winning. */
+int32_t stab_getevec_select(const double* eig, int32_t nmax, double vr, double vi);
+/*
+ * The time.N / space.N text for one eigenpair (getevec.f90:176-227): four
+ * header lines, then rows wall to free stream "y Re/Im(rho u v w T)" in
+ * 1P E21.13E3 with the scale quirk of getevec.f90:179-189 (the vector is
+ * divided by the real part of its running max-modulus pick).  Returns the
+ * text length; the text (NUL-terminated) is stored when cap > length.
+ */
+int64_t stab_eigfunction_text(const stab_evec_header* h, const double* y, const double* eig_j,
+                              const double* vec_j, char* buf, int64_t cap);
+
 /* ---- batched least-stable mode ---------------------------------------- */
 /*
  * Upload `count` instances (parameters + profiles) to device memory.
@@ -165,6 +236,33 @@ int stab_batch_destroy(stab_batch* b);
 int stab_solve_batch(stab_ctx* ctx, int32_t count, const stab_params* p, const int32_t* nym,
                      const double* const* profiles, int32_t mode, const double* seeds,
                      double* eig_out, double* err_out, int32_t* status_out, double* const* vec_out);
+
+/* ---- surrogate network (no counterpart in the reference) -------------- */
+/*
+ * A multilayer perceptron run and trained on the GPU by the library's own
+ * BF16 kernels (tensor-core GEMMs with bf16 operands and float32
+ * accumulation, fused bias + GELU epilogues, Adam on float32 master weights).
+ * sizes[0..nlayers]: layer widths; hidden layers use GELU (erf form), the
+ * last layer is linear.  Parameters pack as [W_0, b_0, W_1, b_1, ...] with
+ * W_l of shape sizes[l] x sizes[l+1], row-major.  x, t, y are row-major
+ * float32 device arrays (batch x width); w holds one loss weight per output:
+ * loss = sum_ij w_j (y_ij - t_ij)^2 / batch.  Runs on the context stream;
+ * destroying the context first releases the network's device memory.
+ */
+int stab_mlp_create(stab_ctx* ctx, int32_t nlayers, const int32_t* sizes, int32_t max_batch, stab_mlp** out);
+int64_t stab_mlp_param_count(const stab_mlp* m);
+/* host float32 parameters in; resets the Adam moments and step */
+int stab_mlp_set_params(stab_mlp* m, const float* params);
+/* float32 parameters and the gradients of the last backward pass out (either may be NULL) */
+int stab_mlp_get_params(stab_mlp* m, float* params_out, float* grads_out);
+int stab_mlp_forward(stab_mlp* m, int32_t batch, const float* x_dev, float* y_dev);
+/* forward + backward; loss_out (host, may be NULL: no synchronisation) */
+int stab_mlp_gradients(stab_mlp* m, int32_t batch, const float* x_dev, const float* t_dev, const float* w_dev,
+                       double* loss_out);
+/* forward + backward + one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) */
+int stab_mlp_train_step(stab_mlp* m, int32_t batch, const float* x_dev, const float* t_dev, const float* w_dev,
+                        float lr, double* loss_out);
+int stab_mlp_destroy(stab_mlp* m);
 
 /* ---- allocation-free eigenvalues -------------------------------------- */
 #define STAB_NOALLOC_MAX_M 256

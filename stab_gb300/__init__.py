@@ -19,7 +19,8 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-__all__ = ["StabParams", "Context", "load", "LIB_PATH", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE",
+__all__ = ["StabParams", "EvecHeader", "Context", "Network", "load", "LIB_PATH", "parse_input", "profile_name",
+           "read_profile", "grid", "write_evec", "read_evec", "getevec_select", "eigfunction_text", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE",
            "ST_OK", "ST_SINGULAR", "ST_NOCONV", "ST_NAN", "ST_FELLBACK", "ST_NOMODE", "StabError"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -33,12 +34,24 @@ EXPORTED = (
     "stab_set_profiling", "stab_kernel_stats", "stab_reset_kernel_stats", "stab_assemble",
     "stab_full_spectrum", "stab_batch_create", "stab_batch_set_seeds", "stab_batch_run",
     "stab_batch_results", "stab_batch_work", "stab_batch_destroy", "stab_solve_batch",
-    "stab_eigvals_noalloc",
+    "stab_eigvals_noalloc", "stab_eigenvectors", "stab_parse_input", "stab_profile_name", "stab_read_profile",
+    "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
+    "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
+    "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy",
 )
 
 
 class StabError(RuntimeError):
     pass
+
+
+class EvecHeader(ctypes.Structure):
+    """Mirror of ``stab_evec_header``: records R1-R3 of evec.dat."""
+
+    _fields_ = [(k, ctypes.c_int32) for k in ("ind", "ny", "ndof", "itype", "ievec", "curve", "top", "wall",
+                                              "wallt", "ider", "nmax", "has_vectors")] + [
+        ("omega", ctypes.c_double * 2), ("alpha", ctypes.c_double * 2), ("beta", ctypes.c_double * 2)] + [
+        (k, ctypes.c_double) for k in ("Re", "Ma", "Pr", "x", "yi", "ymax")]
 
 
 class StabParams(ctypes.Structure):
@@ -111,6 +124,27 @@ def load(path: str = LIB_PATH):
     lib.stab_eigvals_noalloc.argtypes = [vp, i32, vp, vp, vp]
     lib.stab_solve_batch.argtypes = [vp, i32, P(StabParams), P(i32), P(P(dbl)), i32, P(dbl), P(dbl), P(dbl),
                                      P(i32), P(P(dbl))]
+    lib.stab_eigenvectors.argtypes = [vp, P(StabParams), i32, P(dbl), i32, P(dbl), P(dbl), P(i32)]
+    lib.stab_parse_input.argtypes = [ctypes.c_char_p, P(StabParams), ctypes.c_char_p, ctypes.c_size_t]
+    lib.stab_profile_name.argtypes = [i32, ctypes.c_char_p, ctypes.c_size_t]
+    lib.stab_read_profile.argtypes = [ctypes.c_char_p, i32, P(dbl), P(i32)]
+    lib.stab_grid.argtypes = [i32, dbl, dbl, P(dbl), P(dbl), P(dbl), P(dbl)]
+    lib.stab_write_evec.argtypes = [ctypes.c_char_p, P(StabParams), P(dbl), P(dbl)]
+    lib.stab_read_evec.argtypes = [ctypes.c_char_p, P(EvecHeader), P(dbl), P(dbl), P(dbl)]
+    lib.stab_getevec_select.argtypes = [P(dbl), i32, dbl, dbl]
+    lib.stab_getevec_select.restype = i32
+    lib.stab_eigfunction_text.argtypes = [P(EvecHeader), P(dbl), P(dbl), P(dbl), ctypes.c_char_p, i64]
+    lib.stab_eigfunction_text.restype = i64
+    f32p = P(ctypes.c_float)
+    lib.stab_mlp_create.argtypes = [vp, i32, P(i32), i32, P(vp)]
+    lib.stab_mlp_param_count.argtypes = [vp]
+    lib.stab_mlp_param_count.restype = i64
+    lib.stab_mlp_set_params.argtypes = [vp, f32p]
+    lib.stab_mlp_get_params.argtypes = [vp, f32p, f32p]
+    lib.stab_mlp_forward.argtypes = [vp, i32, vp, vp]
+    lib.stab_mlp_gradients.argtypes = [vp, i32, vp, vp, vp, P(dbl)]
+    lib.stab_mlp_train_step.argtypes = [vp, i32, vp, vp, vp, ctypes.c_float, P(dbl)]
+    lib.stab_mlp_destroy.argtypes = [vp]
     _lib = lib
     return lib
 
@@ -187,6 +221,76 @@ class Batch:
             pass
 
 
+class Network:
+    """A ``stab_mlp``: BF16 MLP trained and run by the library's kernels.
+
+    Device arrays are passed as raw device addresses (``tensor.data_ptr()``
+    of contiguous float32 CUDA tensors): row-major batch x width."""
+
+    def __init__(self, ctx: "Context", sizes: Sequence[int], max_batch: int):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.sizes = tuple(int(v) for v in sizes)
+        arr = np.asarray(self.sizes, dtype=np.int32)
+        h = ctypes.c_void_p()
+        ctx._check(self.lib.stab_mlp_create(ctx.h, len(arr) - 1, _iptr(arr), int(max_batch), ctypes.byref(h)))
+        self.h = h
+        self.max_batch = int(max_batch)
+        self.count = int(self.lib.stab_mlp_param_count(self.h))
+        ctx._nets.add(self)
+
+    def set_params(self, params: np.ndarray) -> None:
+        a = np.ascontiguousarray(params, dtype=np.float32)
+        if a.size != self.count:
+            raise ValueError(f"expected {self.count} parameters")
+        self.ctx._check(self.lib.stab_mlp_set_params(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def get_params(self, grads: bool = False):
+        p = np.zeros(self.count, dtype=np.float32)
+        g = np.zeros(self.count, dtype=np.float32) if grads else None
+        fp = ctypes.POINTER(ctypes.c_float)
+        self.ctx._check(self.lib.stab_mlp_get_params(self.h, p.ctypes.data_as(fp),
+                                                     g.ctypes.data_as(fp) if grads else None))
+        return (p, g) if grads else p
+
+    def forward(self, batch: int, x_ptr: int, y_ptr: int) -> None:
+        self.ctx._check(self.lib.stab_mlp_forward(self.h, int(batch), ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr)))
+
+    def gradients(self, batch: int, x_ptr: int, t_ptr: int, w_ptr: int) -> float:
+        loss = ctypes.c_double(0.0)
+        self.ctx._check(self.lib.stab_mlp_gradients(self.h, int(batch), ctypes.c_void_p(x_ptr), ctypes.c_void_p(t_ptr),
+                                                    ctypes.c_void_p(w_ptr), ctypes.byref(loss)))
+        return loss.value
+
+    def train_step(self, batch: int, x_ptr: int, t_ptr: int, w_ptr: int, lr: float, want_loss: bool = False):
+        loss = ctypes.c_double(0.0)
+        self.ctx._check(self.lib.stab_mlp_train_step(self.h, int(batch), ctypes.c_void_p(x_ptr), ctypes.c_void_p(t_ptr),
+                                                     ctypes.c_void_p(w_ptr), float(lr),
+                                                     ctypes.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def split(self, flat: np.ndarray) -> list:
+        """Packed parameters -> [(W_l, b_l)] views."""
+        out, o = [], 0
+        for k, n in zip(self.sizes[:-1], self.sizes[1:]):
+            W = flat[o:o + k * n].reshape(k, n)
+            o += k * n
+            out.append((W, flat[o:o + n]))
+            o += n
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.stab_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Context:
     """A ``stab_ctx`` on one CUDA device."""
 
@@ -194,6 +298,7 @@ class Context:
         self.lib = load()
         h = ctypes.c_void_p()
         self._batches = weakref.WeakSet()
+        self._nets = weakref.WeakSet()
         rc = self.lib.stab_create(ctypes.byref(h), int(device))
         if rc != 0:
             raise StabError(f"stab_create failed ({rc}): no usable CUDA device {device}")
@@ -203,6 +308,8 @@ class Context:
         if getattr(self, "h", None):
             for b in list(self._batches):
                 b.close()
+            for m in list(self._nets):
+                m.close()
             self.lib.stab_destroy(self.h)
             self.h = None
 
@@ -268,6 +375,18 @@ class Context:
                                                 ctypes.byref(li), ctypes.byref(st)))
         return eig, vec, li.value, st.value
 
+    def eigenvectors(self, p: StabParams, profile, eig) -> tuple:
+        """Eigenvectors at the given eigenvalues (columns) and their status."""
+        prof = _prof(profile)
+        ev = np.ascontiguousarray(eig, dtype=np.complex128)
+        m = p.m()
+        vec = np.zeros((len(ev), m), dtype=np.complex128)
+        st = np.zeros(len(ev), dtype=np.int32)
+        self._check(self.lib.stab_eigenvectors(self.h, ctypes.byref(p), prof.shape[0], _dptr(prof), len(ev),
+                                               _dptr(ev.view(np.float64)), _dptr(vec.view(np.float64)),
+                                               _iptr(st)))
+        return vec.T.copy(), st
+
     # -- batches -------------------------------------------------------------
     def batch(self, params: Sequence[StabParams], profiles: Sequence[np.ndarray]) -> Batch:
         return Batch(self, params, profiles)
@@ -282,3 +401,93 @@ class Context:
             return b.results(want_vectors)
         finally:
             b.close()
+
+
+# -- the reference's file interface (host only) ---------------------------------
+def parse_input(text: str) -> StabParams:
+    """``stab < input.dat`` stdin protocol (input.f90:15-123, stab.f90:46-55)."""
+    lib = load()
+    p = StabParams()
+    msg = ctypes.create_string_buffer(256)
+    rc = lib.stab_parse_input(text.encode(), ctypes.byref(p), msg, 256)
+    if rc:
+        raise StabError(f"input: {msg.value.decode()}")
+    return p
+
+
+def profile_name(ind: int) -> str:
+    buf = ctypes.create_string_buffer(64)
+    if load().stab_profile_name(ind, buf, 64):
+        raise StabError("profile index out of range")
+    return buf.value.decode()
+
+
+def read_profile(path: str) -> np.ndarray:
+    """profile.<ind> rows (nym, 6): y rho u v w T (getmean.f90:27-80)."""
+    lib = load()
+    n = ctypes.c_int32(0)
+    rc = lib.stab_read_profile(path.encode(), 0, None, ctypes.byref(n))
+    if rc:
+        raise StabError(f"cannot read {path} ({rc})")
+    rows = np.zeros((n.value, 6), dtype=np.float64)
+    rc = lib.stab_read_profile(path.encode(), n.value, _dptr(rows), ctypes.byref(n))
+    if rc:
+        raise StabError(f"cannot read {path} ({rc})")
+    return rows
+
+
+def grid(ny: int, yi: float, ymax: float):
+    """y, eta, deta, d2eta of the collocation grid (sgengrid.f90:18-45)."""
+    out = [np.zeros(ny) for _ in range(4)]
+    if load().stab_grid(ny, yi, ymax, *[_dptr(a) for a in out]):
+        raise StabError("bad grid arguments")
+    return tuple(out)
+
+
+def write_evec(path: str, p: StabParams, eig, vecs=None) -> None:
+    """evec.dat (temporal.f90:883-890, spatial.f90:1120-1126); vecs (m, m)."""
+    ev = np.ascontiguousarray(eig, dtype=np.complex128)
+    vp = None
+    if vecs is not None:
+        va = np.asfortranarray(vecs, dtype=np.complex128)
+        vp = va.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    rc = load().stab_write_evec(path.encode(), ctypes.byref(p), _dptr(ev.view(np.float64)), vp)
+    if rc:
+        raise StabError(f"cannot write {path} ({rc})")
+
+
+def read_evec(path: str):
+    """(header, y, eigenvalues, eigenvectors or None) of an evec.dat."""
+    lib = load()
+    h = EvecHeader()
+    if lib.stab_read_evec(path.encode(), ctypes.byref(h), None, None, None):
+        raise StabError(f"cannot read {path}")
+    y = np.zeros(h.ny)
+    eig = np.zeros(h.nmax, dtype=np.complex128)
+    vec = np.zeros((h.nmax, h.nmax), dtype=np.complex128, order="F") if h.has_vectors else None
+    rc = lib.stab_read_evec(path.encode(), ctypes.byref(h), _dptr(y), _dptr(eig.view(np.float64)),
+                            vec.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if vec is not None else None)
+    if rc:
+        raise StabError(f"cannot read {path}")
+    return h, y, eig, vec
+
+
+def getevec_select(eig, value: complex) -> int:
+    """getevec -v: 0-based index of the nearest eigenvalue (first wins)."""
+    ev = np.ascontiguousarray(eig, dtype=np.complex128)
+    return int(load().stab_getevec_select(_dptr(ev.view(np.float64)), len(ev), value.real, value.imag))
+
+
+def eigfunction_text(h: EvecHeader, y, eig_j: complex, vec_j) -> str:
+    """time.N / space.N text of one eigenpair (getevec.f90:176-227)."""
+    lib = load()
+    ya = np.ascontiguousarray(y, dtype=np.float64)
+    e = np.array([eig_j], dtype=np.complex128)
+    v = np.ascontiguousarray(vec_j, dtype=np.complex128)
+    args = (ctypes.byref(h), _dptr(ya), _dptr(e.view(np.float64)), _dptr(v.view(np.float64)))
+    n = lib.stab_eigfunction_text(*args, None, 0)
+    if n < 0:
+        raise StabError("bad eigenfunction arguments")
+    buf = ctypes.create_string_buffer(n + 1)
+    lib.stab_eigfunction_text(*args, buf, n + 1)
+    return buf.value.decode()

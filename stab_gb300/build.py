@@ -11,8 +11,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libstab_gb300.so")
+BIN = os.path.join(HERE, "bin")
+# command-line drop-ins over the C ABI: `stab < input.dat` and `getevec`
+TOOLS = {"stab_gpu": "stab_main.cpp", "getevec_gpu": "getevec_main.cpp"}
 
-CU_SOURCES = ["prep.cu", "assemble.cu", "lu.cu", "hqr.cu", "polish.cu", "post.cu", "capi.cu"]
+CU_SOURCES = ["prep.cu", "assemble.cu", "lu.cu", "hqr.cu", "polish.cu", "post.cu", "mlp.cu", "capi.cu", "fileio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", os.path.join(HERE, "..", "include")]
@@ -49,6 +52,18 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.makedirs(BIN, exist_ok=True)
+    inc = os.path.join(HERE, "..", "include")
+    for exe, src in TOOLS.items():
+        out = os.path.join(BIN, exe)
+        path = os.path.join(CSRC, src)
+        if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(path), os.path.getmtime(LIB)):
+            continue
+        cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I", inc, path, "-o", out,
+               "-L", HERE, "-lstab_gb300", "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed for {src}:\n{r.stderr}")
     if verbose:
         print(LIB)
     return LIB

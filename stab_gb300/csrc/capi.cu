@@ -18,6 +18,7 @@
 #include "hqr.cuh"
 #include "kernels.cuh"
 #include "lu.cuh"
+#include "mlp.cuh"
 #include "polish.cuh"
 
 using namespace stab;
@@ -57,7 +58,9 @@ struct stab_ctx {
   std::vector<cudaEvent_t> evpool;
   int sms = 152;
   std::vector<stab_batch*> live;   // caller-visible batches, released by stab_destroy
+  std::vector<stab_mlp*> nets;     // networks, released by stab_destroy
 };
+static void release_net(stab_mlp* m);
 
 static int set_err(stab_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -866,6 +869,8 @@ int stab_destroy(stab_ctx* c) {
     b->ctx = nullptr;
   }
   c->live.clear();
+  for (stab_mlp* m : c->nets) release_net(m);
+  c->nets.clear();
   cudaStreamSynchronize(c->stream);
   for (auto& kv : c->dtabs) {
     cudaFree(kv.second.first);
@@ -1276,6 +1281,69 @@ int stab_assemble(stab_ctx* c, const stab_params* p, int32_t nym, const double* 
   return STAB_OK;
 }
 
+int stab_eigenvectors(stab_ctx* c, const stab_params* p, int32_t nym, const double* profile, int32_t count,
+                      const double* eig, double* vec_out, int32_t* status_out) {
+  if (!c || !p || !profile || !eig || !vec_out || count < 0) return set_err(c, STAB_ERR_ARG, "null argument");
+  if (count == 0) return STAB_OK;
+  if (p->itype != 1 && p->itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 or 2");
+  cudaSetDevice(c->device);
+  const bool spatial = (p->itype == 2);
+  const int64_t mlen = (int64_t)(spatial ? 10 : 5) * p->ny;
+  const zc* ev = reinterpret_cast<const zc*>(eig);
+  // copies of the instance, one per eigenvalue, in chunks that bound memory
+  const int chunk = 256;
+  for (int k0 = 0; k0 < count; k0 += chunk) {
+    const int cnt = std::min(chunk, count - k0);
+    std::vector<stab_params> ps(cnt, *p);
+    std::vector<int32_t> ns(cnt, nym);
+    std::vector<const double*> pr(cnt, profile);
+    stab_batch* b = nullptr;
+    int rc = batch_build(c, cnt, ps.data(), ns.data(), pr.data(), &b, 0);
+    if (rc) return rc;
+    std::unique_ptr<stab_batch> guard(b);
+    rc = run_prep(b);
+    if (rc) return rc;
+    cudaStream_t s = c->stream;
+    CK(c, b->Z64.ensure(sizeof(zc) * b->sum_n2, s));
+    // theta: the eigenvalue in the solver's variable (omega, or lambda =
+    // 1/alpha with alpha = 0 -> lambda = 0); shift: theta moved by a few
+    // ulps so that Q(shift) is not exactly singular
+    std::vector<zc> th(cnt), sh(cnt);
+    for (int k = 0; k < cnt; ++k) {
+      const zc w = ev[k0 + b->perm[k]];
+      zc t = w;
+      if (spatial) t = (w.x != 0.0 || w.y != 0.0) ? zdiv(zmk(1.0, 0.0), w) : zmk(0.0, 0.0);
+      const double d = 1e-14 * (std::hypot(t.x, t.y) + 1.0);
+      th[k] = t;
+      sh[k] = zmk(t.x + d, t.y + d);
+    }
+    CK(c, upload(b->theta, th, s));
+    CK(c, upload(b->sigma, sh, s));
+    rc = eigvec_inverse_iteration(b, Range{0, cnt}, b->sigma.as<zc>());
+    if (rc) return rc;
+    rc = write_vectors(b, Range{0, cnt}, b->theta.as<zc>());
+    if (rc) return rc;
+    std::vector<int32_t> info(cnt);
+    CK(c, cudaMemcpyAsync(info.data(), b->info.p, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, s));
+    for (int k = 0; k < cnt; ++k) {
+      const int u = k0 + b->perm[k];
+      CK(c, cudaMemcpyAsync(vec_out + 2 * (int64_t)u * mlen, b->outvec.as<zc>() + b->h_mof[k], sizeof(zc) * mlen,
+                            cudaMemcpyDeviceToHost, s));
+    }
+    CK(c, cudaStreamSynchronize(s));
+    if (status_out) {
+      for (int k = 0; k < cnt; ++k) {
+        const int u = k0 + b->perm[k];
+        const double* v = vec_out + 2 * (int64_t)u * mlen;
+        bool finite = true;
+        for (int64_t q = 0; q < 2 * mlen; ++q) finite = finite && std::isfinite(v[q]);
+        status_out[u] = !finite ? STAB_ST_NAN : (info[k] ? STAB_ST_SINGULAR : STAB_ST_OK);
+      }
+    }
+  }
+  return STAB_OK;
+}
+
 int stab_full_spectrum(stab_ctx* c, const stab_params* p, int32_t nym, const double* profile, double* eig_out,
                        double* vec_out, int32_t* least_index_out, int32_t* status_out) {
   if (!c || !p || !profile || !eig_out) return set_err(c, STAB_ERR_ARG, "null argument");
@@ -1302,6 +1370,231 @@ int stab_full_spectrum(stab_ctx* c, const stab_params* p, int32_t nym, const dou
   if (st == 0 && li < 0) st = STAB_ST_NOMODE;
   if (least_index_out) *least_index_out = li;
   if (status_out) *status_out = st;
+  return STAB_OK;
+}
+
+
+// ---- surrogate network -----------------------------------------------------
+// A BF16 MLP with float32 master weights, trained and run by the kernels of
+// mlp.cu on the context stream.  Layer l has sizes[l] inputs and
+// sizes[l+1] outputs; W_l is stored sizes[l] x sizes[l+1] row-major, and the
+// packed parameter vector is [W_0, b_0, W_1, b_1, ...].
+}  // extern "C"
+
+struct stab_mlp {
+  stab_ctx* ctx = nullptr;
+  std::vector<int> sz;
+  int L = 0, maxb = 0;
+  std::vector<int64_t> woff, boff;
+  int64_t nparam = 0;
+  DevBuf p32, g32, m32, v32, p16, loss;
+  std::vector<DevBuf> hin16, z32;   // per layer: bf16 input, f32 pre-activation / output
+  DevBuf dz32[2], dz16[2];
+  int batch = 0;                      // batch of the last forward
+  int step = 0;
+};
+
+// free the device memory of a network whose context goes away first
+static void release_net(stab_mlp* m) {
+  std::vector<DevBuf*> all = {&m->p32, &m->g32, &m->m32, &m->v32, &m->p16, &m->loss, &m->dz32[0], &m->dz32[1],
+                              &m->dz16[0], &m->dz16[1]};
+  for (auto& d : m->hin16) all.push_back(&d);
+  for (auto& d : m->z32) all.push_back(&d);
+  for (DevBuf* d : all) {
+    if (d->p) cudaFreeAsync(d->p, d->st);
+    d->p = nullptr;
+    d->bytes = 0;
+  }
+  m->ctx = nullptr;
+}
+
+static int mlp_layers(stab_mlp* m, int b, const float* x) {
+  stab_ctx* c = m->ctx;
+  cudaStream_t s = c->stream;
+  const __nv_bfloat16* P16 = m->p16.as<__nv_bfloat16>();
+  const float* P = m->p32.as<float>();
+  CK(c, timed(c, "k_cast_bf16", [&] {
+    return stab::mlp_cast_bf16((int64_t)b * m->sz[0], x, m->hin16[0].as<__nv_bfloat16>(), s);
+  }));
+  for (int l = 0; l < m->L; ++l) {
+    const int K = m->sz[l], N = m->sz[l + 1];
+    const __nv_bfloat16* W = P16 + m->woff[l];
+    const float* bias = P + m->boff[l];
+    if (l + 1 < m->L) {
+      CK(c, timed(c, "k_gemm_bf16_hidden", [&] {
+        return stab::mlp_gemm_hidden(b, N, K, m->hin16[l].as<__nv_bfloat16>(), W, bias, m->z32[l].as<float>(),
+                                     m->hin16[l + 1].as<__nv_bfloat16>(), s);
+      }));
+    } else {
+      CK(c, timed(c, "k_gemm_bf16_out", [&] {
+        return stab::mlp_gemm_out(b, N, K, m->hin16[l].as<__nv_bfloat16>(), W, bias, m->z32[l].as<float>(), s);
+      }));
+    }
+  }
+  m->batch = b;
+  return 0;
+}
+
+static int mlp_backward(stab_mlp* m, const float* t, const float* w, double* loss_out) {
+  stab_ctx* c = m->ctx;
+  cudaStream_t s = c->stream;
+  const int b = m->batch;
+  const __nv_bfloat16* P16 = m->p16.as<__nv_bfloat16>();
+  float* G = m->g32.as<float>();
+  CK(c, cudaMemsetAsync(m->g32.p, 0, sizeof(float) * m->nparam, s));
+  CK(c, cudaMemsetAsync(m->loss.p, 0, sizeof(double), s));
+  const int Lo = m->L - 1;
+  CK(c, timed(c, "k_loss_grad", [&] {
+    return stab::mlp_loss_grad(b, m->sz[m->L], m->z32[Lo].as<float>(), m->sz[m->L], t, w, m->dz32[0].as<float>(),
+                               m->dz16[0].as<__nv_bfloat16>(), m->loss.as<double>(), s);
+  }));
+  int cur = 0;
+  for (int l = Lo; l >= 0; --l) {
+    const int K = m->sz[l], N = m->sz[l + 1];
+    CK(c, timed(c, "k_gemm_bf16_wgrad", [&] {
+      return stab::mlp_gemm_wgrad(b, N, K, m->hin16[l].as<__nv_bfloat16>(), m->dz16[cur].as<__nv_bfloat16>(),
+                                  G + m->woff[l], s);
+    }));
+    CK(c, timed(c, "k_bias_grad", [&] {
+      return stab::mlp_bias_grad(b, N, m->dz32[cur].as<float>(), G + m->boff[l], s);
+    }));
+    if (l > 0) {
+      CK(c, timed(c, "k_gemm_bf16_dhidden", [&] {
+        return stab::mlp_gemm_dhidden(b, N, K, m->dz16[cur].as<__nv_bfloat16>(), P16 + m->woff[l],
+                                      m->z32[l - 1].as<float>(), m->dz32[1 - cur].as<float>(),
+                                      m->dz16[1 - cur].as<__nv_bfloat16>(), s);
+      }));
+      cur = 1 - cur;
+    }
+  }
+  if (loss_out) {
+    CK(c, cudaMemcpyAsync(loss_out, m->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(c, cudaStreamSynchronize(s));
+  }
+  return 0;
+}
+
+extern "C" {
+
+int stab_mlp_create(stab_ctx* c, int32_t nlayers, const int32_t* sizes, int32_t max_batch, stab_mlp** out) {
+  if (!c || !sizes || !out || nlayers < 1 || nlayers > 16 || max_batch < 1)
+    return set_err(c, STAB_ERR_ARG, "bad network shape");
+  for (int l = 0; l <= nlayers; ++l)
+    if (sizes[l] < 1 || sizes[l] > 4096) return set_err(c, STAB_ERR_ARG, "layer width must be 1..4096");
+  cudaSetDevice(c->device);
+  std::unique_ptr<stab_mlp> m(new stab_mlp());
+  m->ctx = c;
+  m->L = nlayers;
+  m->maxb = max_batch;
+  m->sz.assign(sizes, sizes + nlayers + 1);
+  int64_t off = 0;
+  int maxw = 0;
+  for (int l = 0; l < nlayers; ++l) {
+    m->woff.push_back(off);
+    off += (int64_t)sizes[l] * sizes[l + 1];
+    m->boff.push_back(off);
+    off += sizes[l + 1];
+    maxw = std::max(maxw, std::max(sizes[l], sizes[l + 1]));
+  }
+  m->nparam = off;
+  cudaStream_t s = c->stream;
+  CK(c, m->p32.ensure(sizeof(float) * off, s));
+  CK(c, m->g32.ensure(sizeof(float) * off, s));
+  CK(c, m->m32.ensure(sizeof(float) * off, s));
+  CK(c, m->v32.ensure(sizeof(float) * off, s));
+  CK(c, m->p16.ensure(sizeof(__nv_bfloat16) * off, s));
+  CK(c, m->loss.ensure(sizeof(double), s));
+  CK(c, cudaMemsetAsync(m->p32.p, 0, sizeof(float) * off, s));
+  CK(c, cudaMemsetAsync(m->p16.p, 0, sizeof(__nv_bfloat16) * off, s));
+  m->hin16.resize(nlayers);
+  m->z32.resize(nlayers);
+  for (int l = 0; l < nlayers; ++l) {
+    CK(c, m->hin16[l].ensure(sizeof(__nv_bfloat16) * (size_t)max_batch * sizes[l], s));
+    CK(c, m->z32[l].ensure(sizeof(float) * (size_t)max_batch * sizes[l + 1], s));
+  }
+  for (int q = 0; q < 2; ++q) {
+    CK(c, m->dz32[q].ensure(sizeof(float) * (size_t)max_batch * maxw, s));
+    CK(c, m->dz16[q].ensure(sizeof(__nv_bfloat16) * (size_t)max_batch * maxw, s));
+  }
+  CK(c, cudaStreamSynchronize(s));
+  c->nets.push_back(m.get());
+  *out = m.release();
+  return STAB_OK;
+}
+
+int64_t stab_mlp_param_count(const stab_mlp* m) { return m ? m->nparam : STAB_ERR_ARG; }
+
+int stab_mlp_set_params(stab_mlp* m, const float* params) {
+  if (!m || !params) return STAB_ERR_ARG;
+  if (!m->ctx) return STAB_ERR_STATE;
+  stab_ctx* c = m->ctx;
+  cudaStream_t s = c->stream;
+  CK(c, cudaMemcpyAsync(m->p32.p, params, sizeof(float) * m->nparam, cudaMemcpyHostToDevice, s));
+  CK(c, cudaMemsetAsync(m->m32.p, 0, sizeof(float) * m->nparam, s));
+  CK(c, cudaMemsetAsync(m->v32.p, 0, sizeof(float) * m->nparam, s));
+  CK(c, stab::mlp_cast_bf16(m->nparam, m->p32.as<float>(), m->p16.as<__nv_bfloat16>(), s));
+  CK(c, cudaStreamSynchronize(s));
+  m->step = 0;
+  return STAB_OK;
+}
+
+int stab_mlp_get_params(stab_mlp* m, float* params_out, float* grads_out) {
+  if (!m) return STAB_ERR_ARG;
+  if (!m->ctx) return STAB_ERR_STATE;
+  stab_ctx* c = m->ctx;
+  cudaStream_t s = c->stream;
+  if (params_out)
+    CK(c, cudaMemcpyAsync(params_out, m->p32.p, sizeof(float) * m->nparam, cudaMemcpyDeviceToHost, s));
+  if (grads_out)
+    CK(c, cudaMemcpyAsync(grads_out, m->g32.p, sizeof(float) * m->nparam, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaStreamSynchronize(s));
+  return STAB_OK;
+}
+
+int stab_mlp_forward(stab_mlp* m, int32_t batch, const float* x_dev, float* y_dev) {
+  if (m && !m->ctx) return STAB_ERR_STATE;
+  if (!m || !x_dev || batch < 1 || batch > m->maxb) return set_err(m ? m->ctx : nullptr, STAB_ERR_ARG, "bad batch");
+  int rc = mlp_layers(m, batch, x_dev);
+  if (rc) return rc;
+  if (y_dev)
+    CK(m->ctx, cudaMemcpyAsync(y_dev, m->z32[m->L - 1].p, sizeof(float) * (size_t)batch * m->sz[m->L],
+                               cudaMemcpyDeviceToDevice, m->ctx->stream));
+  return STAB_OK;
+}
+
+int stab_mlp_gradients(stab_mlp* m, int32_t batch, const float* x_dev, const float* t_dev, const float* w_dev,
+                       double* loss_out) {
+  if (m && !m->ctx) return STAB_ERR_STATE;
+  if (!m || !x_dev || !t_dev || !w_dev || batch < 1 || batch > m->maxb)
+    return set_err(m ? m->ctx : nullptr, STAB_ERR_ARG, "bad batch");
+  int rc = mlp_layers(m, batch, x_dev);
+  if (rc) return rc;
+  return mlp_backward(m, t_dev, w_dev, loss_out);
+}
+
+int stab_mlp_train_step(stab_mlp* m, int32_t batch, const float* x_dev, const float* t_dev, const float* w_dev,
+                        float lr, double* loss_out) {
+  int rc = stab_mlp_gradients(m, batch, x_dev, t_dev, w_dev, loss_out);
+  if (rc) return rc;
+  stab_ctx* c = m->ctx;
+  m->step += 1;
+  CK(c, timed(c, "k_adam", [&] {
+    return stab::mlp_adam(m->nparam, m->p32.as<float>(), m->g32.as<float>(), m->m32.as<float>(), m->v32.as<float>(),
+                          m->p16.as<__nv_bfloat16>(), lr, 0.9f, 0.999f, 1e-8f, m->step, c->stream);
+  }));
+  return STAB_OK;
+}
+
+int stab_mlp_destroy(stab_mlp* m) {
+  if (!m) return STAB_ERR_ARG;
+  if (m->ctx) {
+    stab_ctx* c = m->ctx;
+    cudaSetDevice(c->device);
+    c->nets.erase(std::remove(c->nets.begin(), c->nets.end(), m), c->nets.end());
+    release_net(m);
+    cudaStreamSynchronize(c->stream);
+  }
+  delete m;
   return STAB_OK;
 }
 

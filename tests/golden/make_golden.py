@@ -13,6 +13,8 @@ inputs and outputs for the Chebyshev path into small files:
   space1.ref          test/space.1 (spatial N=32 eigenfunction)
   thesis_time.ref     thesis/TStest/time.ref (temporal N=96 eigenfunction)
   thesis_space.ref    thesis/TStest/space.ref (spatial N=96 eigenfunction)
+  *.inp               the stdin files of those runs, verbatim: test/input.dat,
+                      TStest/input.dat, thesis/TStest/temporal.inp, spatial.inp
 """
 import json
 import os
@@ -78,6 +80,10 @@ def main(ref):
     cases["thesis_spatial_n96"] = c
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1)
+    for src, dst in [("test/input.dat", "test_input.inp"), ("TStest/input.dat", "tstest_input.inp"),
+                     ("thesis/TStest/temporal.inp", "thesis_temporal.inp"),
+                     ("thesis/TStest/spatial.inp", "thesis_spatial.inp")]:
+        shutil.copyfile(os.path.join(ref, src), os.path.join(HERE, dst))
     shutil.copyfile(os.path.join(ref, "test", "space.1"), os.path.join(HERE, "space1.ref"))
     shutil.copyfile(os.path.join(ref, "thesis", "TStest", "time.ref"), os.path.join(HERE, "thesis_time.ref"))
     shutil.copyfile(os.path.join(ref, "thesis", "TStest", "space.ref"), os.path.join(HERE, "thesis_space.ref"))

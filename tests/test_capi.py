@@ -13,7 +13,7 @@ def _declared_functions():
     for f in os.listdir(os.path.join(ROOT, "include")):
         if f.endswith(".h"):
             src = open(os.path.join(ROOT, "include", f)).read()
-            names += re.findall(r"^\s*(?:int|const char\*)\s+(stab_\w+)\s*\(", src, flags=re.M)
+            names += re.findall(r"^\s*(?:int|int32_t|int64_t|const char\*)\s+(stab_\w+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 

@@ -51,6 +51,9 @@ extern "C" {
 #define STAB_MODE_SEEDED 1    /* mixed-precision polish from caller seeds        */
 #define STAB_MODE_COARSE 2    /* seeds from an FP64 full spectrum at N = 32,     *
                                * then the mixed-precision polish                 */
+#define STAB_MODE_SURROGATE 3 /* polish from predicted seeds (and start vectors, *
+                               * stab_batch_set_start); pairs that fail the      *
+                               * acceptance gate take the STAB_MODE_COARSE path  */
 
 /*
  * Run parameters of one solve: a mirror of module `stuff` (stuff.f90:11-55)
@@ -210,8 +213,25 @@ int stab_batch_create(stab_ctx* ctx, int32_t count, const stab_params* p, const 
 /* Seeds for STAB_MODE_SEEDED: count complex values (omega for temporal,
  * alpha for spatial), copied to the device. */
 int stab_batch_set_seeds(stab_batch* b, const double* seeds);
-/* Run the whole path on the device (asynchronous on the context stream). */
+/*
+ * Start vectors for STAB_MODE_SURROGATE: per instance 5 x ncheb complex
+ * Chebyshev coefficients (field-major: rho, u, v, w, T), evaluated at the
+ * instance's collocation points, x(i, e) = sum_q c[e][q] cos(q pi i/(ny-1)).
+ * ncheb = 0 clears them (the generic start vector is used).
+ */
+int stab_batch_set_start(stab_batch* b, const double* coef, int32_t ncheb);
+/*
+ * Run the whole path on the device.  STAB_MODE_SURROGATE keeps a polished
+ * pair only when it converged within 6 Newton steps, within 0.1 |seed| of
+ * its seed, passes the least-stable filter and (temporal) lies above the
+ * vorticity-continuum branch point omega = alpha - i (alpha^2 + beta^2)/Re;
+ * the other instances (and every spatial one) run the STAB_MODE_COARSE path.
+ */
 int stab_batch_run(stab_batch* b, int32_t mode);
+/* After a run: counts_out[0] instances resolved by the first stage (the
+ * seeds, the coarse candidates, or the plain path), [1] resolved by the
+ * coarse sub-batch of STAB_MODE_SURROGATE, [2] sent to the FP64 fallback. */
+int stab_batch_counts(stab_batch* b, int32_t* counts_out);
 /*
  * Copy results back (synchronises): eig_out[2*k] least-stable eigenvalue,
  * err_out[k] relative FP64 residual estimate |r|/(|M||x|) of the final pair,

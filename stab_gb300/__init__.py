@@ -20,13 +20,13 @@ from typing import Optional, Sequence
 import numpy as np
 
 __all__ = ["StabParams", "EvecHeader", "Context", "Network", "load", "LIB_PATH", "parse_input", "profile_name",
-           "read_profile", "grid", "write_evec", "read_evec", "getevec_select", "eigfunction_text", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE",
+           "read_profile", "grid", "write_evec", "read_evec", "getevec_select", "eigfunction_text", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE", "MODE_SURROGATE",
            "ST_OK", "ST_SINGULAR", "ST_NOCONV", "ST_NAN", "ST_FELLBACK", "ST_NOMODE", "StabError"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libstab_gb300.so")
 
-MODE_PLAIN, MODE_SEEDED, MODE_COARSE = 0, 1, 2
+MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE = 0, 1, 2, 3
 ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE = 0, 1, 2, 3, 4, 5
 
 EXPORTED = (
@@ -37,7 +37,7 @@ EXPORTED = (
     "stab_eigvals_noalloc", "stab_eigenvectors", "stab_parse_input", "stab_profile_name", "stab_read_profile",
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
-    "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy",
+    "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
 )
 
 
@@ -145,6 +145,8 @@ def load(path: str = LIB_PATH):
     lib.stab_mlp_gradients.argtypes = [vp, i32, vp, vp, vp, P(dbl)]
     lib.stab_mlp_train_step.argtypes = [vp, i32, vp, vp, vp, ctypes.c_float, P(dbl)]
     lib.stab_mlp_destroy.argtypes = [vp]
+    lib.stab_batch_set_start.argtypes = [vp, P(dbl), i32]
+    lib.stab_batch_counts.argtypes = [vp, P(i32)]
     _lib = lib
     return lib
 
@@ -185,8 +187,22 @@ class Batch:
         s = np.ascontiguousarray(np.asarray(seeds, dtype=np.complex128)).view(np.float64)
         self.ctx._check(self.lib.stab_batch_set_seeds(self.h, _dptr(s)))
 
+    def set_start(self, coef) -> None:
+        """Chebyshev coefficients of start vectors: (count, 5, ncheb) complex."""
+        a = np.ascontiguousarray(np.asarray(coef, dtype=np.complex128))
+        if a.ndim != 3 or a.shape[0] != self.count or a.shape[1] != 5:
+            raise ValueError("coef must be (count, 5, ncheb)")
+        self._start = a
+        self.ctx._check(self.lib.stab_batch_set_start(self.h, _dptr(a.view(np.float64)), a.shape[2]))
+
     def run(self, mode: int) -> None:
         self.ctx._check(self.lib.stab_batch_run(self.h, int(mode)))
+
+    def counts(self) -> dict:
+        """Where the last run resolved its instances (stab_batch_counts)."""
+        c = np.zeros(3, dtype=np.int32)
+        self.ctx._check(self.lib.stab_batch_counts(self.h, _iptr(c)))
+        return {"first_stage": int(c[0]), "coarse_sub_batch": int(c[1]), "fp64_fallback": int(c[2])}
 
     def results(self, want_vectors: bool = False):
         n = self.count

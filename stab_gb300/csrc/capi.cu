@@ -199,11 +199,23 @@ struct stab_batch {
   bool ran = false;
   // instances re-solved by the plain FP64 path after a failed polish
   std::vector<int> fell_back;                 // internal indices
-  double fb_work[2] = {0.0, 0.0};             // fallback sub-batch: eigensolver flops, complex128 LU flops
+  double fb_work[4] = {0.0, 0.0, 0.0, 0.0};   // sub-batch work, indexed as stab_batch_work's output
+  std::vector<double> fb_err;
+  std::vector<int32_t> fb_iters;
+  int32_t counts[3] = {0, 0, 0};              // from seeds, from the coarse sub-batch, plain fallback
+  std::vector<double> start_coef;             // caller order: count x 5 x ncheb complex
+  int ncheb = 0;
+  bool use_start = false;
+  DevBuf startc;
   std::vector<zc> fb_val;
   std::vector<int32_t> fb_status;
   std::vector<std::vector<zc>> fb_vec;
   stab_batch* coarse = nullptr;               // N = 32 batch of STAB_MODE_COARSE, built on first use
+  // the device work of a STAB_MODE_COARSE pass (prep, N = 32 eigensolve,
+  // candidate rounds) captured once as a CUDA graph and replayed
+  cudaGraphExec_t coarse_graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  int coarse_runs = 0;
   ~stab_batch();
   // free every device buffer now (used when the owning context goes away first)
   void release() {
@@ -224,6 +236,8 @@ struct stab_batch {
     }
     delete coarse;
     coarse = nullptr;
+    if (coarse_graph) cudaGraphExecDestroy(coarse_graph);
+    coarse_graph = nullptr;
   }
 };
 
@@ -670,7 +684,13 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
     });
   };
   CK(c, lu32());
-  CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
+  if (b->use_start) {
+    CK(c, timed(c, "k_cheb_start", [&] {
+      return launch_cheb_start(b->count, b->nmax, D, b->startc.as<zc>(), b->ncheb, V, 0, skip, s);
+    }));
+  } else {
+    CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
+  }
   for (int it = 0; it < 2; ++it) {   // inverse iteration at the shift
     CK(c, qmv(1, 0, 1, skip));
     CK(c, solve32(1, skip));
@@ -714,6 +734,9 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
 // ratio |sigma - lambda_1| / |sigma - lambda_2| per step, which separates
 // mode clusters that complex64 factors cannot resolve.
 static const int kInverseSteps = 12;
+// gate of the surrogate-seeded mode (k_seed_accept)
+static const double kSeedAcceptTol = 0.1;
+static const int kSeedAcceptIters = 6;
 static const double kInverseTol = 1e-13;
 
 static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
@@ -784,10 +807,19 @@ static void finalize_polish_host(std::vector<zc>& val, std::vector<int32_t>& st,
 static int batch_run(stab_batch* b, int32_t mode) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
+  // other modes may grow pools the captured coarse pass points into
+  if (b->coarse_graph) {
+    cudaGraphExecDestroy(b->coarse_graph);
+    b->coarse_graph = nullptr;
+  }
   b->fell_back.clear();
-  b->fb_work[0] = b->fb_work[1] = 0.0;
+  for (double& w : b->fb_work) w = 0.0;
   b->last_mode = mode;
   int rc = run_prep(b);
+  if (mode != STAB_MODE_PLAIN) {
+    CK(c, cudaMemsetAsync(b->lus32.p, 0, sizeof(int32_t) * b->count, s));
+    CK(c, cudaMemsetAsync(b->lus64.p, 0, sizeof(int32_t) * b->count, s));
+  }
   if (rc) return rc;
   if (mode == STAB_MODE_PLAIN) {
     rc = run_plain(b, true);
@@ -795,8 +827,8 @@ static int batch_run(stab_batch* b, int32_t mode) {
     b->ran = true;
     return 0;
   }
-  if (mode == STAB_MODE_SEEDED) {
-    if (!b->have_seeds) return set_err(c, STAB_ERR_STATE, "STAB_MODE_SEEDED needs stab_batch_set_seeds first");
+  if (mode == STAB_MODE_SEEDED || mode == STAB_MODE_SURROGATE) {
+    if (!b->have_seeds) return set_err(c, STAB_ERR_STATE, "seeded modes need stab_batch_set_seeds first");
     std::vector<zc> sg(b->count);
     for (int k = 0; k < b->count; ++k) {
       const int u = b->perm[k];
@@ -808,12 +840,33 @@ static int batch_run(stab_batch* b, int32_t mode) {
       sg[k] = a;
     }
     CK(c, cudaMemcpyAsync(b->sigma.p, sg.data(), sizeof(zc) * b->count, cudaMemcpyHostToDevice, s));
+    b->use_start = false;
+    if (mode == STAB_MODE_SURROGATE && b->ncheb > 0) {
+      // start vectors from the predicted Chebyshev coefficients, internal order
+      const size_t per = (size_t)5 * b->ncheb;
+      std::vector<zc> co(per * b->count);
+      for (int k = 0; k < b->count; ++k) {
+        const double* src = b->start_coef.data() + 2 * per * b->perm[k];
+        for (size_t q = 0; q < per; ++q) co[per * k + q] = zmk(src[2 * q], src[2 * q + 1]);
+      }
+      CK(c, upload(b->startc, co, s));
+      b->use_start = true;
+    }
     CK(c, cudaStreamSynchronize(s));
   } else {
     return set_err(c, STAB_ERR_ARG, "unknown mode");
   }
   rc = run_polish(b, true);
+  b->use_start = false;
   if (rc) return rc;
+  if (mode == STAB_MODE_SURROGATE) {
+    CK(c, timed(c, "k_seed_accept", [&] {
+      k_seed_accept<<<(b->count + 127) / 128, 128, 0, s>>>(b->count, b->desc.as<InstDesc>(), b->sigma.as<zc>(),
+                                                            b->theta.as<zc>(), b->done.as<int32_t>(),
+                                                            b->iters.as<int32_t>(), kSeedAcceptTol, kSeedAcceptIters);
+      return cudaGetLastError();
+    }));
+  }
   b->ran = true;
   return 0;
 }
@@ -1041,12 +1094,17 @@ static int run_fallback(stab_batch* b) {
   CK(c, cudaMemcpyAsync(dn.data(), b->done.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   b->fell_back.clear();
-  b->fb_work[0] = b->fb_work[1] = 0.0;
+  for (double& w : b->fb_work) w = 0.0;
   b->fb_val.clear();
   b->fb_status.clear();
   b->fb_vec.clear();
+  b->fb_err.clear();
+  b->fb_iters.clear();
   for (int k = 0; k < n; ++k)
     if (dn[k] != 1) b->fell_back.push_back(k);
+  b->counts[0] = n - (int)b->fell_back.size();
+  b->counts[1] = 0;
+  b->counts[2] = (int)b->fell_back.size();
   if (b->fell_back.empty()) return 0;
   auto it = g_inputs.find(b);
   if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
@@ -1086,13 +1144,15 @@ static int run_fallback(stab_batch* b) {
     CK(c, cudaMemcpy(f.data(), fb->flops.p, sizeof(double) * nf, cudaMemcpyDeviceToHost));
     for (int q = 0; q < nf; ++q) {
       b->fb_work[0] += f[q];
-      b->fb_work[1] += (8.0 / 3.0) * (double)fb->hn[q] * fb->hn[q] * fb->hn[q];
+      b->fb_work[3] += (8.0 / 3.0) * (double)fb->hn[q] * fb->hn[q] * fb->hn[q];
     }
   }
   // the sub-batch orders its instances temporal-first internally; map back
   b->fb_val.assign(b->fell_back.size(), zmk(0, 0));
   b->fb_status.assign(b->fell_back.size(), 0);
   b->fb_vec.assign(b->fell_back.size(), {});
+  b->fb_err.assign(b->fell_back.size(), 0.0);
+  b->fb_iters.assign(b->fell_back.size(), 0);
   for (int q = 0; q < nf; ++q) {
     const int j = fb->perm[q];            // index into fell_back
     b->fb_val[j] = val[q];
@@ -1102,19 +1162,119 @@ static int run_fallback(stab_batch* b) {
   return 0;
 }
 
+// Surrogate-seeded mode: the instances the gate did not accept run the
+// coarse-seeded path as a sub-batch (with its own FP64 fallback); their
+// results replace the polish's.
+static int run_coarse_sub(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  const int n = b->count;
+  std::vector<int32_t> dn(n);
+  CK(c, cudaMemcpyAsync(dn.data(), b->done.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  b->fell_back.clear();
+  for (double& w : b->fb_work) w = 0.0;
+  b->fb_val.clear();
+  b->fb_status.clear();
+  b->fb_vec.clear();
+  b->fb_err.clear();
+  b->fb_iters.clear();
+  for (int k = 0; k < n; ++k)
+    if (dn[k] != 1) b->fell_back.push_back(k);
+  b->counts[0] = n - (int)b->fell_back.size();
+  b->counts[1] = b->counts[2] = 0;
+  if (b->fell_back.empty()) return 0;
+  auto it = g_inputs.find(b);
+  if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
+  BatchInputs sub;
+  for (int k : b->fell_back) {
+    const int u = b->perm[k];
+    sub.p.push_back(it->second.p[u]);
+    sub.nym.push_back(it->second.nym[u]);
+    sub.prof.push_back(it->second.prof[u]);
+  }
+  const int nf = (int)sub.p.size();
+  stab_batch* fb = nullptr;
+  int rc = batch_build(c, nf, sub.p.data(), sub.nym.data(), sub.prof.data(), &fb, 0);
+  if (rc) return rc;
+  std::unique_ptr<stab_batch> guard(fb);
+  g_inputs[fb] = sub;
+  rc = stab_batch_run(fb, STAB_MODE_COARSE);
+  std::vector<double> eig(2 * (size_t)nf), er(nf), w(4, 0.0);
+  std::vector<int32_t> itv(nf), st(nf);
+  std::vector<std::vector<zc>> vecs(nf);
+  std::vector<double*> vp(nf);
+  for (int q = 0; q < nf; ++q) {
+    vecs[q].resize(b->hm[b->fell_back[q]]);
+    vp[q] = reinterpret_cast<double*>(vecs[q].data());
+  }
+  if (rc == 0) rc = stab_batch_results(fb, eig.data(), er.data(), itv.data(), st.data(), vp.data());
+  if (rc == 0) rc = stab_batch_work(fb, w.data());
+  g_inputs.erase(fb);
+  if (rc) return rc;
+  for (int i = 0; i < 4; ++i) b->fb_work[i] += w[i];
+  b->fb_val.resize(nf);
+  b->fb_status.assign(st.begin(), st.end());
+  b->fb_err = er;
+  b->fb_iters = itv;
+  b->fb_vec = std::move(vecs);
+  for (int q = 0; q < nf; ++q) {
+    b->fb_val[q] = zmk(eig[2 * q], eig[2 * q + 1]);
+    if (st[q] == STAB_ST_FELLBACK) b->counts[2] += 1;
+    else b->counts[1] += 1;
+  }
+  return 0;
+}
+
+static int coarse_sequence(stab_batch* b) {
+  int rc = run_prep(b);
+  if (rc) return rc;
+  rc = coarse_seeds(b);
+  if (rc) return rc;
+  return polish_candidate_rounds(b);
+}
+
+// The device part of a STAB_MODE_COARSE pass is a fixed sequence of ~400
+// launches whose per-instance choices live in device masks, so after a first
+// eager pass (which sizes every pool) it is captured into a CUDA graph and
+// replayed.  Per-kernel profiling and the legacy stream run eagerly.
+static int run_coarse_device(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const bool graphable = !c->profiling && s != nullptr && b->coarse_runs > 0;
+  if (b->coarse_graph && b->graph_stream != s) {
+    cudaGraphExecDestroy(b->coarse_graph);
+    b->coarse_graph = nullptr;
+  }
+  if (graphable && !b->coarse_graph) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int rc = coarse_sequence(b);
+      const cudaError_t e = cudaStreamEndCapture(s, &g);
+      if (rc == 0 && e == cudaSuccess && g) {
+        if (cudaGraphInstantiate(&b->coarse_graph, g, 0) != cudaSuccess) b->coarse_graph = nullptr;
+        b->graph_stream = s;
+      }
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();   // a failed capture leaves no sticky error: run eagerly below
+    }
+  }
+  b->coarse_runs += 1;
+  if (graphable && b->coarse_graph) {
+    CK(c, cudaGraphLaunch(b->coarse_graph, s));
+    return 0;
+  }
+  return coarse_sequence(b);
+}
+
 int stab_batch_run(stab_batch* b, int32_t mode) {
   if (!b) return STAB_ERR_ARG;
   if (!b->ctx) return STAB_ERR_STATE;
   stab_ctx* c = b->ctx;
   cudaSetDevice(c->device);
   if (mode == STAB_MODE_COARSE) {
-    int rc = run_prep(b);
-    if (rc) return rc;
-    rc = coarse_seeds(b);
-    if (rc) return rc;
     b->fell_back.clear();
     b->last_mode = mode;
-    rc = polish_candidate_rounds(b);
+    int rc = run_coarse_device(b);
     if (rc) return rc;
     rc = run_fallback(b);
     if (rc) return rc;
@@ -1124,6 +1284,25 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
   int rc = batch_run(b, mode);
   if (rc) return rc;
   if (mode == STAB_MODE_SEEDED) return run_fallback(b);
+  if (mode == STAB_MODE_SURROGATE) return run_coarse_sub(b);
+  b->counts[0] = b->count;
+  b->counts[1] = b->counts[2] = 0;
+  return STAB_OK;
+}
+
+int stab_batch_set_start(stab_batch* b, const double* coef, int32_t ncheb) {
+  if (!b) return STAB_ERR_ARG;
+  if (!b->ctx) return STAB_ERR_STATE;
+  if (ncheb < 0 || ncheb > 64 || (ncheb > 0 && !coef)) return set_err(b->ctx, STAB_ERR_ARG, "ncheb must be 0..64");
+  b->ncheb = ncheb;
+  b->start_coef.assign(coef ? coef : nullptr, coef ? coef + 2 * (size_t)5 * ncheb * b->count : nullptr);
+  return STAB_OK;
+}
+
+int stab_batch_counts(stab_batch* b, int32_t* counts_out) {
+  if (!b || !counts_out) return STAB_ERR_ARG;
+  if (!b->ran) return STAB_ERR_STATE;
+  for (int i = 0; i < 3; ++i) counts_out[i] = b->counts[i];
   return STAB_OK;
 }
 
@@ -1161,6 +1340,8 @@ int stab_batch_results(stab_batch* b, double* eig_out, double* err_out, int32_t*
     fbpos[k] = (int)j;
     val[k] = b->fb_val[j];
     st[k] = b->fb_status[j];
+    if (j < b->fb_err.size()) er[k] = b->fb_err[j];
+    if (j < b->fb_iters.size()) it[k] = b->fb_iters[j];
   }
   for (int k = 0; k < n; ++k) {
     if (fl[k] & 2) { st[k] = STAB_ST_NAN; val[k] = zmk(NAN, NAN); }
@@ -1201,12 +1382,8 @@ int stab_batch_work(stab_batch* b, double* work_out) {
   const bool plain = (b->last_mode == STAB_MODE_PLAIN);
   std::vector<int32_t> l32(b->count, 0), l64(b->count, 0);
   if (!plain) {
-    if (b->last_mode == STAB_MODE_COARSE) {
-      cudaMemcpy(l32.data(), b->lus32.p, sizeof(int32_t) * b->count, cudaMemcpyDeviceToHost);
-      cudaMemcpy(l64.data(), b->lus64.p, sizeof(int32_t) * b->count, cudaMemcpyDeviceToHost);
-    } else {
-      for (auto& v : l32) v = 2;
-    }
+    cudaMemcpy(l32.data(), b->lus32.p, sizeof(int32_t) * b->count, cudaMemcpyDeviceToHost);
+    cudaMemcpy(l64.data(), b->lus64.p, sizeof(int32_t) * b->count, cudaMemcpyDeviceToHost);
   }
   double lu_c = 0.0, lu_z = 0.0;
   for (int k = 0; k < b->count; ++k) {
@@ -1215,9 +1392,9 @@ int stab_batch_work(stab_batch* b, double* work_out) {
     lu_z += (plain ? 1 : l64[k]) * (8.0 / 3.0) * n3;
   }
   work_out[0] = (plain ? eig_flops(b) : 0.0) + b->fb_work[0];
-  work_out[1] = (b->last_mode == STAB_MODE_COARSE && b->coarse) ? eig_flops(b->coarse) : 0.0;
-  work_out[2] = lu_c;
-  work_out[3] = lu_z + b->fb_work[1];
+  work_out[1] = ((b->last_mode == STAB_MODE_COARSE && b->coarse) ? eig_flops(b->coarse) : 0.0) + b->fb_work[1];
+  work_out[2] = lu_c + b->fb_work[2];
+  work_out[3] = lu_z + b->fb_work[3];
   return STAB_OK;
 }
 

@@ -60,6 +60,8 @@ __global__ void k_fold_best(int count, const InstDesc* desc, const zc* sigma, co
                             int32_t* final_, int32_t* have, double* best_key, zc* best_theta, double* best_err,
                             int32_t* best_iters, zc* best_out, int quick, double quick_tol, int32_t* skip64,
                             int slow_iters);
+__global__ void k_seed_accept(int count, const InstDesc* desc, const zc* sigma, const zc* theta, int32_t* done,
+                              const int32_t* iters, double tau, int max_iters);
 __global__ void k_take_best(int count, const InstDesc* desc, const int32_t* have, const zc* best_theta,
                             const double* best_err, const int32_t* best_iters, const zc* best_out,
                             const int64_t* out_off, zc* theta, int32_t* done, double* err, int32_t* iters, zc* out);

@@ -300,6 +300,112 @@ __global__ void __launch_bounds__(256) k_getrs(int count, const int32_t* __restr
   }
 }
 
+__device__ __forceinline__ zc shfl_cx(zc v, int src) {
+  return zmk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+__device__ __forceinline__ cc shfl_cx(cc v, int src) {
+  return cmk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// The same solve for few right-hand sides: one CTA per (instance, column),
+// blocked by 32 columns.  Warp 0 solves each 32 x 32 diagonal block from
+// shared memory (one row per lane, shuffles broadcast the solved entry) and
+// then all warps update the remaining rows with the block's 32 columns, so
+// the O(n^2) work runs on every SM sub-partition instead of one warp's.
+template <typename T>
+__global__ void __launch_bounds__(256) k_getrs_blk(int count, const int32_t* __restrict__ nsz,
+                                                   const T* __restrict__ LU, const int64_t* __restrict__ mat_off,
+                                                   const int32_t* __restrict__ piv, const int64_t* __restrict__ piv_off,
+                                                   zc* __restrict__ X, const int64_t* __restrict__ x_off,
+                                                   int nrhs_fixed, int nrhs_mul, int ldmul,
+                                                   const int32_t* __restrict__ skip, const float* __restrict__ rs,
+                                                   const float* __restrict__ cs) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int k = blockIdx.y;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const int n = nsz[k];
+  const int nrhs = nrhs_fixed > 0 ? nrhs_fixed : nrhs_mul * n;
+  const int col = blockIdx.x;
+  if (col >= nrhs) return;
+  const int64_t ldx = (int64_t)ldmul * n;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  T* xs = reinterpret_cast<T*>(smraw);
+  T* tile = xs + n;                                  // 32 x 32 block, column-major, ld 33
+  const T* M = LU + mat_off[k];
+  const int32_t* ip = piv + piv_off[k];
+  zc* xg = X + x_off[k] + (size_t)col * ldx;
+  const float* R = rs ? rs + piv_off[k] : nullptr;
+  const float* C = cs ? cs + piv_off[k] : nullptr;
+  const T zero = cx<T>::make(0, 0);
+  for (int r = tid; r < n; r += blockDim.x) {
+    zc b = xg[r];
+    if (R) b = zscale(b, (double)R[r]);
+    xs[r] = cx<T>::from(b);
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int j = 0; j < n; ++j) {
+      const int p = ip[j];
+      if (p != j) { T t = xs[j]; xs[j] = xs[p]; xs[p] = t; }
+    }
+  __syncthreads();
+  // L y = b, unit diagonal
+  for (int jb = 0; jb < n; jb += 32) {
+    const int bs = min(32, n - jb);
+    for (int e = tid; e < bs * bs; e += blockDim.x) {
+      const int c = e / bs, r = e % bs;
+      tile[c * 33 + r] = M[(size_t)(jb + c) * n + jb + r];
+    }
+    __syncthreads();
+    if (warp == 0) {
+      T x = lane < bs ? xs[jb + lane] : zero;
+      for (int j = 0; j < bs; ++j) {
+        const T xj = shfl_cx(x, j);
+        if (lane > j && lane < bs) x = cx<T>::sub(x, cx<T>::mul(tile[j * 33 + lane], xj));
+      }
+      if (lane < bs) xs[jb + lane] = x;
+    }
+    __syncthreads();
+    for (int r = jb + bs + tid; r < n; r += blockDim.x) {
+      T acc = xs[r];
+      for (int j = 0; j < bs; ++j) acc = cx<T>::sub(acc, cx<T>::mul(M[(size_t)(jb + j) * n + r], xs[jb + j]));
+      xs[r] = acc;
+    }
+    __syncthreads();
+  }
+  // U x = y, blocks from the bottom; a zero diagonal entry is skipped
+  for (int jb = ((n - 1) / 32) * 32; jb >= 0; jb -= 32) {
+    const int bs = min(32, n - jb);
+    for (int e = tid; e < bs * bs; e += blockDim.x) {
+      const int c = e / bs, r = e % bs;
+      tile[c * 33 + r] = M[(size_t)(jb + c) * n + jb + r];
+    }
+    __syncthreads();
+    if (warp == 0) {
+      T x = lane < bs ? xs[jb + lane] : zero;
+      for (int j = bs - 1; j >= 0; --j) {
+        const T d = tile[j * 33 + j];
+        if (lane == j && cx<T>::abs1(d) != 0) x = cx<T>::div(x, d);
+        const T xj = shfl_cx(x, j);
+        if (lane < j) x = cx<T>::sub(x, cx<T>::mul(tile[j * 33 + lane], xj));
+      }
+      if (lane < bs) xs[jb + lane] = x;
+    }
+    __syncthreads();
+    for (int r = tid; r < jb; r += blockDim.x) {
+      T acc = xs[r];
+      for (int j = 0; j < bs; ++j) acc = cx<T>::sub(acc, cx<T>::mul(M[(size_t)(jb + j) * n + r], xs[jb + j]));
+      xs[r] = acc;
+    }
+    __syncthreads();
+  }
+  for (int r = tid; r < n; r += blockDim.x) {
+    zc y = cx<T>::to64(xs[r]);
+    xg[r] = C ? zscale(y, (double)C[r]) : y;
+  }
+}
+
 // ---- host launchers ------------------------------------------------------
 template <typename T>
 int lu_nb_for(int n) {
@@ -338,7 +444,16 @@ cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, c
                          const float* cs) {
   const int nrhs_max = nrhs_fixed > 0 ? nrhs_fixed : nrhs_mul * nmax;
   if (count <= 0 || nrhs_max <= 0) return cudaSuccess;
-  const int warps = nrhs_max >= 8 ? 8 : 1;
+  if (nrhs_max < 8) {   // few right-hand sides: a whole CTA per column
+    size_t sm = (size_t)nmax * sizeof(T) + 32 * 33 * sizeof(T);
+    cudaError_t e = cudaFuncSetAttribute(k_getrs_blk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    dim3 g(nrhs_max, count);
+    k_getrs_blk<T><<<g, 256, sm, s>>>(count, nsz, LU, mat_off, piv, piv_off, X, x_off, nrhs_fixed, nrhs_mul, ldmul,
+                                      skip, rs, cs);
+    return cudaGetLastError();
+  }
+  const int warps = 8;
   size_t sm = (size_t)warps * nmax * sizeof(T);
   cudaError_t e = cudaFuncSetAttribute(k_getrs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;

@@ -110,6 +110,29 @@ __global__ void k_vec_init(int count, const InstDesc* __restrict__ desc, zc* __r
   vec[d.off_vec + (int64_t)slot * d.n + q] = zmk(1.0 + a, b - 0.5);
 }
 
+// Start vector from Chebyshev coefficients of the five fields (a surrogate's
+// prediction): x(node i, field e) = sum_{q < ncheb} c[e][q] T_q(eta_i) with
+// eta_i = cos(pi i / (ny - 1)), so T_q(eta_i) = cos(q pi i / (ny - 1)).
+// coef: ncheb * 5 complex values per instance (field-major), internal order.
+__global__ void k_cheb_start(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ coef, int ncheb,
+                             zc* __restrict__ vec, int slot, const int32_t* __restrict__ skip) {
+  const int k = blockIdx.y;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const InstDesc d = desc[k];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.n) return;
+  const int i = q / 5, e = q % 5;
+  const zc* c = coef + ((int64_t)k * 5 + e) * ncheb;
+  const double th = 3.14159265358979323846 * (double)i / (double)(d.ny - 1);
+  zc s = zmk(0.0, 0.0);
+  for (int t = 0; t < ncheb; ++t) {
+    const double w = cos((double)t * th);
+    s = zmk(s.x + w * c[t].x, s.y + w * c[t].y);
+  }
+  vec[d.off_vec + (int64_t)slot * d.n + q] = s;
+}
+
 // x <- x / x_p with p = first index of max |x|; writes p to piv_out when non-null
 __global__ void k_normalize(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int slot,
                             int32_t* __restrict__ piv_out, const int32_t* __restrict__ skip) {
@@ -373,6 +396,14 @@ cudaError_t launch_reset_polish(int count, int32_t* done, int32_t* iters, const 
                                 int32_t* lus, int nlu) {
   if (count <= 0) return cudaSuccess;
   k_reset_polish<<<(count + 255) / 256, 256, 0, s>>>(count, done, iters, skip, lus, nlu);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cheb_start(int count, int nmax, const InstDesc* desc, const zc* coef, int ncheb, zc* vec,
+                              int slot, const int32_t* skip, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  dim3 g((nmax + 127) / 128, count);
+  k_cheb_start<<<g, 128, 0, s>>>(count, desc, coef, ncheb, vec, slot, skip);
   return cudaGetLastError();
 }
 

@@ -206,3 +206,20 @@ def test_bad_profile_is_reported_not_solved(ctx):
     eig, err, iters, status, _ = ctx.solve_batch([H.stab_params(d), H.stab_params(d)], [prof, bad], sg.MODE_PLAIN)
     assert status[0] == sg.ST_OK
     assert status[1] != sg.ST_OK
+
+
+def test_coarse_graph_replay_matches_eager(ctx):
+    """The second and later STAB_MODE_COARSE passes replay a captured CUDA
+    graph of the device sequence; results must equal the eager first pass."""
+    rng = np.random.Generator(np.random.PCG64(23))
+    cases = [H.synth_case(1, int(rng.choice([24, 32, 48])), float(rng.uniform(0.2, 1.5)),
+                          float(10 ** rng.uniform(2.5, 3.4)), a=float(rng.uniform(0.05, 0.4)),
+                          b=float(rng.uniform(0, 0.3))) for _ in range(6)]
+    b = ctx.batch([H.stab_params(d) for d, _ in cases], [p for _, p in cases])
+    outs = []
+    for _ in range(3):
+        b.run(sg.MODE_COARSE)
+        outs.append(b.results())
+    for o in outs[1:]:
+        assert np.array_equal(o[0], outs[0][0]) and np.array_equal(o[3], outs[0][3])
+    b.close()

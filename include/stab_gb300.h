@@ -51,6 +51,9 @@ extern "C" {
 #define STAB_MODE_SEEDED 1    /* mixed-precision polish from caller seeds        */
 #define STAB_MODE_COARSE 2    /* seeds from an FP64 full spectrum at N = 32,     *
                                * then the mixed-precision polish                 */
+#define STAB_MODE_TRACK 4     /* polish from caller guesses; where it fails, the *
+                               * FP64 spectrum's eigenvalue nearest the guess    *
+                               * (the pick of getab.f90:185-192)                 */
 #define STAB_MODE_SURROGATE 3 /* polish from predicted seeds (and start vectors, *
                                * stab_batch_set_start); pairs that fail the      *
                                * acceptance gate take the STAB_MODE_COARSE path  */
@@ -214,7 +217,8 @@ int stab_batch_create(stab_ctx* ctx, int32_t count, const stab_params* p, const 
  * alpha for spatial), copied to the device. */
 int stab_batch_set_seeds(stab_batch* b, const double* seeds);
 /*
- * Start vectors for STAB_MODE_SURROGATE: per instance 5 x ncheb complex
+ * Start vectors for STAB_MODE_SURROGATE and STAB_MODE_TRACK (ncheb <= 256):
+ * per instance 5 x ncheb complex
  * Chebyshev coefficients (field-major: rho, u, v, w, T), evaluated at the
  * instance's collocation points, x(i, e) = sum_q c[e][q] cos(q pi i/(ny-1)).
  * ncheb = 0 clears them (the generic start vector is used).

@@ -1092,3 +1092,39 @@ def synthetic_profile(M: float, ymax: float = 50.0, nym: int = 2000, erf_width: 
     rho = 1.0 / T
     vt = np.stack([rho, U, np.zeros_like(y), W, T], axis=1)
     return y, vt
+
+
+# ---------------------------------------------------------------------------
+# mode tracking across sweep files (getab / getax / getalpha)
+# ---------------------------------------------------------------------------
+def track_pick(spectra, param, start, rule):
+    """Picks of the reference's post-processors over a sweep.
+
+    spectra[j]: eigenvalues of point j; param[j]: swept value; start: the
+    user's typed values for the first 1 ('nearest', getalpha.f90:120-146) or
+    2 ('extrapolate', getab.f90:161-201, getax.f90:161-201) points.  Each pick
+    is the first eigenvalue nearest the guess (strict '<' scan, as the
+    reference's loops)."""
+    picks = []
+    for j, ev in enumerate(spectra):
+        if j < len(start):
+            g = complex(start[j])
+        elif rule == "nearest" or j < 2:
+            g = picks[j - 1]
+        else:
+            e1, p1 = picks[j - 1], param[j - 1]
+            e2, p2 = picks[j - 2], param[j - 2]
+            g = e1 + (e2 - e1) / (p2 - p1) * (param[j] - p1)
+        d = np.abs(np.asarray(ev) - g)
+        picks.append(complex(ev[int(np.argmin(d))]))
+    return picks
+
+
+def stab_out_text(param, values, ind=None):
+    """stab.out of getab (format 60: 3(1x,1pe20.13)) or, with ind, of getax /
+    parm.new of getalpha (format 50: i4,3(1x,1pe20.13))."""
+    lines = []
+    for j, (p, v) in enumerate(zip(param, values)):
+        f = "".join(" " + fortran_e(float(t), 20, 13, None) for t in (p, v.real, v.imag))
+        lines.append((f"{int(ind[j]):4d}" if ind is not None else "") + f)
+    return "\n".join(lines) + "\n"

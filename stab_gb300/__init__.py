@@ -20,13 +20,13 @@ from typing import Optional, Sequence
 import numpy as np
 
 __all__ = ["StabParams", "EvecHeader", "Context", "Network", "load", "LIB_PATH", "parse_input", "profile_name",
-           "read_profile", "grid", "write_evec", "read_evec", "getevec_select", "eigfunction_text", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE", "MODE_SURROGATE",
+           "read_profile", "grid", "write_evec", "read_evec", "getevec_select", "eigfunction_text", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE", "MODE_SURROGATE", "MODE_TRACK",
            "ST_OK", "ST_SINGULAR", "ST_NOCONV", "ST_NAN", "ST_FELLBACK", "ST_NOMODE", "StabError"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libstab_gb300.so")
 
-MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE = 0, 1, 2, 3
+MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE, MODE_TRACK = 0, 1, 2, 3, 4
 ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE = 0, 1, 2, 3, 4, 5
 
 EXPORTED = (

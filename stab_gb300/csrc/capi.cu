@@ -5,6 +5,7 @@
 // first and all spatial ones after (stable), so each phase launches on
 // contiguous ranges; results are mapped back to the caller's order.
 #include <algorithm>
+#include <cmath>
 #include <type_traits>
 #include <cstdio>
 #include <cstring>
@@ -827,7 +828,7 @@ static int batch_run(stab_batch* b, int32_t mode) {
     b->ran = true;
     return 0;
   }
-  if (mode == STAB_MODE_SEEDED || mode == STAB_MODE_SURROGATE) {
+  if (mode == STAB_MODE_SEEDED || mode == STAB_MODE_SURROGATE || mode == STAB_MODE_TRACK) {
     if (!b->have_seeds) return set_err(c, STAB_ERR_STATE, "seeded modes need stab_batch_set_seeds first");
     std::vector<zc> sg(b->count);
     for (int k = 0; k < b->count; ++k) {
@@ -841,7 +842,7 @@ static int batch_run(stab_batch* b, int32_t mode) {
     }
     CK(c, cudaMemcpyAsync(b->sigma.p, sg.data(), sizeof(zc) * b->count, cudaMemcpyHostToDevice, s));
     b->use_start = false;
-    if (mode == STAB_MODE_SURROGATE && b->ncheb > 0) {
+    if ((mode == STAB_MODE_SURROGATE || mode == STAB_MODE_TRACK) && b->ncheb > 0) {
       // start vectors from the predicted Chebyshev coefficients, internal order
       const size_t per = (size_t)5 * b->ncheb;
       std::vector<zc> co(per * b->count);
@@ -1087,7 +1088,11 @@ static int polish_candidate_rounds(stab_batch* b) {
 // Re-solve, with the plain FP64 path, every instance whose polish did not
 // converge (or had no accepted shift); results are kept on the host for
 // stab_batch_results.
-static int run_fallback(stab_batch* b) {
+// FP64 fallback on the instances whose polish did not converge.  With
+// `track` (STAB_MODE_TRACK) the kept eigenvalue is the one nearest the
+// instance's seed, as the reference's post-processors pick a mode from a
+// guess (getevec.f90:161-172, getab.f90:185-192), instead of the least-stable.
+static int run_fallback(stab_batch* b, bool track = false) {
   stab_ctx* c = b->ctx;
   const int n = b->count;
   std::vector<int32_t> dn(n);
@@ -1124,9 +1129,45 @@ static int run_fallback(stab_batch* b) {
   std::unique_ptr<stab_batch> guard(fb);
   rc = run_prep(fb);
   if (rc) return rc;
-  rc = run_plain(fb, true, "k_eig_plain_fallback");
+  rc = run_plain(fb, !track, "k_eig_plain_fallback");
   if (rc) return rc;
   const int nf = fb->count;
+  if (track) {
+    // nearest eigenvalue (user variable: omega or alpha) to the seed; then
+    // its eigenvector by the same FP64 inverse iteration
+    std::vector<zc> spec(fb->sum_m), pick_raw(nf), pick_val(nf);
+    std::vector<int32_t> pidx(nf, -1);
+    CK(c, cudaMemcpyAsync(spec.data(), fb->eigsorted.p, sizeof(zc) * fb->sum_m, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < nf; ++q) {
+      const int u = b->perm[b->fell_back[fb->perm[q]]];   // caller index of sub-batch entry q
+      const zc sd = zmk(b->seeds[2 * u], b->seeds[2 * u + 1]);
+      const zc* e = spec.data() + fb->h_mof[q];
+      double best = INFINITY;
+      int j = 0;
+      for (int t = 0; t < fb->hm[q]; ++t) {
+        const double d = std::hypot(e[t].x - sd.x, e[t].y - sd.y);
+        if (d < best) { best = d; j = t; }
+      }
+      pidx[q] = j;
+      pick_val[q] = e[j];
+      zc r = e[j];
+      if (fb->P[q].itype == 2) {
+        const double dd = r.x * r.x + r.y * r.y;
+        r = dd > 0 ? zmk(r.x / dd, -r.y / dd) : zmk(0.0, 0.0);
+      }
+      pick_raw[q] = r;
+    }
+    CK(c, cudaMemcpyAsync(fb->least_val.p, pick_val.data(), sizeof(zc) * nf, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(fb->least_raw.p, pick_raw.data(), sizeof(zc) * nf, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(fb->least_idx.p, pidx.data(), sizeof(int32_t) * nf, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(fb->theta.p, fb->least_raw.p, sizeof(zc) * nf, cudaMemcpyDeviceToDevice, c->stream));
+    const Range fall{0, nf};
+    rc = eigvec_inverse_iteration(fb, fall, fb->theta.as<zc>());
+    if (rc) return rc;
+    rc = write_vectors(fb, fall, fb->theta.as<zc>());
+    if (rc) return rc;
+  }
   std::vector<zc> val(nf);
   std::vector<int32_t> st(nf), li(nf);
   CK(c, cudaMemcpyAsync(val.data(), fb->least_val.p, sizeof(zc) * nf, cudaMemcpyDeviceToHost, c->stream));
@@ -1284,6 +1325,7 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
   int rc = batch_run(b, mode);
   if (rc) return rc;
   if (mode == STAB_MODE_SEEDED) return run_fallback(b);
+  if (mode == STAB_MODE_TRACK) return run_fallback(b, true);
   if (mode == STAB_MODE_SURROGATE) return run_coarse_sub(b);
   b->counts[0] = b->count;
   b->counts[1] = b->counts[2] = 0;
@@ -1293,7 +1335,7 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
 int stab_batch_set_start(stab_batch* b, const double* coef, int32_t ncheb) {
   if (!b) return STAB_ERR_ARG;
   if (!b->ctx) return STAB_ERR_STATE;
-  if (ncheb < 0 || ncheb > 64 || (ncheb > 0 && !coef)) return set_err(b->ctx, STAB_ERR_ARG, "ncheb must be 0..64");
+  if (ncheb < 0 || ncheb > 256 || (ncheb > 0 && !coef)) return set_err(b->ctx, STAB_ERR_ARG, "ncheb must be 0..256");
   b->ncheb = ncheb;
   b->start_coef.assign(coef ? coef : nullptr, coef ? coef + 2 * (size_t)5 * ncheb * b->count : nullptr);
   return STAB_OK;

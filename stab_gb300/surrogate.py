@@ -13,7 +13,7 @@ Outputs: Re(omega)/alpha, 100 Im(omega)/alpha, then Re and Im of the
 
 The network is trained on the GPU by the library's own kernels (the
 ``stab_mlp_*`` entry points, tensor-core BF16 GEMMs with float32
-accumulation), on solves of the plain FP64 batched path at N = 32, and it
+accumulation), on solves of the plain FP64 batched path at N = 64, and it
 seeds ``MODE_SURROGATE``: the polish starts from the predicted omega and the
 start vector evaluated from the predicted coefficients, and instances whose
 pair fails the acceptance gate take the coarse-seeded path.  PyTorch only
@@ -31,7 +31,7 @@ import stab_gb300 as sg
 
 SIZES = (6, 256, 256, 256, 256, 162)
 NCHEB = 16
-TRAIN_NY = 32
+TRAIN_NY = 64
 T0_SUTHERLAND = 110.4 / 0.3815      # S / T_inf = 0.3815 with S = 110.4 K
 LOSS_WEIGHTS = np.concatenate([[4.0, 4.0], np.full(160, 0.1)]).astype(np.float32)
 
@@ -104,9 +104,12 @@ def chebyshev_eval(coef: np.ndarray, ny: int) -> np.ndarray:
     return (T @ coef.T).reshape(-1)                # node-major: 5 i + e
 
 
-def make_dataset(ctx: sg.Context, count: int, seed: int, ranges: Optional[dict] = None, chunk: int = 4096) -> dict:
+def make_dataset(ctx: sg.Context, count: int, seed: int, ranges: Optional[dict] = None, chunk: int = 4096,
+                 ny: int = TRAIN_NY) -> dict:
     """Least-stable omega and eigenvector coefficients from the plain FP64
-    batched path at N = 32 on `count` sampled instances."""
+    batched path at N = ny (default 64, where the supersonic discrete modes
+    are resolved; N = 32 still carries unresolved modes above them) on
+    `count` sampled instances."""
     P = sample_params(count, seed, ranges)
     w = np.zeros(count, dtype=np.complex128)
     coef = np.zeros((count, 5, NCHEB), dtype=np.complex128)
@@ -114,14 +117,14 @@ def make_dataset(ctx: sg.Context, count: int, seed: int, ranges: Optional[dict] 
     t0 = time.perf_counter()
     for k0 in range(0, count, chunk):
         idx = range(k0, min(count, k0 + chunk))
-        params = [stab_params(P["M"][k], P["Re"][k], P["alpha"][k], P["beta"][k], TRAIN_NY) for k in idx]
+        params = [stab_params(P["M"][k], P["Re"][k], P["alpha"][k], P["beta"][k], ny) for k in idx]
         profs = [erf_profile(P["M"][k], P["width"][k]) for k in idx]
         eig, err, iters, st, vecs = ctx.solve_batch(params, profs, sg.MODE_PLAIN, want_vectors=True)
         for j, k in enumerate(idx):
             if st[j] == sg.ST_OK and np.all(np.isfinite(vecs[j])):
                 ok[k] = True
                 w[k] = eig[j]
-                coef[k] = chebyshev_coefficients(vecs[j], TRAIN_NY)
+                coef[k] = chebyshev_coefficients(vecs[j], ny)
     return {"params": P, "omega": w, "coef": coef, "valid": ok, "seconds": time.perf_counter() - t0}
 
 

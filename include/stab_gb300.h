@@ -54,9 +54,9 @@ extern "C" {
 #define STAB_MODE_TRACK 4     /* polish from caller guesses; where it fails, the *
                                * FP64 spectrum's eigenvalue nearest the guess    *
                                * (the pick of getab.f90:185-192)                 */
-#define STAB_MODE_SURROGATE 3 /* polish from predicted seeds (and start vectors, *
-                               * stab_batch_set_start); pairs that fail the      *
-                               * acceptance gate take the STAB_MODE_COARSE path  */
+#define STAB_MODE_SURROGATE 3 /* STAB_MODE_COARSE plus the caller's predicted    *
+                               * seed (and start vector, stab_batch_set_start)   *
+                               * as one more candidate round                     */
 
 /*
  * Run parameters of one solve: a mirror of module `stuff` (stuff.f90:11-55)
@@ -116,6 +116,16 @@ int stab_reset_kernel_stats(stab_ctx* ctx);
  */
 int stab_assemble(stab_ctx* ctx, const stab_params* p, int32_t nym, const double* profile,
                   double* mats_out);
+
+/* ---- autotuning --------------------------------------------------------- */
+/*
+ * Time the batched LU of both precisions at each order in orders[] with
+ * every shared-memory-feasible panel width (8, 16, 32) on a full wave of
+ * test matrices, and keep the fastest per size class in the context; later
+ * factorisations of that class use it.  nb_out / ms_out (may be NULL):
+ * 2 * norders entries, [2q] complex64 and [2q+1] complex128 choice and time.
+ */
+int stab_autotune(stab_ctx* ctx, const int32_t* orders, int32_t norders, int32_t* nb_out, float* ms_out);
 
 /* ---- full spectrum (plain FP64 path) --------------------------------- */
 /*
@@ -225,16 +235,22 @@ int stab_batch_set_seeds(stab_batch* b, const double* seeds);
  */
 int stab_batch_set_start(stab_batch* b, const double* coef, int32_t ncheb);
 /*
- * Run the whole path on the device.  STAB_MODE_SURROGATE keeps a polished
- * pair only when it converged within 6 Newton steps, within 0.1 |seed| of
- * its seed, passes the least-stable filter and (temporal) lies above the
- * vorticity-continuum branch point omega = alpha - i (alpha^2 + beta^2)/Re;
- * the other instances (and every spatial one) run the STAB_MODE_COARSE path.
+ * Run the whole path on the device.  STAB_MODE_SURROGATE polishes the coarse
+ * candidates and then, for the instances not yet final, the caller's seed
+ * (a surrogate's prediction); the least-stable converged pair wins.  It adds
+ * what the N = 32 spectrum cannot give: discrete modes that N = 32 does not
+ * resolve (supersonic second modes), whose coarse candidates are spurious.
  */
 int stab_batch_run(stab_batch* b, int32_t mode);
+/* After a STAB_MODE_PLAIN run: every instance's full spectrum, sorted as
+ * stab_full_spectrum sorts it; eig_out[k] (caller order, NULL skips) receives
+ * n_k complex values.  The eigenvalue record of a sweep point's evec.dat
+ * (the eig.N files of mtemporal.f90:29-39 and mspatial.f90:77-96). */
+int stab_batch_spectra(stab_batch* b, double* const* eig_out);
 /* After a run: counts_out[0] instances resolved by the first stage (the
- * seeds, the coarse candidates, or the plain path), [1] resolved by the
- * coarse sub-batch of STAB_MODE_SURROGATE, [2] sent to the FP64 fallback. */
+ * seeds, the coarse candidates, or the plain path), [1] whose kept pair came
+ * from the caller's seed in STAB_MODE_SURROGATE, [2] sent to the FP64
+ * fallback. */
 int stab_batch_counts(stab_batch* b, int32_t* counts_out);
 /*
  * Copy results back (synchronises): eig_out[2*k] least-stable eigenvalue,

@@ -38,6 +38,7 @@ EXPORTED = (
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
+    "stab_batch_spectra", "stab_autotune",
 )
 
 
@@ -147,6 +148,8 @@ def load(path: str = LIB_PATH):
     lib.stab_mlp_destroy.argtypes = [vp]
     lib.stab_batch_set_start.argtypes = [vp, P(dbl), i32]
     lib.stab_batch_counts.argtypes = [vp, P(i32)]
+    lib.stab_batch_spectra.argtypes = [vp, P(P(dbl))]
+    lib.stab_autotune.argtypes = [vp, P(i32), i32, P(i32), P(ctypes.c_float)]
     _lib = lib
     return lib
 
@@ -198,11 +201,18 @@ class Batch:
     def run(self, mode: int) -> None:
         self.ctx._check(self.lib.stab_batch_run(self.h, int(mode)))
 
+    def spectra(self) -> list:
+        """Sorted full spectra after a MODE_PLAIN run (stab_batch_spectra)."""
+        out = [np.zeros(p.m(), dtype=np.complex128) for p in self.params]
+        ptrs = (ctypes.POINTER(ctypes.c_double) * self.count)(*[_dptr(v.view(np.float64)) for v in out])
+        self.ctx._check(self.lib.stab_batch_spectra(self.h, ptrs))
+        return out
+
     def counts(self) -> dict:
         """Where the last run resolved its instances (stab_batch_counts)."""
         c = np.zeros(3, dtype=np.int32)
         self.ctx._check(self.lib.stab_batch_counts(self.h, _iptr(c)))
-        return {"first_stage": int(c[0]), "coarse_sub_batch": int(c[1]), "fp64_fallback": int(c[2])}
+        return {"first_stage": int(c[0]), "surrogate_seed": int(c[1]), "fp64_fallback": int(c[2])}
 
     def results(self, want_vectors: bool = False):
         n = self.count
@@ -362,6 +372,16 @@ class Context:
                                                    ctypes.byref(ms), None))
             out[name.value.decode()] = (la.value, ms.value)
         return out
+
+    def autotune(self, orders: Sequence[int]) -> dict:
+        """Tune the LU panel width per order (stab_autotune): {n: {"c64": (nb, ms), "c128": (nb, ms)}}."""
+        o = np.asarray(orders, dtype=np.int32)
+        nb = np.zeros(2 * len(o), dtype=np.int32)
+        ms = np.zeros(2 * len(o), dtype=np.float32)
+        self._check(self.lib.stab_autotune(self.h, _iptr(o), len(o), _iptr(nb),
+                                           ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return {int(n): {"c64": (int(nb[2 * q]), float(ms[2 * q])), "c128": (int(nb[2 * q + 1]), float(ms[2 * q + 1]))}
+                for q, n in enumerate(o)}
 
     def reset_kernel_stats(self) -> None:
         self._check(self.lib.stab_reset_kernel_stats(self.h))

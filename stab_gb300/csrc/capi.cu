@@ -60,7 +60,20 @@ struct stab_ctx {
   int sms = 152;
   std::vector<stab_batch*> live;   // caller-visible batches, released by stab_destroy
   std::vector<stab_mlp*> nets;     // networks, released by stab_destroy
+  std::map<std::pair<int, int>, int> lu_nb;   // (complex128?, size class) -> tuned LU panel width
 };
+
+// size class of an LU order for the tuned panel-width table
+static int lu_class(int n) {
+  static const int cls[] = {160, 240, 320, 480, 640, 960, 1280, 1920};
+  for (int q : cls)
+    if (n <= q) return q;
+  return 1 << 30;
+}
+static int tuned_nb(stab_ctx* c, bool z, int n) {
+  auto it = c->lu_nb.find({z ? 1 : 0, lu_class(n)});
+  return it == c->lu_nb.end() ? 0 : it->second;
+}
 static void release_net(stab_mlp* m);
 
 static int set_err(stab_ctx* c, int code, const std::string& msg) {
@@ -208,6 +221,8 @@ struct stab_batch {
   int ncheb = 0;
   bool use_start = false;
   DevBuf startc;
+  DevBuf seed_raw, best_src;                  // STAB_MODE_SURROGATE: the extra candidate, winner per instance
+  int graph_mode = -1;                        // mode of the captured graph
   std::vector<zc> fb_val;
   std::vector<int32_t> fb_status;
   std::vector<std::vector<zc>> fb_vec;
@@ -510,7 +525,7 @@ static int eigvec_inverse_iteration(stab_batch* b, Range r, const zc* theta_dev)
   CK(c, timed(c, "k_lu_z", [&] {
     return launch_lu<zc>(r.cnt, D, b->nsz.as<int32_t>() + r.k0, b->nmax, b->Z64.as<zc>(),
                          b->off_n2.as<int64_t>() + r.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + r.k0,
-                         b->info.as<int32_t>() + r.k0, s);
+                         b->info.as<int32_t>() + r.k0, s, nullptr, tuned_nb(c, true, b->nmax));
   }));
   CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(r.cnt, b->nmax, D, b->vec.as<zc>(), 0, s); }));
   for (int it = 0; it < 3; ++it) {
@@ -571,7 +586,7 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
     CK(c, timed(c, "k_lu_z", [&] {
       return launch_lu<zc>(sr.cnt, D, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<zc>(),
                            b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + sr.k0,
-                           b->info.as<int32_t>() + sr.k0, s);
+                           b->info.as<int32_t>() + sr.k0, s, nullptr, tuned_nb(c, true, b->nmax));
     }));
     rc = node_ops(b, sr, OP_S_C1, OP_S_C1, nullptr);
     if (rc) return rc;
@@ -669,7 +684,8 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
     }
     return timed(c, n_lu, [&] {
       return launch_lu<T>(b->count, D, b->nsz.as<int32_t>(), b->nmax, MP, b->off_n2.as<int64_t>(),
-                          b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip);
+                          b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
+                          tuned_nb(c, !c64, b->nmax));
     });
   };
   auto solve32 = [&](int slot, const int32_t* sk) {
@@ -735,9 +751,6 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
 // ratio |sigma - lambda_1| / |sigma - lambda_2| per step, which separates
 // mode clusters that complex64 factors cannot resolve.
 static const int kInverseSteps = 12;
-// gate of the surrogate-seeded mode (k_seed_accept)
-static const double kSeedAcceptTol = 0.1;
-static const int kSeedAcceptIters = 6;
 static const double kInverseTol = 1e-13;
 
 static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
@@ -757,7 +770,8 @@ static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
   if (rc) return rc;
   CK(c, timed(c, "k_lu_z", [&] {
     return launch_lu<zc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
-                         b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip);
+                         b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
+                         tuned_nb(c, true, b->nmax));
   }));
   CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
   CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, b->pcol.as<int32_t>(), skip, s); }));
@@ -805,6 +819,19 @@ static void finalize_polish_host(std::vector<zc>& val, std::vector<int32_t>& st,
   }
 }
 
+// caller start-vector coefficients -> device, internal order
+static int upload_start(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  const size_t per = (size_t)5 * b->ncheb;
+  std::vector<zc> co(per * b->count);
+  for (int k = 0; k < b->count; ++k) {
+    const double* src = b->start_coef.data() + 2 * per * b->perm[k];
+    for (size_t q = 0; q < per; ++q) co[per * k + q] = zmk(src[2 * q], src[2 * q + 1]);
+  }
+  CK(c, upload(b->startc, co, c->stream));
+  return 0;
+}
+
 static int batch_run(stab_batch* b, int32_t mode) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
@@ -828,7 +855,7 @@ static int batch_run(stab_batch* b, int32_t mode) {
     b->ran = true;
     return 0;
   }
-  if (mode == STAB_MODE_SEEDED || mode == STAB_MODE_SURROGATE || mode == STAB_MODE_TRACK) {
+  if (mode == STAB_MODE_SEEDED || mode == STAB_MODE_TRACK) {
     if (!b->have_seeds) return set_err(c, STAB_ERR_STATE, "seeded modes need stab_batch_set_seeds first");
     std::vector<zc> sg(b->count);
     for (int k = 0; k < b->count; ++k) {
@@ -842,15 +869,9 @@ static int batch_run(stab_batch* b, int32_t mode) {
     }
     CK(c, cudaMemcpyAsync(b->sigma.p, sg.data(), sizeof(zc) * b->count, cudaMemcpyHostToDevice, s));
     b->use_start = false;
-    if ((mode == STAB_MODE_SURROGATE || mode == STAB_MODE_TRACK) && b->ncheb > 0) {
-      // start vectors from the predicted Chebyshev coefficients, internal order
-      const size_t per = (size_t)5 * b->ncheb;
-      std::vector<zc> co(per * b->count);
-      for (int k = 0; k < b->count; ++k) {
-        const double* src = b->start_coef.data() + 2 * per * b->perm[k];
-        for (size_t q = 0; q < per; ++q) co[per * k + q] = zmk(src[2 * q], src[2 * q + 1]);
-      }
-      CK(c, upload(b->startc, co, s));
+    if (mode == STAB_MODE_TRACK && b->ncheb > 0) {
+      int rc2 = upload_start(b);
+      if (rc2) return rc2;
       b->use_start = true;
     }
     CK(c, cudaStreamSynchronize(s));
@@ -860,14 +881,6 @@ static int batch_run(stab_batch* b, int32_t mode) {
   rc = run_polish(b, true);
   b->use_start = false;
   if (rc) return rc;
-  if (mode == STAB_MODE_SURROGATE) {
-    CK(c, timed(c, "k_seed_accept", [&] {
-      k_seed_accept<<<(b->count + 127) / 128, 128, 0, s>>>(b->count, b->desc.as<InstDesc>(), b->sigma.as<zc>(),
-                                                            b->theta.as<zc>(), b->done.as<int32_t>(),
-                                                            b->iters.as<int32_t>(), kSeedAcceptTol, kSeedAcceptIters);
-      return cudaGetLastError();
-    }));
-  }
   b->ran = true;
   return 0;
 }
@@ -1035,7 +1048,7 @@ static int coarse_seeds(stab_batch* b) {
 // kQuickAcceptTol of its shift the instance is final; otherwise the next
 // candidates are polished too.  Instances with no converged pair go to the
 // FP64 full-spectrum fallback.
-static int polish_candidate_rounds(stab_batch* b) {
+static int polish_candidate_rounds(stab_batch* b, bool extra) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   const int n = b->count;
@@ -1053,16 +1066,23 @@ static int polish_candidate_rounds(stab_batch* b) {
   CK(c, cudaMemsetAsync(b->have.p, 0, sizeof(int32_t) * n, s));
   // per candidate: a complex64 round, then a complex128 retry for the
   // instances where it failed or contracted slowly
-  for (int r = 0; r < 2 * kShiftCandidates; ++r) {
+  CK(c, b->best_src.ensure(sizeof(int32_t) * n, s));
+  const int rounds = 2 * kShiftCandidates + (extra ? 2 : 0);
+  for (int r = 0; r < rounds; ++r) {
     const int j = r / 2;
     const bool fp64 = (r & 1) != 0;
-    if (!fp64) {
+    const bool surrogate = (j == kShiftCandidates);   // the caller's predicted seed
+    if (!fp64 && !surrogate) {
       CK(c, timed(c, "k_take_candidate", [&] {
         k_take_candidate<<<(n + 255) / 256, 256, 0, s>>>(n, b->cand.as<zc>(), kShiftCandidates, j, b->sigma.as<zc>());
         return cudaGetLastError();
       }));
+    } else if (!fp64) {
+      CK(c, cudaMemcpyAsync(b->sigma.p, b->seed_raw.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
     }
+    b->use_start = surrogate && !fp64 && b->ncheb > 0;
     int rc = fp64 ? run_polish64_ii(b, true, b->skip64.as<int32_t>()) : run_polish_t<cc>(b, true, fin);
+    b->use_start = false;
     if (rc) return rc;
     CK(c, timed(c, "k_fold_best", [&] {
       k_fold_best<<<n, 128, 0, s>>>(n, b->desc.as<InstDesc>(), b->sigma.as<zc>(), b->theta.as<zc>(),
@@ -1070,7 +1090,8 @@ static int polish_candidate_rounds(stab_batch* b) {
                                     b->outvec.as<zc>(), b->off_mof.as<int64_t>(), fin, b->have.as<int32_t>(),
                                     b->best_key.as<double>(), b->best_theta.as<zc>(), b->best_err.as<double>(),
                                     b->best_iters.as<int32_t>(), b->best_out.as<zc>(), j == 0 ? 1 : 0,
-                                    kQuickAcceptTol, fp64 ? nullptr : b->skip64.as<int32_t>(), kSlowNewton);
+                                    kQuickAcceptTol, fp64 ? nullptr : b->skip64.as<int32_t>(), kSlowNewton, j,
+                                    b->best_src.as<int32_t>());
       return cudaGetLastError();
     }));
   }
@@ -1110,6 +1131,15 @@ static int run_fallback(stab_batch* b, bool track = false) {
   b->counts[0] = n - (int)b->fell_back.size();
   b->counts[1] = 0;
   b->counts[2] = (int)b->fell_back.size();
+  if (b->last_mode == STAB_MODE_SURROGATE) {
+    std::vector<int32_t> src(n), hv(n);
+    CK(c, cudaMemcpyAsync(src.data(), b->best_src.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(hv.data(), b->have.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < n; ++k)
+      if (dn[k] == 1 && hv[k] && src[k] == kShiftCandidates) b->counts[1] += 1;
+    b->counts[0] -= b->counts[1];
+  }
   if (b->fell_back.empty()) return 0;
   auto it = g_inputs.find(b);
   if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
@@ -1203,93 +1233,31 @@ static int run_fallback(stab_batch* b, bool track = false) {
   return 0;
 }
 
-// Surrogate-seeded mode: the instances the gate did not accept run the
-// coarse-seeded path as a sub-batch (with its own FP64 fallback); their
-// results replace the polish's.
-static int run_coarse_sub(stab_batch* b) {
-  stab_ctx* c = b->ctx;
-  const int n = b->count;
-  std::vector<int32_t> dn(n);
-  CK(c, cudaMemcpyAsync(dn.data(), b->done.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaStreamSynchronize(c->stream));
-  b->fell_back.clear();
-  for (double& w : b->fb_work) w = 0.0;
-  b->fb_val.clear();
-  b->fb_status.clear();
-  b->fb_vec.clear();
-  b->fb_err.clear();
-  b->fb_iters.clear();
-  for (int k = 0; k < n; ++k)
-    if (dn[k] != 1) b->fell_back.push_back(k);
-  b->counts[0] = n - (int)b->fell_back.size();
-  b->counts[1] = b->counts[2] = 0;
-  if (b->fell_back.empty()) return 0;
-  auto it = g_inputs.find(b);
-  if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
-  BatchInputs sub;
-  for (int k : b->fell_back) {
-    const int u = b->perm[k];
-    sub.p.push_back(it->second.p[u]);
-    sub.nym.push_back(it->second.nym[u]);
-    sub.prof.push_back(it->second.prof[u]);
-  }
-  const int nf = (int)sub.p.size();
-  stab_batch* fb = nullptr;
-  int rc = batch_build(c, nf, sub.p.data(), sub.nym.data(), sub.prof.data(), &fb, 0);
-  if (rc) return rc;
-  std::unique_ptr<stab_batch> guard(fb);
-  g_inputs[fb] = sub;
-  rc = stab_batch_run(fb, STAB_MODE_COARSE);
-  std::vector<double> eig(2 * (size_t)nf), er(nf), w(4, 0.0);
-  std::vector<int32_t> itv(nf), st(nf);
-  std::vector<std::vector<zc>> vecs(nf);
-  std::vector<double*> vp(nf);
-  for (int q = 0; q < nf; ++q) {
-    vecs[q].resize(b->hm[b->fell_back[q]]);
-    vp[q] = reinterpret_cast<double*>(vecs[q].data());
-  }
-  if (rc == 0) rc = stab_batch_results(fb, eig.data(), er.data(), itv.data(), st.data(), vp.data());
-  if (rc == 0) rc = stab_batch_work(fb, w.data());
-  g_inputs.erase(fb);
-  if (rc) return rc;
-  for (int i = 0; i < 4; ++i) b->fb_work[i] += w[i];
-  b->fb_val.resize(nf);
-  b->fb_status.assign(st.begin(), st.end());
-  b->fb_err = er;
-  b->fb_iters = itv;
-  b->fb_vec = std::move(vecs);
-  for (int q = 0; q < nf; ++q) {
-    b->fb_val[q] = zmk(eig[2 * q], eig[2 * q + 1]);
-    if (st[q] == STAB_ST_FELLBACK) b->counts[2] += 1;
-    else b->counts[1] += 1;
-  }
-  return 0;
-}
-
-static int coarse_sequence(stab_batch* b) {
+static int coarse_sequence(stab_batch* b, bool extra) {
   int rc = run_prep(b);
   if (rc) return rc;
   rc = coarse_seeds(b);
   if (rc) return rc;
-  return polish_candidate_rounds(b);
+  return polish_candidate_rounds(b, extra);
 }
 
 // The device part of a STAB_MODE_COARSE pass is a fixed sequence of ~400
 // launches whose per-instance choices live in device masks, so after a first
 // eager pass (which sizes every pool) it is captured into a CUDA graph and
 // replayed.  Per-kernel profiling and the legacy stream run eagerly.
-static int run_coarse_device(stab_batch* b) {
+static int run_coarse_device(stab_batch* b, bool extra) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
-  const bool graphable = !c->profiling && s != nullptr && b->coarse_runs > 0;
-  if (b->coarse_graph && b->graph_stream != s) {
+  const int gmode = extra ? STAB_MODE_SURROGATE : STAB_MODE_COARSE;
+  const bool graphable = !c->profiling && s != nullptr && b->coarse_runs > 0 && b->graph_mode == gmode;
+  if (b->coarse_graph && (b->graph_stream != s || b->graph_mode != gmode)) {
     cudaGraphExecDestroy(b->coarse_graph);
     b->coarse_graph = nullptr;
   }
   if (graphable && !b->coarse_graph) {
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      const int rc = coarse_sequence(b);
+      const int rc = coarse_sequence(b, extra);
       const cudaError_t e = cudaStreamEndCapture(s, &g);
       if (rc == 0 && e == cudaSuccess && g) {
         if (cudaGraphInstantiate(&b->coarse_graph, g, 0) != cudaSuccess) b->coarse_graph = nullptr;
@@ -1299,12 +1267,13 @@ static int run_coarse_device(stab_batch* b) {
       cudaGetLastError();   // a failed capture leaves no sticky error: run eagerly below
     }
   }
-  b->coarse_runs += 1;
+  b->coarse_runs = (b->graph_mode == gmode) ? b->coarse_runs + 1 : 1;
+  b->graph_mode = gmode;
   if (graphable && b->coarse_graph) {
     CK(c, cudaGraphLaunch(b->coarse_graph, s));
     return 0;
   }
-  return coarse_sequence(b);
+  return coarse_sequence(b, extra);
 }
 
 int stab_batch_run(stab_batch* b, int32_t mode) {
@@ -1312,10 +1281,29 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
   if (!b->ctx) return STAB_ERR_STATE;
   stab_ctx* c = b->ctx;
   cudaSetDevice(c->device);
-  if (mode == STAB_MODE_COARSE) {
+  if (mode == STAB_MODE_COARSE || mode == STAB_MODE_SURROGATE) {
+    const bool extra = (mode == STAB_MODE_SURROGATE);
+    if (extra) {
+      if (!b->have_seeds) return set_err(c, STAB_ERR_STATE, "STAB_MODE_SURROGATE needs stab_batch_set_seeds first");
+      std::vector<zc> sg(b->count);
+      for (int k = 0; k < b->count; ++k) {
+        const int u = b->perm[k];
+        zc a = zmk(b->seeds[2 * u], b->seeds[2 * u + 1]);
+        if (b->P[k].itype == 2) {
+          const double d = a.x * a.x + a.y * a.y;
+          a = d > 0 ? zmk(a.x / d, -a.y / d) : zmk(0.0, 0.0);
+        }
+        sg[k] = a;
+      }
+      CK(c, upload(b->seed_raw, sg, c->stream));
+      if (b->ncheb > 0) {
+        int rc0 = upload_start(b);
+        if (rc0) return rc0;
+      }
+    }
     b->fell_back.clear();
     b->last_mode = mode;
-    int rc = run_coarse_device(b);
+    int rc = run_coarse_device(b, extra);
     if (rc) return rc;
     rc = run_fallback(b);
     if (rc) return rc;
@@ -1326,7 +1314,6 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
   if (rc) return rc;
   if (mode == STAB_MODE_SEEDED) return run_fallback(b);
   if (mode == STAB_MODE_TRACK) return run_fallback(b, true);
-  if (mode == STAB_MODE_SURROGATE) return run_coarse_sub(b);
   b->counts[0] = b->count;
   b->counts[1] = b->counts[2] = 0;
   return STAB_OK;
@@ -1338,6 +1325,94 @@ int stab_batch_set_start(stab_batch* b, const double* coef, int32_t ncheb) {
   if (ncheb < 0 || ncheb > 256 || (ncheb > 0 && !coef)) return set_err(b->ctx, STAB_ERR_ARG, "ncheb must be 0..256");
   b->ncheb = ncheb;
   b->start_coef.assign(coef ? coef : nullptr, coef ? coef + 2 * (size_t)5 * ncheb * b->count : nullptr);
+  return STAB_OK;
+}
+
+}  // extern "C"
+
+// Autotuner of the LU panel width: for each requested order and both
+// precisions, time every panel width shared memory admits (8, 16, 32) on a
+// full wave of well-conditioned test matrices (CUDA events on the context
+// stream, best of two) and keep the fastest for that size class.
+template <typename T>
+static int tune_lu_one(stab_ctx* c, int n, int reps, int* best_nb, float* best_ms) {
+  cudaStream_t s = c->stream;
+  const int count = std::max(1, c->sms * reps);
+  DevBuf A, piv, info, nsz, moff, poff;
+  CK(c, A.ensure(sizeof(T) * (size_t)count * n * n, s));
+  CK(c, piv.ensure(sizeof(int32_t) * (size_t)count * n, s));
+  CK(c, info.ensure(sizeof(int32_t) * count, s));
+  std::vector<int32_t> ns(count, n);
+  std::vector<int64_t> mo(count), po(count);
+  for (int k = 0; k < count; ++k) {
+    mo[k] = (int64_t)k * n * n;
+    po[k] = (int64_t)k * n;
+  }
+  CK(c, upload(nsz, ns, s));
+  CK(c, upload(moff, mo, s));
+  CK(c, upload(poff, po, s));
+  cudaEvent_t e0 = get_ev(c), e1 = get_ev(c);
+  *best_nb = 0;
+  *best_ms = 1e30f;
+  for (int nb : {8, 16, 32}) {
+    if (nb > lu_nb_max<T>(n)) continue;
+    float t = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(c, launch_tune_matrix<T>(count, n, A.as<T>(), s));
+      CK(c, cudaEventRecord(e0, s));
+      CK(c, launch_lu<T>(count, nullptr, nsz.as<int32_t>(), n, A.as<T>(), moff.as<int64_t>(), piv.as<int32_t>(),
+                         poff.as<int64_t>(), info.as<int32_t>(), s, nullptr, nb));
+      CK(c, cudaEventRecord(e1, s));
+      CK(c, cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(c, cudaEventElapsedTime(&ms, e0, e1));
+      t = std::min(t, ms);
+    }
+    if (t < *best_ms) {
+      *best_ms = t;
+      *best_nb = nb;
+    }
+  }
+  c->evpool.push_back(e0);
+  c->evpool.push_back(e1);
+  CK(c, cudaStreamSynchronize(s));
+  return 0;
+}
+
+extern "C" {
+
+int stab_autotune(stab_ctx* c, const int32_t* orders, int32_t norders, int32_t* nb_out, float* ms_out) {
+  if (!c || !orders || norders < 1) return set_err(c, STAB_ERR_ARG, "no orders to tune");
+  cudaSetDevice(c->device);
+  for (int q = 0; q < norders; ++q) {
+    const int n = orders[q];
+    if (n < 2 || n > 2048) return set_err(c, STAB_ERR_ARG, "order must be 2..2048");
+    for (int z = 0; z < 2; ++z) {
+      int nb = 0;
+      float ms = 0.f;
+      const int reps = n <= 480 ? 2 : 1;
+      const int rc = z ? tune_lu_one<zc>(c, n, reps, &nb, &ms) : tune_lu_one<cc>(c, n, reps, &nb, &ms);
+      if (rc) return rc;
+      c->lu_nb[{z, lu_class(n)}] = nb;
+      if (nb_out) nb_out[2 * q + z] = nb;
+      if (ms_out) ms_out[2 * q + z] = ms;
+    }
+  }
+  return STAB_OK;
+}
+
+int stab_batch_spectra(stab_batch* b, double* const* eig_out) {
+  if (!b || !eig_out) return STAB_ERR_ARG;
+  if (!b->ctx) return STAB_ERR_STATE;
+  stab_ctx* c = b->ctx;
+  if (!b->ran || b->last_mode != STAB_MODE_PLAIN) return set_err(c, STAB_ERR_STATE, "needs a STAB_MODE_PLAIN run");
+  for (int k = 0; k < b->count; ++k) {
+    double* dst = eig_out[b->perm[k]];
+    if (dst)
+      CK(c, cudaMemcpyAsync(dst, b->eigsorted.as<zc>() + b->h_mof[k], sizeof(zc) * b->hm[k], cudaMemcpyDeviceToHost,
+                            c->stream));
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
   return STAB_OK;
 }
 

@@ -59,9 +59,7 @@ __global__ void k_fold_best(int count, const InstDesc* desc, const zc* sigma, co
                             const double* err, const int32_t* iters, const zc* out, const int64_t* out_off,
                             int32_t* final_, int32_t* have, double* best_key, zc* best_theta, double* best_err,
                             int32_t* best_iters, zc* best_out, int quick, double quick_tol, int32_t* skip64,
-                            int slow_iters);
-__global__ void k_seed_accept(int count, const InstDesc* desc, const zc* sigma, const zc* theta, int32_t* done,
-                              const int32_t* iters, double tau, int max_iters);
+                            int slow_iters, int src, int32_t* best_src);
 __global__ void k_take_best(int count, const InstDesc* desc, const int32_t* have, const zc* best_theta,
                             const double* best_err, const int32_t* best_iters, const zc* best_out,
                             const int64_t* out_off, zc* theta, int32_t* done, double* err, int32_t* iters, zc* out);

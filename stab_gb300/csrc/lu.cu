@@ -147,11 +147,19 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
       }
       __syncthreads();
       for (int tr0 = 0; tr0 < m2; tr0 += 64) {
-        T acc[4][4];
+        T acc[4][4], cur[4][4];
+        // the A22 tile is loaded before the rank-w product so that its
+        // global-memory latency overlaps the shared-memory FMAs
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) {
+          const int c = c1 + tc0 + tc + 16 * b;
 #pragma unroll
-          for (int b = 0; b < 4; ++b) acc[a][b] = cx<T>::make(0, 0);
+          for (int a = 0; a < 4; ++a) {
+            const int r = c1 + tr0 + tr + 16 * a;
+            acc[a][b] = cx<T>::make(0, 0);
+            cur[a][b] = (c < n && r < n) ? M[(size_t)c * n + r] : cx<T>::make(0, 0);
+          }
+        }
         for (int j = 0; j < w; ++j) {
           T lv[4], uv[4];
 #pragma unroll
@@ -174,8 +182,7 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
           for (int a = 0; a < 4; ++a) {
             const int r = c1 + tr0 + tr + 16 * a;
             if (r >= n) continue;
-            T* e = &M[(size_t)c * n + r];
-            *e = cx<T>::sub(*e, acc[a][b]);
+            M[(size_t)c * n + r] = cx<T>::sub(cur[a][b], acc[a][b]);
           }
         }
       }
@@ -428,10 +435,18 @@ static cudaError_t launch_lu_nb(int count, const InstDesc* desc, const int32_t* 
 }
 
 template <typename T>
+int lu_nb_max(int n) {
+  return lu_nb_for<T>(n);
+}
+
+template <typename T>
 cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
-                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip) {
+                      int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip,
+                      int nb_hint) {
   if (count <= 0) return cudaSuccess;
   int nb = lu_nb_for<T>(nmax);
+  // a tuned panel width no wider than shared memory allows
+  if ((nb_hint == 8 || nb_hint == 16 || nb_hint == 32) && nb_hint <= nb) nb = nb_hint;
   if (nb == 32) return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
   if (nb == 16) return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
   return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
@@ -464,9 +479,35 @@ cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, c
 }
 
 template cudaError_t launch_lu<zc>(int, const InstDesc*, const int32_t*, int, zc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int);
 template cudaError_t launch_lu<cc>(int, const InstDesc*, const int32_t*, int, cc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int);
+template int lu_nb_max<zc>(int);
+template int lu_nb_max<cc>(int);
+
+// Autotuning input: count dense n x n matrices with hashed entries in
+// [-1, 1) + i[-1, 1) and the diagonal raised by n, so that every panel width
+// factors the same well-conditioned problem.
+template <typename T>
+__global__ void k_tune_matrix(int count, int n, T* A) {
+  const int64_t total = (int64_t)count * n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)(e * 2654435761u) ^ (uint32_t)(e >> 32) ^ 0x9e3779b9u;
+    h ^= h >> 15; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16;
+    double re = (double)(h & 0xffff) / 32768.0 - 1.0, im = (double)(h >> 16) / 32768.0 - 1.0;
+    const int64_t rc = e % ((int64_t)n * n);
+    if (rc / n == rc % n) re += n;
+    A[e] = cx<T>::from(zmk(re, im));
+  }
+}
+
+template <typename T>
+cudaError_t launch_tune_matrix(int count, int n, T* A, cudaStream_t s) {
+  k_tune_matrix<T><<<1024, 256, 0, s>>>(count, n, A);
+  return cudaGetLastError();
+}
+template cudaError_t launch_tune_matrix<zc>(int, int, zc*, cudaStream_t);
+template cudaError_t launch_tune_matrix<cc>(int, int, cc*, cudaStream_t);
 template cudaError_t launch_getrs<zc>(int, const int32_t*, int, const zc*, const int64_t*, const int32_t*,
                                       const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
                                       cudaStream_t, const float*, const float*);

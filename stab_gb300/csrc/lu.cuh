@@ -9,7 +9,13 @@ namespace stab {
 template <typename T>
 cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
                       int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s,
-                      const int32_t* skip = nullptr);
+                      const int32_t* skip = nullptr, int nb_hint = 0);
+// widest panel the shared memory admits for order n (8, 16 or 32)
+template <typename T>
+int lu_nb_max(int n);
+// autotuning input: count well-conditioned n x n test matrices
+template <typename T>
+cudaError_t launch_tune_matrix(int count, int n, T* A, cudaStream_t s);
 // Solve with the factors for complex128 right-hand sides at X + x_off[k]:
 // nrhs = nrhs_fixed if > 0, else nrhs_mul * n; leading dimension ldmul * n.
 // The solve runs in the factor's precision; instances with skip[k] != 0

@@ -6,7 +6,6 @@
 //   k_take_candidate,  seed rounds of the coarse-shift mode
 //   k_fold_best,
 //   k_take_best
-//   k_seed_accept      gate of the surrogate-seeded mode (rule below)
 //   k_post_spectrum    alpha = 1/lambda with lambda = 0 -> 0
 //                      (spatial.f90:1065-1069), ascending stable sort on the
 //                      imaginary part (the PIKSR2 call, temporal.f90:844-855,
@@ -138,7 +137,7 @@ __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const 
                             int32_t* __restrict__ final_, int32_t* __restrict__ have, double* __restrict__ best_key,
                             zc* __restrict__ best_theta, double* __restrict__ best_err, int32_t* __restrict__ best_iters,
                             zc* __restrict__ best_out, int quick, double quick_tol, int32_t* __restrict__ skip64,
-                            int slow_iters) {
+                            int slow_iters, int src, int32_t* __restrict__ best_src) {
   __shared__ int s_take;
   const int k = blockIdx.x;
   if (k >= count) return;
@@ -162,6 +161,7 @@ __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const 
         best_theta[k] = t;
         best_err[k] = err[k];
         best_iters[k] = iters[k];
+        if (best_src) best_src[k] = src;
         s_take = 1;
       }
       if (quick && zabs(zsub(t, sigma[k])) <= quick_tol * zabs(sigma[k])) final_[k] = 1;
@@ -273,33 +273,6 @@ __global__ void k_spatial_vec(int count, const InstDesc* __restrict__ desc, cons
   if (mk == 0.0) return;
   const zc ph = zscale(zconj(vk), 1.0 / mk);
   for (int q = threadIdx.x; q < 2 * n; q += blockDim.x) o[q] = (q == s_k) ? zmk(mk, 0.0) : zmul(o[q], ph);
-}
-
-// Gate of the surrogate-seeded mode: a polished pair from a predicted seed is
-// kept (done = 1) only when it converged within max_iters Newton steps, lies
-// within tau |sigma| of the seed, passes the least-stable filter, and (the
-// temporal problem) sits above the branch point of the vorticity continuum,
-// omega = alpha - i (alpha^2 + beta^2) / Re, under which the discretised
-// continuum modes cluster too densely for a prediction to pick the right
-// one.  Every other instance gets done = 2 and goes to the coarse path.
-// Spatial instances always go to the coarse path.
-__global__ void k_seed_accept(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ sigma,
-                              const zc* __restrict__ theta, int32_t* __restrict__ done,
-                              const int32_t* __restrict__ iters, double tau, int max_iters) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= count) return;
-  const InstDesc d = desc[k];
-  bool ok = (done[k] == 1) && (d.itype == 1) && (iters[k] <= max_iters);
-  const zc t = theta[k], s = sigma[k];
-  ok = ok && zabs(zsub(t, s)) <= tau * zabs(s);
-  double key;
-  ok = ok && least_key(d, t, key);
-  if (ok) {
-    const zc a = zmk(d.ar, d.ai), b = zmk(d.br, d.bi);
-    const zc k2 = zadd(zmul(a, a), zmul(b, b));
-    ok = t.y > -k2.x / d.Re;
-  }
-  done[k] = ok ? 1 : 2;
 }
 
 }  // namespace stab

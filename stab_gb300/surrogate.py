@@ -14,10 +14,12 @@ Outputs: Re(omega)/alpha, 100 Im(omega)/alpha, then Re and Im of the
 The network is trained on the GPU by the library's own kernels (the
 ``stab_mlp_*`` entry points, tensor-core BF16 GEMMs with float32
 accumulation), on solves of the plain FP64 batched path at N = 64, and it
-seeds ``MODE_SURROGATE``: the polish starts from the predicted omega and the
-start vector evaluated from the predicted coefficients, and instances whose
-pair fails the acceptance gate take the coarse-seeded path.  PyTorch only
-holds device buffers here.
+seeds ``MODE_SURROGATE``: after the coarse N = 32 candidates, the instances
+that are not yet final polish the predicted omega from the start vector
+evaluated from the predicted coefficients, and the least-stable converged
+pair wins.  That recovers discrete modes N = 32 does not resolve (the
+supersonic second modes), whose coarse candidates are spurious.  PyTorch
+only holds device buffers here.
 """
 from __future__ import annotations
 

@@ -223,3 +223,15 @@ def test_coarse_graph_replay_matches_eager(ctx):
     for o in outs[1:]:
         assert np.array_equal(o[0], outs[0][0]) and np.array_equal(o[3], outs[0][3])
     b.close()
+
+
+def test_batch_spectra_equal_single_instance_spectra(ctx):
+    cases = [H.synth_case(1, 24, 0.5, 1000.0, a=0.2), H.synth_case(2, 16, 0.8, 2000.0, w=0.05, b=0.1),
+             H.synth_case(1, 32, 1.2, 800.0, a=0.3, b=0.1)]
+    b = ctx.batch([H.stab_params(d) for d, _ in cases], [p for _, p in cases])
+    b.run(sg.MODE_PLAIN)
+    spec = b.spectra()
+    for (d, prof), s in zip(cases, spec):
+        eig, _, _, _ = ctx.full_spectrum(H.stab_params(d), prof, want_vector=False)
+        assert np.array_equal(s, eig)
+    b.close()

@@ -1,0 +1,23 @@
+"""The LU panel-width autotuner: every variant it times is a correct
+factorisation, and its choice is used afterwards (a polish through the tuned
+width reproduces the oracle)."""
+import numpy as np
+import pytest
+
+import stab_gb300 as sg
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autotune_picks_a_feasible_width_and_keeps_results(ctx):
+    table = ctx.autotune([160, 320])
+    for n, row in table.items():
+        for prec in ("c64", "c128"):
+            nb, ms = row[prec]
+            assert nb in (8, 16, 32) and ms > 0.0
+    d, prof = H.synth_case(1, 48, 1.2, 800.0, a=0.25, b=0.05)
+    es = H.oracle_solve(d, prof, want_vectors=False)
+    w = es.eig[H.select_least(es.eig, d)]
+    eig, err, iters, st, _ = ctx.solve_batch([H.stab_params(d)], [prof], sg.MODE_SEEDED, seeds=[w * (1 + 1e-7)])
+    assert st[0] == sg.ST_OK and abs(eig[0] - w) / abs(w) < 1e-10

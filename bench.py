@@ -358,10 +358,12 @@ def main():
 
     # per-kernel breakdown of one extra step (CUDA events on the launch stream)
     ctx.reset_kernel_stats()
+    ctx.eig_phases(reset=True)
     ctx.set_profiling(True)
     batch.run(sg.MODE_COARSE)
     stats = ctx.kernel_stats()
     ctx.set_profiling(False)
+    phases = ctx.eig_phases(reset=True)
     launches_per_step = sum(v[0] for v in stats.values())
 
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None
@@ -431,6 +433,7 @@ def main():
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in sorted(stats.items(),
                                                                                key=lambda kv: -kv[1][1])},
         "gpu_launches": int(launches_per_step * args.steps),
+        "eig_phase_share": {k: round(v / max(1, sum(phases.values())), 4) for k, v in phases.items()},
         "autotune_lu_panel": {str(n): {"c64": v["c64"][0], "c128": v["c128"][0]} for n, v in tune.items()},
         "cuda_graph": "device part of each timed pass replayed from a captured CUDA graph",
         "surrogate": sur,

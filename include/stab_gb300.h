@@ -102,6 +102,11 @@ int stab_sync(stab_ctx* ctx);
 int stab_set_profiling(stab_ctx* ctx, int on);
 int stab_kernel_stats(stab_ctx* ctx, int32_t k, const char** name, int64_t* launches, double* total_ms, int32_t* count);
 int stab_reset_kernel_stats(stab_ctx* ctx);
+/* SM cycles of the full-spectrum eigensolver per phase, summed over every
+ * instance solved on this device since the last reset: [0] isolation,
+ * [1] compaction, [2] balancing, [3] Hessenberg reduction, [4] repacking,
+ * [5] QR iteration.  reset != 0 zeroes them after reading. */
+int stab_eig_phases(stab_ctx* ctx, uint64_t* cycles_out, int32_t reset);
 
 /* ---- operator assembly (parity / inspection) -------------------------- */
 /*

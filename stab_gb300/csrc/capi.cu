@@ -1401,6 +1401,16 @@ int stab_autotune(stab_ctx* c, const int32_t* orders, int32_t norders, int32_t* 
   return STAB_OK;
 }
 
+int stab_eig_phases(stab_ctx* c, uint64_t* cycles_out, int32_t reset) {
+  if (!c || !cycles_out) return STAB_ERR_ARG;
+  cudaSetDevice(c->device);
+  CK(c, cudaStreamSynchronize(c->stream));
+  unsigned long long v[6];
+  CK(c, eig_phase_cycles(v, reset != 0));
+  for (int i = 0; i < 6; ++i) cycles_out[i] = v[i];
+  return STAB_OK;
+}
+
 int stab_batch_spectra(stab_batch* b, double* const* eig_out) {
   if (!b || !eig_out) return STAB_ERR_ARG;
   if (!b->ctx) return STAB_ERR_STATE;

@@ -280,6 +280,11 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
   return st;
 }
 
+// SM cycles spent per phase of k_eig_plain, summed over instances (thread 0
+// of each CTA adds clock64 differences): isolation, compaction, balancing,
+// Hessenberg reduction, repacking, QR iteration.  Read by stab_eig_phases.
+__device__ unsigned long long g_eig_phase_cycles[6];
+
 __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
                                                    const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
                                                    const int64_t* __restrict__ h_off, zc* __restrict__ eig,
@@ -310,6 +315,14 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
     for (int i = tid; i < m; i += HQ_T) active[i] = 1;
     if (tid == 0) s.mp = 0;
     __syncthreads();
+    long long t_ph = clock64();
+    auto phase = [&](int q) {
+      if (tid == 0) {
+        const long long t = clock64();
+        atomicAdd(&g_eig_phase_cycles[q], (unsigned long long)(t - t_ph));
+        t_ph = t;
+      }
+    };
     // ---- 1. isolation -----------------------------------------------------
     int n_iso = 0;           // isolated eigenvalues are written from the top: ev[m-1-q]
     for (int pass = 0; pass < m; ++pass) {
@@ -348,6 +361,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       n_iso = s.kk;
       __syncthreads();
     }
+    phase(0);
     // ---- 2. compaction ------------------------------------------------------
     if (tid == 0) {
       int q = 0;
@@ -363,6 +377,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       for (int r = lane; r < mp; r += 32) Hg[(size_t)c * ld + r] = M[(size_t)sc * m + act[r]];
     }
     __syncthreads();
+    phase(1);
     // ---- 3. balancing -------------------------------------------------------
     for (int sweep = 0; sweep < 64; ++sweep) {
       if (tid == 0) s.flag = 0;
@@ -410,6 +425,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       if (!s.flag) break;
       __syncthreads();
     }
+    phase(2);
     // ---- 4. Hessenberg reduction -----------------------------------------
     double flops = 0.0;   // FP64 work of the reduction and the sweeps (thread 0)
     for (int k = 0; k + 2 < mp; ++k) {
@@ -476,6 +492,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       }
       __syncthreads();
     }
+    phase(3);
     // ---- 5. QR iteration on the packed matrix ---------------------------------
     // in-place repack of H (ld = mp) to the column-packed layout: a packed
     // offset never exceeds the unpacked one, so moving column by column in
@@ -488,13 +505,22 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       for (int r = tid; r <= rmax; r += HQ_T) Hg[o + r] = v[r];
       __syncthreads();
     }
+    phase(4);
     int st = qr_eigs(SAcc{Hg, mp}, mp, ev, s, flops);
+    phase(5);
     if (tid == 0) {
       status[inst] = st;
       if (flops_out) flops_out[inst] = flops;
     }
     __syncthreads();
   }
+}
+
+cudaError_t eig_phase_cycles(unsigned long long* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_eig_phase_cycles, sizeof(unsigned long long) * 6);
+  if (e != cudaSuccess || !reset) return e;
+  static const unsigned long long zero[6] = {0, 0, 0, 0, 0, 0};
+  return cudaMemcpyToSymbol(g_eig_phase_cycles, zero, sizeof(zero));
 }
 
 size_t eig_plain_smem(int mmax) {

@@ -111,9 +111,12 @@ def surrogate_leg(ctx, stream, args):
     t_inf = time.perf_counter()
     w_hat = sur.seed_batch(b, Xq, Q["alpha"])
     infer_s = time.perf_counter() - t_inf
+    rel = np.abs(w_hat - truth) / np.abs(truth)
+    resolved = (np.real(truth / Q["alpha"]) > 0.0) & (np.real(truth / Q["alpha"]) < 3.0)
     out = {"workload": f"{n} temporal instances at N=128 (n=640), s~U[1.5,3], seed 20261204",
            "train": train, "inference_s": infer_s,
-           "pred_rel_err_median": float(np.median(np.abs(w_hat - truth) / np.abs(truth)))}
+           "pred_rel_err_median": float(np.median(rel[resolved])) if np.any(resolved) else None,
+           "pred_rel_err_note": "instances whose least-stable phase speed is in (0, 3)"}
     for name, mode in (("coarse_seeded", sg.MODE_COARSE), ("surrogate_seeded", sg.MODE_SURROGATE)):
         b.run(mode)          # warm-up (sizes pools, captures the graph)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -223,6 +223,7 @@ struct stab_batch {
   DevBuf startc;
   DevBuf seed_raw, best_src;                  // STAB_MODE_SURROGATE: the extra candidate, winner per instance
   int graph_mode = -1;                        // mode of the captured graph
+  int coarse_ny = 32;                         // N of the seed spectrum of STAB_MODE_COARSE
   std::vector<zc> fb_val;
   std::vector<int32_t> fb_status;
   std::vector<std::vector<zc>> fb_vec;
@@ -751,6 +752,8 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
 // ratio |sigma - lambda_1| / |sigma - lambda_2| per step, which separates
 // mode clusters that complex64 factors cannot resolve.
 static const int kInverseSteps = 12;
+// N of the second candidate level of the fallback
+static const int kMediumNy = 48;
 static const double kInverseTol = 1e-13;
 
 static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
@@ -1022,7 +1025,8 @@ static int coarse_seeds(stab_batch* b) {
   if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
   if (!b->coarse) {
     stab_batch* cb = nullptr;
-    int rc = batch_build(c, b->count, it->second.p.data(), it->second.nym.data(), it->second.prof.data(), &cb, 32);
+    int rc = batch_build(c, b->count, it->second.p.data(), it->second.nym.data(), it->second.prof.data(), &cb,
+                         b->coarse_ny);
     if (rc) return rc;
     b->coarse = cb;
   }
@@ -1157,6 +1161,40 @@ static int run_fallback(stab_batch* b, bool track = false) {
   int rc = batch_build(c, (int)fp.size(), fp.data(), fn.data(), fpr.data(), &fb, 0);
   if (rc) return rc;
   std::unique_ptr<stab_batch> guard(fb);
+  if (!track && b->coarse_ny < kMediumNy) {
+    // A second candidate level first: seeds from the spectrum at N = 48,
+    // which resolves what N = 32 did not, at a fraction of the full
+    // eigensolve's cost for the large instances; its own failures take the
+    // plain path.  Results keep the fallback status.
+    fb->coarse_ny = kMediumNy;
+    BatchInputs sub{fp, fn, fpr};
+    g_inputs[fb] = sub;
+    rc = stab_batch_run(fb, STAB_MODE_COARSE);
+    const int nf = fb->count;
+    std::vector<double> eig(2 * (size_t)nf), er(nf), w(4, 0.0);
+    std::vector<int32_t> itv(nf), st(nf);
+    std::vector<std::vector<zc>> vecs(nf);
+    std::vector<double*> vp(nf);
+    for (int q = 0; q < nf; ++q) {
+      vecs[q].resize(b->hm[b->fell_back[q]]);
+      vp[q] = reinterpret_cast<double*>(vecs[q].data());
+    }
+    if (rc == 0) rc = stab_batch_results(fb, eig.data(), er.data(), itv.data(), st.data(), vp.data());
+    if (rc == 0) rc = stab_batch_work(fb, w.data());
+    g_inputs.erase(fb);
+    if (rc) return rc;
+    for (int i = 0; i < 4; ++i) b->fb_work[i] += w[i];
+    b->fb_val.assign(nf, zmk(0, 0));
+    b->fb_status.assign(nf, 0);
+    b->fb_err = er;
+    b->fb_iters = itv;
+    b->fb_vec = std::move(vecs);
+    for (int q = 0; q < nf; ++q) {
+      b->fb_val[q] = zmk(eig[2 * q], eig[2 * q + 1]);
+      b->fb_status[q] = (st[q] == STAB_ST_OK) ? STAB_ST_FELLBACK : st[q];
+    }
+    return 0;
+  }
   rc = run_prep(fb);
   if (rc) return rc;
   rc = run_plain(fb, !track, "k_eig_plain_fallback");

@@ -123,7 +123,11 @@ def make_dataset(ctx: sg.Context, count: int, seed: int, ranges: Optional[dict] 
         profs = [erf_profile(P["M"][k], P["width"][k]) for k in idx]
         eig, err, iters, st, vecs = ctx.solve_batch(params, profs, sg.MODE_PLAIN, want_vectors=True)
         for j, k in enumerate(idx):
-            if st[j] == sg.ST_OK and np.all(np.isfinite(vecs[j])):
+            c = eig[j] / P["alpha"][k]
+            # phase speeds outside (0, 3) are the unresolved acoustic modes of
+            # the near-incompressible end (|c| up to 10 (1 + 1/M) passes the
+            # selection filter): kept out of the training targets
+            if st[j] == sg.ST_OK and np.all(np.isfinite(vecs[j])) and 0.0 < c.real < 3.0 and abs(c.imag) < 0.2:
                 ok[k] = True
                 w[k] = eig[j]
                 coef[k] = chebyshev_coefficients(vecs[j], ny)

@@ -1,0 +1,61 @@
+"""What the trained network gains over the method without it.
+
+Region: supersonic second modes (M in [1.5, 2], alpha in [0.2, 0.4],
+Re in [1500, 3000], beta in [0, 0.1]).  Here the N = 32 seed spectrum does
+not resolve the least-stable discrete mode, so the coarse-seeded method
+(STAB_MODE_COARSE, the method without the network) converges to the plain
+FP64 least-stable mode for only about half of the instances.  The network,
+trained here by the library's BF16 kernels on plain FP64 solves at N = 64,
+adds its prediction as one more candidate (STAB_MODE_SURROGATE).
+
+Checks: every instance the coarse method gets right stays right (at most one
+exception for rounding at the 1e-10 bar); at least two more instances match
+the plain FP64 result within 1e-10; some kept pairs came from the network's
+seed.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import stab_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+pytest.importorskip("torch")
+
+REGION = {"M": (1.5, 2.0), "alpha": (0.2, 0.4), "log10Re": (math.log10(1500.0), math.log10(3000.0)),
+          "beta": (0.0, 0.1)}
+
+
+def test_network_gain_over_coarse_seeds(ctx):
+    from stab_gb300 import surrogate as su
+    ds = su.make_dataset(ctx, 4096, 21, REGION)
+    P, v = ds["params"], ds["valid"]
+    X = su.features(P["M"], P["Re"], P["alpha"], P["beta"], P["width"])[v]
+    sur = su.Surrogate(ctx, max_batch=4096)
+    fit = sur.fit(X, ds["omega"][v], P["alpha"][v], ds["coef"][v], steps=4000, batch=1024)
+    assert fit["losses"][-1][1] < 0.5 * fit["losses"][0][1]
+    n = 128
+    Q = su.sample_params(n, 98, REGION)
+    params = [su.stab_params(Q["M"][k], Q["Re"][k], Q["alpha"][k], Q["beta"][k], 64) for k in range(n)]
+    profs = [su.erf_profile(Q["M"][k], Q["width"][k]) for k in range(n)]
+    b = ctx.batch(params, profs)
+    b.run(sg.MODE_PLAIN)
+    truth, _, _, tst, _ = b.results()
+
+    def right(eig, st):
+        return (np.abs(eig - truth) / np.abs(truth) <= 1e-10) & np.isin(st, [sg.ST_OK, sg.ST_FELLBACK]) & (tst == 0)
+
+    b.run(sg.MODE_COARSE)
+    e_c, _, _, s_c, _ = b.results()
+    ok_c = right(e_c, s_c)
+    sur.seed_batch(b, su.features(Q["M"], Q["Re"], Q["alpha"], Q["beta"], Q["width"]), Q["alpha"])
+    b.run(sg.MODE_SURROGATE)
+    e_s, _, _, s_s, _ = b.results()
+    ok_s = right(e_s, s_s)
+    counts = b.counts()
+    b.close()
+    sur.close()
+    assert np.sum(ok_c & ~ok_s) <= 1
+    assert np.sum(ok_s & ~ok_c) >= 2, (int(ok_c.sum()), int(ok_s.sum()), counts)
+    assert counts["surrogate_seed"] >= 1

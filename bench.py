@@ -138,6 +138,51 @@ def surrogate_leg(ctx, stream, args):
     return out
 
 
+def single_instance_leg(ctx, stream, cpu: bool):
+    """Configs 0 and 1 as single-instance latencies: the plain temporal solve
+    (N = 64, Streett map on [0, 50], full spectrum + least-stable
+    eigenvector, M = 0.5, Re = 1000, alpha = 0.2) and the spatial solve
+    (N = 96 crossflow, omega = 0.05, beta = 0.1, M = 0.8, Re = 2000: full
+    spectrum of order 960, then the polish of the least-stable alpha), each
+    checked against the CPU oracle on the same inputs when `cpu`."""
+    import torch
+    import stab_gb300 as sg
+    from oracle import stab_oracle as so
+    out = {}
+    for name, itype, N, M, Re, a, b_, w, cross in (("config0_temporal_n64", 1, 64, 0.5, 1000.0, 0.2, 0.0, 0.0, False),
+                                                  ("config1_spatial_n96", 2, 96, 0.8, 2000.0, 0.0, 0.1, 0.05, True)):
+        y, vt = so.synthetic_profile(M, 50.0, crossflow=cross)
+        prof = np.column_stack([y, vt])
+        p = sg.StabParams.make(itype=itype, ny=N, Ma=M, Re=Re, Pr=0.72, mattyp=1, T0=T0_SUTH, yi=1.0 / 23.0,
+                               ymax=50.0, alpha=a, beta=b_, omega=w)
+        ctx.full_spectrum(p, prof)                       # warm-up: derivative tables, pools
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        eig, vec, li, st = ctx.full_spectrum(p, prof)
+        gpu_s = time.perf_counter() - t
+        rec = {"gpu_full_spectrum_ms": 1000.0 * gpu_s, "order": p.m(), "status": int(st),
+               "least": [float(eig[li].real), float(eig[li].imag)] if li >= 0 else None}
+        if itype == 2 and li >= 0:
+            t = time.perf_counter()
+            pe, perr, pit, pst, _ = ctx.solve_batch([p], [prof], sg.MODE_SEEDED, seeds=[eig[li]])
+            rec["gpu_polish_ms"] = 1000.0 * (time.perf_counter() - t)
+            rec["polish_rel_change"] = float(abs(pe[0] - eig[li]) / abs(eig[li]))
+        if cpu:
+            sp = so.StabParams(mattyp=1, T0=T0_SUTH, Ma=M, Re=Re, Pr=0.72, ny=N, yi=1.0 / 23.0, ymax=50.0, ievec=1,
+                               ider=1, top=0, wall=0, wallt=0, curve=0, itype=itype, alpha=complex(a),
+                               beta=complex(b_), omega=complex(w))
+            vt2 = vt.copy()
+            vt2[:, 2] = 0.0
+            t = time.perf_counter()
+            es = so.solve(sp, y, vt2, want_vectors=(itype == 1))
+            rec["cpu_oracle_s"] = time.perf_counter() - t
+            if li >= 0:
+                j = so.getevec_select(es.eig, eig[li])
+                rec["rel_err_vs_oracle"] = float(abs(es.eig[j] - eig[li]) / abs(es.eig[j]))
+        out[name] = rec
+    return out
+
+
 def to_stab(d):
     import stab_gb300 as sg
     return sg.StabParams.make(itype=d["itype"], ny=d["ny"], Ma=d["Ma"], Re=d["Re"], Pr=d["Pr"],
@@ -370,6 +415,7 @@ def main():
     launches_per_step = sum(v[0] for v in stats.values())
 
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None
+    single = single_instance_leg(ctx, stream, cpu=args.cpu_sample > 0) if rank == 0 else None
 
     # end-to-end through the C ABI call with host buffers (pinned), results read back
     barrier(world)
@@ -440,6 +486,7 @@ def main():
         "autotune_lu_panel": {str(n): {"c64": v["c64"][0], "c128": v["c128"][0]} for n, v in tune.items()},
         "cuda_graph": "device part of each timed pass replayed from a captured CUDA graph",
         "surrogate": sur,
+        "single_instance": single,
         "clocks": clk,
         "cpu_baseline": cpu,
     }

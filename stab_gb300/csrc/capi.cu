@@ -31,7 +31,7 @@ static const int kShiftCandidates = 4;
 static const double kQuickAcceptTol = 1e-7;
 // a complex64 polish that needed this many Newton-chord steps or more is
 // retried with complex128 factors (slow contraction: an unresolved cluster)
-static const int kSlowNewton = 7;
+static const int kSlowNewton = 14;
 
 namespace {
 
@@ -638,7 +638,7 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
 }
 
 // mixed-precision polish from sigma (device, internal order)
-static const int kNewtonSteps = 10;
+static const int kNewtonSteps = 20;
 static const double kNewtonTol = 1e-13;      // |d theta| / |theta| of the last Newton-chord step
 static const double kNewtonTolVec = 1e-11;   // max |d x| / max |x|
 

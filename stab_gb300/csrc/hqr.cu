@@ -39,6 +39,11 @@ namespace stab {
 #define HQ_T 128
 #define HQ_W (HQ_T / 32)
 
+// multi-bulge sweeps: at most MS_MAXB bulges; the trailing MS_MAXB x
+// MS_MAXB block that supplies their shifts is kept packed in MS_SMALL entries
+#define MS_MAXB 6
+#define MS_SMALL 48
+
 struct Refl {
   double tr, ti, ur, ui, beta, v1r, v1i;
   int ident;
@@ -52,6 +57,11 @@ struct HqrSmem {
   int kk;
   double sc[8];   // broadcast scalars (Householder step, shift)
   Refl refl[2];   // reflector of the next bulge step, double buffered
+  // multi-bulge sweeps: shifts, the trailing block they come from (packed),
+  // and one reflector per bulge
+  zc shifts[MS_MAXB];
+  zc small[MS_SMALL];
+  Refl mrefl[MS_MAXB];
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -81,8 +91,8 @@ struct GAcc {
   __device__ __forceinline__ zc& operator()(int r, int c) const { return H[(size_t)c * ld + r]; }
 };
 
-// packed Hessenberg-plus-one storage in shared memory: column c keeps rows
-// 0 .. min(c + 2, mp - 1)
+// packed Hessenberg-plus-one storage: column c keeps rows 0 .. min(c + 2,
+// mp - 1)
 __host__ __device__ __forceinline__ int64_t hess_coff(int c, int mp) {
   return (int64_t)c * (c + 5) / 2 - ((c == mp - 1 && mp >= 2) ? 1 : 0);
 }
@@ -94,10 +104,18 @@ struct SAcc {
   int mp;
   __device__ __forceinline__ zc& operator()(int r, int c) const { return S[hess_coff(c, mp) + r]; }
 };
+struct SmallAcc {
+  zc* S;
+  int mp;
+  __device__ __forceinline__ zc& operator()(int r, int c) const { return S[hess_coff(c, mp) + r]; }
+};
+// windows at least this wide use multi-bulge sweeps
+#define MS_MIN_WINDOW 16
 
-// 2-element reflector (as ZLARFG): (v1, v2) -> (beta, 0).  One square root
-// and two reciprocals: FP64 division and square root are multi-instruction
-// sequences, and this sits on the serial path of every bulge step.
+// 2-element reflector (as ZLARFG): (v1, v2) -> (beta, 0).  It sits on the
+// serial path of every bulge step, where each FP64 instruction of a single
+// thread costs a full warp issue of the 1/64-rate FP64 pipe, so it uses one
+// reciprocal square root (|beta| and 1/beta from it) and one reciprocal.
 __device__ __forceinline__ Refl make_refl(zc v1, zc v2) {
   Refl f;
   f.v1r = v1.x;
@@ -110,13 +128,15 @@ __device__ __forceinline__ Refl make_refl(zc v1, zc v2) {
     return f;
   }
   f.ident = 0;
-  const double beta = -copysign(sqrt(fma(v1.x, v1.x, fma(v1.y, v1.y, n2))), v1.x);
-  const double ib = 1.0 / beta;
+  const double S = fma(v1.x, v1.x, fma(v1.y, v1.y, n2));
+  const double r = rsqrt(S);
+  const double beta = -copysign(S * r, v1.x);
+  const double ib = -copysign(r, v1.x);                    // 1 / beta
   f.beta = beta;
   f.tr = (beta - v1.x) * ib;
   f.ti = -v1.y * ib;
   const double dr = v1.x - beta, di = v1.y;                // u2 = v2 / (v1 - beta)
-  const double idd = 1.0 / fma(dr, dr, di * di);
+  const double idd = __drcp_rn(fma(dr, dr, di * di));
   f.ur = fma(v2.x, dr, v2.y * di) * idd;
   f.ui = fma(v2.y, dr, -v2.x * di) * idd;
   return f;
@@ -140,9 +160,104 @@ __device__ __forceinline__ void apply_right(const Acc& H, int k, int j, zc tau, 
 
 // Single-shift QR on the mp x mp upper Hessenberg matrix behind H; writes
 // the eigenvalues to ev[0..mp).  Returns 0 or STAB_ST_NOCONV.
+template <class Acc, bool MULTI>
+__device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& flops);
+
+// One sweep of nb bulges over the active window [l, i] (i - l + 1 >=
+// 3 nb + 2), with the shifts in s.shifts.  Bulge q enters at row l at step
+// 3q and sits at row k = l + step - 3q.  Rows of different bulges are three
+// apart, so within a step the left updates of all bulges (rows k, k+1) are
+// disjoint, and so are the right updates (columns k, k+1).  Left and right
+// updates commute, so a step runs all left updates, then all right updates,
+// then forms every bulge's next reflector on lanes of warp 0, with a barrier
+// between phases.  That puts the serial reflector work of nb bulges into
+// the same warp instructions.
 template <class Acc>
-__device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& flops) {
+__device__ void multi_bulge_sweep(const Acc& H, int l, int i, int nb, HqrSmem& s, double& flops) {
   const int tid = threadIdx.x;
+  const int steps = (i - l) + 3 * (nb - 1);
+  // entering reflector of bulge 0
+  if (tid == 0) {
+    const zc h11s = zsub(H(l, l), s.shifts[0]);
+    const zc h21 = H(l + 1, l);
+    double sc = zabs1(h11s) + zabs1(h21);
+    if (sc == 0.0) sc = 1.0;
+    s.mrefl[0] = make_refl(zscale(h11s, 1.0 / sc), zscale(h21, 1.0 / sc));
+  }
+  __syncthreads();
+  for (int st = 0; st < steps; ++st) {
+    // active bulges: q with 0 <= st - 3q <= i - l - 1
+    const int qhi = min(nb - 1, st / 3);
+    const int qlo = max(0, (st - (i - l - 1) + 2) / 3);
+    // phase L: annihilation writes (column k-1) and left updates of columns k..i
+    int ltask = 0;
+    for (int q = qlo; q <= qhi; ++q) ltask += 1 + (i - (l + st - 3 * q) + 1);
+    if (tid == 0) flops += 24.0 * (double)ltask;
+    for (int t = tid; t < ltask; t += HQ_T) {
+      int q = qlo, rem = t;
+      for (;;) {
+        const int cnt = 1 + (i - (l + st - 3 * q) + 1);
+        if (rem < cnt) break;
+        rem -= cnt;
+        ++q;
+      }
+      const int k = l + st - 3 * q;
+      const Refl& f = s.mrefl[q];
+      if (rem == 0) {
+        if (k > l) {
+          H(k, k - 1) = zmk(f.ident ? f.v1r : f.beta, f.ident ? f.v1i : 0.0);
+          H(k + 1, k - 1) = zmk(0.0, 0.0);
+        }
+      } else if (!f.ident) {
+        apply_left(H, k, k + rem - 1, zmk(f.tr, f.ti), zmk(f.ur, f.ui));
+      }
+    }
+    __syncthreads();
+    // phase R: right updates of rows l..min(k+2, i)
+    int rtask = 0;
+    for (int q = qlo; q <= qhi; ++q) {
+      const int k = l + st - 3 * q;
+      rtask += min(k + 2, i) - l + 1;
+    }
+    if (tid == 0) flops += 24.0 * (double)rtask;
+    for (int t = tid; t < rtask; t += HQ_T) {
+      int q = qlo, rem = t;
+      for (;;) {
+        const int k = l + st - 3 * q;
+        const int cnt = min(k + 2, i) - l + 1;
+        if (rem < cnt) break;
+        rem -= cnt;
+        ++q;
+      }
+      const int k = l + st - 3 * q;
+      const Refl& f = s.mrefl[q];
+      if (!f.ident) apply_right(H, k, l + rem, zmk(f.tr, f.ti), zmk(f.ur, f.ui));
+    }
+    __syncthreads();
+    // phase C: next reflector of every bulge that moves on, and the
+    // entering reflector of the bulge that starts next step
+    if (tid < 32) {
+      const int q = tid;
+      if (q < nb) {
+        const int k = l + st - 3 * q;          // position this step
+        if (k >= l && k + 1 <= i - 1) {
+          s.mrefl[q] = make_refl(H(k + 1, k), H(k + 2, k));
+        } else if (k + 1 == l) {               // enters next step
+          const zc h11s = zsub(H(l, l), s.shifts[q]);
+          const zc h21 = H(l + 1, l);
+          double sc = zabs1(h11s) + zabs1(h21);
+          if (sc == 0.0) sc = 1.0;
+          s.mrefl[q] = make_refl(zscale(h11s, 1.0 / sc), zscale(h21, 1.0 / sc));
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <class Acc, bool MULTI>
+__device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& flops) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const double ulp = 2.220446049250313e-16;
   const double safmin = 2.2250738585072014e-308;
   const double smlnum = safmin * ((double)mp / ulp);
@@ -185,6 +300,24 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
       if (total_its >= its_cap) { st = STAB_ST_NOCONV; break; }
       ++kdefl;
       ++total_its;
+      if (MULTI && (i - l + 1) >= MS_MIN_WINDOW && kdefl % 10 != 0) {
+        // shifts: eigenvalues of the trailing nb x nb block (a small
+        // single-shift QR on a packed copy), then one sweep of nb bulges
+        const int nb = (i - l + 1) >= 3 * MS_MAXB + 2 + 24 ? MS_MAXB : 2;
+        const int o = i - nb + 1;
+        for (int c = tid; c < nb; c += HQ_T)
+          for (int r = 0; r <= min(c + 2, nb - 1); ++r) s.small[hess_coff(c, nb) + r] = (r <= c + 1) ? H(o + r, o + c) : zmk(0.0, 0.0);
+        __syncthreads();
+        double fl = 0.0;
+        const int sst = qr_eigs<SmallAcc, false>(SmallAcc{s.small, nb}, nb, s.shifts, s, fl);
+        flops += fl;
+        if (sst == 0) {
+          multi_bulge_sweep(H, l, i, nb, s, flops);
+          total_its += nb - 1;
+          continue;
+        }
+        // the small eigensolve did not converge: a single-shift iteration
+      }
       // shift (one thread)
       if (tid == 0) {
         zc t;
@@ -240,31 +373,46 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
         s.refl[m0 & 1] = make_refl(zscale(h11s, 1.0 / sc), zscale(h21, 1.0 / sc));
       }
       __syncthreads();
-      // bulge chase, one barrier per step
+      // bulge chase, one barrier per step.  The serial corner of a step is
+      // reflector k on columns k, k+1, then on rows k, k+1, then reflector
+      // k+1 formed from the new bulge.  It runs on lanes of warp 0 in three
+      // dependent stages of one update each.  Every other update of the step
+      // (columns k+2..i, rows l..k-1 and k+2) is independent of it and of the
+      // others and runs on all threads.
       for (int k = m0; k < i; ++k) {
         const Refl f = s.refl[k & 1];
         const zc tau = zmk(f.tr, f.ti), u2 = zmk(f.ur, f.ui);
         const int nleft = i - k - 1;        // columns k+2..i
-        const int ntask = i - l;            // corner + nleft + (k - l) rows above
-        if (tid == 0) flops += 24.0 * (double)(ntask + 4);
+        const int nrows = k - l;            // rows l..k-1
+        const int ntask = 4 + nleft + nrows;
+        if (tid == 0) flops += 24.0 * (double)(i - l + 4);
         for (int q = tid; q < ntask; q += HQ_T) {
           if (q == 0) {
-            if (k > m0) { H(k, k - 1) = zmk(f.ident ? f.v1r : f.beta, f.ident ? f.v1i : 0.0); H(k + 1, k - 1) = zmk(0.0, 0.0); }
-            if (!f.ident) {
-              // a sweep started below l still applies the first reflector to
-              // column m0-1: H(m0, m0-1) picks up (1 - conj(tau)); the fill-in
-              // at H(m0+1, m0-1) is what the start test bounds
-              if (k == m0 && m0 > l) H(m0, m0 - 1) = zmul(H(m0, m0 - 1), zsub(zmk(1.0, 0.0), zconj(tau)));
-              apply_left(H, k, k, tau, u2);
-              apply_left(H, k, k + 1, tau, u2);
-              const int rmax = (k + 2 <= i) ? k + 2 : i;
-              for (int j = k; j <= rmax; ++j) apply_right(H, k, j, tau, u2);
+            if (!f.ident) apply_left(H, k, k, tau, u2);
+          } else if (q == 1) {
+            if (!f.ident) apply_left(H, k, k + 1, tau, u2);
+          } else if (q == 2) {
+            if (!f.ident && k + 2 <= i) apply_right(H, k, k + 2, tau, u2);
+          } else if (q == 3) {
+            if (k > m0) {
+              H(k, k - 1) = zmk(f.ident ? f.v1r : f.beta, f.ident ? f.v1i : 0.0);
+              H(k + 1, k - 1) = zmk(0.0, 0.0);
             }
-            if (k + 1 < i) s.refl[(k + 1) & 1] = make_refl(H(k + 1, k), H(k + 2, k));
+            // a sweep started below l still applies the first reflector to
+            // column m0-1: H(m0, m0-1) picks up (1 - conj(tau)); the fill-in
+            // at H(m0+1, m0-1) is what the start test bounds
+            if (!f.ident && k == m0 && m0 > l) H(m0, m0 - 1) = zmul(H(m0, m0 - 1), zsub(zmk(1.0, 0.0), zconj(tau)));
           } else if (!f.ident) {
-            if (q <= nleft) apply_left(H, k, k + 1 + q, tau, u2);
-            else apply_right(H, k, l + (q - nleft - 1), tau, u2);
+            const int t = q - 4;
+            if (t < nleft) apply_left(H, k, k + 2 + t, tau, u2);
+            else apply_right(H, k, l + (t - nleft), tau, u2);
           }
+        }
+        if (warp == 0) {
+          __syncwarp();
+          if (lane < 2 && !f.ident) apply_right(H, k, k + lane, tau, u2);   // rows k, k+1
+          __syncwarp();
+          if (lane == 0 && k + 1 < i) s.refl[(k + 1) & 1] = make_refl(H(k + 1, k), H(k + 2, k));
         }
         __syncthreads();
       }
@@ -506,7 +654,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       __syncthreads();
     }
     phase(4);
-    int st = qr_eigs(SAcc{Hg, mp}, mp, ev, s, flops);
+    int st = qr_eigs<SAcc, true>(SAcc{Hg, mp}, mp, ev, s, flops);
     phase(5);
     if (tid == 0) {
       status[inst] = st;

@@ -686,7 +686,7 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
     return timed(c, n_lu, [&] {
       return launch_lu<T>(b->count, D, b->nsz.as<int32_t>(), b->nmax, MP, b->off_n2.as<int64_t>(),
                           b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
-                          tuned_nb(c, !c64, b->nmax));
+                          tuned_nb(c, !c64, b->nmax), b->order.as<int32_t>());
     });
   };
   auto solve32 = [&](int slot, const int32_t* sk) {
@@ -774,7 +774,7 @@ static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
   CK(c, timed(c, "k_lu_z", [&] {
     return launch_lu<zc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
                          b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
-                         tuned_nb(c, true, b->nmax));
+                         tuned_nb(c, true, b->nmax), b->order.as<int32_t>());
   }));
   CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
   CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, b->pcol.as<int32_t>(), skip, s); }));

@@ -36,8 +36,12 @@
 
 namespace stab {
 
-#define HQ_T 128
-#define HQ_W (HQ_T / 32)
+#define HQ_T 128        // block of the batched (persistent) eigensolver
+#define HQ_WIDE 512     // block for a few large instances (latency)
+#define HQ_MAXW (HQ_WIDE / 32)
+// the device code runs with either block size
+#define NTH ((int)blockDim.x)
+#define NWA ((int)(blockDim.x >> 5))
 
 // multi-bulge sweeps: at most MS_MAXB bulges; the trailing MS_MAXB x
 // MS_MAXB block that supplies their shifts is kept packed in MS_SMALL entries
@@ -50,7 +54,7 @@ struct Refl {
 };
 
 struct HqrSmem {
-  double red[2 * HQ_W];
+  double red[2 * HQ_MAXW];
   int flag;
   int found;
   int mp;
@@ -75,10 +79,10 @@ __device__ void block_sum2(HqrSmem& s, double& a, double& b) {
   a = warp_sum(a);
   b = warp_sum(b);
   __syncthreads();
-  if (lane == 0) { s.red[warp] = a; s.red[HQ_W + warp] = b; }
+  if (lane == 0) { s.red[warp] = a; s.red[HQ_MAXW + warp] = b; }
   __syncthreads();
   double ta = 0.0, tb = 0.0;
-  for (int q = 0; q < HQ_W; ++q) { ta += s.red[q]; tb += s.red[HQ_W + q]; }
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { ta += s.red[q]; tb += s.red[HQ_MAXW + q]; }
   a = ta;
   b = tb;
   __syncthreads();
@@ -193,7 +197,7 @@ __device__ void multi_bulge_sweep(const Acc& H, int l, int i, int nb, HqrSmem& s
     int ltask = 0;
     for (int q = qlo; q <= qhi; ++q) ltask += 1 + (i - (l + st - 3 * q) + 1);
     if (tid == 0) flops += 24.0 * (double)ltask;
-    for (int t = tid; t < ltask; t += HQ_T) {
+    for (int t = tid; t < ltask; t += NTH) {
       int q = qlo, rem = t;
       for (;;) {
         const int cnt = 1 + (i - (l + st - 3 * q) + 1);
@@ -220,7 +224,7 @@ __device__ void multi_bulge_sweep(const Acc& H, int l, int i, int nb, HqrSmem& s
       rtask += min(k + 2, i) - l + 1;
     }
     if (tid == 0) flops += 24.0 * (double)rtask;
-    for (int t = tid; t < rtask; t += HQ_T) {
+    for (int t = tid; t < rtask; t += NTH) {
       int q = qlo, rem = t;
       for (;;) {
         const int k = l + st - 3 * q;
@@ -272,7 +276,7 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
       // largest k in [l+1, i] with a negligible subdiagonal; l if none
       if (tid == 0) s.kk = l;
       __syncthreads();
-      for (int k = i - tid; k >= l + 1; k -= HQ_T) {
+      for (int k = i - tid; k >= l + 1; k -= NTH) {
         const zc h = H(k, k - 1);
         bool ok = zabs1(h) <= smlnum;
         if (!ok) {
@@ -305,7 +309,7 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
         // single-shift QR on a packed copy), then one sweep of nb bulges
         const int nb = (i - l + 1) >= 3 * MS_MAXB + 2 + 24 ? MS_MAXB : 2;
         const int o = i - nb + 1;
-        for (int c = tid; c < nb; c += HQ_T)
+        for (int c = tid; c < nb; c += NTH)
           for (int r = 0; r <= min(c + 2, nb - 1); ++r) s.small[hess_coff(c, nb) + r] = (r <= c + 1) ? H(o + r, o + c) : zmk(0.0, 0.0);
         __syncthreads();
         double fl = 0.0;
@@ -350,7 +354,7 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
       const zc t = zmk(s.sc[0], s.sc[1]);
       // start row: largest m in [l+1, i-1] where two consecutive small
       // subdiagonals decouple the sweep; l otherwise
-      for (int mm = i - 1 - tid; mm >= l + 1; mm -= HQ_T) {
+      for (int mm = i - 1 - tid; mm >= l + 1; mm -= NTH) {
         const zc h11 = H(mm, mm), h22 = H(mm + 1, mm + 1);
         const zc h11s = zsub(h11, t);
         const zc h21 = H(mm + 1, mm);
@@ -386,7 +390,7 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
         const int nrows = k - l;            // rows l..k-1
         const int ntask = 4 + nleft + nrows;
         if (tid == 0) flops += 24.0 * (double)(i - l + 4);
-        for (int q = tid; q < ntask; q += HQ_T) {
+        for (int q = tid; q < ntask; q += NTH) {
           if (q == 0) {
             if (!f.ident) apply_left(H, k, k, tau, u2);
           } else if (q == 1) {
@@ -423,7 +427,7 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
     __syncthreads();
   }
   if (st)
-    for (int q = tid; q <= i; q += HQ_T) ev[q] = zmk(nan(""), nan(""));
+    for (int q = tid; q <= i; q += NTH) ev[q] = zmk(nan(""), nan(""));
   __syncthreads();
   return st;
 }
@@ -433,15 +437,15 @@ __device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& fl
 // Hessenberg reduction, repacking, QR iteration.  Read by stab_eig_phases.
 __device__ unsigned long long g_eig_phase_cycles[6];
 
-__global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
-                                                   const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
-                                                   const int64_t* __restrict__ h_off, zc* __restrict__ eig,
-                                                   const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
-                                                   int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
-                                                   double* __restrict__ flops_out) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ HqrSmem s;
-  __shared__ int s_inst;
+// The eigensolver of one CTA over a persistent queue of instances; it runs
+// with either block size (HQ_T for the batch, HQ_WIDE for a few instances).
+__device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
+                                               const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
+                                               const int64_t* __restrict__ h_off, zc* __restrict__ eig,
+                                               const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
+                                               int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
+                                               double* __restrict__ flops_out, unsigned char* smraw, HqrSmem& s,
+                                               int& s_inst) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (;;) {
     if (tid == 0) s_inst = atomicAdd(work_counter, 1);
@@ -460,7 +464,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
     zc* v = zs;
     zc* w = v + m;
     zc* z = w + m;
-    for (int i = tid; i < m; i += HQ_T) active[i] = 1;
+    for (int i = tid; i < m; i += NTH) active[i] = 1;
     if (tid == 0) s.mp = 0;
     __syncthreads();
     long long t_ph = clock64();
@@ -476,7 +480,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
     for (int pass = 0; pass < m; ++pass) {
       if (tid == 0) s.found = 0;
       __syncthreads();
-      for (int r = tid; r < m; r += HQ_T) {           // rows: thread per row
+      for (int r = tid; r < m; r += NTH) {           // rows: thread per row
         if (!active[r]) continue;
         bool zero = true;
         for (int c = 0; c < m && zero; ++c) {
@@ -486,7 +490,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
         }
         if (zero) { active[r] = 2; atomicAdd(&s.found, 1); }
       }
-      for (int c = warp; c < m; c += HQ_W) {          // columns: warp per column
+      for (int c = warp; c < m; c += NWA) {          // columns: warp per column
         if (active[c] != 1) continue;
         bool zero = true;
         for (int r = lane; r < m; r += 32) {
@@ -520,7 +524,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
     __syncthreads();
     const int mp = s.mp;
     const int ld = mp;
-    for (int c = warp; c < mp; c += HQ_W) {
+    for (int c = warp; c < mp; c += NWA) {
       const int sc = act[c];
       for (int r = lane; r < mp; r += 32) Hg[(size_t)c * ld + r] = M[(size_t)sc * m + act[r]];
     }
@@ -532,7 +536,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       __syncthreads();
       for (int i = 0; i < mp; ++i) {
         double cs = 0.0, rs = 0.0;
-        for (int r = tid; r < mp; r += HQ_T) {
+        for (int r = tid; r < mp; r += NTH) {
           if (r == i) continue;
           const zc a = Hg[(size_t)i * ld + r];
           cs += a.x * a.x + a.y * a.y;
@@ -558,12 +562,12 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
         const double f = s.sc[0];
         if (f != 1.0) {
           const double gi = 1.0 / f;
-          for (int q = tid; q < mp; q += HQ_T) {
+          for (int q = tid; q < mp; q += NTH) {
             zc* a = &Hg[(size_t)q * ld + i];    // row i
             *a = zscale(*a, gi);
           }
           __syncthreads();
-          for (int q = tid; q < mp; q += HQ_T) {
+          for (int q = tid; q < mp; q += NTH) {
             zc* a = &Hg[(size_t)i * ld + q];    // column i
             *a = zscale(*a, f);
           }
@@ -580,7 +584,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       const int L = mp - k - 1;
       if (tid == 0) flops += 16.0 * (double)mp * L + 16.0 * (double)L * L;
       double ss = 0.0, dummy = 0.0;
-      for (int r = tid; r < L; r += HQ_T) {
+      for (int r = tid; r < L; r += NTH) {
         const zc x = Hg[(size_t)k * ld + k + 1 + r];
         v[r] = x;
         if (r >= 1) ss += x.x * x.x + x.y * x.y;
@@ -606,19 +610,19 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       const zc tau = zmk(s.sc[0], s.sc[1]);
       const zc scal = zmk(s.sc[2], s.sc[3]);
       const double beta = s.sc[4];
-      for (int r = tid; r < L; r += HQ_T) v[r] = (r == 0) ? zmk(1.0, 0.0) : zmul(v[r], scal);
+      for (int r = tid; r < L; r += NTH) v[r] = (r == 0) ? zmk(1.0, 0.0) : zmul(v[r], scal);
       if (tid == 0) Hg[(size_t)k * ld + k + 1] = zmk(beta, 0.0);
-      for (int r = 2 + tid; r <= L; r += HQ_T) Hg[(size_t)k * ld + k + r] = zmk(0.0, 0.0);
+      for (int r = 2 + tid; r <= L; r += NTH) Hg[(size_t)k * ld + k + r] = zmk(0.0, 0.0);
       __syncthreads();
       // right: w = tau H(:, k+1:) v
-      for (int r = tid; r < mp; r += HQ_T) {
+      for (int r = tid; r < mp; r += NTH) {
         zc acc = zmk(0.0, 0.0);
         for (int c = 0; c < L; ++c) acc = zfma(Hg[(size_t)(k + 1 + c) * ld + r], v[c], acc);
         w[r] = zmul(tau, acc);
       }
       __syncthreads();
       // right update fused with the left product z = conj(tau) v^H H(k+1:, k+1:), warp per column
-      for (int c = warp; c < L; c += HQ_W) {
+      for (int c = warp; c < L; c += NWA) {
         const zc vc = zconj(v[c]);
         zc* col = Hg + (size_t)(k + 1 + c) * ld;
         zc acc = zmk(0.0, 0.0);
@@ -633,7 +637,7 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
       }
       __syncthreads();
       // left update: H(k+1:, k+1:) -= v z
-      for (int c = warp; c < L; c += HQ_W) {
+      for (int c = warp; c < L; c += NWA) {
         const zc zc_ = z[c];
         zc* col = Hg + (size_t)(k + 1 + c) * ld + k + 1;
         for (int r = lane; r < L; r += 32) col[r] = zsub(col[r], zmul(v[r], zc_));
@@ -647,10 +651,10 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
     // increasing order through shared memory is safe
     for (int c = 0; c < mp; ++c) {
       const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
-      for (int r = tid; r <= rmax; r += HQ_T) v[r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : zmk(0.0, 0.0);
+      for (int r = tid; r <= rmax; r += NTH) v[r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : zmk(0.0, 0.0);
       __syncthreads();
       const int64_t o = hess_coff(c, mp);
-      for (int r = tid; r <= rmax; r += HQ_T) Hg[o + r] = v[r];
+      for (int r = tid; r <= rmax; r += NTH) Hg[o + r] = v[r];
       __syncthreads();
     }
     phase(4);
@@ -663,6 +667,35 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t*
     __syncthreads();
   }
 }
+
+__global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
+                                                   const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
+                                                   const int64_t* __restrict__ h_off, zc* __restrict__ eig,
+                                                   const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
+                                                   int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
+                                                   double* __restrict__ flops_out) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ HqrSmem s;
+  __shared__ int s_inst;
+  eig_plain_body(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
+                 s_inst);
+}
+
+__global__ void __launch_bounds__(HQ_WIDE, 1) k_eig_plain_wide(int count, const int32_t* __restrict__ msz,
+                                                           zc* __restrict__ A, const int64_t* __restrict__ a_off,
+                                                           zc* __restrict__ Hp, const int64_t* __restrict__ h_off,
+                                                           zc* __restrict__ eig, const int64_t* __restrict__ eig_off,
+                                                           int32_t* __restrict__ status,
+                                                           int32_t* __restrict__ work_counter,
+                                                           const int32_t* __restrict__ order,
+                                                           double* __restrict__ flops_out) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ HqrSmem s;
+  __shared__ int s_inst;
+  eig_plain_body(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
+                 s_inst);
+}
+
 
 cudaError_t eig_phase_cycles(unsigned long long* out, bool reset) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_eig_phase_cycles, sizeof(unsigned long long) * 6);
@@ -686,10 +719,18 @@ cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, con
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(work_counter, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
-  // persistent grid: as many CTAs as can be resident at once
   int dev = 0, sms = 1, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (count * 2 <= sms) {
+    // a few instances: one wide CTA each, so every phase spreads over 16 warps
+    e = cudaFuncSetAttribute(k_eig_plain_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_eig_plain_wide<<<count, HQ_WIDE, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
+                                                order, flops);
+    return cudaGetLastError();
+  }
+  // persistent grid: as many CTAs as can be resident at once
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eig_plain, HQ_T, sm) != cudaSuccess || per_sm < 1)
     per_sm = 1;
   const int resident = sms * per_sm;

@@ -34,10 +34,13 @@ template <typename T, int NB>
 __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restrict__ desc, const int32_t* __restrict__ nsz,
                                             T* __restrict__ A, const int64_t* __restrict__ mat_off,
                                             int32_t* __restrict__ piv, const int64_t* __restrict__ piv_off,
-                                            int32_t* __restrict__ info, const int32_t* __restrict__ skip) {
+                                            int32_t* __restrict__ info, const int32_t* __restrict__ skip,
+                                            const int32_t* __restrict__ order) {
   typedef typename cx<T>::real R;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int k = blockIdx.x;
+  // CTAs start in block order: with `order` largest first, the last wave
+  // holds the small factorisations
+  const int k = order ? order[blockIdx.x] : blockIdx.x;
   if (k >= count) return;
   if (skip && skip[k]) return;
   const int n = nsz[k];
@@ -426,11 +429,11 @@ int lu_nb_for(int n) {
 template <typename T, int NB>
 static cudaError_t launch_lu_nb(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A,
                                 const int64_t* mat_off, int32_t* piv, const int64_t* piv_off, int32_t* info,
-                                cudaStream_t s, const int32_t* skip) {
+                                cudaStream_t s, const int32_t* skip, const int32_t* order) {
   size_t sm = (size_t)nmax * NB * sizeof(T) + (size_t)NB * 65 * sizeof(T);
   cudaError_t e = cudaFuncSetAttribute(k_lu<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_lu<T, NB><<<count, 256, sm, s>>>(count, desc, nsz, A, mat_off, piv, piv_off, info, skip);
+  k_lu<T, NB><<<count, 256, sm, s>>>(count, desc, nsz, A, mat_off, piv, piv_off, info, skip, order);
   return cudaGetLastError();
 }
 
@@ -442,14 +445,14 @@ int lu_nb_max(int n) {
 template <typename T>
 cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
                       int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip,
-                      int nb_hint) {
+                      int nb_hint, const int32_t* order) {
   if (count <= 0) return cudaSuccess;
   int nb = lu_nb_for<T>(nmax);
   // a tuned panel width no wider than shared memory allows
   if ((nb_hint == 8 || nb_hint == 16 || nb_hint == 32) && nb_hint <= nb) nb = nb_hint;
-  if (nb == 32) return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
-  if (nb == 16) return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
-  return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip);
+  if (nb == 32) return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order);
+  if (nb == 16) return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order);
+  return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order);
 }
 
 template <typename T>
@@ -479,9 +482,9 @@ cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, c
 }
 
 template cudaError_t launch_lu<zc>(int, const InstDesc*, const int32_t*, int, zc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*);
 template cudaError_t launch_lu<cc>(int, const InstDesc*, const int32_t*, int, cc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*);
 template int lu_nb_max<zc>(int);
 template int lu_nb_max<cc>(int);
 

@@ -77,7 +77,7 @@ __global__ void k_spline(int nprof, const ProfDesc* __restrict__ pdesc, const do
   const ProfDesc d = pdesc[k];
   const int n = d.nym;
   const double* P = prof + d.off_prof;   // row i: y rho u v w T
-  double* S = spl + d.off_spl;           // row i: r[5] then b
+  double* S = spl + d.off_spl;           // row i: five second derivatives, then 1/b(i) (scratch)
   // the interval search of SPEVAL needs strictly ascending, finite abscissae
   int ok = 1;
   for (int i = 0; i < n; ++i) {
@@ -87,43 +87,52 @@ __global__ void k_spline(int nprof, const ProfDesc* __restrict__ pdesc, const do
   bad[k] = ok ? 0 : 1;
   auto X = [&](int i) { return P[6 * i]; };
   auto Y = [&](int i, int f) { return f == 2 ? 0.0 : P[6 * i + 1 + f]; };  // v forced to 0
-  // assemble c(i), a(i), b(i), r(i) and eliminate forward in one pass
+  // assemble c(i), a(i), b(i), r(i) and eliminate forward in one pass.
+  // One thread runs the whole recurrence, and on GB300 each FP64 division is
+  // a multi-instruction sequence at 1/64 rate.  So every row takes one
+  // reciprocal of its interval and one of the pivot, shared by the five
+  // fields; the pivot's reciprocal is stored in place of b(i) for the back
+  // substitution.
   double c_prev = X(1) - X(0);           // C(1)
-  double b_prev = 0.0, r_prev[5] = {0, 0, 0, 0, 0};
+  double ic_prev = 1.0 / c_prev;
+  double ib_prev = 0.0, r_prev[5] = {0, 0, 0, 0, 0};
   for (int i = 1; i <= n - 2; ++i) {
-    double ci = X(i + 1) - X(i);
-    double ai = c_prev;
+    const double ci = X(i + 1) - X(i);
+    const double ici = 1.0 / ci;
+    const double ai = c_prev;
     double bi = 2.0 * (ai + ci);
     double ri[5];
 #pragma unroll
-    for (int f = 0; f < 5; ++f) ri[f] = 6.0 * ((Y(i + 1, f) - Y(i, f)) / ci - (Y(i, f) - Y(i - 1, f)) / c_prev);
+    for (int f = 0; f < 5; ++f) ri[f] = 6.0 * ((Y(i + 1, f) - Y(i, f)) * ici - (Y(i, f) - Y(i - 1, f)) * ic_prev);
     if (i == 1) bi += 1.0 * (X(1) - X(0));          // B(2) += lambda*C(1)
     if (i == n - 2) bi += 1.0 * ci;                  // B(NM1) += lambda*C(NM1)
     if (i >= 2) {
-      double t = ai / b_prev;
+      const double t = ai * ib_prev;
       bi = bi - t * c_prev;
 #pragma unroll
       for (int f = 0; f < 5; ++f) ri[f] = ri[f] - t * r_prev[f];
     }
+    const double ibi = 1.0 / bi;
 #pragma unroll
     for (int f = 0; f < 5; ++f) { S[6 * i + f] = ri[f]; r_prev[f] = ri[f]; }
-    S[6 * i + 5] = bi;
-    b_prev = bi;
+    S[6 * i + 5] = ibi;
+    ib_prev = ibi;
     c_prev = ci;
+    ic_prev = ici;
   }
   // back substitution, FDP(NM1) = R(NM1)/B(NM1); FDP(k) = (R(k) - C(k) FDP(k+1))/B(k)
   double nxt[5];
   {
     int i = n - 2;
-    double bi = S[6 * i + 5];
+    const double ibi = S[6 * i + 5];
 #pragma unroll
-    for (int f = 0; f < 5; ++f) { nxt[f] = S[6 * i + f] / bi; S[6 * i + f] = nxt[f]; }
+    for (int f = 0; f < 5; ++f) { nxt[f] = S[6 * i + f] * ibi; S[6 * i + f] = nxt[f]; }
   }
   for (int i = n - 3; i >= 1; --i) {
-    double ci = X(i + 1) - X(i);
-    double bi = S[6 * i + 5];
+    const double ci = X(i + 1) - X(i);
+    const double ibi = S[6 * i + 5];
 #pragma unroll
-    for (int f = 0; f < 5; ++f) { nxt[f] = (S[6 * i + f] - ci * nxt[f]) / bi; S[6 * i + f] = nxt[f]; }
+    for (int f = 0; f < 5; ++f) { nxt[f] = (S[6 * i + f] - ci * nxt[f]) * ibi; S[6 * i + f] = nxt[f]; }
   }
 #pragma unroll
   for (int f = 0; f < 5; ++f) {

@@ -132,6 +132,15 @@ int stab_assemble(stab_ctx* ctx, const stab_params* p, int32_t nym, const double
  */
 int stab_autotune(stab_ctx* ctx, const int32_t* orders, int32_t norders, int32_t* nb_out, float* ms_out);
 
+/*
+ * Self-check of the cluster path of the batched LU: count test matrices of
+ * order n factored with one CTA each and with clusters of four CTAs (one
+ * matrix per cluster).  max_diff: largest |difference| of the factors,
+ * piv_diff: number of differing pivots; both 0 when the paths agree.
+ */
+int stab_lu_cluster_check(stab_ctx* ctx, int32_t n, int32_t count, int32_t complex128, double* max_diff,
+                          int32_t* piv_diff);
+
 /* ---- full spectrum (plain FP64 path) --------------------------------- */
 /*
  * All eigenvalues of one instance, sorted ascending by imaginary part with

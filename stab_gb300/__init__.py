@@ -38,7 +38,7 @@ EXPORTED = (
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
-    "stab_batch_spectra", "stab_autotune", "stab_eig_phases",
+    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check",
 )
 
 
@@ -151,6 +151,7 @@ def load(path: str = LIB_PATH):
     lib.stab_batch_spectra.argtypes = [vp, P(P(dbl))]
     lib.stab_autotune.argtypes = [vp, P(i32), i32, P(i32), P(ctypes.c_float)]
     lib.stab_eig_phases.argtypes = [vp, P(ctypes.c_uint64), i32]
+    lib.stab_lu_cluster_check.argtypes = [vp, i32, i32, i32, P(dbl), P(i32)]
     _lib = lib
     return lib
 
@@ -383,6 +384,14 @@ class Context:
                                            ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
         return {int(n): {"c64": (int(nb[2 * q]), float(ms[2 * q])), "c128": (int(nb[2 * q + 1]), float(ms[2 * q + 1]))}
                 for q, n in enumerate(o)}
+
+    def lu_cluster_check(self, n: int, count: int, complex128: bool = True):
+        """(max |difference|, differing pivots) of one-CTA vs four-CTA-cluster LU."""
+        md = ctypes.c_double(0.0)
+        pd = ctypes.c_int32(0)
+        self._check(self.lib.stab_lu_cluster_check(self.h, n, count, 1 if complex128 else 0, ctypes.byref(md),
+                                                   ctypes.byref(pd)))
+        return md.value, pd.value
 
     def eig_phases(self, reset: bool = True) -> dict:
         """SM cycles per phase of the eigensolver (stab_eig_phases)."""

@@ -772,9 +772,11 @@ static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
   rc = dense<zc>(b, all, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z", skip);
   if (rc) return rc;
   CK(c, timed(c, "k_lu_z", [&] {
+    // the retried instances are few and their FP64 factorisations long:
+    // a cluster of four SMs shares each one
     return launch_lu<zc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
                          b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
-                         tuned_nb(c, true, b->nmax), b->order.as<int32_t>());
+                         tuned_nb(c, true, b->nmax), b->order.as<int32_t>(), b->nmax >= 240 ? 4 : 1);
   }));
   CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
   CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, b->pcol.as<int32_t>(), skip, s); }));
@@ -1417,7 +1419,59 @@ static int tune_lu_one(stab_ctx* c, int n, int reps, int* best_nb, float* best_m
   return 0;
 }
 
+// Factor the same test matrices with one CTA per matrix and with clusters of
+// four CTAs; the factors and pivots must agree bit for bit.
+template <typename T>
+static int lu_cluster_check(stab_ctx* c, int n, int count, double* max_diff, int32_t* piv_diff) {
+  cudaStream_t s = c->stream;
+  DevBuf A1, A4, piv1, piv4, info, nsz, moff, poff;
+  const size_t elems = (size_t)count * n * n;
+  CK(c, A1.ensure(sizeof(T) * elems, s));
+  CK(c, A4.ensure(sizeof(T) * elems, s));
+  CK(c, piv1.ensure(sizeof(int32_t) * (size_t)count * n, s));
+  CK(c, piv4.ensure(sizeof(int32_t) * (size_t)count * n, s));
+  CK(c, info.ensure(sizeof(int32_t) * count, s));
+  std::vector<int32_t> ns(count, n);
+  std::vector<int64_t> mo(count), po(count);
+  for (int k = 0; k < count; ++k) {
+    mo[k] = (int64_t)k * n * n;
+    po[k] = (int64_t)k * n;
+  }
+  CK(c, upload(nsz, ns, s));
+  CK(c, upload(moff, mo, s));
+  CK(c, upload(poff, po, s));
+  CK(c, launch_tune_matrix<T>(count, n, A1.as<T>(), s));
+  CK(c, launch_tune_matrix<T>(count, n, A4.as<T>(), s));
+  CK(c, launch_lu<T>(count, nullptr, nsz.as<int32_t>(), n, A1.as<T>(), moff.as<int64_t>(), piv1.as<int32_t>(),
+                     poff.as<int64_t>(), info.as<int32_t>(), s, nullptr, 0, nullptr, 1));
+  CK(c, launch_lu<T>(count, nullptr, nsz.as<int32_t>(), n, A4.as<T>(), moff.as<int64_t>(), piv4.as<int32_t>(),
+                     poff.as<int64_t>(), info.as<int32_t>(), s, nullptr, 0, nullptr, 4));
+  std::vector<T> h1(elems), h4(elems);
+  std::vector<int32_t> p1((size_t)count * n), p4((size_t)count * n);
+  CK(c, cudaMemcpyAsync(h1.data(), A1.p, sizeof(T) * elems, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(h4.data(), A4.p, sizeof(T) * elems, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(p1.data(), piv1.p, sizeof(int32_t) * p1.size(), cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(p4.data(), piv4.p, sizeof(int32_t) * p4.size(), cudaMemcpyDeviceToHost, s));
+  CK(c, cudaStreamSynchronize(s));
+  double md = 0.0;
+  for (size_t q = 0; q < elems; ++q)
+    md = std::max(md, std::max(std::fabs((double)h1[q].x - (double)h4[q].x), std::fabs((double)h1[q].y - (double)h4[q].y)));
+  int32_t pd = 0;
+  for (size_t q = 0; q < p1.size(); ++q) pd += (p1[q] != p4[q]) ? 1 : 0;
+  *max_diff = md;
+  *piv_diff = pd;
+  return 0;
+}
+
 extern "C" {
+
+int stab_lu_cluster_check(stab_ctx* c, int32_t n, int32_t count, int32_t complex128, double* max_diff,
+                          int32_t* piv_diff) {
+  if (!c || !max_diff || !piv_diff || n < 2 || n > 1024 || count < 1) return STAB_ERR_ARG;
+  cudaSetDevice(c->device);
+  return complex128 ? lu_cluster_check<zc>(c, n, count, max_diff, piv_diff)
+                    : lu_cluster_check<cc>(c, n, count, max_diff, piv_diff);
+}
 
 int stab_autotune(stab_ctx* c, const int32_t* orders, int32_t norders, int32_t* nb_out, float* ms_out) {
   if (!c || !orders || norders < 1) return set_err(c, STAB_ERR_ARG, "no orders to tune");

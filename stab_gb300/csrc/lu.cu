@@ -13,9 +13,13 @@
 //   3. U12 = L11^-1 A12 (forward substitution, one thread per column);
 //   4. A22 -= L21 U12 as a 64x64-tiled GEMM with L21 read from shared memory
 //      and each thread holding a 4x4 block of complex accumulators.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "lu.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace stab {
 
@@ -30,7 +34,14 @@ __device__ __forceinline__ void argmax_merge(typename cx<T>::real& bv, int& bi, 
   if (v > bv || (v == bv && i < bi)) { bv = v; bi = i; }
 }
 
-template <typename T, int NB>
+// CL > 1: a thread-block cluster of CL CTAs factors one matrix.  Rank 0
+// factors each panel and writes it (and its pivots) to global memory; after
+// a cluster barrier every rank loads the panel and applies the swaps, the
+// U12 solve and the trailing update to its own 64-column tiles of the
+// trailing matrix (tile t of the columns right of the panel belongs to rank
+// t mod CL); a second cluster barrier closes the step.  The barriers are
+// cluster-scope release/acquire, which orders the global-memory writes.
+template <typename T, int NB, int CL>
 __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restrict__ desc, const int32_t* __restrict__ nsz,
                                             T* __restrict__ A, const int64_t* __restrict__ mat_off,
                                             int32_t* __restrict__ piv, const int64_t* __restrict__ piv_off,
@@ -38,9 +49,11 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
                                             const int32_t* __restrict__ order) {
   typedef typename cx<T>::real R;
   extern __shared__ __align__(16) unsigned char smraw[];
+  const int rank = (CL > 1) ? (int)(cg::this_cluster().block_rank()) : 0;
   // CTAs start in block order: with `order` largest first, the last wave
   // holds the small factorisations
-  const int k = order ? order[blockIdx.x] : blockIdx.x;
+  const int slot = (int)blockIdx.x / CL;
+  const int k = order ? order[slot] : slot;
   if (k >= count) return;
   if (skip && skip[k]) return;
   const int n = nsz[k];
@@ -56,6 +69,7 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int w = min(NB, n - k0);
     const int rows = n - k0;
+    if (rank == 0) {
     // 1. load panel
     for (int c = 0; c < w; ++c)
       for (int r = tid; r < rows; r += blockDim.x) P[(size_t)c * n + r] = M[(size_t)(k0 + c) * n + k0 + r];
@@ -106,9 +120,25 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
     // write the factored panel back
     for (int c = 0; c < w; ++c)
       for (int r = tid; r < rows; r += blockDim.x) M[(size_t)(k0 + c) * n + k0 + r] = P[(size_t)c * n + r];
+    }   // rank 0
+    if constexpr (CL > 1) {
+      cg::this_cluster().sync();
+      if (rank != 0)
+        for (int c = 0; c < w; ++c)
+          for (int r = tid; r < rows; r += blockDim.x) P[(size_t)c * n + r] = M[(size_t)(k0 + c) * n + k0 + r];
+      __syncthreads();
+    }
+    const int c1 = k0 + w;
+    // owner of column c: left of the panel by 64-column tiles, right of it by
+    // 64-column tiles counted from c1 (the tiles of the trailing update)
+    auto mine = [&](int c) {
+      if (CL == 1) return true;
+      return ((c < k0 ? c : c - c1) >> 6) % CL == rank;
+    };
     // 2. row swaps on the columns outside the panel (one thread per column)
     for (int c = tid; c < n; c += blockDim.x) {
       if (c >= k0 && c < k0 + w) continue;
+      if (!mine(c)) continue;
       for (int j = 0; j < w; ++j) {
         const int p = ip[k0 + j];
         if (p != k0 + j) {
@@ -119,10 +149,10 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
       }
     }
     __syncthreads();
-    const int c1 = k0 + w;
     if (c1 >= n) break;
     // 3. U12 = L11^-1 A12 (unit lower), one thread per column
     for (int c = c1 + tid; c < n; c += blockDim.x) {
+      if (!mine(c)) continue;
       T x[NB];
 #pragma unroll
       for (int j = 0; j < NB; ++j) x[j] = (j < w) ? M[(size_t)c * n + k0 + j] : cx<T>::make(0, 0);
@@ -141,7 +171,7 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
     // 4. A22 -= L21 U12, 64x64 tiles, 4x4 complex per thread (16x16 threads)
     const int m2 = n - c1;
     const int tr = tid & 15, tc = tid >> 4;
-    for (int tc0 = 0; tc0 < m2; tc0 += 64) {
+    for (int tc0 = 64 * rank; tc0 < m2; tc0 += 64 * CL) {
       // stage U12 tile (w x 64) in shared memory
       for (int q = tid; q < NB * 64; q += blockDim.x) {
         const int j = q % NB, cc_ = q / NB;   // coalesced along the column
@@ -191,8 +221,9 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
       }
       __syncthreads();
     }
+    if constexpr (CL > 1) cg::this_cluster().sync();   // the next panel reads other ranks' tiles
   }
-  if (tid == 0) info[k] = first_zero;
+  if (tid == 0 && rank == 0) info[k] = first_zero;
 }
 
 // Power-of-two row and column equilibration of complex64 matrices before the
@@ -429,11 +460,33 @@ int lu_nb_for(int n) {
 template <typename T, int NB>
 static cudaError_t launch_lu_nb(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A,
                                 const int64_t* mat_off, int32_t* piv, const int64_t* piv_off, int32_t* info,
-                                cudaStream_t s, const int32_t* skip, const int32_t* order) {
+                                cudaStream_t s, const int32_t* skip, const int32_t* order, int cluster) {
   size_t sm = (size_t)nmax * NB * sizeof(T) + (size_t)NB * 65 * sizeof(T);
-  cudaError_t e = cudaFuncSetAttribute(k_lu<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (cluster == 4) {
+    cudaError_t e = cudaFuncSetAttribute(k_lu<T, NB, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e == cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(4 * count);
+      cfg.blockDim = dim3(256);
+      cfg.dynamicSmemBytes = sm;
+      cfg.stream = s;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 4;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, k_lu<T, NB, 4>, &cfg) == cudaSuccess && nclusters > 0)
+        return cudaLaunchKernelEx(&cfg, k_lu<T, NB, 4>, count, desc, nsz, A, mat_off, piv, piv_off, info, skip,
+                                  order);
+    }
+    cudaGetLastError();   // no cluster of this size fits: one CTA per matrix
+  }
+  cudaError_t e = cudaFuncSetAttribute(k_lu<T, NB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_lu<T, NB><<<count, 256, sm, s>>>(count, desc, nsz, A, mat_off, piv, piv_off, info, skip, order);
+  k_lu<T, NB, 1><<<count, 256, sm, s>>>(count, desc, nsz, A, mat_off, piv, piv_off, info, skip, order);
   return cudaGetLastError();
 }
 
@@ -445,14 +498,16 @@ int lu_nb_max(int n) {
 template <typename T>
 cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
                       int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip,
-                      int nb_hint, const int32_t* order) {
+                      int nb_hint, const int32_t* order, int cluster) {
   if (count <= 0) return cudaSuccess;
   int nb = lu_nb_for<T>(nmax);
   // a tuned panel width no wider than shared memory allows
   if ((nb_hint == 8 || nb_hint == 16 || nb_hint == 32) && nb_hint <= nb) nb = nb_hint;
-  if (nb == 32) return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order);
-  if (nb == 16) return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order);
-  return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order);
+  if (nb == 32)
+    return launch_lu_nb<T, 32>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order, cluster);
+  if (nb == 16)
+    return launch_lu_nb<T, 16>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order, cluster);
+  return launch_lu_nb<T, 8>(count, desc, nsz, nmax, A, mat_off, piv, piv_off, info, s, skip, order, cluster);
 }
 
 template <typename T>
@@ -482,9 +537,9 @@ cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, c
 }
 
 template cudaError_t launch_lu<zc>(int, const InstDesc*, const int32_t*, int, zc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*, int);
 template cudaError_t launch_lu<cc>(int, const InstDesc*, const int32_t*, int, cc*, const int64_t*, int32_t*,
-                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*);
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*, int);
 template int lu_nb_max<zc>(int);
 template int lu_nb_max<cc>(int);
 

@@ -9,7 +9,8 @@ namespace stab {
 template <typename T>
 cudaError_t launch_lu(int count, const InstDesc* desc, const int32_t* nsz, int nmax, T* A, const int64_t* mat_off,
                       int32_t* piv, const int64_t* piv_off, int32_t* info, cudaStream_t s,
-                      const int32_t* skip = nullptr, int nb_hint = 0, const int32_t* order = nullptr);
+                      const int32_t* skip = nullptr, int nb_hint = 0, const int32_t* order = nullptr,
+                      int cluster = 1);
 // widest panel the shared memory admits for order n (8, 16 or 32)
 template <typename T>
 int lu_nb_max(int n);

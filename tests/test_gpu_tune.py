@@ -21,3 +21,9 @@ def test_autotune_picks_a_feasible_width_and_keeps_results(ctx):
     w = es.eig[H.select_least(es.eig, d)]
     eig, err, iters, st, _ = ctx.solve_batch([H.stab_params(d)], [prof], sg.MODE_SEEDED, seeds=[w * (1 + 1e-7)])
     assert st[0] == sg.ST_OK and abs(eig[0] - w) / abs(w) < 1e-10
+
+
+@pytest.mark.parametrize("n,z", [(240, True), (640, True), (320, False)])
+def test_cluster_lu_matches_single_cta(ctx, n, z):
+    md, pd = ctx.lu_cluster_check(n, 8, complex128=z)
+    assert pd == 0 and md == 0.0

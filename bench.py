@@ -196,6 +196,25 @@ def single_instance_leg(ctx, stream, cpu: bool):
     return out
 
 
+def serving_leg(ctx, args):
+    """The serving loop (stab_gb300/serve.py): Poisson arrivals at 2000/s for
+    args.serve_seconds of temporal and spatial requests with N ~ U{32..192},
+    admitted by free device memory and solved in batches through the
+    coarse-seeded path.  Reports throughput and latency percentiles."""
+    import torch
+    import stab_gb300 as sg
+    from stab_gb300 import serve as sv
+    reqs = sv.make_requests(2000.0, args.serve_seconds, 20261205)
+    solve = sv.gpu_solver(ctx, sg.MODE_COARSE)
+    solve(sv.make_requests(200.0, 0.05, 20261206))          # warm-up
+    st = sv.serve(reqs, solve, lambda: torch.cuda.mem_get_info()[0], 4096)
+    out = st.summary()
+    out.update({"requests": len(reqs), "rate_per_s": 2000.0, "arrival_window_s": args.serve_seconds,
+                "solved_ok_or_fellback": sum(1 for r in reqs if r.status in (sg.ST_OK, sg.ST_FELLBACK)),
+                "mix": "50/50 temporal/spatial, N~U{32..192}, seed 20261205"})
+    return out
+
+
 def to_stab(d):
     import stab_gb300 as sg
     return sg.StabParams.make(itype=d["itype"], ny=d["ny"], Ma=d["Ma"], Re=d["Re"], Pr=d["Pr"],
@@ -350,6 +369,7 @@ def main():
     ap.add_argument("--surrogate", type=int, default=1, help="1: also run the surrogate-seeded leg")
     ap.add_argument("--sur-train", type=int, default=8192)
     ap.add_argument("--sur-count", type=int, default=1024)
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the serving leg (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_setup(args.gpus)
@@ -433,6 +453,7 @@ def main():
 
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None
     single = single_instance_leg(ctx, stream, cpu=args.cpu_sample > 0) if rank == 0 else None
+    serving = serving_leg(ctx, args) if (rank == 0 and args.serve_seconds > 0) else None
 
     # end-to-end through the C ABI call with host buffers (pinned), results read back
     barrier(world)
@@ -507,6 +528,7 @@ def main():
         "cuda_graph": "device part of each timed pass replayed from a captured CUDA graph",
         "surrogate": sur,
         "single_instance": single,
+        "serving": serving,
         "clocks": clk,
         "cpu_baseline": cpu,
     }

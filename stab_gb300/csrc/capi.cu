@@ -751,7 +751,7 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
 // Q(sigma).  The eigenvalue estimate sigma - x_p / y_p converges with the
 // ratio |sigma - lambda_1| / |sigma - lambda_2| per step, which separates
 // mode clusters that complex64 factors cannot resolve.
-static const int kInverseSteps = 12;
+static const int kInverseSteps = 8;
 // N of the second candidate level of the fallback
 static const int kMediumNy = 48;
 static const double kInverseTol = 1e-13;

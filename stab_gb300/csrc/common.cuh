@@ -30,6 +30,15 @@ __host__ __device__ __forceinline__ zc zfma(zc a, zc b, zc c) {
 __host__ __device__ __forceinline__ zc zcfma(zc a, zc b, zc c) {
   return zmk(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
 }
+// c - a*b in four FMAs (a separate product and subtraction take six FP64
+// instructions, and GB300 issues FP64 at 1/64 of the FP32 rate)
+__host__ __device__ __forceinline__ zc zfnma(zc a, zc b, zc c) {
+  return zmk(fma(-a.x, b.x, fma(a.y, b.y, c.x)), fma(-a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+// c - a*conj(b)
+__host__ __device__ __forceinline__ zc zfnmac(zc a, zc b, zc c) {
+  return zmk(fma(-a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
 // robust complex division a/b (Smith's method)
 __host__ __device__ __forceinline__ zc zdiv(zc a, zc b) {
   if (fabs(b.x) >= fabs(b.y)) {
@@ -64,6 +73,7 @@ template <> struct cx<zc> {
   __device__ static zc mul(zc a, zc b) { return zmul(a, b); }
   __device__ static zc fma_(zc a, zc b, zc c) { return zfma(a, b, c); }
   __device__ static zc sub(zc a, zc b) { return zsub(a, b); }
+  __device__ static zc fnma(zc a, zc b, zc c) { return zfnma(a, b, c); }   // c - a*b
   __device__ static zc div(zc a, zc b) { return zdiv(a, b); }
   __device__ static double abs1(zc a) { return zabs1(a); }
   __device__ static zc from(zc a) { return a; }
@@ -75,6 +85,9 @@ template <> struct cx<cc> {
   __device__ static cc mul(cc a, cc b) { return cmul(a, b); }
   __device__ static cc fma_(cc a, cc b, cc c) { return cfma(a, b, c); }
   __device__ static cc sub(cc a, cc b) { return cmk(a.x - b.x, a.y - b.y); }
+  __device__ static cc fnma(cc a, cc b, cc c) {   // c - a*b
+    return cmk(fmaf(-a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(-a.x, b.y, fmaf(-a.y, b.x, c.y)));
+  }
   __device__ static cc div(cc a, cc b) {
     // float Smith division
     if (fabsf(b.x) >= fabsf(b.y)) {

@@ -152,14 +152,14 @@ __device__ __forceinline__ void apply_left(const Acc& H, int k, int j, zc tau, z
   zc a = H(k, j), b = H(k + 1, j);
   zc sm = zmul(zconj(tau), zcfma(u2, b, a));
   H(k, j) = zsub(a, sm);
-  H(k + 1, j) = zsub(b, zmul(sm, u2));
+  H(k + 1, j) = zfnma(sm, u2, b);
 }
 template <class Acc>
 __device__ __forceinline__ void apply_right(const Acc& H, int k, int j, zc tau, zc u2) {
   zc a = H(j, k), b = H(j, k + 1);
   zc sm = zmul(tau, zfma(u2, b, a));
   H(j, k) = zsub(a, sm);
-  H(j, k + 1) = zsub(b, zmul(sm, zconj(u2)));
+  H(j, k + 1) = zfnmac(sm, u2, b);
 }
 
 // Single-shift QR on the mp x mp upper Hessenberg matrix behind H; writes
@@ -464,6 +464,7 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
     zc* v = zs;
     zc* w = v + m;
     zc* z = w + m;
+    zc* vn = z + m;           // next step's reflector vector (Hessenberg reduction)
     for (int i = tid; i < m; i += NTH) active[i] = 1;
     if (tid == 0) s.mp = 0;
     __syncthreads();
@@ -579,17 +580,30 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
     }
     phase(2);
     // ---- 4. Hessenberg reduction -----------------------------------------
+    // The left update of step k leaves column k+1 final, so the warp that
+    // updates it also copies it into the next step's reflector vector and
+    // sums its squared tail: step k+1 starts without a pass or a block
+    // reduction of its own.
     double flops = 0.0;   // FP64 work of the reduction and the sweeps (thread 0)
+    bool have_next = false;
     for (int k = 0; k + 2 < mp; ++k) {
       const int L = mp - k - 1;
       if (tid == 0) flops += 16.0 * (double)mp * L + 16.0 * (double)L * L;
       double ss = 0.0, dummy = 0.0;
-      for (int r = tid; r < L; r += NTH) {
-        const zc x = Hg[(size_t)k * ld + k + 1 + r];
-        v[r] = x;
-        if (r >= 1) ss += x.x * x.x + x.y * x.y;
+      if (have_next) {
+        zc* t = v;                       // the vector gathered by the last step
+        v = vn;
+        vn = t;
+        ss = s.sc[5];
+      } else {
+        for (int r = tid; r < L; r += NTH) {
+          const zc x = Hg[(size_t)k * ld + k + 1 + r];
+          v[r] = x;
+          if (r >= 1) ss += x.x * x.x + x.y * x.y;
+        }
+        block_sum2(s, ss, dummy);
       }
-      block_sum2(s, ss, dummy);
+      have_next = false;
       if (tid == 0) {
         const zc alpha = v[0];
         if (ss == 0.0 && alpha.y == 0.0) {
@@ -627,7 +641,7 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
         zc* col = Hg + (size_t)(k + 1 + c) * ld;
         zc acc = zmk(0.0, 0.0);
         for (int r = lane; r < mp; r += 32) {
-          const zc h = zsub(col[r], zmul(w[r], vc));
+          const zc h = zfnma(w[r], vc, col[r]);
           col[r] = h;
           if (r >= k + 1) acc = zcfma(v[r - k - 1], h, acc);
         }
@@ -636,12 +650,26 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
         if (lane == 0) z[c] = zmul(zconj(tau), acc);
       }
       __syncthreads();
-      // left update: H(k+1:, k+1:) -= v z
+      // left update: H(k+1:, k+1:) -= v z; column k+1 (c = 0, warp 0) also
+      // feeds the next step: vn = H(k+2:, k+1), s.sc[5] = sum |vn[1:]|^2
       for (int c = warp; c < L; c += NWA) {
         const zc zc_ = z[c];
         zc* col = Hg + (size_t)(k + 1 + c) * ld + k + 1;
-        for (int r = lane; r < L; r += 32) col[r] = zsub(col[r], zmul(v[r], zc_));
+        if (c == 0) {
+          double sn = 0.0;
+          for (int r = lane; r < L; r += 32) {
+            const zc h = zfnma(v[r], zc_, col[r]);
+            col[r] = h;
+            if (r >= 1) vn[r - 1] = h;
+            if (r >= 2) sn = fma(h.x, h.x, fma(h.y, h.y, sn));
+          }
+          sn = warp_sum(sn);
+          if (lane == 0) s.sc[5] = sn;
+        } else {
+          for (int r = lane; r < L; r += 32) col[r] = zfnma(v[r], zc_, col[r]);
+        }
       }
+      have_next = true;
       __syncthreads();
     }
     phase(3);
@@ -706,7 +734,7 @@ cudaError_t eig_phase_cycles(unsigned long long* out, bool reset) {
 
 size_t eig_plain_smem(int mmax) {
   const size_t head = ((2 * (size_t)mmax * sizeof(int) + 15) / 16) * 16;
-  return head + 3 * (size_t)mmax * sizeof(zc);
+  return head + 4 * (size_t)mmax * sizeof(zc);
 }
 
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
         P[(size_t)j * n + r] = l;
         for (int c = j + 1; c < w; ++c) {
           T u = P[(size_t)c * n + j];
-          P[(size_t)c * n + r] = cx<T>::sub(P[(size_t)c * n + r], cx<T>::mul(l, u));
+          P[(size_t)c * n + r] = cx<T>::fnma(l, u, P[(size_t)c * n + r]);
         }
       }
       __syncthreads();
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256) k_lu(int count, const InstDesc* __restric
         if (j >= w) break;
 #pragma unroll
         for (int r = j + 1; r < NB; ++r)
-          if (r < w) x[r] = cx<T>::sub(x[r], cx<T>::mul(P[(size_t)j * n + r], x[j]));
+          if (r < w) x[r] = cx<T>::fnma(P[(size_t)j * n + r], x[j], x[r]);
       }
 #pragma unroll
       for (int j = 0; j < NB; ++j)
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(256) k_getrs(int count, const int32_t* __restr
   __syncwarp();
   for (int j = 0; j < n; ++j) {       // L y = b (unit diagonal)
     const T xj = xs[j];
-    for (int r = j + 1 + lane; r < n; r += 32) xs[r] = cx<T>::sub(xs[r], cx<T>::mul(M[(size_t)j * n + r], xj));
+    for (int r = j + 1 + lane; r < n; r += 32) xs[r] = cx<T>::fnma(M[(size_t)j * n + r], xj, xs[r]);
     __syncwarp();
   }
   for (int j = n - 1; j >= 0; --j) {  // U x = y
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(256) k_getrs(int count, const int32_t* __restr
     if (cx<T>::abs1(d) != 0) xj = cx<T>::div(xj, d);
     __syncwarp();
     if (lane == 0) xs[j] = xj;
-    for (int r = lane; r < j; r += 32) xs[r] = cx<T>::sub(xs[r], cx<T>::mul(M[(size_t)j * n + r], xj));
+    for (int r = lane; r < j; r += 32) xs[r] = cx<T>::fnma(M[(size_t)j * n + r], xj, xs[r]);
     __syncwarp();
   }
   for (int r = lane; r < n; r += 32) {
@@ -403,14 +403,14 @@ __global__ void __launch_bounds__(256) k_getrs_blk(int count, const int32_t* __r
       T x = lane < bs ? xs[jb + lane] : zero;
       for (int j = 0; j < bs; ++j) {
         const T xj = shfl_cx(x, j);
-        if (lane > j && lane < bs) x = cx<T>::sub(x, cx<T>::mul(tile[j * 33 + lane], xj));
+        if (lane > j && lane < bs) x = cx<T>::fnma(tile[j * 33 + lane], xj, x);
       }
       if (lane < bs) xs[jb + lane] = x;
     }
     __syncthreads();
     for (int r = jb + bs + tid; r < n; r += blockDim.x) {
       T acc = xs[r];
-      for (int j = 0; j < bs; ++j) acc = cx<T>::sub(acc, cx<T>::mul(M[(size_t)(jb + j) * n + r], xs[jb + j]));
+      for (int j = 0; j < bs; ++j) acc = cx<T>::fnma(M[(size_t)(jb + j) * n + r], xs[jb + j], acc);
       xs[r] = acc;
     }
     __syncthreads();
@@ -429,14 +429,14 @@ __global__ void __launch_bounds__(256) k_getrs_blk(int count, const int32_t* __r
         const T d = tile[j * 33 + j];
         if (lane == j && cx<T>::abs1(d) != 0) x = cx<T>::div(x, d);
         const T xj = shfl_cx(x, j);
-        if (lane < j) x = cx<T>::sub(x, cx<T>::mul(tile[j * 33 + lane], xj));
+        if (lane < j) x = cx<T>::fnma(tile[j * 33 + lane], xj, x);
       }
       if (lane < bs) xs[jb + lane] = x;
     }
     __syncthreads();
     for (int r = tid; r < jb; r += blockDim.x) {
       T acc = xs[r];
-      for (int j = 0; j < bs; ++j) acc = cx<T>::sub(acc, cx<T>::mul(M[(size_t)(jb + j) * n + r], xs[jb + j]));
+      for (int j = 0; j < bs; ++j) acc = cx<T>::fnma(M[(size_t)(jb + j) * n + r], xs[jb + j], acc);
       xs[r] = acc;
     }
     __syncthreads();

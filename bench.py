@@ -449,6 +449,9 @@ def main():
     stats = ctx.kernel_stats()
     ctx.set_profiling(False)
     phases = ctx.eig_phases(reset=True)
+    # "stage:" entries time whole candidate rounds; they are not kernels
+    stages = {k[6:]: round(v[1], 3) for k, v in stats.items() if k.startswith("stage:")}
+    stats = {k: v for k, v in stats.items() if not k.startswith("stage:")}
     launches_per_step = sum(v[0] for v in stats.values())
 
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None
@@ -523,6 +526,7 @@ def main():
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in sorted(stats.items(),
                                                                                key=lambda kv: -kv[1][1])},
         "gpu_launches": int(launches_per_step * args.steps),
+        "round_ms": stages,
         "eig_phase_share": {k: round(v / max(1, sum(phases.values())), 4) for k, v in phases.items()},
         "autotune_lu_panel": {str(n): {"c64": v["c64"][0], "c128": v["c128"][0]} for n, v in tune.items()},
         "cuda_graph": "device part of each timed pass replayed from a captured CUDA graph",
@@ -535,8 +539,15 @@ def main():
     if cpu is not None and args.cpu_sample > 0:
         s = args.cpu_sample
         d = np.abs(eig[:s] - cpu_eig) / np.abs(cpu_eig)
+        bad = [int(q) for q in np.nonzero(~(d <= TOL))[0]]
         line["oracle_check"] = {"sample": s, "max_rel_err_vs_cpu_oracle": float(np.nanmax(d)),
-                                "within_1e-10": int(np.sum(d <= TOL))}
+                                "within_1e-10": int(np.sum(d <= TOL)),
+                                "plain_gpu_vs_cpu_within_1e-10": int(np.sum(np.abs(ref_eig[:s] - cpu_eig)
+                                                                           / np.abs(cpu_eig) <= TOL)),
+                                "mismatches": [{"index": q, "gpu": [float(eig[q].real), float(eig[q].imag)],
+                                                "gpu_plain": [float(ref_eig[q].real), float(ref_eig[q].imag)],
+                                                "cpu": [float(cpu_eig[q].real), float(cpu_eig[q].imag)]}
+                                               for q in bad[:5]]}
     print(json.dumps(line), flush=True)
     batch.close()
     ctx.close()

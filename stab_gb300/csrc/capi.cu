@@ -1087,8 +1087,21 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
       CK(c, cudaMemcpyAsync(b->sigma.p, b->seed_raw.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
     }
     b->use_start = surrogate && !fp64 && b->ncheb > 0;
+    // per-round wall time in profiling mode ("stage:" entries wrap launches)
+    cudaEvent_t ra = nullptr, rb = nullptr;
+    if (c->profiling) {
+      ra = get_ev(c);
+      rb = get_ev(c);
+      cudaEventRecord(ra, s);
+    }
     int rc = fp64 ? run_polish64_ii(b, true, b->skip64.as<int32_t>()) : run_polish_t<cc>(b, true, fin);
     b->use_start = false;
+    if (c->profiling) {
+      cudaEventRecord(rb, s);
+      char nm[32];
+      std::snprintf(nm, sizeof(nm), "stage:round%d_%s", j, fp64 ? "c128" : "c64");
+      c->pending.push_back(PendingEv{stat_index(c, nm), ra, rb});
+    }
     if (rc) return rc;
     CK(c, timed(c, "k_fold_best", [&] {
       k_fold_best<<<n, 128, 0, s>>>(n, b->desc.as<InstDesc>(), b->sigma.as<zc>(), b->theta.as<zc>(),

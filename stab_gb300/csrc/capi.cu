@@ -1050,10 +1050,11 @@ static int coarse_seeds(stab_batch* b) {
 // and spurious acoustic ones at M < 0.03, and resolves the right one only
 // to ~1e-2.  Each candidate gets a complex64 round, and a complex128 retry
 // where that failed or contracted slowly (a mode cluster closer than
-// complex64 factors resolve).  When the top candidate's polish lands within
-// kQuickAcceptTol of its shift the instance is final; otherwise the next
+// complex64 factors resolve).  Candidates go in selection order, and the
+// first one whose polish lands within kQuickAcceptTol of its shift (a mode
+// the N = 32 spectrum resolved) makes the instance final; otherwise the next
 // candidates are polished too.  Instances with no converged pair go to the
-// FP64 full-spectrum fallback.
+// FP64 fallback.
 static int polish_candidate_rounds(stab_batch* b, bool extra) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
@@ -1108,7 +1109,7 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
                                     b->done.as<int32_t>(), b->err.as<double>(), b->iters.as<int32_t>(),
                                     b->outvec.as<zc>(), b->off_mof.as<int64_t>(), fin, b->have.as<int32_t>(),
                                     b->best_key.as<double>(), b->best_theta.as<zc>(), b->best_err.as<double>(),
-                                    b->best_iters.as<int32_t>(), b->best_out.as<zc>(), j == 0 ? 1 : 0,
+                                    b->best_iters.as<int32_t>(), b->best_out.as<zc>(), 1,
                                     kQuickAcceptTol, fp64 ? nullptr : b->skip64.as<int32_t>(), kSlowNewton, j,
                                     b->best_src.as<int32_t>());
       return cudaGetLastError();

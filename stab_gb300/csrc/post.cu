@@ -128,8 +128,9 @@ __global__ void k_take_candidate(int count, const zc* __restrict__ cand, int nca
 // Fold the result of a polish round into the per-instance best: a pair
 // counts when it converged and passes the selection filter; the less stable
 // one is kept (theta, err, iters and the output vector).  With `quick`, a
-// pair within quick_tol of its shift is final: the top coarse candidate is
-// then a resolved mode and later rounds skip the instance.
+// pair within quick_tol of its shift is final: that coarse candidate is a
+// resolved mode, the candidates after it are less stable at N = 32, and
+// later rounds skip the instance.
 __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ sigma,
                             const zc* __restrict__ theta, const int32_t* __restrict__ done,
                             const double* __restrict__ err, const int32_t* __restrict__ iters,

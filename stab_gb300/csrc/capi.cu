@@ -61,6 +61,8 @@ struct stab_ctx {
   std::vector<stab_batch*> live;   // caller-visible batches, released by stab_destroy
   std::vector<stab_mlp*> nets;     // networks, released by stab_destroy
   std::map<std::pair<int, int>, int> lu_nb;   // (complex128?, size class) -> tuned LU panel width
+  int seed_eig = STAB_EIG_DOUBLE_WORD;   // arithmetic of the seed spectra
+  int plain_eig = STAB_EIG_FP64;         // arithmetic of the plain spectra (the answer)
 };
 
 // size class of an LU order for the tuned panel-width table
@@ -562,9 +564,10 @@ static int write_vectors(stab_batch* b, Range r, const zc* theta_dev, const int3
   return 0;
 }
 
-// plain FP64 path on all instances: standard-form matrices, full spectrum,
-// sort + select, optional eigenvector of the selected mode
-static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig_plain") {
+// plain path on all instances: standard-form matrices, full spectrum, sort +
+// select, optional eigenvector of the selected mode.  `seed` marks a spectrum
+// that only seeds a polish (the seed arithmetic applies).
+static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig_plain", bool seed = false) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   int rc = ensure_plain_pools(b);
@@ -614,7 +617,8 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
     return launch_eig_plain(b->count, b->mmax, b->msz.as<int32_t>(), b->Abig.as<zc>(), b->off_m2.as<int64_t>(),
                             b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
                             b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
-                            b->flops.as<double>(), grid, s);
+                            b->flops.as<double>(), grid, s,
+                            (seed ? c->seed_eig : c->plain_eig) == STAB_EIG_DOUBLE_WORD);
   }));
   CK(c, timed(c, "k_post_spectrum", [&] {
     size_t sm = sizeof(zc) * b->mmax;
@@ -1035,7 +1039,7 @@ static int coarse_seeds(stab_batch* b) {
   stab_batch* cb = b->coarse;
   int rc = run_prep(cb);
   if (rc) return rc;
-  rc = run_plain(cb, false, "k_eig_plain_coarse");
+  rc = run_plain(cb, false, "k_eig_plain_coarse", true);
   if (rc) return rc;
   // same internal order in both batches (same stable itype sort)
   CK(c, cudaMemcpyAsync(b->cand.p, cb->cand.p, sizeof(zc) * b->count * kShiftCandidates, cudaMemcpyDeviceToDevice,
@@ -1504,6 +1508,15 @@ int stab_autotune(stab_ctx* c, const int32_t* orders, int32_t norders, int32_t* 
       if (ms_out) ms_out[2 * q + z] = ms;
     }
   }
+  return STAB_OK;
+}
+
+int stab_set_eig_precision(stab_ctx* c, int32_t seed, int32_t plain) {
+  if (!c) return STAB_ERR_ARG;
+  auto ok = [](int32_t v) { return v == STAB_EIG_FP64 || v == STAB_EIG_DOUBLE_WORD; };
+  if (!ok(seed) || !ok(plain)) return set_err(c, STAB_ERR_ARG, "eigensolve arithmetic must be STAB_EIG_FP64 or STAB_EIG_DOUBLE_WORD");
+  c->seed_eig = seed;
+  c->plain_eig = plain;
   return STAB_OK;
 }
 

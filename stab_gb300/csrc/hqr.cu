@@ -1,7 +1,7 @@
-// Plain FP64 full-spectrum eigensolver: the GPU replacement of ZGEEV
-// (temporal.f90:803, spatial.f90:1043) for all eigenvalues.
+// Full-spectrum eigensolver: the GPU replacement of ZGEEV (temporal.f90:803,
+// spatial.f90:1043) for all eigenvalues.
 //
-// Per instance (one 256-thread CTA, instances taken from a work counter):
+// Per instance (one CTA, instances taken from a work counter):
 //   1. isolation: rows (columns) whose off-diagonal entries are exactly zero
 //      within the active set give eigenvalue a_ii and are removed, repeated
 //      until none is found (the permutation step of ZGEBAL).  The temporal
@@ -10,427 +10,40 @@
 //   2. compaction of the active submatrix into H;
 //   3. diagonal balancing by powers of two (the scaling step of ZGEBAL);
 //   4. Householder reduction to upper Hessenberg form (as ZGEHD2);
-//   5. single-shift complex QR with Wilkinson shifts, exceptional shifts
-//      every 10th iteration and the conservative deflation test of Ahues and
-//      Tisseur (the algorithm of ZLAHQR, eigenvalues only).  The 2-element
-//      reflectors are general complex ones, so the subdiagonal need not be
-//      kept real.
+//   5. complex QR (the algorithm of ZLAHQR, eigenvalues only): multi-bulge
+//      sweeps with shifts from the trailing block, single-shift steps with
+//      Wilkinson shifts on small windows, exceptional shifts every 10th
+//      iteration and the deflation test of Ahues and Tisseur.  The
+//      2-element reflectors are general complex ones, so the subdiagonal need
+//      not be kept real.
 //
-// GB300 shape of step 5: FP64 issues at 1/59 of the FP32 rate, so no FP64
-// scalar work is repeated across threads.  The thread that updates the
-// 2x2/3x2 corner of a bulge step also forms the next step's reflector and
-// publishes it through a double-buffered shared slot: one barrier per bulge
-// step.  The corner is a serial chain of FP64 instructions, so the kernel
-// runs small CTAs, several per SM, letting the chains of different
-// instances overlap; the Hessenberg matrix is repacked in place into a
-// column-packed layout with two subdiagonals (room for the bulge), which
-// keeps the working set of the resident instances in L2.
+// Steps 2-5 run in the working precision C: complex128 for the answer, or
+// double-word complex (dw.cuh) for spectra that only seed a polish.  GB300
+// issues FP64 at 1/59 of the FP32 rate, so the FP64 form is bound by the
+// FP64 pipe; the double-word form runs the same algorithm on the FP32 pipe,
+// with no FP64 instruction on the serial path of a QR step.
 //
-// All arithmetic is FP64.  Every loop has an iteration cap; an instance
-// that hits it gets status STAB_ST_NOCONV and NaN for the missing values.
+// GB300 shape of step 5: the serial work of a bulge step (the next
+// reflector) runs on lanes of warp 0 while all threads do the row and column
+// updates, with a barrier per phase.  The serial chains of different
+// instances overlap because the kernel runs small CTAs, several per SM; the
+// Hessenberg matrix is repacked in place into a column-packed layout with two
+// subdiagonals (room for the bulge), which keeps the working set of the
+// resident instances in L2.
+//
+// Every loop has an iteration cap; an instance that hits it gets status
+// STAB_ST_NOCONV and NaN for the missing values.
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
+#include "dw.cuh"
 #include "kernels.cuh"
 #include "hqr.cuh"
 
 namespace stab {
 
-#define HQ_T 128        // block of the batched (persistent) eigensolver
-#define HQ_WIDE 512     // block for a few large instances (latency)
-#define HQ_MAXW (HQ_WIDE / 32)
-// the device code runs with either block size
-#define NTH ((int)blockDim.x)
-#define NWA ((int)(blockDim.x >> 5))
-
-// multi-bulge sweeps: at most MS_MAXB bulges; the trailing MS_MAXB x
-// MS_MAXB block that supplies their shifts is kept packed in MS_SMALL entries
-#define MS_MAXB 6
-#define MS_SMALL 48
-
-struct Refl {
-  double tr, ti, ur, ui, beta, v1r, v1i;
-  int ident;
-};
-
-struct HqrSmem {
-  double red[2 * HQ_MAXW];
-  int flag;
-  int found;
-  int mp;
-  int kk;
-  double sc[8];   // broadcast scalars (Householder step, shift)
-  Refl refl[2];   // reflector of the next bulge step, double buffered
-  // multi-bulge sweeps: shifts, the trailing block they come from (packed),
-  // and one reflector per bulge
-  zc shifts[MS_MAXB];
-  zc small[MS_SMALL];
-  Refl mrefl[MS_MAXB];
-};
-
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// block sum of two doubles; result valid in all threads after return
-__device__ void block_sum2(HqrSmem& s, double& a, double& b) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  a = warp_sum(a);
-  b = warp_sum(b);
-  __syncthreads();
-  if (lane == 0) { s.red[warp] = a; s.red[HQ_MAXW + warp] = b; }
-  __syncthreads();
-  double ta = 0.0, tb = 0.0;
-  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { ta += s.red[q]; tb += s.red[HQ_MAXW + q]; }
-  a = ta;
-  b = tb;
-  __syncthreads();
-}
-
-// column-major storage in global memory
-struct GAcc {
-  zc* H;
-  int ld;
-  __device__ __forceinline__ zc& operator()(int r, int c) const { return H[(size_t)c * ld + r]; }
-};
-
-// packed Hessenberg-plus-one storage: column c keeps rows 0 .. min(c + 2,
-// mp - 1)
-__host__ __device__ __forceinline__ int64_t hess_coff(int c, int mp) {
-  return (int64_t)c * (c + 5) / 2 - ((c == mp - 1 && mp >= 2) ? 1 : 0);
-}
-__host__ __device__ __forceinline__ int64_t hess_packed_size(int mp) {
-  return mp <= 0 ? 0 : hess_coff(mp - 1, mp) + mp;
-}
-struct SAcc {
-  zc* S;
-  int mp;
-  __device__ __forceinline__ zc& operator()(int r, int c) const { return S[hess_coff(c, mp) + r]; }
-};
-struct SmallAcc {
-  zc* S;
-  int mp;
-  __device__ __forceinline__ zc& operator()(int r, int c) const { return S[hess_coff(c, mp) + r]; }
-};
-// windows at least this wide use multi-bulge sweeps
-#define MS_MIN_WINDOW 16
-
-// 2-element reflector (as ZLARFG): (v1, v2) -> (beta, 0).  It sits on the
-// serial path of every bulge step, where each FP64 instruction of a single
-// thread costs a full warp issue of the 1/64-rate FP64 pipe, so it uses one
-// reciprocal square root (|beta| and 1/beta from it) and one reciprocal.
-__device__ __forceinline__ Refl make_refl(zc v1, zc v2) {
-  Refl f;
-  f.v1r = v1.x;
-  f.v1i = v1.y;
-  const double n2 = v2.x * v2.x + v2.y * v2.y;
-  if (n2 == 0.0 && v1.y == 0.0) {
-    f.ident = 1;
-    f.tr = f.ti = f.ur = f.ui = 0.0;
-    f.beta = v1.x;
-    return f;
-  }
-  f.ident = 0;
-  const double S = fma(v1.x, v1.x, fma(v1.y, v1.y, n2));
-  const double r = rsqrt(S);
-  const double beta = -copysign(S * r, v1.x);
-  const double ib = -copysign(r, v1.x);                    // 1 / beta
-  f.beta = beta;
-  f.tr = (beta - v1.x) * ib;
-  f.ti = -v1.y * ib;
-  const double dr = v1.x - beta, di = v1.y;                // u2 = v2 / (v1 - beta)
-  const double idd = __drcp_rn(fma(dr, dr, di * di));
-  f.ur = fma(v2.x, dr, v2.y * di) * idd;
-  f.ui = fma(v2.y, dr, -v2.x * di) * idd;
-  return f;
-}
-
-// left: rows k, k+1 of column j;  right: columns k, k+1 of row j
-template <class Acc>
-__device__ __forceinline__ void apply_left(const Acc& H, int k, int j, zc tau, zc u2) {
-  zc a = H(k, j), b = H(k + 1, j);
-  zc sm = zmul(zconj(tau), zcfma(u2, b, a));
-  H(k, j) = zsub(a, sm);
-  H(k + 1, j) = zfnma(sm, u2, b);
-}
-template <class Acc>
-__device__ __forceinline__ void apply_right(const Acc& H, int k, int j, zc tau, zc u2) {
-  zc a = H(j, k), b = H(j, k + 1);
-  zc sm = zmul(tau, zfma(u2, b, a));
-  H(j, k) = zsub(a, sm);
-  H(j, k + 1) = zfnmac(sm, u2, b);
-}
-
-// Single-shift QR on the mp x mp upper Hessenberg matrix behind H; writes
-// the eigenvalues to ev[0..mp).  Returns 0 or STAB_ST_NOCONV.
-template <class Acc, bool MULTI>
-__device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& flops);
-
-// One sweep of nb bulges over the active window [l, i] (i - l + 1 >=
-// 3 nb + 2), with the shifts in s.shifts.  Bulge q enters at row l at step
-// 3q and sits at row k = l + step - 3q.  Rows of different bulges are three
-// apart, so within a step the left updates of all bulges (rows k, k+1) are
-// disjoint, and so are the right updates (columns k, k+1).  Left and right
-// updates commute, so a step runs all left updates, then all right updates,
-// then forms every bulge's next reflector on lanes of warp 0, with a barrier
-// between phases.  That puts the serial reflector work of nb bulges into
-// the same warp instructions.
-template <class Acc>
-__device__ void multi_bulge_sweep(const Acc& H, int l, int i, int nb, HqrSmem& s, double& flops) {
-  const int tid = threadIdx.x;
-  const int steps = (i - l) + 3 * (nb - 1);
-  // entering reflector of bulge 0
-  if (tid == 0) {
-    const zc h11s = zsub(H(l, l), s.shifts[0]);
-    const zc h21 = H(l + 1, l);
-    double sc = zabs1(h11s) + zabs1(h21);
-    if (sc == 0.0) sc = 1.0;
-    s.mrefl[0] = make_refl(zscale(h11s, 1.0 / sc), zscale(h21, 1.0 / sc));
-  }
-  __syncthreads();
-  for (int st = 0; st < steps; ++st) {
-    // active bulges: q with 0 <= st - 3q <= i - l - 1
-    const int qhi = min(nb - 1, st / 3);
-    const int qlo = max(0, (st - (i - l - 1) + 2) / 3);
-    // phase L: annihilation writes (column k-1) and left updates of columns k..i
-    int ltask = 0;
-    for (int q = qlo; q <= qhi; ++q) ltask += 1 + (i - (l + st - 3 * q) + 1);
-    if (tid == 0) flops += 24.0 * (double)ltask;
-    for (int t = tid; t < ltask; t += NTH) {
-      int q = qlo, rem = t;
-      for (;;) {
-        const int cnt = 1 + (i - (l + st - 3 * q) + 1);
-        if (rem < cnt) break;
-        rem -= cnt;
-        ++q;
-      }
-      const int k = l + st - 3 * q;
-      const Refl& f = s.mrefl[q];
-      if (rem == 0) {
-        if (k > l) {
-          H(k, k - 1) = zmk(f.ident ? f.v1r : f.beta, f.ident ? f.v1i : 0.0);
-          H(k + 1, k - 1) = zmk(0.0, 0.0);
-        }
-      } else if (!f.ident) {
-        apply_left(H, k, k + rem - 1, zmk(f.tr, f.ti), zmk(f.ur, f.ui));
-      }
-    }
-    __syncthreads();
-    // phase R: right updates of rows l..min(k+2, i)
-    int rtask = 0;
-    for (int q = qlo; q <= qhi; ++q) {
-      const int k = l + st - 3 * q;
-      rtask += min(k + 2, i) - l + 1;
-    }
-    if (tid == 0) flops += 24.0 * (double)rtask;
-    for (int t = tid; t < rtask; t += NTH) {
-      int q = qlo, rem = t;
-      for (;;) {
-        const int k = l + st - 3 * q;
-        const int cnt = min(k + 2, i) - l + 1;
-        if (rem < cnt) break;
-        rem -= cnt;
-        ++q;
-      }
-      const int k = l + st - 3 * q;
-      const Refl& f = s.mrefl[q];
-      if (!f.ident) apply_right(H, k, l + rem, zmk(f.tr, f.ti), zmk(f.ur, f.ui));
-    }
-    __syncthreads();
-    // phase C: next reflector of every bulge that moves on, and the
-    // entering reflector of the bulge that starts next step
-    if (tid < 32) {
-      const int q = tid;
-      if (q < nb) {
-        const int k = l + st - 3 * q;          // position this step
-        if (k >= l && k + 1 <= i - 1) {
-          s.mrefl[q] = make_refl(H(k + 1, k), H(k + 2, k));
-        } else if (k + 1 == l) {               // enters next step
-          const zc h11s = zsub(H(l, l), s.shifts[q]);
-          const zc h21 = H(l + 1, l);
-          double sc = zabs1(h11s) + zabs1(h21);
-          if (sc == 0.0) sc = 1.0;
-          s.mrefl[q] = make_refl(zscale(h11s, 1.0 / sc), zscale(h21, 1.0 / sc));
-        }
-      }
-    }
-    __syncthreads();
-  }
-}
-
-template <class Acc, bool MULTI>
-__device__ int qr_eigs(const Acc H, const int mp, zc* ev, HqrSmem& s, double& flops) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const double ulp = 2.220446049250313e-16;
-  const double safmin = 2.2250738585072014e-308;
-  const double smlnum = safmin * ((double)mp / ulp);
-  const int its_cap = 40 * (mp > 10 ? mp : 10);
-  int st = 0;
-  int total_its = 0;
-  int i = mp - 1;
-  while (i >= 0 && st == 0) {
-    int l = 0;
-    int kdefl = 0;
-    for (;;) {
-      // largest k in [l+1, i] with a negligible subdiagonal; l if none
-      if (tid == 0) s.kk = l;
-      __syncthreads();
-      for (int k = i - tid; k >= l + 1; k -= NTH) {
-        const zc h = H(k, k - 1);
-        bool ok = zabs1(h) <= smlnum;
-        if (!ok) {
-          double tst = zabs1(H(k - 1, k - 1)) + zabs1(H(k, k));
-          if (tst == 0.0) {
-            if (k - 2 >= 0) tst += zabs1(H(k - 1, k - 2));
-            if (k + 1 <= mp - 1) tst += zabs1(H(k + 1, k));
-          }
-          if (zabs1(h) <= ulp * tst) {
-            const double h1 = zabs1(h), h2 = zabs1(H(k - 1, k));
-            const double ab = fmax(h1, h2), ba = fmin(h1, h2);
-            const double d1 = zabs1(H(k, k)), d2 = zabs1(zsub(H(k - 1, k - 1), H(k, k)));
-            const double aa = fmax(d1, d2), bb = fmin(d1, d2);
-            const double sm = aa + ab;
-            ok = ba * (ab / sm) <= fmax(smlnum, ulp * (bb * (aa / sm)));
-          }
-        }
-        if (ok) { atomicMax(&s.kk, k); break; }   // this thread's larger k's were tested first
-      }
-      __syncthreads();
-      l = s.kk;
-      __syncthreads();
-      if (l > 0 && tid == 0) H(l, l - 1) = zmk(0.0, 0.0);
-      if (l >= i) break;
-      if (total_its >= its_cap) { st = STAB_ST_NOCONV; break; }
-      ++kdefl;
-      ++total_its;
-      if (MULTI && (i - l + 1) >= MS_MIN_WINDOW && kdefl % 10 != 0) {
-        // shifts: eigenvalues of the trailing nb x nb block (a small
-        // single-shift QR on a packed copy), then one sweep of nb bulges
-        const int nb = (i - l + 1) >= 3 * MS_MAXB + 2 + 24 ? MS_MAXB : 2;
-        const int o = i - nb + 1;
-        for (int c = tid; c < nb; c += NTH)
-          for (int r = 0; r <= min(c + 2, nb - 1); ++r) s.small[hess_coff(c, nb) + r] = (r <= c + 1) ? H(o + r, o + c) : zmk(0.0, 0.0);
-        __syncthreads();
-        double fl = 0.0;
-        const int sst = qr_eigs<SmallAcc, false>(SmallAcc{s.small, nb}, nb, s.shifts, s, fl);
-        flops += fl;
-        if (sst == 0) {
-          multi_bulge_sweep(H, l, i, nb, s, flops);
-          total_its += nb - 1;
-          continue;
-        }
-        // the small eigensolve did not converge: a single-shift iteration
-      }
-      // shift (one thread)
-      if (tid == 0) {
-        zc t;
-        if (kdefl % 20 == 0) {
-          t = zadd(zmk(0.75 * zabs(H(i, i - 1)), 0.0), H(i, i));
-        } else if (kdefl % 10 == 0) {
-          t = zadd(zmk(0.75 * zabs(H(l + 1, l)), 0.0), H(l, l));
-        } else {
-          t = H(i, i);
-          const zc u = zmul(zsqrt(H(i - 1, i)), zsqrt(H(i, i - 1)));
-          const double su = zabs1(u);
-          if (su != 0.0) {
-            const zc x = zscale(zsub(H(i - 1, i - 1), t), 0.5);
-            const double sx = zabs1(x);
-            const double sc = fmax(su, sx);
-            const zc xs = zscale(x, 1.0 / sc), us = zscale(u, 1.0 / sc);
-            zc y = zscale(zsqrt(zadd(zmul(xs, xs), zmul(us, us))), sc);
-            if (sx > 0.0) {
-              const zc xn = zscale(x, 1.0 / sx);
-              if (xn.x * y.x + xn.y * y.y < 0.0) y = zmk(-y.x, -y.y);
-            }
-            t = zsub(t, zmul(u, zdiv(u, zadd(x, y))));
-          }
-        }
-        s.sc[0] = t.x;
-        s.sc[1] = t.y;
-        s.kk = l;
-      }
-      __syncthreads();
-      const zc t = zmk(s.sc[0], s.sc[1]);
-      // start row: largest m in [l+1, i-1] where two consecutive small
-      // subdiagonals decouple the sweep; l otherwise
-      for (int mm = i - 1 - tid; mm >= l + 1; mm -= NTH) {
-        const zc h11 = H(mm, mm), h22 = H(mm + 1, mm + 1);
-        const zc h11s = zsub(h11, t);
-        const zc h21 = H(mm + 1, mm);
-        const double sc = zabs1(h11s) + zabs1(h21);
-        if (sc == 0.0) continue;
-        const double h10 = zabs1(H(mm, mm - 1));
-        // |h10| |h21/sc| <= ulp |h11s/sc| (|h11| + |h22|), multiplied through by sc
-        if (h10 * zabs1(h21) <= ulp * (zabs1(h11s) * (zabs1(h11) + zabs1(h22)))) {
-          atomicMax(&s.kk, mm);
-          break;
-        }
-      }
-      __syncthreads();
-      const int m0 = s.kk;
-      if (tid == 0) {
-        const zc h11s = zsub(H(m0, m0), t);
-        const zc h21 = H(m0 + 1, m0);
-        double sc = zabs1(h11s) + zabs1(h21);
-        if (sc == 0.0) sc = 1.0;
-        s.refl[m0 & 1] = make_refl(zscale(h11s, 1.0 / sc), zscale(h21, 1.0 / sc));
-      }
-      __syncthreads();
-      // bulge chase, one barrier per step.  The serial corner of a step is
-      // reflector k on columns k, k+1, then on rows k, k+1, then reflector
-      // k+1 formed from the new bulge.  It runs on lanes of warp 0 in three
-      // dependent stages of one update each.  Every other update of the step
-      // (columns k+2..i, rows l..k-1 and k+2) is independent of it and of the
-      // others and runs on all threads.
-      for (int k = m0; k < i; ++k) {
-        const Refl f = s.refl[k & 1];
-        const zc tau = zmk(f.tr, f.ti), u2 = zmk(f.ur, f.ui);
-        const int nleft = i - k - 1;        // columns k+2..i
-        const int nrows = k - l;            // rows l..k-1
-        const int ntask = 4 + nleft + nrows;
-        if (tid == 0) flops += 24.0 * (double)(i - l + 4);
-        for (int q = tid; q < ntask; q += NTH) {
-          if (q == 0) {
-            if (!f.ident) apply_left(H, k, k, tau, u2);
-          } else if (q == 1) {
-            if (!f.ident) apply_left(H, k, k + 1, tau, u2);
-          } else if (q == 2) {
-            if (!f.ident && k + 2 <= i) apply_right(H, k, k + 2, tau, u2);
-          } else if (q == 3) {
-            if (k > m0) {
-              H(k, k - 1) = zmk(f.ident ? f.v1r : f.beta, f.ident ? f.v1i : 0.0);
-              H(k + 1, k - 1) = zmk(0.0, 0.0);
-            }
-            // a sweep started below l still applies the first reflector to
-            // column m0-1: H(m0, m0-1) picks up (1 - conj(tau)); the fill-in
-            // at H(m0+1, m0-1) is what the start test bounds
-            if (!f.ident && k == m0 && m0 > l) H(m0, m0 - 1) = zmul(H(m0, m0 - 1), zsub(zmk(1.0, 0.0), zconj(tau)));
-          } else if (!f.ident) {
-            const int t = q - 4;
-            if (t < nleft) apply_left(H, k, k + 2 + t, tau, u2);
-            else apply_right(H, k, l + (t - nleft), tau, u2);
-          }
-        }
-        if (warp == 0) {
-          __syncwarp();
-          if (lane < 2 && !f.ident) apply_right(H, k, k + lane, tau, u2);   // rows k, k+1
-          __syncwarp();
-          if (lane == 0 && k + 1 < i) s.refl[(k + 1) & 1] = make_refl(H(k + 1, k), H(k + 2, k));
-        }
-        __syncthreads();
-      }
-    }
-    if (st) break;
-    if (tid == 0) ev[i] = H(i, i);
-    i = l - 1;
-    __syncthreads();
-  }
-  if (st)
-    for (int q = tid; q <= i; q += NTH) ev[q] = zmk(nan(""), nan(""));
-  __syncthreads();
-  return st;
-}
+#include "qr.cuh"
 
 // SM cycles spent per phase of k_eig_plain, summed over instances (thread 0
 // of each CTA adds clock64 differences): isolation, compaction, balancing,
@@ -439,13 +52,20 @@ __device__ unsigned long long g_eig_phase_cycles[6];
 
 // The eigensolver of one CTA over a persistent queue of instances; it runs
 // with either block size (HQ_T for the batch, HQ_WIDE for a few instances).
+// C is the working precision from the compaction on: complex128, or
+// double-word complex.  In double-word form the compacted matrix is scaled
+// by a power of two that brings its largest entry near 1 (the float exponent
+// range is narrow) and the QR eigenvalues are scaled back; the isolated
+// eigenvalues come straight from the FP64 input.
+template <class C>
 __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
                                                const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
                                                const int64_t* __restrict__ h_off, zc* __restrict__ eig,
                                                const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
                                                int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
-                                               double* __restrict__ flops_out, unsigned char* smraw, HqrSmem& s,
+                                               double* __restrict__ flops_out, unsigned char* smraw, HqrSmem<C>& s,
                                                int& s_inst) {
+  typedef typename ew<C>::real R;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (;;) {
     if (tid == 0) s_inst = atomicAdd(work_counter, 1);
@@ -455,18 +75,18 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
     const int inst = order ? order[slot] : slot;
     const int m = msz[inst];
     zc* M = A + a_off[inst];
-    zc* Hg = Hp + h_off[inst];
+    C* Hg = reinterpret_cast<C*>(Hp + h_off[inst]);
     zc* ev = eig + eig_off[inst];
     // shared scratch: active flags and act list (m ints each), then v, w, z
     int* active = reinterpret_cast<int*>(smraw);
     int* act = active + m;
-    zc* zs = reinterpret_cast<zc*>(smraw + ((2 * (size_t)m * sizeof(int) + 15) / 16) * 16);
-    zc* v = zs;
-    zc* w = v + m;
-    zc* z = w + m;
-    zc* vn = z + m;           // next step's reflector vector (Hessenberg reduction)
+    C* zs = reinterpret_cast<C*>(smraw + ((2 * (size_t)m * sizeof(int) + 15) / 16) * 16);
+    C* v = zs;
+    C* w = v + m;
+    C* z = w + m;
+    C* vn = z + m;            // next step's reflector vector (Hessenberg reduction)
     for (int i = tid; i < m; i += NTH) active[i] = 1;
-    if (tid == 0) s.mp = 0;
+    if (tid == 0) { s.mp = 0; s.emax = 0; }
     __syncthreads();
     long long t_ph = clock64();
     auto phase = [&](int q) {
@@ -525,51 +145,75 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
     __syncthreads();
     const int mp = s.mp;
     const int ld = mp;
-    for (int c = warp; c < mp; c += NWA) {
-      const int sc = act[c];
-      for (int r = lane; r < mp; r += 32) Hg[(size_t)c * ld + r] = M[(size_t)sc * m + act[r]];
+    double unscale = 1.0;
+    if constexpr (std::is_same<C, zc>::value) {
+      for (int c = warp; c < mp; c += NWA) {
+        const int sc = act[c];
+        for (int r = lane; r < mp; r += 32) Hg[(size_t)c * ld + r] = M[(size_t)sc * m + act[r]];
+      }
+    } else {
+      // largest binary exponent of the active entries (integer work), then
+      // the scaled copy in double-word form
+      int emax = 0;
+      for (int c = warp; c < mp; c += NWA) {
+        const int sc = act[c];
+        for (int r = lane; r < mp; r += 32) {
+          const zc a = M[(size_t)sc * m + act[r]];
+          emax = max(emax, max((__double2hiint(a.x) >> 20) & 0x7ff, (__double2hiint(a.y) >> 20) & 0x7ff));
+        }
+      }
+      atomicMax(&s.emax, emax);
+      __syncthreads();
+      // 2^-e with e the unbiased exponent (0 for an all-zero matrix)
+      const int e = (s.emax == 0 || s.emax == 0x7ff) ? 0 : s.emax - 1023;
+      const double scale = ldexp(1.0, -e);
+      unscale = ldexp(1.0, e);
+      for (int c = warp; c < mp; c += NWA) {
+        const int sc = act[c];
+        for (int r = lane; r < mp; r += 32) Hg[(size_t)c * ld + r] = ew<C>::from64(zscale(M[(size_t)sc * m + act[r]], scale));
+      }
     }
     __syncthreads();
     phase(1);
     // ---- 3. balancing -------------------------------------------------------
+    // (powers of two only, so the norms need little precision: in the
+    // double-word form they are taken from the high words in FP32)
     for (int sweep = 0; sweep < 64; ++sweep) {
       if (tid == 0) s.flag = 0;
       __syncthreads();
       for (int i = 0; i < mp; ++i) {
-        double cs = 0.0, rs = 0.0;
+        R cs = 0, rs = 0;
         for (int r = tid; r < mp; r += NTH) {
           if (r == i) continue;
-          const zc a = Hg[(size_t)i * ld + r];
-          cs += a.x * a.x + a.y * a.y;
-          const zc b = Hg[(size_t)r * ld + i];
-          rs += b.x * b.x + b.y * b.y;
+          cs += ew<C>::mag2(Hg[(size_t)i * ld + r]);
+          rs += ew<C>::mag2(Hg[(size_t)r * ld + i]);
         }
         block_sum2(s, cs, rs);
         if (tid == 0) {
-          double c = sqrt(cs), r = sqrt(rs), f = 1.0;
-          if (c != 0.0 && r != 0.0) {
-            double g = r / 2.0;
-            const double sum = c + r;
+          R c = sqrt(cs), r = sqrt(rs), f = 1;
+          if (c != (R)0 && r != (R)0) {
+            R g = r / (R)2;
+            const R sum = c + r;
             int guard = 0;
-            while (c < g && guard++ < 2000) { f *= 2.0; c *= 2.0; r /= 2.0; g /= 2.0; }
-            g = c / 2.0;
-            while (g >= r && guard++ < 4000) { f /= 2.0; c /= 2.0; g /= 2.0; r *= 2.0; }
-            if (c + r >= 0.95 * sum) f = 1.0;
+            while (c < g && guard++ < 2000) { f *= (R)2; c *= (R)2; r /= (R)2; g /= (R)2; }
+            g = c / (R)2;
+            while (g >= r && guard++ < 4000) { f /= (R)2; c /= (R)2; g /= (R)2; r *= (R)2; }
+            if (c + r >= (R)0.95 * sum) f = 1;
           }
-          s.sc[0] = f;
-          if (f != 1.0) s.flag = 1;
+          s.sc[0] = (double)f;
+          if (f != (R)1) s.flag = 1;
         }
         __syncthreads();
-        const double f = s.sc[0];
-        if (f != 1.0) {
-          const double gi = 1.0 / f;
+        const R f = (R)s.sc[0];
+        if (f != (R)1) {
+          const R gi = (R)1 / f;
           for (int q = tid; q < mp; q += NTH) {
-            zc* a = &Hg[(size_t)q * ld + i];    // row i
+            C* a = &Hg[(size_t)q * ld + i];    // row i
             *a = zscale(*a, gi);
           }
           __syncthreads();
           for (int q = tid; q < mp; q += NTH) {
-            zc* a = &Hg[(size_t)i * ld + q];    // column i
+            C* a = &Hg[(size_t)i * ld + q];    // column i
             *a = zscale(*a, f);
           }
         }
@@ -584,87 +228,84 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
     // updates it also copies it into the next step's reflector vector and
     // sums its squared tail: step k+1 starts without a pass or a block
     // reduction of its own.
-    double flops = 0.0;   // FP64 work of the reduction and the sweeps (thread 0)
+    double flops = 0.0;   // counted work of the reduction and the sweeps (thread 0)
     bool have_next = false;
     for (int k = 0; k + 2 < mp; ++k) {
       const int L = mp - k - 1;
       if (tid == 0) flops += 16.0 * (double)mp * L + 16.0 * (double)L * L;
-      double ss = 0.0, dummy = 0.0;
+      double ss = 0.0;
       if (have_next) {
-        zc* t = v;                       // the vector gathered by the last step
+        C* t = v;                        // the vector gathered by the last step
         v = vn;
         vn = t;
         ss = s.sc[5];
       } else {
+        typename ew<C>::sq acc = ew<C>::sq_zero();
         for (int r = tid; r < L; r += NTH) {
-          const zc x = Hg[(size_t)k * ld + k + 1 + r];
+          const C x = Hg[(size_t)k * ld + k + 1 + r];
           v[r] = x;
-          if (r >= 1) ss += x.x * x.x + x.y * x.y;
+          if (r >= 1) ew<C>::sq_add(acc, x);
         }
-        block_sum2(s, ss, dummy);
+        ss = block_sum_sq<C>(s, acc);
       }
       have_next = false;
       if (tid == 0) {
-        const zc alpha = v[0];
+        const zc alpha = ew<C>::to64(v[0]);
         if (ss == 0.0 && alpha.y == 0.0) {
           s.flag = 0;                                      // H(k) = I
         } else {
           s.flag = 1;
           const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + ss), alpha.x);
           const zc scal = zdiv(zmk(1.0, 0.0), zmk(alpha.x - beta, alpha.y));
-          s.sc[0] = (beta - alpha.x) / beta;   // tau
-          s.sc[1] = -alpha.y / beta;
-          s.sc[2] = scal.x;
-          s.sc[3] = scal.y;
-          s.sc[4] = beta;
+          s.hc[0] = ew<C>::from64(zmk((beta - alpha.x) / beta, -alpha.y / beta));   // tau
+          s.hc[1] = ew<C>::from64(scal);
+          s.hc[2] = ew<C>::from64(zmk(beta, 0.0));
         }
       }
       __syncthreads();
       if (!s.flag) continue;
-      const zc tau = zmk(s.sc[0], s.sc[1]);
-      const zc scal = zmk(s.sc[2], s.sc[3]);
-      const double beta = s.sc[4];
-      for (int r = tid; r < L; r += NTH) v[r] = (r == 0) ? zmk(1.0, 0.0) : zmul(v[r], scal);
-      if (tid == 0) Hg[(size_t)k * ld + k + 1] = zmk(beta, 0.0);
-      for (int r = 2 + tid; r <= L; r += NTH) Hg[(size_t)k * ld + k + r] = zmk(0.0, 0.0);
+      const C tau = s.hc[0];
+      const C scal = s.hc[1];
+      for (int r = tid; r < L; r += NTH) v[r] = (r == 0) ? ew<C>::one() : zmul(v[r], scal);
+      if (tid == 0) Hg[(size_t)k * ld + k + 1] = s.hc[2];
+      for (int r = 2 + tid; r <= L; r += NTH) Hg[(size_t)k * ld + k + r] = ew<C>::zero();
       __syncthreads();
       // right: w = tau H(:, k+1:) v
       for (int r = tid; r < mp; r += NTH) {
-        zc acc = zmk(0.0, 0.0);
+        C acc = ew<C>::zero();
         for (int c = 0; c < L; ++c) acc = zfma(Hg[(size_t)(k + 1 + c) * ld + r], v[c], acc);
         w[r] = zmul(tau, acc);
       }
       __syncthreads();
       // right update fused with the left product z = conj(tau) v^H H(k+1:, k+1:), warp per column
       for (int c = warp; c < L; c += NWA) {
-        const zc vc = zconj(v[c]);
-        zc* col = Hg + (size_t)(k + 1 + c) * ld;
-        zc acc = zmk(0.0, 0.0);
+        const C vc = zconj(v[c]);
+        C* col = Hg + (size_t)(k + 1 + c) * ld;
+        C acc = ew<C>::zero();
         for (int r = lane; r < mp; r += 32) {
-          const zc h = zfnma(w[r], vc, col[r]);
+          const C h = zfnma(w[r], vc, col[r]);
           col[r] = h;
           if (r >= k + 1) acc = zcfma(v[r - k - 1], h, acc);
         }
-        acc.x = warp_sum(acc.x);
-        acc.y = warp_sum(acc.y);
+        acc = ew<C>::warp_sum_c(acc);
         if (lane == 0) z[c] = zmul(zconj(tau), acc);
       }
       __syncthreads();
       // left update: H(k+1:, k+1:) -= v z; column k+1 (c = 0, warp 0) also
       // feeds the next step: vn = H(k+2:, k+1), s.sc[5] = sum |vn[1:]|^2
       for (int c = warp; c < L; c += NWA) {
-        const zc zc_ = z[c];
-        zc* col = Hg + (size_t)(k + 1 + c) * ld + k + 1;
+        const C zc_ = z[c];
+        C* col = Hg + (size_t)(k + 1 + c) * ld + k + 1;
         if (c == 0) {
-          double sn = 0.0;
+          typename ew<C>::sq sn = ew<C>::sq_zero();
           for (int r = lane; r < L; r += 32) {
-            const zc h = zfnma(v[r], zc_, col[r]);
+            const C h = zfnma(v[r], zc_, col[r]);
             col[r] = h;
             if (r >= 1) vn[r - 1] = h;
-            if (r >= 2) sn = fma(h.x, h.x, fma(h.y, h.y, sn));
+            if (r >= 2) ew<C>::sq_add(sn, h);
           }
           sn = warp_sum(sn);
-          if (lane == 0) s.sc[5] = sn;
+          if (lane == 0) s.sc[5] = ew<C>::sq_64(sn);
         } else {
           for (int r = lane; r < L; r += 32) col[r] = zfnma(v[r], zc_, col[r]);
         }
@@ -679,14 +320,18 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
     // increasing order through shared memory is safe
     for (int c = 0; c < mp; ++c) {
       const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
-      for (int r = tid; r <= rmax; r += NTH) v[r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : zmk(0.0, 0.0);
+      for (int r = tid; r <= rmax; r += NTH) v[r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : ew<C>::zero();
       __syncthreads();
       const int64_t o = hess_coff(c, mp);
       for (int r = tid; r <= rmax; r += NTH) Hg[o + r] = v[r];
       __syncthreads();
     }
     phase(4);
-    int st = qr_eigs<SAcc, true>(SAcc{Hg, mp}, mp, ev, s, flops);
+    long long upd = 0;   // 2-element reflector applications (24 flops each), thread 0
+    int st = qr_eigs<C, true>(SAcc<C>{Hg, mp}, mp, ev, s, s.refl, upd);
+    flops += 24.0 * (double)upd;
+    if (unscale != 1.0)
+      for (int q = tid; q < mp; q += NTH) ev[q] = zscale(ev[q], unscale);
     phase(5);
     if (tid == 0) {
       status[inst] = st;
@@ -696,32 +341,28 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
   }
 }
 
-__global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
-                                                   const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
-                                                   const int64_t* __restrict__ h_off, zc* __restrict__ eig,
-                                                   const int64_t* __restrict__ eig_off, int32_t* __restrict__ status,
-                                                   int32_t* __restrict__ work_counter, const int32_t* __restrict__ order,
-                                                   double* __restrict__ flops_out) {
+#define EIG_PLAIN_ARGS                                                                                       \
+  int count, const int32_t *__restrict__ msz, zc *__restrict__ A, const int64_t *__restrict__ a_off,         \
+      zc *__restrict__ Hp, const int64_t *__restrict__ h_off, zc *__restrict__ eig,                          \
+      const int64_t *__restrict__ eig_off, int32_t *__restrict__ status, int32_t *__restrict__ work_counter, \
+      const int32_t *__restrict__ order, double *__restrict__ flops_out
+
+template <class C>
+__global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(EIG_PLAIN_ARGS) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ HqrSmem s;
+  __shared__ HqrSmem<C> s;
   __shared__ int s_inst;
-  eig_plain_body(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
-                 s_inst);
+  eig_plain_body<C>(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
+                    s_inst);
 }
 
-__global__ void __launch_bounds__(HQ_WIDE, 1) k_eig_plain_wide(int count, const int32_t* __restrict__ msz,
-                                                           zc* __restrict__ A, const int64_t* __restrict__ a_off,
-                                                           zc* __restrict__ Hp, const int64_t* __restrict__ h_off,
-                                                           zc* __restrict__ eig, const int64_t* __restrict__ eig_off,
-                                                           int32_t* __restrict__ status,
-                                                           int32_t* __restrict__ work_counter,
-                                                           const int32_t* __restrict__ order,
-                                                           double* __restrict__ flops_out) {
+template <class C>
+__global__ void __launch_bounds__(HQ_WIDE, 1) k_eig_plain_wide(EIG_PLAIN_ARGS) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ HqrSmem s;
+  __shared__ HqrSmem<C> s;
   __shared__ int s_inst;
-  eig_plain_body(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
-                 s_inst);
+  eig_plain_body<C>(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
+                    s_inst);
 }
 
 
@@ -737,13 +378,13 @@ size_t eig_plain_smem(int mmax) {
   return head + 4 * (size_t)mmax * sizeof(zc);
 }
 
-cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
-                             const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
-                             int32_t* work_counter, const int32_t* order, double* flops, int grid,
-                             cudaStream_t s) {
-  if (count <= 0) return cudaSuccess;
+template <class C>
+static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
+                                const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
+                                int32_t* work_counter, const int32_t* order, double* flops, int grid,
+                                cudaStream_t s) {
   size_t sm = eig_plain_smem(mmax);
-  cudaError_t e = cudaFuncSetAttribute(k_eig_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e = cudaFuncSetAttribute(k_eig_plain<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(work_counter, 0, sizeof(int32_t), s);
   if (e != cudaSuccess) return e;
@@ -752,21 +393,32 @@ cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, con
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (count * 2 <= sms) {
     // a few instances: one wide CTA each, so every phase spreads over 16 warps
-    e = cudaFuncSetAttribute(k_eig_plain_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    e = cudaFuncSetAttribute(k_eig_plain_wide<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_eig_plain_wide<<<count, HQ_WIDE, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
-                                                order, flops);
+    k_eig_plain_wide<C><<<count, HQ_WIDE, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status,
+                                                   work_counter, order, flops);
     return cudaGetLastError();
   }
   // persistent grid: as many CTAs as can be resident at once
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eig_plain, HQ_T, sm) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eig_plain<C>, HQ_T, sm) != cudaSuccess || per_sm < 1)
     per_sm = 1;
   const int resident = sms * per_sm;
   if (grid <= 0 || grid > resident) grid = resident;
   if (grid > count) grid = count;
-  k_eig_plain<<<grid, HQ_T, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter, order,
-                                     flops);
+  k_eig_plain<C><<<grid, HQ_T, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter, order,
+                                        flops);
   return cudaGetLastError();
+}
+
+cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
+                             const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
+                             int32_t* work_counter, const int32_t* order, double* flops, int grid,
+                             cudaStream_t s, bool double_word) {
+  if (count <= 0) return cudaSuccess;
+  return double_word ? launch_eig_t<dz>(count, mmax, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
+                                        order, flops, grid, s)
+                     : launch_eig_t<zc>(count, mmax, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
+                                        order, flops, grid, s);
 }
 
 }  // namespace stab
@@ -842,9 +494,9 @@ extern "C" int stab_eigvals_noalloc(const double* a_dev, int32_t m, double* eig_
   k_noalloc_header<<<1, 1, 0, s>>>(hdr, m);   // resets the work counter left by the previous call
   if (cudaGetLastError() != cudaSuccess) return STAB_ERR_CUDA;
   const size_t sm = eig_plain_smem(m);
-  if (cudaFuncSetAttribute(k_eig_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_eig_plain<zc>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
     return STAB_ERR_CUDA;
-  k_eig_plain<<<1, HQ_T, sm, s>>>(1, &hdr->m, const_cast<zc*>(reinterpret_cast<const zc*>(a_dev)), &hdr->a_off, H,
+  k_eig_plain<zc><<<1, HQ_T, sm, s>>>(1, &hdr->m, const_cast<zc*>(reinterpret_cast<const zc*>(a_dev)), &hdr->a_off, H,
                                   &hdr->h_off, reinterpret_cast<zc*>(eig_dev), &hdr->eig_off, status_dev,
                                   &hdr->counter, nullptr, nullptr);
   return cudaGetLastError() == cudaSuccess ? STAB_OK : STAB_ERR_CUDA;

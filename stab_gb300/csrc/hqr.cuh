@@ -9,11 +9,13 @@ size_t eig_plain_smem(int mmax);
 // size; eig receives m eigenvalues per instance (QR eigenvalues first, then
 // the isolated ones); status[k] = 0 or STAB_ST_NOCONV.  `order` (may be null)
 // is the processing order (largest first balances the persistent grid).
-// flops (may be null) receives the FP64 flops each instance executed in the
-// Hessenberg reduction and the QR sweeps.
+// flops (may be null) receives the flops each instance executed in the
+// Hessenberg reduction and the QR sweeps.  double_word runs the reduction
+// and the QR iteration in double-word (float-float) arithmetic, for spectra
+// that seed a polish.
 cudaError_t eig_phase_cycles(unsigned long long* out, bool reset);
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
                              const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
                              int32_t* work_counter, const int32_t* order, double* flops, int grid,
-                             cudaStream_t s);
+                             cudaStream_t s, bool double_word = false);
 }  // namespace stab

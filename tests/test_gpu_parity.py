@@ -235,3 +235,31 @@ def test_batch_spectra_equal_single_instance_spectra(ctx):
         eig, _, _, _ = ctx.full_spectrum(H.stab_params(d), prof, want_vector=False)
         assert np.array_equal(s, eig)
     b.close()
+
+
+def test_double_word_spectra_match_fp64(ctx):
+    """Full spectra at the seed size (N = 32) in double-word arithmetic against
+    FP64.  Tolerances: selected least-stable eigenvalue within 1e-9 relative
+    (the seeds need that); each of the 8 least-stable eigenvalues within 1e-10
+    relative of the nearest double-word one."""
+    rng = np.random.Generator(np.random.PCG64(21))
+    cases = [H.synth_case(1, 32, float(rng.uniform(0.05, 2.0)), float(10 ** rng.uniform(2.5, 3.5)),
+                          a=float(rng.uniform(0.05, 0.4)), b=float(rng.uniform(0, 0.3))) for _ in range(16)]
+    out = {}
+    try:
+        for prec in (sg.EIG_FP64, sg.EIG_DOUBLE_WORD):
+            ctx.set_eig_precision(seed=sg.EIG_DOUBLE_WORD, plain=prec)
+            b = ctx.batch([H.stab_params(d) for d, _ in cases], [p for _, p in cases])
+            b.run(sg.MODE_PLAIN)
+            eig, _, _, status, _ = b.results()
+            out[prec] = (eig, status, b.spectra())
+            b.close()
+    finally:
+        ctx.set_eig_precision()
+    e64, s64, sp64 = out[sg.EIG_FP64]
+    edw, sdw, spdw = out[sg.EIG_DOUBLE_WORD]
+    assert np.all(s64 == sg.ST_OK) and np.all(sdw == sg.ST_OK)
+    assert np.max(np.abs(edw - e64) / np.abs(e64)) < 1e-9
+    for a, d in zip(sp64, spdw):
+        for r in a[np.argsort(-a.imag)[:8]]:
+            assert np.min(np.abs(d - r)) / abs(r) < 1e-10

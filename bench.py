@@ -46,10 +46,12 @@ COARSE_TRAFFIC_PER_INSTANCE = (22.22e9 + 20.61e9) / 512
 # kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
 KERNEL_WORK = {
     "k_eig_plain": ("eig_fp64", "fp64", "FP64 flops counted by the kernel (Householder reduction + QR sweeps)"),
-    "k_eig_plain_coarse": ("eig_fp64_coarse", "fp64", "FP64 flops counted by the kernel on the N=32 seed batch"),
+    "k_eig_plain_coarse": ("eig_fp64_coarse", "dw", "flops counted by the kernel on the N=32 seed batch, run in "
+                           "double-word arithmetic"),
     "k_eig_plain_fallback": ("eig_fp64", "fp64", "FP64 flops counted by the kernel on the fallback instances"),
     "k_lu_c": ("lu_c64", "fp32", "8/3 n^3 real flops per complex64 LU, per factorisation run"),
     "k_lu_z": ("lu_c128", "fp64", "8/3 n^3 real flops per complex128 LU, per factorisation run"),
+    "k_lu_dz": ("lu_c128", "dw", "8/3 n^3 real flops per double-word complex LU, per factorisation run"),
 }
 
 
@@ -487,7 +489,9 @@ def main():
         if kname not in KERNEL_WORK or kms <= 0:
             continue
         wkey, bound, note = KERNEL_WORK[kname]
-        peak = FP64_PEAK_TFLOPS if bound == "fp64" else FP32_PEAK_TFLOPS
+        # double-word kernels: a double-word multiply-add (2 flops) is 15 FP32
+        # instructions, so their flop peak is the FP32 instruction rate * 2 / 15
+        peak = {"fp64": FP64_PEAK_TFLOPS, "fp32": FP32_PEAK_TFLOPS, "dw": FP32_PEAK_TFLOPS / 15.0}[bound]
         ach = work[wkey] / (kms / 1000.0) / 1e12    # flops and time of the same launches
         rooflines[kname] = {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                             "frac": ach / peak, "traffic": None, "kernel": kname, "launches": kl,

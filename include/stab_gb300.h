@@ -102,16 +102,25 @@ int stab_sync(stab_ctx* ctx);
 int stab_set_profiling(stab_ctx* ctx, int on);
 int stab_kernel_stats(stab_ctx* ctx, int32_t k, const char** name, int64_t* launches, double* total_ms, int32_t* count);
 int stab_reset_kernel_stats(stab_ctx* ctx);
-/* Arithmetic of the Hessenberg reduction and QR iteration of the
- * full-spectrum eigensolve: STAB_EIG_FP64 (as ZGEEV, temporal.f90:803) or
- * STAB_EIG_DOUBLE_WORD (float-float pairs, about 48 significant bits, run on
- * the FP32 pipe).  `seed` applies to the spectra that only seed the polish
- * (STAB_MODE_COARSE / STAB_MODE_SURROGATE and their N = 48 level), `plain` to
- * STAB_MODE_PLAIN, stab_full_spectrum and the FP64 fallback.  Defaults: seed
- * STAB_EIG_DOUBLE_WORD, plain STAB_EIG_FP64.  No reference counterpart. */
-#define STAB_EIG_FP64 0
-#define STAB_EIG_DOUBLE_WORD 1
-int stab_set_eig_precision(stab_ctx* ctx, int32_t seed, int32_t plain);
+/* Arithmetic of three stages (no reference counterpart):
+ *   STAB_STAGE_SEED_EIG   Hessenberg reduction and QR of the spectra that
+ *                         only seed the polish (STAB_MODE_COARSE /
+ *                         STAB_MODE_SURROGATE and their N = 48 level);
+ *                         default STAB_ARITH_DOUBLE_WORD;
+ *   STAB_STAGE_PLAIN_EIG  the same for STAB_MODE_PLAIN, stab_full_spectrum
+ *                         and the FP64 fallback (ZGEEV, temporal.f90:803);
+ *                         default STAB_ARITH_FP64;
+ *   STAB_STAGE_RETRY_LU   LU and solves of the complex128 inverse-iteration
+ *                         retry of the polish (residuals and eigenvalue
+ *                         updates stay FP64); default STAB_ARITH_DOUBLE_WORD.
+ * STAB_ARITH_DOUBLE_WORD is float-float pairs (about 48 significant bits)
+ * run on the FP32 pipe. */
+#define STAB_STAGE_SEED_EIG 0
+#define STAB_STAGE_PLAIN_EIG 1
+#define STAB_STAGE_RETRY_LU 2
+#define STAB_ARITH_FP64 0
+#define STAB_ARITH_DOUBLE_WORD 1
+int stab_set_arithmetic(stab_ctx* ctx, int32_t stage, int32_t arithmetic);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,
  * [1] compaction, [2] balancing, [3] Hessenberg reduction, [4] repacking,

@@ -27,8 +27,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libstab_gb300.so")
 
 MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE, MODE_TRACK = 0, 1, 2, 3, 4
-# arithmetic of the full-spectrum eigensolve (stab_set_eig_precision)
-EIG_FP64, EIG_DOUBLE_WORD = 0, 1
+# arithmetic per stage (stab_set_arithmetic)
+STAGE_SEED_EIG, STAGE_PLAIN_EIG, STAGE_RETRY_LU = 0, 1, 2
+ARITH_FP64, ARITH_DOUBLE_WORD = 0, 1
 ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE = 0, 1, 2, 3, 4, 5
 
 EXPORTED = (
@@ -40,7 +41,7 @@ EXPORTED = (
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
-    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_set_eig_precision",
+    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_set_arithmetic",
 )
 
 
@@ -153,7 +154,7 @@ def load(path: str = LIB_PATH):
     lib.stab_batch_spectra.argtypes = [vp, P(P(dbl))]
     lib.stab_autotune.argtypes = [vp, P(i32), i32, P(i32), P(ctypes.c_float)]
     lib.stab_eig_phases.argtypes = [vp, P(ctypes.c_uint64), i32]
-    lib.stab_set_eig_precision.argtypes = [vp, i32, i32]
+    lib.stab_set_arithmetic.argtypes = [vp, i32, i32]
     lib.stab_lu_cluster_check.argtypes = [vp, i32, i32, i32, P(dbl), P(i32)]
     _lib = lib
     return lib
@@ -396,10 +397,17 @@ class Context:
                                                    ctypes.byref(pd)))
         return md.value, pd.value
 
-    def set_eig_precision(self, seed: int = EIG_DOUBLE_WORD, plain: int = EIG_FP64) -> None:
-        """Arithmetic of the eigensolve for seed spectra and for plain spectra
-        (stab_set_eig_precision): EIG_FP64 or EIG_DOUBLE_WORD."""
-        self._check(self.lib.stab_set_eig_precision(self.h, int(seed), int(plain)))
+    DEFAULT_ARITHMETIC = {STAGE_SEED_EIG: ARITH_DOUBLE_WORD, STAGE_PLAIN_EIG: ARITH_FP64,
+                          STAGE_RETRY_LU: ARITH_DOUBLE_WORD}
+
+    def set_arithmetic(self, stage: int, arithmetic: int) -> None:
+        """Arithmetic of one stage (stab_set_arithmetic): STAGE_SEED_EIG,
+        STAGE_PLAIN_EIG or STAGE_RETRY_LU; ARITH_FP64 or ARITH_DOUBLE_WORD."""
+        self._check(self.lib.stab_set_arithmetic(self.h, int(stage), int(arithmetic)))
+
+    def reset_arithmetic(self) -> None:
+        for st, ar in self.DEFAULT_ARITHMETIC.items():
+            self.set_arithmetic(st, ar)
 
     def eig_phases(self, reset: bool = True) -> dict:
         """SM cycles per phase of the eigensolver (stab_eig_phases)."""

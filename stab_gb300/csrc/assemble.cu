@@ -8,6 +8,7 @@
 // column-major matrix in complex128 or complex64, and k_opmv applies the
 // operator in O(N^2) without forming it (used for the FP64 residuals).
 #include "common.cuh"
+#include "dw.cuh"
 #include "kernels.cuh"
 
 namespace stab {
@@ -71,6 +72,7 @@ __global__ void k_node_ops(int count, const InstDesc* __restrict__ desc, const z
 template <typename T> __device__ __forceinline__ T store_cast(zc v);
 template <> __device__ __forceinline__ zc store_cast<zc>(zc v) { return v; }
 template <> __device__ __forceinline__ cc store_cast<cc>(zc v) { return cmk((float)v.x, (float)v.y); }
+template <> __device__ __forceinline__ dz store_cast<dz>(zc v) { return dz_from64(v); }
 
 // Dense column-major n x n.  Grid (ceil(n / 8), count); 256 threads walk the
 // rows of 8 consecutive columns, so each warp writes contiguous addresses.
@@ -117,6 +119,8 @@ cudaError_t launch_dense(int count, int nmax, const InstDesc* desc, const double
 template cudaError_t launch_dense<zc>(int, int, const InstDesc*, const double* const*, const zc*, zc*,
                                       const int64_t*, int, double, cudaStream_t, const int32_t*);
 template cudaError_t launch_dense<cc>(int, int, const InstDesc*, const double* const*, const zc*, cc*,
+                                      const int64_t*, int, double, cudaStream_t, const int32_t*);
+template cudaError_t launch_dense<dz>(int, int, const InstDesc*, const double* const*, const zc*, dz*,
                                       const int64_t*, int, double, cudaStream_t, const int32_t*);
 
 // Structured product y = M x (FP64).  One CTA per instance: x staged in

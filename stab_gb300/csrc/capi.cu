@@ -16,6 +16,7 @@
 
 #include "../../include/stab_gb300.h"
 #include "common.cuh"
+#include "dw.cuh"
 #include "hqr.cuh"
 #include "kernels.cuh"
 #include "lu.cuh"
@@ -61,8 +62,8 @@ struct stab_ctx {
   std::vector<stab_batch*> live;   // caller-visible batches, released by stab_destroy
   std::vector<stab_mlp*> nets;     // networks, released by stab_destroy
   std::map<std::pair<int, int>, int> lu_nb;   // (complex128?, size class) -> tuned LU panel width
-  int seed_eig = STAB_EIG_DOUBLE_WORD;   // arithmetic of the seed spectra
-  int plain_eig = STAB_EIG_FP64;         // arithmetic of the plain spectra (the answer)
+  // arithmetic per stage (STAB_STAGE_*)
+  int arith[3] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD};
 };
 
 // size class of an LU order for the tuned panel-width table
@@ -618,7 +619,7 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
                             b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
                             b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
                             b->flops.as<double>(), grid, s,
-                            (seed ? c->seed_eig : c->plain_eig) == STAB_EIG_DOUBLE_WORD);
+                            c->arith[seed ? STAB_STAGE_SEED_EIG : STAB_STAGE_PLAIN_EIG] == STAB_ARITH_DOUBLE_WORD);
   }));
   CK(c, timed(c, "k_post_spectrum", [&] {
     size_t sm = sizeof(zc) * b->mmax;
@@ -773,15 +774,28 @@ static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
   }));
   int rc = node_ops(b, all, OP_T_Q, OP_S_Q, b->sigma.as<zc>(), skip);
   if (rc) return rc;
-  rc = dense<zc>(b, all, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z", skip);
-  if (rc) return rc;
-  CK(c, timed(c, "k_lu_z", [&] {
-    // the retried instances are few and their FP64 factorisations long:
-    // a cluster of four SMs shares each one
-    return launch_lu<zc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
-                         b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
-                         tuned_nb(c, true, b->nmax), b->order.as<int32_t>(), b->nmax >= 240 ? 4 : 1);
-  }));
+  // the factorisation in double-word form (same bytes per entry) or FP64;
+  // the retried instances are few and their factorisations long: a cluster
+  // of four SMs shares each large one
+  const bool dwlu = c->arith[STAB_STAGE_RETRY_LU] == STAB_ARITH_DOUBLE_WORD;
+  const int lu_cluster = b->nmax >= 240 ? 4 : 1;
+  if (dwlu) {
+    rc = dense<dz>(b, all, b->Z64.as<dz>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_dz", skip);
+    if (rc) return rc;
+    CK(c, timed(c, "k_lu_dz", [&] {
+      return launch_lu<dz>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<dz>(), b->off_n2.as<int64_t>(),
+                           b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
+                           tuned_nb(c, true, b->nmax), b->order.as<int32_t>(), lu_cluster);
+    }));
+  } else {
+    rc = dense<zc>(b, all, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z", skip);
+    if (rc) return rc;
+    CK(c, timed(c, "k_lu_z", [&] {
+      return launch_lu<zc>(b->count, D, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
+                           b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
+                           tuned_nb(c, true, b->nmax), b->order.as<int32_t>(), lu_cluster);
+    }));
+  }
   CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
   CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, b->pcol.as<int32_t>(), skip, s); }));
   CK(c, timed(c, "k_reset_polish", [&] {
@@ -792,10 +806,13 @@ static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
       return launch_qmv(b->count, b->nmax, D, b->dtab.as<const double*>(), b->blk.as<zc>(), b->sigma.as<zc>(), 1, V,
                         0, 1, done, s);
     }));
-    CK(c, timed(c, "k_getrs_z", [&] {
-      return launch_getrs<zc>(b->count, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(), b->off_n2.as<int64_t>(),
-                              b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V, b->xoff[1].as<int64_t>(), 1, 0, 1,
-                              done, s);
+    CK(c, timed(c, dwlu ? "k_getrs_dz" : "k_getrs_z", [&] {
+      return dwlu ? launch_getrs<dz>(b->count, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<dz>(),
+                                     b->off_n2.as<int64_t>(), b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V,
+                                     b->xoff[1].as<int64_t>(), 1, 0, 1, done, s)
+                  : launch_getrs<zc>(b->count, b->nsz.as<int32_t>(), b->nmax, b->Z64.as<zc>(),
+                                     b->off_n2.as<int64_t>(), b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), V,
+                                     b->xoff[1].as<int64_t>(), 1, 0, 1, done, s);
     }));
     CK(c, timed(c, "k_ii_update", [&] {
       return launch_ii_update(b->count, D, V, 0, 1, b->pcol.as<int32_t>(), b->sigma.as<zc>(), b->theta.as<zc>(), done,
@@ -1511,12 +1528,13 @@ int stab_autotune(stab_ctx* c, const int32_t* orders, int32_t norders, int32_t* 
   return STAB_OK;
 }
 
-int stab_set_eig_precision(stab_ctx* c, int32_t seed, int32_t plain) {
+int stab_set_arithmetic(stab_ctx* c, int32_t stage, int32_t arithmetic) {
   if (!c) return STAB_ERR_ARG;
-  auto ok = [](int32_t v) { return v == STAB_EIG_FP64 || v == STAB_EIG_DOUBLE_WORD; };
-  if (!ok(seed) || !ok(plain)) return set_err(c, STAB_ERR_ARG, "eigensolve arithmetic must be STAB_EIG_FP64 or STAB_EIG_DOUBLE_WORD");
-  c->seed_eig = seed;
-  c->plain_eig = plain;
+  if (stage < STAB_STAGE_SEED_EIG || stage > STAB_STAGE_RETRY_LU)
+    return set_err(c, STAB_ERR_ARG, "stage must be one of STAB_STAGE_*");
+  if (arithmetic != STAB_ARITH_FP64 && arithmetic != STAB_ARITH_DOUBLE_WORD)
+    return set_err(c, STAB_ERR_ARG, "arithmetic must be STAB_ARITH_FP64 or STAB_ARITH_DOUBLE_WORD");
+  c->arith[stage] = arithmetic;
   return STAB_OK;
 }
 

@@ -110,22 +110,6 @@ __device__ __forceinline__ dz zfnmac(dz a, dz b, dz c) {
 __device__ __forceinline__ zc dz_to64(dz a) { return zmk(dw_to64(dz_re(a)), dw_to64(dz_im(a))); }
 __device__ __forceinline__ dz dz_from64(zc a) { return dz_mk(dw_from64(a.x), dw_from64(a.y)); }
 
-// ---- complex64 helpers (shift formulas of the double-word QR) ---------------
-__device__ __forceinline__ cc zadd(cc a, cc b) { return cmk(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ cc zsub(cc a, cc b) { return cmk(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ cc zmul(cc a, cc b) { return cmul(a, b); }
-__device__ __forceinline__ cc zscale(cc a, float s) { return cmk(a.x * s, a.y * s); }
-__device__ __forceinline__ float zabs1(cc a) { return fabsf(a.x) + fabsf(a.y); }
-__device__ __forceinline__ float zabs(cc a) { return hypotf(a.x, a.y); }
-__device__ __forceinline__ cc zdiv(cc a, cc b) { return cx<cc>::div(a, b); }
-__device__ __forceinline__ cc zsqrt(cc a) {
-  const float m = zabs(a);
-  if (m == 0.f) return cmk(0.f, 0.f);
-  const float t = sqrtf(0.5f * (m + fabsf(a.x)));
-  if (a.x >= 0.f) return cmk(t, 0.5f * a.y / t);
-  return cmk(0.5f * fabsf(a.y) / t, copysignf(t, a.y));
-}
-
 // ---- reciprocal and reciprocal square root ----------------------------------
 // Newton steps in double-word arithmetic from a float seed: each step doubles
 // the number of correct bits (reciprocal: y + y (1 - d y); reciprocal square
@@ -147,3 +131,26 @@ __device__ __forceinline__ dw dw_rsqrt(dw s) {
   }
   return r;
 }
+
+// ---- the LU / triangular-solve traits (cx<T> of common.cuh) -----------------
+template <> struct cx<dz> {
+  typedef float real;
+  __device__ static dz make(float r, float i) { return make_float4(r, 0.f, i, 0.f); }
+  __device__ static dz mul(dz a, dz b) { return zmul(a, b); }
+  __device__ static dz fma_(dz a, dz b, dz c) { return zfma(a, b, c); }
+  __device__ static dz sub(dz a, dz b) { return zsub(a, b); }
+  __device__ static dz fnma(dz a, dz b, dz c) { return zfnma(a, b, c); }   // c - a*b
+  // a conj(b) / |b|^2, with b first scaled by the power of two that brings
+  // it near 1 (the squares stay inside the float exponent range)
+  __device__ static dz div(dz a, dz b) {
+    const float mx = zabs1(b);
+    const float p = (mx == 0.f) ? 1.f : ldexpf(1.f, -ilogbf(mx));
+    const dz bs = zscale(b, p);
+    const dw r = dw_rcp(dw_fma(dz_re(bs), dz_re(bs), dw_mul(dz_im(bs), dz_im(bs))));
+    const dz q = zmul(a, zconj(bs));
+    return zscale(dz_mk(dw_mul(dz_re(q), r), dw_mul(dz_im(q), r)), p);
+  }
+  __device__ static float abs1(dz a) { return zabs1(a); }
+  __device__ static dz from(zc a) { return dz_from64(a); }
+  __device__ static zc to64(dz a) { return dz_to64(a); }
+};

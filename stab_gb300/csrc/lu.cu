@@ -1,8 +1,9 @@
 // Batched dense complex LU with partial pivoting and triangular solves.
 //
 // Replaces ZGETRF (spatial.f90:978), ZGETRS (spatial.f90:996,1002) and the
-// factorisation inside ZGESV (temporal.f90:774); complex64 instances of the
-// same kernels factor A - s B for the mixed-precision polish.
+// factorisation inside ZGESV (temporal.f90:774); complex64 and double-word
+// (dw.cuh) instances of the same kernels factor A - s B for the
+// mixed-precision polish.
 //
 // Layout: column-major n x n per instance at pool offset mat_off[k].  One
 // CTA per instance (n <= 960 here).  Blocked right-looking algorithm:
@@ -16,6 +17,7 @@
 #include <cooperative_groups.h>
 
 #include "common.cuh"
+#include "dw.cuh"
 #include "kernels.cuh"
 #include "lu.cuh"
 
@@ -347,6 +349,10 @@ __device__ __forceinline__ zc shfl_cx(zc v, int src) {
 __device__ __forceinline__ cc shfl_cx(cc v, int src) {
   return cmk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
+__device__ __forceinline__ dz shfl_cx(dz v, int src) {
+  return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                     __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+}
 
 // The same solve for few right-hand sides: one CTA per (instance, column),
 // blocked by 32 columns.  Warp 0 solves each 32 x 32 diagonal block from
@@ -540,8 +546,11 @@ template cudaError_t launch_lu<zc>(int, const InstDesc*, const int32_t*, int, zc
                                    const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*, int);
 template cudaError_t launch_lu<cc>(int, const InstDesc*, const int32_t*, int, cc*, const int64_t*, int32_t*,
                                    const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*, int);
+template cudaError_t launch_lu<dz>(int, const InstDesc*, const int32_t*, int, dz*, const int64_t*, int32_t*,
+                                   const int64_t*, int32_t*, cudaStream_t, const int32_t*, int, const int32_t*, int);
 template int lu_nb_max<zc>(int);
 template int lu_nb_max<cc>(int);
+template int lu_nb_max<dz>(int);
 
 // Autotuning input: count dense n x n matrices with hashed entries in
 // [-1, 1) + i[-1, 1) and the diagonal raised by n, so that every panel width
@@ -566,10 +575,14 @@ cudaError_t launch_tune_matrix(int count, int n, T* A, cudaStream_t s) {
 }
 template cudaError_t launch_tune_matrix<zc>(int, int, zc*, cudaStream_t);
 template cudaError_t launch_tune_matrix<cc>(int, int, cc*, cudaStream_t);
+template cudaError_t launch_tune_matrix<dz>(int, int, dz*, cudaStream_t);
 template cudaError_t launch_getrs<zc>(int, const int32_t*, int, const zc*, const int64_t*, const int32_t*,
                                       const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
                                       cudaStream_t, const float*, const float*);
 template cudaError_t launch_getrs<cc>(int, const int32_t*, int, const cc*, const int64_t*, const int32_t*,
+                                      const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
+                                      cudaStream_t, const float*, const float*);
+template cudaError_t launch_getrs<dz>(int, const int32_t*, int, const dz*, const int64_t*, const int32_t*,
                                       const int64_t*, zc*, const int64_t*, int, int, int, const int32_t*,
                                       cudaStream_t, const float*, const float*);
 

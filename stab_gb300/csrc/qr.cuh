@@ -40,7 +40,8 @@ template <class C> struct ew;
 template <> struct ew<zc> {
   typedef double real;
   typedef double sq;
-  typedef zc S;        // one-thread shift formulas
+  typedef zc S;        // one-thread shift formulas, and their real type
+  typedef double SR;
   __device__ static zc to_s(zc a) { return a; }
   __device__ static zc from_s(zc a) { return a; }
   __device__ static zc smk(double r, double i) { return zmk(r, i); }
@@ -58,13 +59,16 @@ template <> struct ew<zc> {
 };
 template <> struct ew<dz> {
   typedef float real;
-  typedef dw sq;
-  // shifts only steer convergence, so their formulas take the high words in
-  // complex64: no FP64 instruction on the serial path of an iteration
-  typedef cc S;
-  __device__ static cc to_s(dz a) { return cmk(a.x, a.z); }
-  __device__ static dz from_s(cc a) { return make_float4(a.x, 0.f, a.y, 0.f); }
-  __device__ static cc smk(float r, float i) { return cmk(r, i); }
+  typedef double sq;
+  // the shift formulas of one thread run in FP64: a complex64 shift carries an
+  // absolute error of 2^-24 times the trailing block's entries, which stalls
+  // the convergence of small clustered eigenvalues (spatial companion
+  // matrices)
+  typedef zc S;
+  typedef double SR;
+  __device__ static zc to_s(dz a) { return dz_to64(a); }
+  __device__ static dz from_s(zc a) { return dz_from64(a); }
+  __device__ static zc smk(double r, double i) { return zmk(r, i); }
   // deflation and start tests use 2^-46, a few units of the double-word
   // rounding error; magnitudes in those tests are the high words
   __device__ static float ulp() { return 1.42108547e-14f; }
@@ -74,9 +78,14 @@ template <> struct ew<dz> {
   __device__ static dz from64(zc a) { return dz_from64(a); }
   __device__ static zc to64(dz a) { return dz_to64(a); }
   __device__ static float mag2(dz a) { return a.x * a.x + a.z * a.z; }
-  __device__ static dw sq_zero() { return make_float2(0.f, 0.f); }
-  __device__ static void sq_add(dw& acc, dz a) { acc = dw_fma(dz_re(a), dz_re(a), dw_fma(dz_im(a), dz_im(a), acc)); }
-  __device__ static double sq_64(dw v) { return dw_to64(v); }
+  // sums of squares (O(n) per Householder step) in FP64: squares of the
+  // ~1e-20 entries of a balanced low-Mach operator underflow in float
+  __device__ static double sq_zero() { return 0.0; }
+  __device__ static void sq_add(double& acc, dz a) {
+    const zc v = dz_to64(a);
+    acc = fma(v.x, v.x, fma(v.y, v.y, acc));
+  }
+  __device__ static double sq_64(double v) { return v; }
   __device__ static dz warp_sum_c(dz a) { return dz_mk(warp_sum(dz_re(a)), warp_sum(dz_im(a))); }
 };
 
@@ -429,6 +438,7 @@ __device__ int qr_eigs(const SAcc<E> H, const int mp, zc* ev, SM& s, ReflC<E>* r
       // shift (one thread)
       if (tid == 0) {
         typedef typename ew<E>::S S;
+        typedef typename ew<E>::SR SR;
         S t;
         if (kdefl % 20 == 0) {
           t = zadd(ew<E>::smk(0.75 * zabs(ew<E>::to_s(H(i, i - 1))), 0.0), ew<E>::to_s(H(i, i)));
@@ -437,16 +447,16 @@ __device__ int qr_eigs(const SAcc<E> H, const int mp, zc* ev, SM& s, ReflC<E>* r
         } else {
           t = ew<E>::to_s(H(i, i));
           const S u = zmul(zsqrt(ew<E>::to_s(H(i - 1, i))), zsqrt(ew<E>::to_s(H(i, i - 1))));
-          const R su = zabs1(u);
-          if (su != (R)0) {
-            const S x = zscale(zsub(ew<E>::to_s(H(i - 1, i - 1)), t), (R)0.5);
-            const R sx = zabs1(x);
-            const R sc = max(su, sx);
-            const S xs = zscale(x, (R)1 / sc), us = zscale(u, (R)1 / sc);
+          const SR su = zabs1(u);
+          if (su != (SR)0) {
+            const S x = zscale(zsub(ew<E>::to_s(H(i - 1, i - 1)), t), (SR)0.5);
+            const SR sx = zabs1(x);
+            const SR sc = max(su, sx);
+            const S xs = zscale(x, (SR)1 / sc), us = zscale(u, (SR)1 / sc);
             S y = zscale(zsqrt(zadd(zmul(xs, xs), zmul(us, us))), sc);
-            if (sx > (R)0) {
-              const S xn = zscale(x, (R)1 / sx);
-              if (xn.x * y.x + xn.y * y.y < (R)0) y = ew<E>::smk(-y.x, -y.y);
+            if (sx > (SR)0) {
+              const S xn = zscale(x, (SR)1 / sx);
+              if (xn.x * y.x + xn.y * y.y < (SR)0) y = ew<E>::smk(-y.x, -y.y);
             }
             t = zsub(t, zmul(u, zdiv(u, zadd(x, y))));
           }

@@ -1,20 +1,26 @@
-// CPU build of the eigensolver's QR iteration (stab_gb300/csrc/qr.cuh) for
-// the host tests: 32 std::threads stand in for the 32 threads of one warp,
-// with a barrier for __syncthreads / __syncwarp, and the CUDA rounding
-// intrinsics map to IEEE float / double operations (compiled without FMA
-// contraction).  It reads a packed-or-dense Hessenberg matrix, runs the QR in
-// complex128 and in double-word arithmetic, and writes both spectra.
+// CPU build of the per-instance eigensolver (stab_gb300/csrc/qr.cuh and
+// eig_body.cuh) for the host tests.  32 std::threads stand in for the 32
+// threads of one warp: a spinning barrier serves __syncthreads / __syncwarp,
+// warp shuffles and votes go through a shared exchange buffer between two
+// barriers, and the CUDA rounding intrinsics map to IEEE float / double
+// operations (compiled without FMA contraction).
 //
-// input  (argv[1]): int32 mp, then mp*mp complex128, column-major
-// output (argv[2]): int32 status fp64, int32 status double-word,
-//                   int64 updates fp64, int64 updates double-word,
-//                   mp complex128 eigenvalues (fp64), mp (double-word)
+//   dw_qr_host qr   IN OUT [dw]   IN: int32 mp, mp*mp complex128 column-major
+//                                 upper Hessenberg; runs the QR only
+//   dw_qr_host body IN OUT        IN: int32 m, m*m complex128 column-major
+//                                 standard-form matrix; runs isolation,
+//                                 balancing, Hessenberg reduction and QR
+// OUT: int32 status fp64, int32 status double-word, int64 reflector
+// applications fp64, int64 double-word, then the eigenvalues (complex128) of
+// the fp64 run and of the double-word run.  "dw" skips the fp64 run.
 #include <algorithm>
-#include <barrier>
+#include <atomic>
 #include <cmath>
-#include <cstdio>
 #include <cstdint>
+#include <cstdio>
+#include <cstring>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <type_traits>
 #include <vector>
@@ -22,27 +28,71 @@
 #include <cuda_runtime.h>
 
 namespace {
+// generation-counting barrier; waiting threads yield (32 threads share the
+// host's cores)
+struct SpinBarrier {
+  std::atomic<int> count{0}, gen{0};
+  int n = 32;
+  void wait() {
+    const int g = gen.load(std::memory_order_acquire);
+    if (count.fetch_add(1, std::memory_order_acq_rel) == n - 1) {
+      count.store(0, std::memory_order_relaxed);
+      gen.fetch_add(1, std::memory_order_acq_rel);
+    } else {
+      while (gen.load(std::memory_order_acquire) == g) std::this_thread::yield();
+    }
+  }
+};
 thread_local int g_tid = 0;
-std::barrier<>* g_bar = nullptr;
+SpinBarrier g_bar;
 std::mutex g_mu;
+alignas(16) unsigned char g_xch[32][16];
+bool g_pred[32];
 struct TIdx {
   unsigned x;
 };
 }  // namespace
 #define threadIdx (TIdx{(unsigned)g_tid})
 #define blockDim (TIdx{32u})
-inline void __syncthreads() { g_bar->arrive_and_wait(); }
-inline void __syncwarp() { g_bar->arrive_and_wait(); }
+inline void __syncthreads() { g_bar.wait(); }
+inline void __syncwarp() { g_bar.wait(); }
 inline int atomicMax(int* p, int v) {
   std::lock_guard<std::mutex> l(g_mu);
   const int o = *p;
   if (v > o) *p = v;
   return o;
 }
-template <class T>
-T __shfl_down_sync(unsigned, T v, int) {   // only reached through unused block reductions
-  return v;
+inline int atomicAdd(int* p, int v) {
+  std::lock_guard<std::mutex> l(g_mu);
+  const int o = *p;
+  *p = o + v;
+  return o;
 }
+inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v) {
+  std::lock_guard<std::mutex> l(g_mu);
+  const unsigned long long o = *p;
+  *p = o + v;
+  return o;
+}
+template <class T>
+T __shfl_down_sync(unsigned, T v, int o) {
+  static_assert(sizeof(T) <= 16, "exchange slot");
+  std::memcpy(g_xch[g_tid], &v, sizeof(T));
+  g_bar.wait();
+  T r = v;
+  if (g_tid + o < 32) std::memcpy(&r, g_xch[g_tid + o], sizeof(T));
+  g_bar.wait();
+  return r;
+}
+inline bool __all_sync(unsigned, bool p) {
+  g_pred[g_tid] = p;
+  g_bar.wait();
+  bool a = true;
+  for (int q = 0; q < 32; ++q) a = a && g_pred[q];
+  g_bar.wait();
+  return a;
+}
+inline long long clock64() { return 0; }
 inline float __fadd_rn(float a, float b) { return a + b; }
 inline float __fsub_rn(float a, float b) { return a - b; }
 inline float __fmul_rn(float a, float b) { return a * b; }
@@ -51,19 +101,42 @@ inline float __frcp_rn(float x) { return 1.0f / x; }
 inline float rsqrtf(float x) { return 1.0f / std::sqrt(x); }
 inline double rsqrt(double x) { return 1.0 / std::sqrt(x); }
 inline double __drcp_rn(double x) { return 1.0 / x; }
+inline int __double2hiint(double x) {
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  return (int)(b >> 32);
+}
+inline int __float_as_int(float x) {
+  int b;
+  std::memcpy(&b, &x, 4);
+  return b;
+}
 using std::max;
 using std::min;
 
 #include "../../stab_gb300/csrc/common.cuh"
 #include "../../stab_gb300/csrc/dw.cuh"
 namespace stab {
+unsigned long long g_eig_phase_cycles[6];
 #include "../../stab_gb300/csrc/qr.cuh"
-}
+#include "../../stab_gb300/csrc/eig_body.cuh"
+}  // namespace stab
 
 using namespace stab;
 
+template <class F>
+static void run32(F f) {
+  std::vector<std::thread> th;
+  for (int t = 0; t < 32; ++t)
+    th.emplace_back([&, t] {
+      g_tid = t;
+      f(t);
+    });
+  for (auto& x : th) x.join();
+}
+
 template <class E>
-static std::vector<zc> run(const std::vector<zc>& Hd, int mp, int& st, long long& upd) {
+static std::vector<zc> run_qr(const std::vector<zc>& Hd, int mp, int& st, long long& upd) {
   std::vector<E> P(hess_packed_size(mp) + 4);
   for (int c = 0; c < mp; ++c)
     for (int r = 0; r <= std::min(c + 2, mp - 1); ++r) {
@@ -77,48 +150,67 @@ static std::vector<zc> run(const std::vector<zc>& Hd, int mp, int& st, long long
     }
   std::vector<zc> ev(mp);
   static HqrSmem<E> s;
-  std::barrier<> bar(32);
-  g_bar = &bar;
-  long long u0 = 0;
-  int st0 = 0;
-  std::vector<std::thread> th;
-  for (int t = 0; t < 32; ++t)
-    th.emplace_back([&, t] {
-      g_tid = t;
-      long long u = 0;
-      const int r = qr_eigs<E, true>(SAcc<E>{P.data(), mp}, mp, ev.data(), s, s.refl, u);
-      if (t == 0) {
-        u0 = u;
-        st0 = r;
-      }
-    });
-  for (auto& x : th) x.join();
-  st = st0;
-  upd = u0;
+  run32([&](int t) {
+    long long u = 0;
+    const int r = qr_eigs<E, true>(SAcc<E>{P.data(), mp}, mp, ev.data(), s, s.refl, u);
+    if (t == 0) {
+      upd = u;
+      st = r;
+    }
+  });
+  return ev;
+}
+
+template <class C>
+static std::vector<zc> run_body(const std::vector<zc>& A, int m, int& st, long long& upd) {
+  std::vector<zc> M(A), Hw((size_t)m * m), ev(m);
+  std::vector<unsigned char> smraw(eig_plain_smem_bytes(m));
+  const int32_t msz = m;
+  const int64_t off = 0;
+  int32_t status = -1, counter = 0;
+  double flops = 0.0;
+  static HqrSmem<C> s;
+  static int s_inst;
+  run32([&](int) {
+    eig_plain_body<C>(1, &msz, M.data(), &off, Hw.data(), &off, ev.data(), &off, &status, &counter, nullptr, &flops,
+                      smraw.data(), s, s_inst);
+  });
+  st = status;
+  upd = (long long)flops;
   return ev;
 }
 
 int main(int argc, char** argv) {
-  if (argc != 3) return 2;
-  FILE* f = std::fopen(argv[1], "rb");
+  if (argc != 4 && argc != 5) return 2;
+  const std::string mode = argv[1];
+  const bool dw_only = (argc == 5 && std::strcmp(argv[4], "dw") == 0);
+  FILE* f = std::fopen(argv[2], "rb");
   if (!f) return 2;
-  int mp = 0;
-  if (std::fread(&mp, 4, 1, f) != 1 || mp < 1 || mp > 4096) return 2;
-  std::vector<zc> H((size_t)mp * mp);
+  int m = 0;
+  if (std::fread(&m, 4, 1, f) != 1 || m < 1 || m > 4096) return 2;
+  std::vector<zc> H((size_t)m * m);
   if (std::fread(H.data(), sizeof(zc), H.size(), f) != H.size()) return 2;
   std::fclose(f);
   int st1 = 0, st2 = 0;
   long long u1 = 0, u2 = 0;
-  const std::vector<zc> e1 = run<zc>(H, mp, st1, u1);
-  const std::vector<zc> e2 = run<dz>(H, mp, st2, u2);
-  FILE* g = std::fopen(argv[2], "wb");
+  std::vector<zc> e1(m, zmk(0.0, 0.0)), e2;
+  if (mode == "qr") {
+    if (!dw_only) e1 = run_qr<zc>(H, m, st1, u1);
+    e2 = run_qr<dz>(H, m, st2, u2);
+  } else if (mode == "body") {
+    if (!dw_only) e1 = run_body<zc>(H, m, st1, u1);
+    e2 = run_body<dz>(H, m, st2, u2);
+  } else {
+    return 2;
+  }
+  FILE* g = std::fopen(argv[3], "wb");
   if (!g) return 2;
   std::fwrite(&st1, 4, 1, g);
   std::fwrite(&st2, 4, 1, g);
   std::fwrite(&u1, 8, 1, g);
   std::fwrite(&u2, 8, 1, g);
-  std::fwrite(e1.data(), sizeof(zc), mp, g);
-  std::fwrite(e2.data(), sizeof(zc), mp, g);
+  std::fwrite(e1.data(), sizeof(zc), m, g);
+  std::fwrite(e2.data(), sizeof(zc), m, g);
   std::fclose(g);
   return 0;
 }

@@ -1,10 +1,13 @@
-"""Double-word QR of the seed spectra, built for the CPU.
+"""Double-word eigensolver of the seed spectra, built for the CPU.
 
-tests/host/dw_qr_host.cpp compiles the eigensolver's QR iteration
-(stab_gb300/csrc/qr.cuh) with g++, the 32 threads of a warp run as
-std::threads.  The input is the balanced, power-of-two scaled Hessenberg form
-of a temporal operator X = B0^-1 A0 (temporal.f90:771-803) at small N, which
-the test builds with the oracle and scipy; the reference spectrum is numpy's.
+tests/host/dw_qr_host.cpp compiles the per-instance eigensolver
+(stab_gb300/csrc/qr.cuh, eig_body.cuh) with g++, the 32 threads of a warp run
+as std::threads.  Two entry points: the QR iteration alone on a Hessenberg
+matrix, and the whole kernel body (isolation, compaction, balancing,
+Hessenberg reduction, QR) on a standard-form matrix.  The input is the balanced, power-of-two scaled Hessenberg form
+of a temporal operator X = B0^-1 A0 (temporal.f90:771-803) or of a spatial
+companion matrix (spatial.f90:972-1016) at small N, which the test builds
+with the oracle and scipy; the reference spectrum is numpy's.
 
 Tolerances:
   complex128 QR     each of the 8 least-stable eigenvalues within 1e-12
@@ -15,6 +18,8 @@ Tolerances:
                     a largest entry near 1)
   both converge, and the double-word QR in no more than 1.5x the 2-element
   reflector applications of the complex128 one
+Whole body: both converge; the 8 least-stable finite eigenvalues within
+1e-12 (complex128) and 1e-11 (double-word) relative of numpy's.
 """
 import os
 import shutil
@@ -44,16 +49,28 @@ def harness():
     shutil.rmtree(d, ignore_errors=True)
 
 
-def _hessenberg(seed: int, N: int) -> np.ndarray:
+def _operator(itype: int, seed: int, N: int, M=None) -> np.ndarray:
+    """Standard-form operator: B0^-1 A0 (temporal) or the companion matrix."""
     rng = np.random.default_rng(seed)
-    M = float(rng.uniform(0.0, 2.0))
-    Re = float(10 ** rng.uniform(np.log10(300.0), np.log10(3000.0)))
-    a, b = float(rng.uniform(0.05, 0.4)), float(rng.uniform(0.0, 0.3))
-    d, prof = H.synth_case(1, N, max(M, 1e-3), Re, a=a, b=b)
+    if itype == 1:
+        M = float(rng.uniform(0.0, 2.0)) if M is None else M
+        Re = float(10 ** rng.uniform(np.log10(300.0), np.log10(3000.0)))
+        a, b = float(rng.uniform(0.05, 0.4)), float(rng.uniform(0.0, 0.3))
+        d, prof = H.synth_case(1, N, max(M, 1e-3), Re, a=a, b=b)
+    else:
+        M, Re = (float(rng.uniform(0.3, 1.5)) if M is None else M), float(rng.uniform(500, 2500))
+        d, prof = H.synth_case(2, N, M, Re, w=0.05, b=float(rng.uniform(0, 0.2)), crossflow=True)
     p = H.oracle_params(d)
     ms = so.mean_state(p, prof[:, 0], prof[:, 1:])
-    A0, B0 = so.temporal_pencil(p, ms)
-    Xb, _ = sl.matrix_balance(np.linalg.solve(B0, A0), permute=True, separate=True)
+    if itype == 1:
+        A0, B0 = so.temporal_pencil(p, ms)
+        return np.linalg.solve(B0, A0)
+    return so.spatial_companion(p, ms)       # spatial.f90:972-1016
+
+
+def _hessenberg(itype: int, seed: int, N: int) -> np.ndarray:
+    X = _operator(itype, seed, N)
+    Xb, _ = sl.matrix_balance(X, permute=True, separate=True)
     n = Xb.shape[0]
     lo, hi = 0, n - 1   # active block between the isolated rows / columns
     while lo < n and np.all(Xb[lo + 1:, lo] == 0):
@@ -65,16 +82,18 @@ def _hessenberg(seed: int, N: int) -> np.ndarray:
     return sl.hessenberg(Bk)
 
 
-@pytest.mark.parametrize("seed,N", [(0, 8), (2, 12), (5, 12)])
-def test_double_word_qr_matches_numpy(harness, seed, N):
+# the spatial companion case at N = 20 is where complex64 shift formulas took
+# 6x the reflector applications (and failed outright at N = 32)
+@pytest.mark.parametrize("itype,seed,N", [(1, 0, 8), (1, 2, 12), (1, 5, 12), (2, 1, 20)])
+def test_double_word_qr_matches_numpy(harness, itype, seed, N):
     exe, d = harness
-    Hm = _hessenberg(seed, N)
+    Hm = _hessenberg(itype, seed, N)
     mp = Hm.shape[0]
     fin, fout = os.path.join(d, f"h{seed}.bin"), os.path.join(d, f"o{seed}.bin")
     with open(fin, "wb") as f:
         f.write(np.int32(mp).tobytes())
         f.write(np.asfortranarray(Hm).astype(np.complex128).tobytes(order="F"))
-    subprocess.run([exe, fin, fout], check=True, timeout=600)
+    subprocess.run([exe, "qr", fin, fout], check=True, timeout=600)
     raw = open(fout, "rb").read()
     st64, stdw = np.frombuffer(raw[:8], np.int32)
     up64, updw = np.frombuffer(raw[8:24], np.int64)
@@ -88,3 +107,32 @@ def test_double_word_qr_matches_numpy(harness, seed, N):
         assert np.min(np.abs(e64 - r)) / abs(r) < 1e-12
         assert np.min(np.abs(edw - r)) / abs(r) < 1e-11
     assert max(np.min(np.abs(edw - r)) for r in ref) < 1e-9
+
+
+def _run(exe, d, tag, X):
+    m = X.shape[0]
+    fin, fout = os.path.join(d, f"b{tag}.bin"), os.path.join(d, f"bo{tag}.bin")
+    with open(fin, "wb") as f:
+        f.write(np.int32(m).tobytes())
+        f.write(np.asfortranarray(X).astype(np.complex128).tobytes(order="F"))
+    subprocess.run([exe, "body", fin, fout], check=True, timeout=600)
+    raw = open(fout, "rb").read()
+    st64, stdw = np.frombuffer(raw[:8], np.int32)
+    ev = np.frombuffer(raw[24:], np.complex128)
+    return st64, stdw, ev[:m], ev[m:]
+
+
+# low Mach numbers give the operator entries over ~30 decades (the
+# 1/(gamma M^2) pressure terms): the float exponent range and the squares of
+# tiny entries are what the double-word form has to survive
+@pytest.mark.parametrize("itype,seed,N,M", [(1, 4, 12, 0.01), (2, 0, 12, 0.5), (2, 0, 12, 0.001)])
+def test_double_word_eigensolver_body_matches_numpy(harness, itype, seed, N, M):
+    exe, d = harness
+    X = _operator(itype, seed, N, M)
+    st64, stdw, e64, edw = _run(exe, d, f"{itype}_{seed}_{N}_{M}", X)
+    assert st64 == 0 and stdw == 0
+    ref = np.linalg.eigvals(X)
+    fin = ref[np.isfinite(ref) & (np.abs(ref) < 1e10)]
+    for r in fin[np.argsort(-fin.imag)[:8]]:
+        assert np.min(np.abs(e64 - r)) <= 1e-12 * abs(r)
+        assert np.min(np.abs(edw - r)) <= 1e-11 * abs(r)

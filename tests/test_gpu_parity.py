@@ -241,25 +241,53 @@ def test_double_word_spectra_match_fp64(ctx):
     """Full spectra at the seed size (N = 32) in double-word arithmetic against
     FP64.  Tolerances: selected least-stable eigenvalue within 1e-9 relative
     (the seeds need that); each of the 8 least-stable eigenvalues within 1e-10
-    relative of the nearest double-word one."""
+    relative of the nearest double-word one (exact zeros exactly)."""
     rng = np.random.Generator(np.random.PCG64(21))
     cases = [H.synth_case(1, 32, float(rng.uniform(0.05, 2.0)), float(10 ** rng.uniform(2.5, 3.5)),
                           a=float(rng.uniform(0.05, 0.4)), b=float(rng.uniform(0, 0.3))) for _ in range(16)]
     out = {}
     try:
-        for prec in (sg.EIG_FP64, sg.EIG_DOUBLE_WORD):
-            ctx.set_eig_precision(seed=sg.EIG_DOUBLE_WORD, plain=prec)
+        for prec in (sg.ARITH_FP64, sg.ARITH_DOUBLE_WORD):
+            ctx.set_arithmetic(sg.STAGE_PLAIN_EIG, prec)
             b = ctx.batch([H.stab_params(d) for d, _ in cases], [p for _, p in cases])
             b.run(sg.MODE_PLAIN)
             eig, _, _, status, _ = b.results()
             out[prec] = (eig, status, b.spectra())
             b.close()
     finally:
-        ctx.set_eig_precision()
-    e64, s64, sp64 = out[sg.EIG_FP64]
-    edw, sdw, spdw = out[sg.EIG_DOUBLE_WORD]
+        ctx.reset_arithmetic()
+    e64, s64, sp64 = out[sg.ARITH_FP64]
+    edw, sdw, spdw = out[sg.ARITH_DOUBLE_WORD]
     assert np.all(s64 == sg.ST_OK) and np.all(sdw == sg.ST_OK)
     assert np.max(np.abs(edw - e64) / np.abs(e64)) < 1e-9
     for a, d in zip(sp64, spdw):
-        for r in a[np.argsort(-a.imag)[:8]]:
-            assert np.min(np.abs(d - r)) / abs(r) < 1e-10
+        for r in a[np.argsort(-a.imag)[:8]]:   # exact zeros (isolated rows) must match exactly
+            assert np.min(np.abs(d - r)) <= 1e-10 * abs(r)
+
+
+def test_double_word_retry_lu_matches_fp64(ctx):
+    """The complex128 inverse-iteration retry of the coarse-seeded polish with
+    its LU in double-word form against the same retry with an FP64 LU.
+    Tolerance: every instance converged in both, eigenvalues within 1e-10
+    relative (the bench's convergence bar)."""
+    rng = np.random.Generator(np.random.PCG64(33))
+    cases = [H.synth_case(1, int(rng.choice([48, 64])), float(rng.uniform(0.05, 2.0)),
+                          float(10 ** rng.uniform(2.5, 3.5)), a=float(rng.uniform(0.05, 0.4)),
+                          b=float(rng.uniform(0, 0.3))) for _ in range(64)]
+    out = {}
+    try:
+        for ar in (sg.ARITH_FP64, sg.ARITH_DOUBLE_WORD):
+            ctx.set_arithmetic(sg.STAGE_RETRY_LU, ar)
+            b = ctx.batch([H.stab_params(d) for d, _ in cases], [p for _, p in cases])
+            b.run(sg.MODE_COARSE)
+            eig, _, _, status, _ = b.results()
+            out[ar] = (eig, status, b.work()["lu_c128"])
+            b.close()
+    finally:
+        ctx.reset_arithmetic()
+    e64, s64, w64 = out[sg.ARITH_FP64]
+    edw, sdw, wdw = out[sg.ARITH_DOUBLE_WORD]
+    assert wdw > 0, "no instance took the retry"
+    both = (s64 == sg.ST_OK) & (sdw == sg.ST_OK)
+    assert np.array_equal(s64 == sg.ST_OK, sdw == sg.ST_OK)
+    assert np.max(np.abs(edw[both] - e64[both]) / np.abs(e64[both])) < 1e-10

@@ -110,6 +110,16 @@ __device__ __forceinline__ dz zfnmac(dz a, dz b, dz c) {
 __device__ __forceinline__ zc dz_to64(dz a) { return zmk(dw_to64(dz_re(a)), dw_to64(dz_im(a))); }
 __device__ __forceinline__ dz dz_from64(zc a) { return dz_mk(dw_from64(a.x), dw_from64(a.y)); }
 
+// Exponent e of x (x ~ 2^e) for scaling by the exact power of two 2^-e,
+// clamped so that 2^-e and 2^e stay finite floats: below 2^-126 (bulge
+// entries of a nearly deflated stretch of a low-Mach operator reach that) the
+// scaled value stays small instead of the factor overflowing to infinity.
+// 0 for x == 0.
+__device__ __forceinline__ int dw_scale_exponent(float x) {
+  if (!(x > 0.f)) return 0;
+  return min(max(ilogbf(x), -126), 126);
+}
+
 // ---- reciprocal and reciprocal square root ----------------------------------
 // Newton steps in double-word arithmetic from a float seed: each step doubles
 // the number of correct bits (reciprocal: y + y (1 - d y); reciprocal square
@@ -143,8 +153,7 @@ template <> struct cx<dz> {
   // a conj(b) / |b|^2, with b first scaled by the power of two that brings
   // it near 1 (the squares stay inside the float exponent range)
   __device__ static dz div(dz a, dz b) {
-    const float mx = zabs1(b);
-    const float p = (mx == 0.f) ? 1.f : ldexpf(1.f, -ilogbf(mx));
+    const float p = ldexpf(1.f, -dw_scale_exponent(zabs1(b)));
     const dz bs = zscale(b, p);
     const dw r = dw_rcp(dw_fma(dz_re(bs), dz_re(bs), dw_mul(dz_im(bs), dz_im(bs))));
     const dz q = zmul(a, zconj(bs));

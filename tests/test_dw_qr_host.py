@@ -136,3 +136,25 @@ def test_double_word_eigensolver_body_matches_numpy(harness, itype, seed, N, M):
     for r in fin[np.argsort(-fin.imag)[:8]]:
         assert np.min(np.abs(e64 - r)) <= 1e-12 * abs(r)
         assert np.min(np.abs(edw - r)) <= 1e-11 * abs(r)
+
+
+def test_double_word_eigensolver_low_mach_spatial_seed(harness):
+    """A spatial request of the serving mix at the seed size N = 32 (M = 0.045,
+    Re = 426): bulge entries of its QR fall below the float normal range,
+    where an unclamped power-of-two scale factor overflowed to infinity and
+    turned the matrix into NaN."""
+    from stab_gb300 import serve as sv
+    from stab_gb300.surrogate import erf_profile
+    exe, d = harness
+    r = [q for q in sv.make_requests(2000.0, 1.0, 20261205) if q.itype == 2][178]
+    p = so.StabParams(mattyp=1, T0=sv.T0_SUTHERLAND, Ma=r.M, Re=r.Re, Pr=0.72, ny=32, yi=1.0 / 23.0, ymax=50.0,
+                      ievec=1, ider=1, top=0, wall=0, wallt=0, curve=0, itype=2, alpha=0j, beta=complex(r.beta),
+                      omega=complex(r.omega))
+    prof = erf_profile(r.M)
+    X = so.spatial_companion(p, so.mean_state(p, prof[:, 0], prof[:, 1:]))
+    st64, stdw, e64, edw = _run(exe, d, "serve178", X)
+    assert st64 == 0 and stdw == 0
+    ref = np.linalg.eigvals(X)
+    fin = ref[np.isfinite(ref) & (np.abs(ref) < 1e10)]
+    for q in fin[np.argsort(-fin.imag)[:8]]:
+        assert np.min(np.abs(edw - q)) <= 1e-11 * abs(q)

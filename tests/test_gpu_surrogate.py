@@ -8,10 +8,11 @@ FP64 least-stable mode for only about half of the instances.  The network,
 trained here by the library's BF16 kernels on plain FP64 solves at N = 64,
 adds its prediction as one more candidate (STAB_MODE_SURROGATE).
 
-Checks: every instance the coarse method gets right stays right (at most one
-exception for rounding at the 1e-10 bar); at least two more instances match
-the plain FP64 result within 1e-10; some kept pairs came from the network's
-seed.
+Checks on 512 instances: the instances the coarse method gets right stay
+right (at most two exceptions for rounding at the 1e-10 bar); at least eight
+more instances match the plain FP64 result within 1e-10 (measured: 21 more,
+none lost); some kept pairs came from the network's seed.  On 128 instances
+the gain (one to two) was too close to the training noise to test.
 """
 import math
 
@@ -35,8 +36,8 @@ def test_network_gain_over_coarse_seeds(ctx):
     sur = su.Surrogate(ctx, max_batch=4096)
     fit = sur.fit(X, ds["omega"][v], P["alpha"][v], ds["coef"][v], steps=4000, batch=1024)
     assert fit["losses"][-1][1] < 0.5 * fit["losses"][0][1]
-    n = 128
-    Q = su.sample_params(n, 98, REGION)
+    n = 512
+    Q = su.sample_params(n, 99, REGION)
     params = [su.stab_params(Q["M"][k], Q["Re"][k], Q["alpha"][k], Q["beta"][k], 64) for k in range(n)]
     profs = [su.erf_profile(Q["M"][k], Q["width"][k]) for k in range(n)]
     b = ctx.batch(params, profs)
@@ -56,6 +57,6 @@ def test_network_gain_over_coarse_seeds(ctx):
     counts = b.counts()
     b.close()
     sur.close()
-    assert np.sum(ok_c & ~ok_s) <= 1
-    assert np.sum(ok_s & ~ok_c) >= 2, (int(ok_c.sum()), int(ok_s.sum()), counts)
+    assert np.sum(ok_c & ~ok_s) <= 2
+    assert np.sum(ok_s & ~ok_c) >= 8, (int(ok_c.sum()), int(ok_s.sum()), counts)
     assert counts["surrogate_seed"] >= 1

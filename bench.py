@@ -42,7 +42,7 @@ TOL = 1e-10
 T0_SUTH = 110.4 / 0.3815
 FP64_PEAK_TFLOPS = 1.19   # FMA probe on a GB300 (profiles/fp64_fp32_peak_probe.md)
 FP32_PEAK_TFLOPS = 69.9
-COARSE_TRAFFIC_PER_INSTANCE = (22.22e9 + 20.61e9) / 512
+COARSE_TRAFFIC_PER_INSTANCE = (25.59e9 + 21.59e9) / 512
 # kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
 KERNEL_WORK = {
     "k_eig_plain": ("eig_fp64", "fp64", "FP64 flops counted by the kernel (Householder reduction + QR sweeps)"),
@@ -499,7 +499,7 @@ def main():
                             "peak_source": "FMA probe on a GB300 of the same kind (profiles/fp64_fp32_peak_probe.md)"}
     if "k_eig_plain_coarse" in rooflines:
         # DRAM bytes per launch from the committed ncu capture of the same kernel
-        # (profiles/k_eig_plain_coarse_n32_512.md: 42.83 GB for 512 instances),
+        # (profiles/k_eig_plain_coarse_n32_512.md: 47.18 GB for 512 instances),
         # scaled by the instances of this launch (traffic grows with the
         # resident working matrices, one per instance)
         rooflines["k_eig_plain_coarse"]["traffic"] = COARSE_TRAFFIC_PER_INSTANCE * args.count

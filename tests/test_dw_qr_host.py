@@ -158,3 +158,27 @@ def test_double_word_eigensolver_low_mach_spatial_seed(harness):
     fin = ref[np.isfinite(ref) & (np.abs(ref) < 1e10)]
     for q in fin[np.argsort(-fin.imag)[:8]]:
         assert np.min(np.abs(edw - q)) <= 1e-11 * abs(q)
+
+
+def test_kernel_body_memory_safe_under_asan():
+    """The same host build with AddressSanitizer (compute-sanitizer is not
+    available): every index of the kernel body stays inside its buffers on a
+    temporal and a spatial operator, in both working precisions."""
+    if not shutil.which("g++") or not os.path.exists(os.path.join(CUDA_INC, "cuda_runtime.h")):
+        pytest.skip("needs g++ and the CUDA headers")
+    d = tempfile.mkdtemp(prefix="dwasan")
+    try:
+        exe = os.path.join(d, "dw_qr_asan")
+        r = subprocess.run(["g++", "-std=c++20", "-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer",
+                            "-ffp-contract=off", "-pthread", "-I" + CUDA_INC,
+                            os.path.join(ROOT, "tests", "host", "dw_qr_host.cpp"), "-o", exe],
+                           capture_output=True, text=True)
+        if r.returncode != 0 and "asan" in (r.stderr + r.stdout).lower():
+            pytest.skip("AddressSanitizer runtime not available")
+        assert r.returncode == 0, r.stderr
+        for itype, N, M in ((1, 8, 0.5), (2, 8, 0.01)):
+            X = _operator(itype, 3, N, M)
+            st64, stdw, _, _ = _run(exe, d, f"asan{itype}", X)
+            assert st64 == 0 and stdw == 0
+    finally:
+        shutil.rmtree(d, ignore_errors=True)

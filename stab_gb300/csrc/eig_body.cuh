@@ -254,25 +254,54 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
       if (tid == 0) Hg[(size_t)k * ld + k + 1] = s.hc[2];
       for (int r = 2 + tid; r <= L; r += NTH) Hg[(size_t)k * ld + k + r] = ew<C>::zero();
       __syncthreads();
-      // right: w = tau H(:, k+1:) v
+      // right: w = tau H(:, k+1:) v, a row per thread.  Four partial sums
+      // over the columns break the dependency chain of the accumulation (the
+      // batch runs latency bound, with a third of the issue slots busy).
       for (int r = tid; r < mp; r += NTH) {
-        C acc = ew<C>::zero();
-        for (int c = 0; c < L; ++c) acc = zfma(Hg[(size_t)(k + 1 + c) * ld + r], v[c], acc);
-        w[r] = zmul(tau, acc);
+        C a0 = ew<C>::zero(), a1 = a0, a2 = a0, a3 = a0;
+        const C* row = Hg + (size_t)(k + 1) * ld + r;
+        int c = 0;
+        for (; c + 4 <= L; c += 4) {
+          a0 = zfma(row[(size_t)c * ld], v[c], a0);
+          a1 = zfma(row[(size_t)(c + 1) * ld], v[c + 1], a1);
+          a2 = zfma(row[(size_t)(c + 2) * ld], v[c + 2], a2);
+          a3 = zfma(row[(size_t)(c + 3) * ld], v[c + 3], a3);
+        }
+        for (; c < L; ++c) a0 = zfma(row[(size_t)c * ld], v[c], a0);
+        w[r] = zmul(tau, zadd(zadd(a0, a1), zadd(a2, a3)));
       }
       __syncthreads();
-      // right update fused with the left product z = conj(tau) v^H H(k+1:, k+1:), warp per column
-      for (int c = warp; c < L; c += NWA) {
-        const C vc = zconj(v[c]);
+      // right update fused with the left product z = conj(tau) v^H H(k+1:, k+1:),
+      // a warp per two columns (two independent chains per lane)
+      for (int c = warp; c < L; c += 2 * NWA) {
+        const int c2 = c + NWA;
+        const bool two = c2 < L;             // uniform over the warp
+        const C vc = zconj(v[c]), vc2 = two ? zconj(v[c2]) : ew<C>::zero();
         C* col = Hg + (size_t)(k + 1 + c) * ld;
-        C acc = ew<C>::zero();
+        C* col2 = Hg + (size_t)(k + 1 + (two ? c2 : c)) * ld;
+        C acc = ew<C>::zero(), acc2 = acc;
         for (int r = lane; r < mp; r += 32) {
-          const C h = zfnma(w[r], vc, col[r]);
+          const C wr = w[r];
+          const C x = col[r], x2 = col2[r];
+          const C h = zfnma(wr, vc, x);
           col[r] = h;
-          if (r >= k + 1) acc = zcfma(v[r - k - 1], h, acc);
+          C h2 = x2;
+          if (two) {
+            h2 = zfnma(wr, vc2, x2);
+            col2[r] = h2;
+          }
+          if (r >= k + 1) {
+            const C vr = v[r - k - 1];
+            acc = zcfma(vr, h, acc);
+            acc2 = zcfma(vr, h2, acc2);
+          }
         }
         acc = ew<C>::warp_sum_c(acc);
-        if (lane == 0) z[c] = zmul(zconj(tau), acc);
+        acc2 = ew<C>::warp_sum_c(acc2);
+        if (lane == 0) {
+          z[c] = zmul(zconj(tau), acc);
+          if (two) z[c2] = zmul(zconj(tau), acc2);
+        }
       }
       __syncthreads();
       // left update: H(k+1:, k+1:) -= v z; column k+1 (c = 0, warp 0) also
@@ -291,7 +320,15 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
           sn = warp_sum(sn);
           if (lane == 0) s.sc[5] = ew<C>::sq_64(sn);
         } else {
-          for (int r = lane; r < L; r += 32) col[r] = zfnma(v[r], zc_, col[r]);
+          // two rows per lane iteration, both loads before either store
+          for (int r = lane; r < L; r += 64) {
+            const int r2 = r + 32;
+            const bool two = r2 < L;
+            const C x = col[r], x2 = two ? col[r2] : ew<C>::zero();
+            const C v1 = v[r], v2 = two ? v[r2] : ew<C>::zero();
+            col[r] = zfnma(v1, zc_, x);
+            if (two) col[r2] = zfnma(v2, zc_, x2);
+          }
         }
       }
       have_next = true;

@@ -102,7 +102,7 @@ def surrogate_leg(ctx, stream, args):
     trained here by the library's kernels on plain FP64 solves at N = 64 of
     the same distribution (a separate draw), then seeds MODE_SURROGATE; the
     coarse-seeded mode on the same batch is the method without it.  Every
-    result is judged against the plain FP64 path at N = 128."""
+    result is checked against the plain FP64 path at N = 128."""
     import torch
     import stab_gb300 as sg
     from stab_gb300 import surrogate as su
@@ -404,7 +404,7 @@ def main():
     # LU panel widths for the orders of this workload and of the N = 32 seeds
     tune = ctx.autotune(sorted({5 * d["ny"] for d in params} | {160}))
 
-    # judge: plain FP64 full spectrum on every instance (timed once)
+    # reference result: plain FP64 full spectrum on every instance (timed once)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(stream)

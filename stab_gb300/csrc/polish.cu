@@ -264,7 +264,7 @@ __global__ void k_reset_polish(int count, int32_t* __restrict__ done, int32_t* _
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   if (skip && skip[k]) {
-    done[k] = 4;   // not run in this round: later steps of the round pass over it
+    done[k] = 4;   // not run in this candidate round: its later steps pass over it
     return;
   }
   done[k] = 0;

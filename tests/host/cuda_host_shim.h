@@ -1,9 +1,11 @@
 // Host stand-ins for the CUDA thread model and intrinsics used by the
-// eigensolver headers, for the CPU tests in tests/host: 32 std::threads run
-// as the 32 threads of one warp, a spinning barrier serves __syncthreads /
-// __syncwarp, warp shuffles and votes go through a shared exchange buffer
-// between two barriers, and the rounding intrinsics map to IEEE float /
-// double operations (the tests compile without FMA contraction).
+// eigensolver headers, for the CPU tests in tests/host.  A block of
+// g_block_threads std::threads (32 or 128, i.e. one or four warps) runs the
+// device code: a spinning barrier over the block serves __syncthreads, one
+// per warp serves __syncwarp, warp shuffles and votes go through per-warp
+// exchange buffers between two warp barriers, and the rounding intrinsics
+// map to IEEE float / double operations (the tests compile without FMA
+// contraction).
 #pragma once
 #include <algorithm>
 #include <atomic>
@@ -15,9 +17,11 @@
 
 #include <cuda_runtime.h>
 
+#define HOST_MAX_WARPS 4
+
 namespace {
-// generation-counting barrier; waiting threads yield (32 threads share the
-// host's cores)
+// generation-counting barrier; waiting threads yield (the block's threads
+// share the host's cores)
 struct SpinBarrier {
   std::atomic<int> count{0}, gen{0};
   int n = 32;
@@ -32,18 +36,25 @@ struct SpinBarrier {
   }
 };
 thread_local int g_tid = 0;
-SpinBarrier g_bar;
+int g_block_threads = 32;
+SpinBarrier g_bar;                       // the block
+SpinBarrier g_wbar[HOST_MAX_WARPS];      // one per warp
 std::mutex g_mu;
-alignas(16) unsigned char g_xch[32][16];
-bool g_pred[32];
+alignas(16) unsigned char g_xch[32 * HOST_MAX_WARPS][16];
+bool g_pred[32 * HOST_MAX_WARPS];
 struct TIdx {
   unsigned x;
 };
+// set the block size before starting its threads
+inline void host_block(int threads) {
+  g_block_threads = threads;
+  g_bar.n = threads;
+}
 }  // namespace
 #define threadIdx (TIdx{(unsigned)g_tid})
-#define blockDim (TIdx{32u})
+#define blockDim (TIdx{(unsigned)g_block_threads})
 inline void __syncthreads() { g_bar.wait(); }
-inline void __syncwarp() { g_bar.wait(); }
+inline void __syncwarp() { g_wbar[g_tid >> 5].wait(); }
 inline int atomicMax(int* p, int v) {
   std::lock_guard<std::mutex> l(g_mu);
   const int o = *p;
@@ -65,19 +76,21 @@ inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v)
 template <class T>
 T __shfl_down_sync(unsigned, T v, int o) {
   static_assert(sizeof(T) <= 16, "exchange slot");
+  const int lane = g_tid & 31, base = g_tid - lane;
   std::memcpy(g_xch[g_tid], &v, sizeof(T));
-  g_bar.wait();
+  __syncwarp();
   T r = v;
-  if (g_tid + o < 32) std::memcpy(&r, g_xch[g_tid + o], sizeof(T));
-  g_bar.wait();
+  if (lane + o < 32) std::memcpy(&r, g_xch[base + lane + o], sizeof(T));
+  __syncwarp();
   return r;
 }
 inline bool __all_sync(unsigned, bool p) {
+  const int base = g_tid & ~31;
   g_pred[g_tid] = p;
-  g_bar.wait();
+  __syncwarp();
   bool a = true;
-  for (int q = 0; q < 32; ++q) a = a && g_pred[q];
-  g_bar.wait();
+  for (int q = 0; q < 32; ++q) a = a && g_pred[base + q];
+  __syncwarp();
   return a;
 }
 inline long long clock64() { return 0; }

@@ -1,9 +1,8 @@
 // CPU build of the per-instance eigensolver (stab_gb300/csrc/qr.cuh and
-// eig_body.cuh) for the host tests.  32 std::threads stand in for the 32
-// threads of one warp: a spinning barrier serves __syncthreads / __syncwarp,
-// warp shuffles and votes go through a shared exchange buffer between two
-// barriers, and the CUDA rounding intrinsics map to IEEE float / double
-// operations (compiled without FMA contraction).
+// eig_body.cuh) for the host tests, with the CUDA thread model of
+// cuda_host_shim.h.  The block has 32 threads (one warp), or 128 (four
+// warps, the batch kernel's shape) when the environment variable
+// HOST_BLOCK_THREADS is 128.
 //
 //   dw_qr_host qr   IN OUT [dw]   IN: int32 mp, mp*mp complex128 column-major
 //                                 upper Hessenberg; runs the QR only
@@ -14,6 +13,7 @@
 // applications fp64, int64 double-word, then the eigenvalues (complex128) of
 // the fp64 run and of the double-word run.  "dw" skips the fp64 run.
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -31,9 +31,9 @@ unsigned long long g_eig_phase_cycles[6];
 using namespace stab;
 
 template <class F>
-static void run32(F f) {
+static void run_block(F f) {
   std::vector<std::thread> th;
-  for (int t = 0; t < 32; ++t)
+  for (int t = 0; t < g_block_threads; ++t)
     th.emplace_back([&, t] {
       g_tid = t;
       f(t);
@@ -56,7 +56,7 @@ static std::vector<zc> run_qr(const std::vector<zc>& Hd, int mp, int& st, long l
     }
   std::vector<zc> ev(mp);
   static HqrSmem<E> s;
-  run32([&](int t) {
+  run_block([&](int t) {
     long long u = 0;
     const int r = qr_eigs<E, true>(SAcc<E>{P.data(), mp}, mp, ev.data(), s, s.refl, u);
     if (t == 0) {
@@ -77,7 +77,7 @@ static std::vector<zc> run_body(const std::vector<zc>& A, int m, int& st, long l
   double flops = 0.0;
   static HqrSmem<C> s;
   static int s_inst;
-  run32([&](int) {
+  run_block([&](int) {
     eig_plain_body<C>(1, &msz, M.data(), &off, Hw.data(), &off, ev.data(), &off, &status, &counter, nullptr, &flops,
                       smraw.data(), s, s_inst);
   });
@@ -88,6 +88,8 @@ static std::vector<zc> run_body(const std::vector<zc>& A, int m, int& st, long l
 
 int main(int argc, char** argv) {
   if (argc != 4 && argc != 5) return 2;
+  const char* bt = std::getenv("HOST_BLOCK_THREADS");
+  host_block(bt && std::strcmp(bt, "128") == 0 ? 128 : 32);
   const std::string mode = argv[1];
   const bool dw_only = (argc == 5 && std::strcmp(argv[4], "dw") == 0);
   FILE* f = std::fopen(argv[2], "rb");

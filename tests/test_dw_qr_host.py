@@ -18,8 +18,9 @@ Tolerances:
                     a largest entry near 1)
   both converge, and the double-word QR in no more than 1.5x the 2-element
   reflector applications of the complex128 one
-Whole body: both converge; the 8 least-stable finite eigenvalues within
-1e-12 (complex128) and 1e-11 (double-word) relative of numpy's.
+Whole body (one warp, and the batch kernel's four warps): both converge;
+the 8 least-stable finite eigenvalues within 1e-12 (complex128) and 1e-11
+(double-word) relative of numpy's.
 """
 import os
 import shutil
@@ -109,13 +110,16 @@ def test_double_word_qr_matches_numpy(harness, itype, seed, N):
     assert max(np.min(np.abs(edw - r)) for r in ref) < 1e-9
 
 
-def _run(exe, d, tag, X):
+def _run(exe, d, tag, X, threads=32):
+    """Whole kernel body on X with a block of `threads` (32: one warp; 128:
+    the four warps of the batch kernel)."""
     m = X.shape[0]
     fin, fout = os.path.join(d, f"b{tag}.bin"), os.path.join(d, f"bo{tag}.bin")
     with open(fin, "wb") as f:
         f.write(np.int32(m).tobytes())
         f.write(np.asfortranarray(X).astype(np.complex128).tobytes(order="F"))
-    subprocess.run([exe, "body", fin, fout], check=True, timeout=600)
+    env = dict(os.environ, HOST_BLOCK_THREADS=str(threads))
+    subprocess.run([exe, "body", fin, fout], check=True, timeout=600, env=env)
     raw = open(fout, "rb").read()
     st64, stdw = np.frombuffer(raw[:8], np.int32)
     ev = np.frombuffer(raw[24:], np.complex128)
@@ -125,11 +129,12 @@ def _run(exe, d, tag, X):
 # low Mach numbers give the operator entries over ~30 decades (the
 # 1/(gamma M^2) pressure terms): the float exponent range and the squares of
 # tiny entries are what the double-word form has to survive
-@pytest.mark.parametrize("itype,seed,N,M", [(1, 4, 12, 0.01), (2, 0, 12, 0.5), (2, 0, 12, 0.001)])
-def test_double_word_eigensolver_body_matches_numpy(harness, itype, seed, N, M):
+@pytest.mark.parametrize("itype,seed,N,M,threads", [(1, 4, 12, 0.01, 32), (2, 0, 12, 0.5, 32), (2, 0, 12, 0.001, 32),
+                                                    (1, 4, 12, 0.01, 128), (2, 0, 12, 0.001, 128)])
+def test_double_word_eigensolver_body_matches_numpy(harness, itype, seed, N, M, threads):
     exe, d = harness
     X = _operator(itype, seed, N, M)
-    st64, stdw, e64, edw = _run(exe, d, f"{itype}_{seed}_{N}_{M}", X)
+    st64, stdw, e64, edw = _run(exe, d, f"{itype}_{seed}_{N}_{M}_{threads}", X, threads)
     assert st64 == 0 and stdw == 0
     ref = np.linalg.eigvals(X)
     fin = ref[np.isfinite(ref) & (np.abs(ref) < 1e10)]
@@ -176,9 +181,9 @@ def test_kernel_body_memory_safe_under_asan():
         if r.returncode != 0 and "asan" in (r.stderr + r.stdout).lower():
             pytest.skip("AddressSanitizer runtime not available")
         assert r.returncode == 0, r.stderr
-        for itype, N, M in ((1, 8, 0.5), (2, 8, 0.01)):
+        for itype, N, M, threads in ((1, 8, 0.5, 32), (2, 8, 0.01, 128)):
             X = _operator(itype, 3, N, M)
-            st64, stdw, _, _ = _run(exe, d, f"asan{itype}", X)
+            st64, stdw, _, _ = _run(exe, d, f"asan{itype}", X, threads)
             assert st64 == 0 and stdw == 0
     finally:
         shutil.rmtree(d, ignore_errors=True)

@@ -1,6 +1,6 @@
 // Host stand-ins for the CUDA thread model and intrinsics used by the
 // eigensolver headers, for the CPU tests in tests/host.  A block of
-// g_block_threads std::threads (32 or 128, i.e. one or four warps) runs the
+// g_block_threads std::threads (up to 256, eight warps) runs the
 // device code: a spinning barrier over the block serves __syncthreads, one
 // per warp serves __syncwarp, warp shuffles and votes go through per-warp
 // exchange buffers between two warp barriers, and the rounding intrinsics
@@ -17,7 +17,7 @@
 
 #include <cuda_runtime.h>
 
-#define HOST_MAX_WARPS 4
+#define HOST_MAX_WARPS 8
 
 namespace {
 // generation-counting barrier; waiting threads yield (the block's threads

@@ -46,7 +46,7 @@ COARSE_TRAFFIC_PER_INSTANCE = (25.59e9 + 21.59e9) / 512
 # kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
 KERNEL_WORK = {
     "k_eig_plain": ("eig_fp64", "fp64", "FP64 flops counted by the kernel (Householder reduction + QR sweeps)"),
-    "k_eig_plain_coarse": ("eig_fp64_coarse", "dw", "flops counted by the kernel on the N=32 seed batch, run in "
+    "k_eig_plain_coarse": ("eig_fp64_coarse", "dw", "flops counted by the kernel on the seed batch (N=32 by default), run in "
                            "double-word arithmetic"),
     "k_eig_plain_fallback": ("eig_fp64", "fp64", "FP64 flops counted by the kernel on the fallback instances"),
     "k_lu_c": ("lu_c64", "fp32", "8/3 n^3 real flops per complex64 LU, per factorisation run"),
@@ -372,6 +372,7 @@ def main():
     ap.add_argument("--sur-train", type=int, default=8192)
     ap.add_argument("--sur-count", type=int, default=1024)
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the serving leg (0: skip)")
+    ap.add_argument("--seed-ny", type=int, default=32, help="N of the coarse seed spectrum (stab_set_seed_size)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_setup(args.gpus)
@@ -392,6 +393,7 @@ def main():
     import stab_gb300 as sg
     torch.cuda.set_device(local)
     ctx = sg.Context(local)
+    ctx.set_seed_size(args.seed_ny)
     stream = torch.cuda.Stream()          # a real stream: the legacy default would not order with ours
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
@@ -511,10 +513,10 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64 LU + c128 residual (plain path c128)", "data": "synthetic",
+        "vs_baseline": None, "dtype": "c64 LU, double-word seed eigensolve and retry LU, f64 residuals (plain path c128)", "data": "synthetic",
         "config": {"workload": "temporal sweep: 4096 instances/GPU, N in {48,64,96,128} (n = 240-640), "
                                "alpha~U[.05,.4], beta~U[0,.3], Re~logU[300,3000], M~U[0,2], seed 20261203",
-                   "count_per_gpu": args.count, "seeds": "FP64 full spectrum at N=32",
+                   "count_per_gpu": args.count, "seeds": f"double-word full spectrum at N={args.seed_ny}",
                    "l2": "working set > L2 (393 MB profiles, GBs of matrices); no flush"},
         "e2e": {"value": ok_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1000.0 * e2e_s, "call": "stab_solve_batch (host buffers, pinned)"},

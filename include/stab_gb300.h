@@ -121,6 +121,11 @@ int stab_reset_kernel_stats(stab_ctx* ctx);
 #define STAB_ARITH_FP64 0
 #define STAB_ARITH_DOUBLE_WORD 1
 int stab_set_arithmetic(stab_ctx* ctx, int32_t stage, int32_t arithmetic);
+/* N of the seed spectrum that STAB_MODE_COARSE and STAB_MODE_SURROGATE
+ * take their candidate shifts from (16 <= ny < 48; default 32).  Applies to
+ * batches created afterwards.  A smaller N costs less (the eigensolve grows
+ * as N^3) and resolves fewer least-stable modes.  No reference counterpart. */
+int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,
  * [1] compaction, [2] balancing, [3] Hessenberg reduction, [4] repacking,

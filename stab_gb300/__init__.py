@@ -41,7 +41,7 @@ EXPORTED = (
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
-    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_set_arithmetic",
+    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_set_arithmetic", "stab_set_seed_size",
 )
 
 
@@ -155,6 +155,7 @@ def load(path: str = LIB_PATH):
     lib.stab_autotune.argtypes = [vp, P(i32), i32, P(i32), P(ctypes.c_float)]
     lib.stab_eig_phases.argtypes = [vp, P(ctypes.c_uint64), i32]
     lib.stab_set_arithmetic.argtypes = [vp, i32, i32]
+    lib.stab_set_seed_size.argtypes = [vp, i32]
     lib.stab_lu_cluster_check.argtypes = [vp, i32, i32, i32, P(dbl), P(i32)]
     _lib = lib
     return lib
@@ -404,6 +405,10 @@ class Context:
         """Arithmetic of one stage (stab_set_arithmetic): STAGE_SEED_EIG,
         STAGE_PLAIN_EIG or STAGE_RETRY_LU; ARITH_FP64 or ARITH_DOUBLE_WORD."""
         self._check(self.lib.stab_set_arithmetic(self.h, int(stage), int(arithmetic)))
+
+    def set_seed_size(self, ny: int = 32) -> None:
+        """N of the coarse seed spectrum for batches created afterwards (stab_set_seed_size)."""
+        self._check(self.lib.stab_set_seed_size(self.h, int(ny)))
 
     def reset_arithmetic(self) -> None:
         for st, ar in self.DEFAULT_ARITHMETIC.items():

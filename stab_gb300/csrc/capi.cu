@@ -64,6 +64,7 @@ struct stab_ctx {
   std::map<std::pair<int, int>, int> lu_nb;   // (complex128?, size class) -> tuned LU panel width
   // arithmetic per stage (STAB_STAGE_*)
   int arith[3] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD};
+  int seed_ny = 32;        // N of the seed spectrum of STAB_MODE_COARSE / SURROGATE
 };
 
 // size class of an LU order for the tuned panel-width table
@@ -269,6 +270,7 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   std::unique_ptr<stab_batch> b(new stab_batch());
   b->ctx = c;
   b->count = count;
+  b->coarse_ny = c->seed_ny;
   std::vector<int> idx(count);
   for (int i = 0; i < count; ++i) idx[i] = i;
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return p[a].itype < p[bb].itype; });
@@ -1535,6 +1537,13 @@ int stab_set_arithmetic(stab_ctx* c, int32_t stage, int32_t arithmetic) {
   if (arithmetic != STAB_ARITH_FP64 && arithmetic != STAB_ARITH_DOUBLE_WORD)
     return set_err(c, STAB_ERR_ARG, "arithmetic must be STAB_ARITH_FP64 or STAB_ARITH_DOUBLE_WORD");
   c->arith[stage] = arithmetic;
+  return STAB_OK;
+}
+
+int stab_set_seed_size(stab_ctx* c, int32_t ny) {
+  if (!c) return STAB_ERR_ARG;
+  if (ny < 16 || ny >= kMediumNy) return set_err(c, STAB_ERR_ARG, "seed size must be in [16, 48)");
+  c->seed_ny = ny;
   return STAB_OK;
 }
 

@@ -513,7 +513,9 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64 LU, double-word seed eigensolve and retry LU, f64 residuals (plain path c128)", "data": "synthetic",
+        "vs_baseline": None,
+        "dtype": "c64 LU, double-word seed eigensolve and retry LU, f64 residuals (plain path c128)",
+        "data": "synthetic",
         "config": {"workload": "temporal sweep: 4096 instances/GPU, N in {48,64,96,128} (n = 240-640), "
                                "alpha~U[.05,.4], beta~U[0,.3], Re~logU[300,3000], M~U[0,2], seed 20261203",
                    "count_per_gpu": args.count, "seeds": f"double-word full spectrum at N={args.seed_ny}",

@@ -46,8 +46,8 @@ COARSE_TRAFFIC_PER_INSTANCE = (25.59e9 + 21.59e9) / 512
 # kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
 KERNEL_WORK = {
     "k_eig_plain": ("eig_fp64", "fp64", "FP64 flops counted by the kernel (Householder reduction + QR sweeps)"),
-    "k_eig_plain_coarse": ("eig_fp64_coarse", "dw", "flops counted by the kernel on the seed batch (N=32 by default), run in "
-                           "double-word arithmetic"),
+    "k_eig_plain_coarse": ("eig_fp64_coarse", "dw", "flops counted by the kernel on the seed batch (N=32 by "
+                           "default), run in double-word arithmetic"),
     "k_eig_plain_fallback": ("eig_fp64", "fp64", "FP64 flops counted by the kernel on the fallback instances"),
     "k_lu_c": ("lu_c64", "fp32", "8/3 n^3 real flops per complex64 LU, per factorisation run"),
     "k_lu_z": ("lu_c128", "fp64", "8/3 n^3 real flops per complex128 LU, per factorisation run"),

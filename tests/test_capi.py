@@ -56,3 +56,12 @@ def test_create_without_gpu_reports_error(lib):
     h = ctypes.c_void_p()
     rc = lib.stab_create(ctypes.byref(h), 0)
     assert rc != 0
+
+
+def test_settings_reject_null_context(lib):
+    """The per-stage arithmetic, seed-size and tuning setters check their
+    arguments before touching a device: a null context is STAB_ERR_ARG."""
+    import stab_gb300 as sg
+    assert lib.stab_set_arithmetic(None, sg.STAGE_SEED_EIG, sg.ARITH_FP64) != 0
+    assert lib.stab_set_seed_size(None, 32) != 0
+    assert lib.stab_set_profiling(None, 1) != 0

@@ -10,12 +10,15 @@ Sutherland viscosity with S/T_inf = 0.3815, Pr = 0.72, Streett map with
 ymax = 50 and half the points below y = 2.
 
 One step = one pass of the seeded mixed-precision path over the whole batch
-(STAB_MODE_COARSE: FP64 full spectrum at N = 32 for the shifts, complex64 LU
-shift-invert with FP64 residuals at full N, FP64 fallback on failure).  A
-mode counts as converged when it agrees with the plain FP64 path (the full
-GPU spectrum, itself checked against the CPU oracle by the tests) to
-|d omega| / |omega| <= 1e-10.  The working set (393 MB of profiles and
-~7 GB of matrices) is far larger than L2, so no flush is needed.
+(STAB_MODE_COARSE: a full spectrum at N = 32 in double-word arithmetic for
+the candidate shifts, complex64 LU shift-invert with FP64 residuals at full
+N, a double-word LU retry where that contracts slowly; instances whose seed
+spectrum did not resolve the mode take seeds at N = 48 and then the plain
+FP64 path).  A mode counts as converged when it agrees with the plain FP64
+path (the full GPU spectrum, itself checked against the CPU oracle by the
+tests) to |d omega| / |omega| <= 1e-10 and its eigenvector to 1e-8.  The
+working set (393 MB of profiles and ~7 GB of matrices) is far larger than
+L2, so no flush is needed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -143,10 +146,13 @@ def surrogate_leg(ctx, stream, args):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / 2
         eig, err, iters, st, _ = b.results()
-        ok = int(np.sum((np.abs(eig - truth) / np.abs(truth) <= TOL) & np.isin(st, [sg.ST_OK, sg.ST_FELLBACK])
-                        & (tst == sg.ST_OK)))
-        out[name] = {"value": ok / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms, "converged": ok, "of": n,
-                     "counts": b.counts()}
+        match = (np.abs(eig - truth) / np.abs(truth) <= TOL) & (tst == sg.ST_OK)
+        ok = int(np.sum(match & np.isin(st, [sg.ST_OK, sg.ST_FELLBACK])))
+        unv = int(np.sum(st == sg.ST_UNVERIFIED))
+        unv_ok = int(np.sum(match & (st == sg.ST_UNVERIFIED)))
+        out[name] = {"value": (ok + unv_ok) / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms,
+                     "converged": ok + unv_ok, "converged_trusted_status": ok,
+                     "unverified": unv, "unverified_matching": unv_ok, "of": n, "counts": b.counts()}
     out["total_s"] = time.perf_counter() - t0
     b.close()
     sur.close()
@@ -309,16 +315,28 @@ def reduce_sum(x, world):
     return float(t.item())
 
 
-def cpu_leg(params, prof, sample: int, procs: int):
+def cpu_model() -> str:
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for ln in fh:
+                if ln.lower().startswith(("model name", "cpu part", "hardware")):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_leg(params, prof, sample: int, procs: int, threads: int = 1):
     """The oracle (reference algorithm) on `sample` instances with `procs`
-    single-threaded processes: (modes/s, results, seconds)."""
+    processes of `threads` BLAS threads each: (modes/s, results, seconds)."""
     from oracle import baseline
     jobs = []
     for k in range(sample):
         d = dict(params[k])
         d["profile"] = prof[k]
         jobs.append(d)
-    pool = baseline.pool(procs)
+    pool = baseline.pool(procs, threads)
     try:
         t0 = time.perf_counter()
         out = pool.map(baseline.solve_one, jobs, chunksize=1)
@@ -366,6 +384,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=64)
+    ap.add_argument("--cpu-sample-threaded", type=int, default=16,
+                    help="instances of the one-process multi-threaded CPU mode")
+    ap.add_argument("--plain-reps", type=int, default=3, help="timed passes of the plain FP64 path")
     ap.add_argument("--ref-sample", type=int, default=48)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--surrogate", type=int, default=1, help="1: also run the surrogate-seeded leg")
@@ -380,14 +401,25 @@ def main():
         return run_reference(args, rank, world)
 
     params, prof = workload(args.count, 20261203 + rank)
-    # CPU baseline first: the spawn pool starts before any GPU work
+    # CPU baseline first: the spawn pools start before any GPU work.  Two
+    # modes: (ii) one single-thread process per core over the instances,
+    # (i) one process with one BLAS thread per core; the faster is reported.
     cpu = None
     if rank == 0 and args.cpu_sample > 0:
         procs = os.cpu_count() or 1
         rate, cpu_eig, dt = cpu_leg(params, prof, args.cpu_sample, procs)
-        cpu = {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
-               "sample": f"first {args.cpu_sample} instances of the workload, {dt:.1f} s: oracle restatement of "
-                         "ZGESV+ZGEEV('N','V') (scipy LAPACK), one single-thread process per core"}
+        s1 = max(1, min(args.cpu_sample, args.cpu_sample_threaded))
+        rate1, _, dt1 = cpu_leg(params, prof, s1, 1, procs)
+        modes = {"processes": {"value": rate, "sample": args.cpu_sample, "seconds": dt,
+                               "how": f"{procs} single-thread processes"},
+                 "threads": {"value": rate1, "sample": s1, "seconds": dt1,
+                             "how": f"1 process, OPENBLAS_NUM_THREADS={procs}"}}
+        best = max(modes, key=lambda k: modes[k]["value"])
+        cpu = {"value": modes[best]["value"], "unit": UNIT, "cores": procs, "kind": "port",
+               "cpu_model": cpu_model(), "mode": best, "modes": modes,
+               "sample": f"first {modes[best]['sample']} instances of the workload, "
+                         f"{modes[best]['seconds']:.1f} s: oracle restatement of ZGESV+ZGEEV('N','V') "
+                         f"(scipy LAPACK), {modes[best]['how']}"}
 
     import torch
     import stab_gb300 as sg
@@ -406,14 +438,19 @@ def main():
     # LU panel widths for the orders of this workload and of the N = 32 seeds
     tune = ctx.autotune(sorted({5 * d["ny"] for d in params} | {160}))
 
-    # reference result: plain FP64 full spectrum on every instance (timed once)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
+    # reference result: plain FP64 full spectrum on every instance; one
+    # untimed pass (pool growth, first-use costs), then args.plain_reps timed
     batch.run(sg.MODE_PLAIN)
-    e1.record(stream)
     torch.cuda.synchronize()
-    plain_ms = e0.elapsed_time(e1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    plain_times = []
+    for _ in range(args.plain_reps):
+        e0.record(stream)
+        batch.run(sg.MODE_PLAIN)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_times.append(e0.elapsed_time(e1))
+    plain_ms = statistics.mean(plain_times)
     ref_eig, _, _, ref_st, ref_vec = batch.results(want_vectors=True)
     plain_work = batch.work()
 
@@ -444,6 +481,11 @@ def main():
     ok = ok_val & (vdiff <= VEC_TOL)
     converged_local = int(np.sum(ok))
     fell = int(np.sum(status == sg.ST_FELLBACK))
+    # trusted statuses whose eigenvalue is not the plain path's least-stable one
+    wrong_trusted = np.nonzero(np.isin(status, [sg.ST_OK, sg.ST_FELLBACK]) & (ref_st == sg.ST_OK)
+                               & ~(rel <= TOL))[0]
+    st_hist = {int(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))}
+    counts_last = batch.counts()
 
     # per-kernel breakdown of one extra step (CUDA events on the launch stream)
     ctx.reset_kernel_stats()
@@ -525,9 +567,16 @@ def main():
         "converged": {"count": int(converged), "of": total, "fell_back": fell,
                       "criteria": "|d omega|/|omega| <= 1e-10 and eigenvector within 1e-8 after phase normalisation",
                       "eigenvalue_only": int(np.sum(ok_val)),
+                      "status_histogram": st_hist, "stages": counts_last,
+                      "trusted_but_wrong": int(wrong_trusted.size),
+                      "trusted_but_wrong_examples": [
+                          {"index": int(q), "got": [float(eig[q].real), float(eig[q].imag)],
+                           "plain": [float(ref_eig[q].real), float(ref_eig[q].imag)], "status": int(status[q])}
+                          for q in wrong_trusted[:5]],
                       "max_rel_err": float(np.nanmax(rel[ok])) if np.any(ok) else None,
                       "max_vec_err": float(np.nanmax(vdiff[ok])) if np.any(ok) else None},
         "plain_fp64": {"value": total / (plain_ms / 1000.0), "unit": UNIT, "ms_per_step": plain_ms,
+                       "ms_repeats": plain_times, "warmup": 1,
                        "speedup_seeded_over_plain": value / (total / (plain_ms / 1000.0))},
         "roofline": roof,
         "kernel_rooflines": rooflines,

@@ -45,12 +45,20 @@ extern "C" {
 #define STAB_ST_NAN 3         /* non-finite value in the inputs or results      */
 #define STAB_ST_FELLBACK 4    /* polish did not converge; plain FP64 path used   */
 #define STAB_ST_NOMODE 5      /* no eigenvalue passed the least-stable filter    */
+#define STAB_ST_UNVERIFIED 6  /* STAB_MODE_SURROGATE: a converged eigenpair from *
+                               * the caller's seed that no resolved spectrum     *
+                               * confirmed as the least-stable mode              */
 
 /* solve modes for stab_batch_run / stab_solve_batch */
 #define STAB_MODE_PLAIN 0     /* FP64 full spectrum + least-stable eigenvector   */
 #define STAB_MODE_SEEDED 1    /* mixed-precision polish from caller seeds        */
-#define STAB_MODE_COARSE 2    /* seeds from an FP64 full spectrum at N = 32,     *
-                               * then the mixed-precision polish                 */
+#define STAB_MODE_COARSE 2    /* seeds from a full spectrum at N = 32, then the  *
+                               * mixed-precision polish.  STAB_ST_OK only where  *
+                               * a seed candidate (in selection order) polished  *
+                               * to within 1e-7 of itself: the seed spectrum     *
+                               * resolved the mode.  Every other instance takes  *
+                               * seeds from N = 48 under the same rule, then the *
+                               * plain FP64 path (STAB_ST_FELLBACK)              */
 #define STAB_MODE_TRACK 4     /* polish from caller guesses; where it fails, the *
                                * FP64 spectrum's eigenvalue nearest the guess    *
                                * (the pick of getab.f90:185-192)                 */
@@ -257,7 +265,11 @@ int64_t stab_eigfunction_text(const stab_evec_header* h, const double* y, const 
 /*
  * Upload `count` instances (parameters + profiles) to device memory.
  * profiles[k] points at nym[k] x 6 doubles; identical pointers are uploaded
- * once.  The instances may have different ny and itype.
+ * once.  The instances may have different ny and itype.  The call copies
+ * everything it needs and synchronises before it returns: the caller may
+ * free or reuse p, nym and the profile buffers at once.  Each batch keeps
+ * its own state; batches of different contexts may be used from different
+ * host threads.
  */
 int stab_batch_create(stab_ctx* ctx, int32_t count, const stab_params* p, const int32_t* nym,
                       const double* const* profiles, stab_batch** out);
@@ -274,10 +286,14 @@ int stab_batch_set_seeds(stab_batch* b, const double* seeds);
 int stab_batch_set_start(stab_batch* b, const double* coef, int32_t ncheb);
 /*
  * Run the whole path on the device.  STAB_MODE_SURROGATE polishes the coarse
- * candidates and then, for the instances not yet final, the caller's seed
- * (a surrogate's prediction); the least-stable converged pair wins.  It adds
- * what the N = 32 spectrum cannot give: discrete modes that N = 32 does not
- * resolve (supersonic second modes), whose coarse candidates are spurious.
+ * candidates and then, for the instances that no resolved candidate settled,
+ * the caller's seed (a surrogate's prediction).  Where the seed's converged
+ * pair is the least stable of the converged pairs it is kept with
+ * STAB_ST_UNVERIFIED (nothing but the seed supports it); the other
+ * unsettled instances take the fallback chain of STAB_MODE_COARSE.  The
+ * seed adds what the N = 32 spectrum cannot give: discrete modes that
+ * N = 32 does not resolve (supersonic second modes), whose coarse candidates
+ * are spurious.
  */
 int stab_batch_run(stab_batch* b, int32_t mode);
 /* After a STAB_MODE_PLAIN run: every instance's full spectrum, sorted as
@@ -287,8 +303,8 @@ int stab_batch_run(stab_batch* b, int32_t mode);
 int stab_batch_spectra(stab_batch* b, double* const* eig_out);
 /* After a run: counts_out[0] instances resolved by the first stage (the
  * seeds, the coarse candidates, or the plain path), [1] whose kept pair came
- * from the caller's seed in STAB_MODE_SURROGATE, [2] sent to the FP64
- * fallback. */
+ * from the caller's seed in STAB_MODE_SURROGATE (STAB_ST_UNVERIFIED), [2]
+ * sent to the fallback chain (N = 48 seeds, then the plain FP64 path). */
 int stab_batch_counts(stab_batch* b, int32_t* counts_out);
 /*
  * Copy results back (synchronises): eig_out[2*k] least-stable eigenvalue,
@@ -363,7 +379,13 @@ int stab_mlp_destroy(stab_mlp* m);
  * call: calls that overlap on the GPU (different streams, or different host
  * threads) race and must be serialised by the caller.  The first call on a
  * device looks up that array's device address, so make it before any stream
- * capture.  Needs no stab_ctx.
+ * capture; a lookup that fails returns STAB_ERR_CUDA and is tried again by
+ * the next call.  Under CUDA's lazy module loading (the default) that first
+ * call also makes the driver load this part of the library on the device
+ * and allocate the array then: make it at start-up, or set
+ * CUDA_MODULE_LOADING=EAGER to have the array created when the library
+ * loads.  Later calls allocate nothing.  Each call adds its cycles to the
+ * counters stab_eig_phases reads.  Needs no stab_ctx.
  */
 int stab_eigvals_noalloc(const double* a_dev, int32_t m, double* eig_dev, int32_t* status_dev, void* stream);
 

@@ -60,9 +60,9 @@ def select_least(eig, d):
     return bi
 
 
-def pool(processes):
-    """Spawn-started pool with one BLAS thread per process."""
+def pool(processes, threads=1):
+    """Spawn-started pool with `threads` BLAS threads per process."""
     import multiprocessing as mp
     for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ[k] = "1"
+        os.environ[k] = str(int(threads))
     return mp.get_context("spawn").Pool(processes)

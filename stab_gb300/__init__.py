@@ -21,7 +21,8 @@ import numpy as np
 
 __all__ = ["StabParams", "EvecHeader", "Context", "Network", "load", "LIB_PATH", "parse_input", "profile_name",
            "read_profile", "grid", "write_evec", "read_evec", "getevec_select", "eigfunction_text", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE", "MODE_SURROGATE", "MODE_TRACK",
-           "ST_OK", "ST_SINGULAR", "ST_NOCONV", "ST_NAN", "ST_FELLBACK", "ST_NOMODE", "StabError"]
+           "ST_OK", "ST_SINGULAR", "ST_NOCONV", "ST_NAN", "ST_FELLBACK", "ST_NOMODE", "ST_UNVERIFIED",
+           "StabError"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libstab_gb300.so")
@@ -30,7 +31,7 @@ MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE, MODE_TRACK = 0, 1, 2, 3, 4
 # arithmetic per stage (stab_set_arithmetic)
 STAGE_SEED_EIG, STAGE_PLAIN_EIG, STAGE_RETRY_LU = 0, 1, 2
 ARITH_FP64, ARITH_DOUBLE_WORD = 0, 1
-ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE = 0, 1, 2, 3, 4, 5
+ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE, ST_UNVERIFIED = 0, 1, 2, 3, 4, 5, 6
 
 EXPORTED = (
     "stab_abi_version", "stab_create", "stab_destroy", "stab_last_error", "stab_set_stream", "stab_sync",

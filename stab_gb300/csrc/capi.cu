@@ -33,6 +33,10 @@ static const double kQuickAcceptTol = 1e-7;
 // a complex64 polish that needed this many Newton-chord steps or more is
 // retried with complex128 factors (slow contraction: an unresolved cluster)
 static const int kSlowNewton = 14;
+// `done` value of an instance whose kept pair came from the caller's seed in
+// STAB_MODE_SURROGATE without a resolved coarse candidate: a converged
+// eigenpair that nothing verified as the least-stable (STAB_ST_UNVERIFIED)
+static const int kDoneUnverified = 5;
 
 namespace {
 
@@ -197,7 +201,8 @@ cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
 struct stab_batch {
   stab_ctx* ctx = nullptr;
   int count = 0, tcount = 0;             // tcount temporal instances first
-  std::vector<stab_params> P;            // internal order
+  std::vector<stab_params> P;            // internal order (ny of the solve)
+  std::vector<stab_params> Pin;          // internal order, the caller's parameters unchanged
   std::vector<int> perm;                 // internal k -> caller index
   std::vector<InstDesc> hd;
   std::vector<int32_t> hn, hm;
@@ -211,6 +216,13 @@ struct stab_batch {
   DevBuf bad, flops, rsc, csc, cand, accepted, skip64, lus32, lus64, have, best_key, best_theta, best_err, best_iters, best_out;
   DevBuf piv, info, flags, theta, sigma, least_raw, least_val, least_idx, pcol, done, err, iters, status, counter;
   int nprof = 0;
+  // profile pools in use: this batch's own (prof, spl, bad, pdesc), or its
+  // parent's for a sub-batch (shared_prof), whose prep skips k_spline
+  bool shared_prof = false;
+  const double* prof_p = nullptr;
+  double* spl_p = nullptr;
+  int32_t* bad_p = nullptr;
+  const ProfDesc* pdesc_p = nullptr;
   bool have_seeds = false;
   std::vector<double> seeds;             // caller order, 2 per instance
   int last_mode = -1;
@@ -244,7 +256,7 @@ struct stab_batch {
                      &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
                      &bad, &flops, &rsc, &csc, &cand, &accepted, &skip64, &lus32, &lus64, &have, &best_key, &best_theta, &best_err,
                      &best_iters, &best_out, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
-                     &done, &err, &iters, &status, &counter};
+                     &done, &err, &iters, &status, &counter, &startc, &seed_raw, &best_src};
     for (DevBuf* d : all) {
       if (d->p) cudaFreeAsync(d->p, d->st);
       d->p = nullptr;
@@ -264,94 +276,59 @@ struct stab_batch {
 
 stab_batch::~stab_batch() { delete coarse; }
 
-static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const int32_t* nym,
-                       const double* const* profiles, stab_batch** out, int force_ny) {
-  if (!c || count <= 0 || !p || !nym || !profiles || !out) return set_err(c, STAB_ERR_ARG, "null argument or count <= 0");
-  std::unique_ptr<stab_batch> b(new stab_batch());
-  b->ctx = c;
-  b->count = count;
-  b->coarse_ny = c->seed_ny;
-  std::vector<int> idx(count);
-  for (int i = 0; i < count; ++i) idx[i] = i;
-  std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return p[a].itype < p[bb].itype; });
-  b->perm = idx;
-  // profiles: dedupe by pointer; copied straight from caller memory in
-  // contiguous runs (validated on the device by k_spline)
-  std::map<const double*, int> pidx;
-  std::vector<ProfDesc> pds;
-  std::vector<std::pair<const double*, int64_t>> runs;   // (source, doubles)
-  int64_t prof_off = 0, spl_off = 0;
-  for (int i = 0; i < count; ++i) {
-    const double* pp = profiles[i];
-    if (!pp) return set_err(c, STAB_ERR_ARG, "null profile pointer");
-    if (nym[i] < 4) return set_err(c, STAB_ERR_ARG, "profile needs at least 4 rows");
-    auto it = pidx.find(pp);
-    if (it != pidx.end()) {
-      if (pds[it->second].nym != nym[i]) return set_err(c, STAB_ERR_ARG, "same profile pointer with different nym");
-      continue;
-    }
-    ProfDesc pd{};
-    pd.off_prof = prof_off;
-    pd.off_spl = spl_off;
-    pd.nym = nym[i];
-    const int64_t len = (int64_t)nym[i] * 6;
-    if (!runs.empty() && runs.back().first + runs.back().second == pp) runs.back().second += len;
-    else runs.push_back({pp, len});
-    prof_off += len;
-    spl_off += len;
-    pidx[pp] = (int)pds.size();
-    pds.push_back(pd);
-  }
-  b->nprof = (int)pds.size();
-  // tables
+// Descriptor of one instance from its run parameters (validated) and the
+// entry of its mean profile in the profile pools.
+static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDesc& pd, InstDesc& d) {
+  if (q.itype != 1 && q.itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal) or 2 (spatial)");
+  if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
+  if (q.curve != 0) return set_err(c, STAB_ERR_ARG, "curve != 0 (curved walls) is not supported");
+  if (q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider = 0 (external derivatives) is not supported");
+  if (q.wallt != 0 && q.wallt != 2) return set_err(c, STAB_ERR_ARG, "Illegal value of wallt");
+  if (q.yi == 0.0) return set_err(c, STAB_ERR_ARG, "Yi = 0 (tanh map) is not supported");
+  if (q.mattyp != 0 && q.mattyp != 1) return set_err(c, STAB_ERR_ARG, "mattyp must be 0 or 1");
+  if (!(q.Ma > 0.0)) return set_err(c, STAB_ERR_ARG, "Ma must be > 0");
+  d = InstDesc{};
+  d.ny = q.ny;
+  d.n = 5 * q.ny;
+  d.itype = q.itype;
+  d.m = (q.itype == 1) ? d.n : 2 * d.n;
+  d.wallt = q.wallt;
+  d.top = q.top;
+  d.mattyp = q.mattyp;
+  d.navier = !(q.Re >= 1.0e98 || q.Re == 0.0);
+  d.Ma = q.Ma;
+  d.Re = q.Re;
+  d.Pr = q.Pr;
+  d.Te = (q.mattyp == 1) ? q.T0 : 0.0;   // input.f90:25 runs before Ma is read
+  d.yi = q.yi;
+  d.ymax = q.ymax;
+  d.ar = q.alpha[0]; d.ai = q.alpha[1];
+  d.br = q.beta[0]; d.bi = q.beta[1];
+  d.wr = q.omega[0]; d.wi = q.omega[1];
+  d.iprof = iprof;
+  d.nym = pd.nym;
+  d.off_prof = pd.off_prof;
+  d.off_spl = pd.off_spl;
+  return 0;
+}
+
+// Tables, offsets and pools of a batch whose P / Pin / perm / hd (profile
+// fields filled) are set: node, block and vector offsets, derivative
+// tables, per-instance offset arrays and the fixed-size device buffers.
+static int batch_finish(stab_ctx* c, stab_batch* b) {
+  const int count = b->count;
   std::vector<int> tab_ny;
   int64_t node_off = 0, blk_off = 0, vec_off = 0;
-  for (int k = 0; k < count; ++k) {
-    const int u = idx[k];
-    stab_params q = p[u];
-    if (force_ny > 0) q.ny = force_ny;
-    if (q.itype != 1 && q.itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal) or 2 (spatial)");
-    if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
-    if (q.curve != 0) return set_err(c, STAB_ERR_ARG, "curve != 0 (curved walls) is not supported");
-    if (q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider = 0 (external derivatives) is not supported");
-    if (q.wallt != 0 && q.wallt != 2) return set_err(c, STAB_ERR_ARG, "Illegal value of wallt");
-    if (q.yi == 0.0) return set_err(c, STAB_ERR_ARG, "Yi = 0 (tanh map) is not supported");
-    if (q.mattyp != 0 && q.mattyp != 1) return set_err(c, STAB_ERR_ARG, "mattyp must be 0 or 1");
-    if (!(q.Ma > 0.0)) return set_err(c, STAB_ERR_ARG, "Ma must be > 0");
-    b->P.push_back(q);
-    if (std::find(tab_ny.begin(), tab_ny.end(), q.ny) == tab_ny.end()) tab_ny.push_back(q.ny);
-    InstDesc d{};
-    d.ny = q.ny;
-    d.n = 5 * q.ny;
-    d.itype = q.itype;
-    d.m = (q.itype == 1) ? d.n : 2 * d.n;
-    d.wallt = q.wallt;
-    d.top = q.top;
-    d.mattyp = q.mattyp;
-    d.navier = !(q.Re >= 1.0e98 || q.Re == 0.0);
-    d.Ma = q.Ma;
-    d.Re = q.Re;
-    d.Pr = q.Pr;
-    d.Te = (q.mattyp == 1) ? q.T0 : 0.0;   // input.f90:25 runs before Ma is read
-    d.yi = q.yi;
-    d.ymax = q.ymax;
-    d.ar = q.alpha[0]; d.ai = q.alpha[1];
-    d.br = q.beta[0]; d.bi = q.beta[1];
-    d.wr = q.omega[0]; d.wi = q.omega[1];
-    const int ip = pidx[profiles[u]];
-    const ProfDesc& pd = pds[ip];
-    d.iprof = ip;
-    d.nym = pd.nym;
-    d.off_prof = pd.off_prof;
-    d.off_spl = pd.off_spl;
+  b->tcount = 0;
+  for (auto& d : b->hd) {
+    if (std::find(tab_ny.begin(), tab_ny.end(), d.ny) == tab_ny.end()) tab_ny.push_back(d.ny);
     d.off_node = node_off;
     d.off_blk = blk_off;
     d.off_vec = vec_off;
     node_off += (int64_t)NODE_STRIDE * d.ny;
     blk_off += (int64_t)BLK_STRIDE * d.ny;
     vec_off += (int64_t)VEC_SLOTS * d.n;
-    if (q.itype == 1) b->tcount++;
-    b->hd.push_back(d);
+    if (d.itype == 1) b->tcount++;
   }
   for (int ny : tab_ny) {
     int r = ensure_dtab(c, ny);
@@ -385,17 +362,6 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   cudaStream_t s = c->stream;
   CK(c, upload(b->desc, b->hd, s));
   CK(c, upload(b->dtab, hdt, s));
-  CK(c, upload(b->pdesc, pds, s));
-  CK(c, b->prof.ensure(sizeof(double) * std::max<int64_t>(prof_off, 1), c->stream));
-  {
-    int64_t o = 0;
-    for (auto& r : runs) {
-      CK(c, cudaMemcpyAsync(b->prof.as<double>() + o, r.first, sizeof(double) * r.second, cudaMemcpyHostToDevice, s));
-      o += r.second;
-    }
-  }
-  CK(c, b->spl.ensure(sizeof(double) * std::max<int64_t>(spl_off, 1), c->stream));
-  CK(c, b->bad.ensure(sizeof(int32_t) * std::max(b->nprof, 1), c->stream));
   CK(c, b->node.ensure(sizeof(double) * node_off, c->stream));
   CK(c, b->blk.ensure(sizeof(zc) * blk_off, c->stream));
   CK(c, b->ops.ensure(sizeof(zc) * (blk_off / BLK_STRIDE) * 75, c->stream));
@@ -444,6 +410,121 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   CK(c, b->accepted.ensure(I4, c->stream));
   CK(c, b->counter.ensure(sizeof(int32_t) * 4, c->stream));
   CK(c, cudaStreamSynchronize(s));
+  return 0;
+}
+
+// A batch from caller memory.  The profiles are copied to the device here
+// (deduplicated by pointer, in contiguous runs) and the call synchronises
+// before it returns, so the caller may free or reuse its buffers at once.
+static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const int32_t* nym,
+                       const double* const* profiles, stab_batch** out) {
+  if (!c || count <= 0 || !p || !nym || !profiles || !out) return set_err(c, STAB_ERR_ARG, "null argument or count <= 0");
+  std::unique_ptr<stab_batch> b(new stab_batch());
+  b->ctx = c;
+  b->count = count;
+  b->coarse_ny = c->seed_ny;
+  std::vector<int> idx(count);
+  for (int i = 0; i < count; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return p[a].itype < p[bb].itype; });
+  b->perm = idx;
+  // profiles: dedupe by pointer; copied straight from caller memory in
+  // contiguous runs (validated on the device by k_spline)
+  std::map<const double*, int> pidx;
+  std::vector<ProfDesc> pds;
+  std::vector<std::pair<const double*, int64_t>> runs;   // (source, doubles)
+  int64_t prof_off = 0, spl_off = 0;
+  for (int i = 0; i < count; ++i) {
+    const double* pp = profiles[i];
+    if (!pp) return set_err(c, STAB_ERR_ARG, "null profile pointer");
+    if (nym[i] < 4) return set_err(c, STAB_ERR_ARG, "profile needs at least 4 rows");
+    auto it = pidx.find(pp);
+    if (it != pidx.end()) {
+      if (pds[it->second].nym != nym[i]) return set_err(c, STAB_ERR_ARG, "same profile pointer with different nym");
+      continue;
+    }
+    ProfDesc pd{};
+    pd.off_prof = prof_off;
+    pd.off_spl = spl_off;
+    pd.nym = nym[i];
+    const int64_t len = (int64_t)nym[i] * 6;
+    if (!runs.empty() && runs.back().first + runs.back().second == pp) runs.back().second += len;
+    else runs.push_back({pp, len});
+    prof_off += len;
+    spl_off += len;
+    pidx[pp] = (int)pds.size();
+    pds.push_back(pd);
+  }
+  b->nprof = (int)pds.size();
+  for (int k = 0; k < count; ++k) {
+    const int u = idx[k];
+    const int ip = pidx[profiles[u]];
+    InstDesc d;
+    int rc = make_desc(c, p[u], ip, pds[ip], d);
+    if (rc) return rc;
+    b->P.push_back(p[u]);
+    b->Pin.push_back(p[u]);
+    b->hd.push_back(d);
+  }
+  cudaStream_t s = c->stream;
+  CK(c, upload(b->pdesc, pds, s));
+  CK(c, b->prof.ensure(sizeof(double) * std::max<int64_t>(prof_off, 1), c->stream));
+  {
+    int64_t o = 0;
+    for (auto& r : runs) {
+      CK(c, cudaMemcpyAsync(b->prof.as<double>() + o, r.first, sizeof(double) * r.second, cudaMemcpyHostToDevice, s));
+      o += r.second;
+    }
+  }
+  CK(c, b->spl.ensure(sizeof(double) * std::max<int64_t>(spl_off, 1), c->stream));
+  CK(c, b->bad.ensure(sizeof(int32_t) * std::max(b->nprof, 1), c->stream));
+  b->prof_p = b->prof.as<double>();
+  b->spl_p = b->spl.as<double>();
+  b->bad_p = b->bad.as<int32_t>();
+  b->pdesc_p = b->pdesc.as<ProfDesc>();
+  int rc = batch_finish(c, b.get());
+  if (rc) return rc;
+  *out = b.release();
+  return 0;
+}
+
+// A batch of instances ks (internal indices, ascending) of `parent`, with
+// ny forced to force_ny when > 0 (the seed spectra) and the caller's ny
+// otherwise (the fallback).  It reads the parent's device-resident profiles
+// and their spline tables, so its prep skips k_spline: the parent must have
+// run its prep in the same pass, and must outlive the child.  Internal order
+// is the parent's order restricted to ks (still temporal first), perm[q] = q.
+static int batch_build_child(stab_batch* parent, const std::vector<int>& ks, int force_ny, stab_batch** out) {
+  stab_ctx* c = parent->ctx;
+  if (ks.empty()) return set_err(c, STAB_ERR_ARG, "empty sub-batch");
+  std::unique_ptr<stab_batch> b(new stab_batch());
+  b->ctx = c;
+  b->count = (int)ks.size();
+  b->coarse_ny = parent->coarse_ny;
+  b->shared_prof = true;
+  b->nprof = parent->nprof;
+  b->prof_p = parent->prof_p;
+  b->spl_p = parent->spl_p;
+  b->bad_p = parent->bad_p;
+  b->pdesc_p = parent->pdesc_p;
+  for (int q = 0; q < b->count; ++q) {
+    const int k = ks[q];
+    stab_params pq = parent->Pin[k];
+    if (force_ny > 0) pq.ny = force_ny;
+    const InstDesc& pd0 = parent->hd[k];
+    ProfDesc pd{};
+    pd.off_prof = pd0.off_prof;
+    pd.off_spl = pd0.off_spl;
+    pd.nym = pd0.nym;
+    InstDesc d;
+    int rc = make_desc(c, pq, pd0.iprof, pd, d);
+    if (rc) return rc;
+    b->perm.push_back(q);
+    b->P.push_back(pq);
+    b->Pin.push_back(parent->Pin[k]);
+    b->hd.push_back(d);
+  }
+  int rc = batch_finish(c, b.get());
+  if (rc) return rc;
   *out = b.release();
   return 0;
 }
@@ -458,17 +539,18 @@ static int run_prep(stab_batch* b) {
   cudaStream_t s = c->stream;
   const InstDesc* D = b->desc.as<InstDesc>();
   const double* const* T = b->dtab.as<const double*>();
-  CK(c, timed(c, "k_spline", [&] {
-    k_spline<<<(b->nprof + 63) / 64, 64, 0, s>>>(b->nprof, b->pdesc.as<ProfDesc>(), b->prof.as<double>(),
-                                                  b->spl.as<double>(), b->bad.as<int32_t>());
-    return cudaGetLastError();
-  }));
+  if (!b->shared_prof) {
+    CK(c, timed(c, "k_spline", [&] {
+      k_spline<<<(b->nprof + 63) / 64, 64, 0, s>>>(b->nprof, b->pdesc_p, b->prof_p, b->spl_p, b->bad_p);
+      return cudaGetLastError();
+    }));
+  }
   const int nymax = b->nmax / 5;
   CK(c, cudaMemsetAsync(b->flags.p, 0, sizeof(int32_t) * b->count, s));
   CK(c, timed(c, "k_nodes", [&] {
     dim3 g((nymax + 127) / 128, b->count);
-    k_nodes<<<g, 128, 0, s>>>(b->count, D, b->prof.as<double>(), b->spl.as<double>(), b->node.as<double>(),
-                              b->bad.as<int32_t>(), b->flags.as<int32_t>());
+    k_nodes<<<g, 128, 0, s>>>(b->count, D, b->prof_p, b->spl_p, b->node.as<double>(), b->bad_p,
+                              b->flags.as<int32_t>());
     return cudaGetLastError();
   }));
   CK(c, timed(c, "k_meanderiv", [&] {
@@ -843,7 +925,8 @@ static void finalize_polish_host(std::vector<zc>& val, std::vector<int32_t>& st,
       double d = l.x * l.x + l.y * l.y;
       val[k] = d > 0 ? zmk(l.x / d, -l.y / d) : zmk(0.0, 0.0);
     }
-    st[k] = (dn[k] == 1) ? STAB_ST_OK : (dn[k] == 3 ? STAB_ST_NAN : STAB_ST_NOCONV);
+    st[k] = (dn[k] == 1) ? STAB_ST_OK
+            : (dn[k] == 3 ? STAB_ST_NAN : (dn[k] == kDoneUnverified ? STAB_ST_UNVERIFIED : STAB_ST_NOCONV));
   }
 }
 
@@ -912,16 +995,6 @@ static int batch_run(stab_batch* b, int32_t mode) {
   b->ran = true;
   return 0;
 }
-
-// ---------------------------------------------------------------------------
-// the coarse-seed wrapper keeps the caller inputs to build the N = 32 batch
-// ---------------------------------------------------------------------------
-struct BatchInputs {
-  std::vector<stab_params> p;
-  std::vector<int32_t> nym;
-  std::vector<const double*> prof;
-};
-static std::map<stab_batch*, BatchInputs> g_inputs;
 
 extern "C" {
 
@@ -1025,14 +1098,9 @@ int stab_batch_create(stab_ctx* c, int32_t count, const stab_params* p, const in
                       const double* const* profiles, stab_batch** out) {
   if (!c) return STAB_ERR_ARG;
   cudaSetDevice(c->device);
-  int rc = batch_build(c, count, p, nym, profiles, out, 0);
+  int rc = batch_build(c, count, p, nym, profiles, out);
   if (rc) return rc;
   c->live.push_back(*out);
-  BatchInputs in;
-  in.p.assign(p, p + count);
-  in.nym.assign(nym, nym + count);
-  in.prof.assign(profiles, profiles + count);
-  g_inputs[*out] = std::move(in);
   return STAB_OK;
 }
 
@@ -1046,12 +1114,11 @@ int stab_batch_set_seeds(stab_batch* b, const double* seeds) {
 
 static int coarse_seeds(stab_batch* b) {
   stab_ctx* c = b->ctx;
-  auto it = g_inputs.find(b);
-  if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
   if (!b->coarse) {
+    std::vector<int> all(b->count);
+    for (int k = 0; k < b->count; ++k) all[k] = k;
     stab_batch* cb = nullptr;
-    int rc = batch_build(c, b->count, it->second.p.data(), it->second.nym.data(), it->second.prof.data(), &cb,
-                         b->coarse_ny);
+    int rc = batch_build_child(b, all, b->coarse_ny, &cb);
     if (rc) return rc;
     b->coarse = cb;
   }
@@ -1097,6 +1164,7 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
   // per candidate: a complex64 round, then a complex128 retry for the
   // instances where it failed or contracted slowly
   CK(c, b->best_src.ensure(sizeof(int32_t) * n, s));
+  CK(c, cudaMemsetAsync(b->best_src.p, 0xff, sizeof(int32_t) * n, s));
   const int rounds = 2 * kShiftCandidates + (extra ? 2 : 0);
   for (int r = 0; r < rounds; ++r) {
     const int j = r / 2;
@@ -1132,7 +1200,7 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
                                     b->done.as<int32_t>(), b->err.as<double>(), b->iters.as<int32_t>(),
                                     b->outvec.as<zc>(), b->off_mof.as<int64_t>(), fin, b->have.as<int32_t>(),
                                     b->best_key.as<double>(), b->best_theta.as<zc>(), b->best_err.as<double>(),
-                                    b->best_iters.as<int32_t>(), b->best_out.as<zc>(), 1,
+                                    b->best_iters.as<int32_t>(), b->best_out.as<zc>(), surrogate ? 0 : 1,
                                     kQuickAcceptTol, fp64 ? nullptr : b->skip64.as<int32_t>(), kSlowNewton, j,
                                     b->best_src.as<int32_t>());
       return cudaGetLastError();
@@ -1142,7 +1210,8 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
     k_take_best<<<n, 128, 0, s>>>(n, b->desc.as<InstDesc>(), b->have.as<int32_t>(), b->best_theta.as<zc>(),
                                   b->best_err.as<double>(), b->best_iters.as<int32_t>(), b->best_out.as<zc>(),
                                   b->off_mof.as<int64_t>(), b->theta.as<zc>(), b->done.as<int32_t>(),
-                                  b->err.as<double>(), b->iters.as<int32_t>(), b->outvec.as<zc>());
+                                  b->err.as<double>(), b->iters.as<int32_t>(), b->outvec.as<zc>(), fin,
+                                  b->best_src.as<int32_t>(), kShiftCandidates, kDoneUnverified);
     return cudaGetLastError();
   }));
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
@@ -1169,35 +1238,16 @@ static int run_fallback(stab_batch* b, bool track = false) {
   b->fb_vec.clear();
   b->fb_err.clear();
   b->fb_iters.clear();
-  for (int k = 0; k < n; ++k)
-    if (dn[k] != 1) b->fell_back.push_back(k);
-  b->counts[0] = n - (int)b->fell_back.size();
-  b->counts[1] = 0;
+  b->counts[0] = b->counts[1] = 0;
+  for (int k = 0; k < n; ++k) {
+    if (dn[k] == 1) b->counts[0] += 1;
+    else if (dn[k] == kDoneUnverified) b->counts[1] += 1;
+    else b->fell_back.push_back(k);
+  }
   b->counts[2] = (int)b->fell_back.size();
-  if (b->last_mode == STAB_MODE_SURROGATE) {
-    std::vector<int32_t> src(n), hv(n);
-    CK(c, cudaMemcpyAsync(src.data(), b->best_src.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
-    CK(c, cudaMemcpyAsync(hv.data(), b->have.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
-    CK(c, cudaStreamSynchronize(c->stream));
-    for (int k = 0; k < n; ++k)
-      if (dn[k] == 1 && hv[k] && src[k] == kShiftCandidates) b->counts[1] += 1;
-    b->counts[0] -= b->counts[1];
-  }
   if (b->fell_back.empty()) return 0;
-  auto it = g_inputs.find(b);
-  if (it == g_inputs.end()) return set_err(c, STAB_ERR_STATE, "batch inputs not recorded");
-  const BatchInputs& in = it->second;
-  std::vector<stab_params> fp;
-  std::vector<int32_t> fn;
-  std::vector<const double*> fpr;
-  for (int k : b->fell_back) {
-    const int u = b->perm[k];
-    fp.push_back(in.p[u]);
-    fn.push_back(in.nym[u]);
-    fpr.push_back(in.prof[u]);
-  }
   stab_batch* fb = nullptr;
-  int rc = batch_build(c, (int)fp.size(), fp.data(), fn.data(), fpr.data(), &fb, 0);
+  int rc = batch_build_child(b, b->fell_back, 0, &fb);
   if (rc) return rc;
   std::unique_ptr<stab_batch> guard(fb);
   if (!track && b->coarse_ny < kMediumNy) {
@@ -1206,8 +1256,6 @@ static int run_fallback(stab_batch* b, bool track = false) {
     // eigensolve's cost for the large instances; its own failures take the
     // plain path.  Results keep the fallback status.
     fb->coarse_ny = kMediumNy;
-    BatchInputs sub{fp, fn, fpr};
-    g_inputs[fb] = sub;
     rc = stab_batch_run(fb, STAB_MODE_COARSE);
     const int nf = fb->count;
     std::vector<double> eig(2 * (size_t)nf), er(nf), w(4, 0.0);
@@ -1220,7 +1268,6 @@ static int run_fallback(stab_batch* b, bool track = false) {
     }
     if (rc == 0) rc = stab_batch_results(fb, eig.data(), er.data(), itv.data(), st.data(), vp.data());
     if (rc == 0) rc = stab_batch_work(fb, w.data());
-    g_inputs.erase(fb);
     if (rc) return rc;
     for (int i = 0; i < 4; ++i) b->fb_work[i] += w[i];
     b->fb_val.assign(nf, zmk(0, 0));
@@ -1673,7 +1720,6 @@ int stab_batch_work(stab_batch* b, double* work_out) {
 
 int stab_batch_destroy(stab_batch* b) {
   if (!b) return STAB_ERR_ARG;
-  g_inputs.erase(b);
   if (!b->ctx) {            // context already destroyed: device memory is gone
     delete b;
     return STAB_OK;
@@ -1706,7 +1752,7 @@ int stab_assemble(stab_ctx* c, const stab_params* p, int32_t nym, const double* 
   cudaSetDevice(c->device);
   stab_batch* b = nullptr;
   const double* pr[1] = {profile};
-  int rc = batch_build(c, 1, p, &nym, pr, &b, 0);
+  int rc = batch_build(c, 1, p, &nym, pr, &b);
   if (rc) return rc;
   std::unique_ptr<stab_batch> guard(b);
   rc = run_prep(b);
@@ -1748,7 +1794,7 @@ int stab_eigenvectors(stab_ctx* c, const stab_params* p, int32_t nym, const doub
     std::vector<int32_t> ns(cnt, nym);
     std::vector<const double*> pr(cnt, profile);
     stab_batch* b = nullptr;
-    int rc = batch_build(c, cnt, ps.data(), ns.data(), pr.data(), &b, 0);
+    int rc = batch_build(c, cnt, ps.data(), ns.data(), pr.data(), &b);
     if (rc) return rc;
     std::unique_ptr<stab_batch> guard(b);
     rc = run_prep(b);
@@ -1800,7 +1846,7 @@ int stab_full_spectrum(stab_ctx* c, const stab_params* p, int32_t nym, const dou
   cudaSetDevice(c->device);
   stab_batch* b = nullptr;
   const double* pr[1] = {profile};
-  int rc = batch_build(c, 1, p, &nym, pr, &b, 0);
+  int rc = batch_build(c, 1, p, &nym, pr, &b);
   if (rc) return rc;
   std::unique_ptr<stab_batch> guard(b);
   rc = run_prep(b);

@@ -140,8 +140,12 @@ cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, con
 // loops where the device-wide synchronisation of cudaFree is not acceptable.
 // For them the full-spectrum kernel above runs with its working matrix in a
 // fixed array of this translation unit instead of a pool allocation.  The
-// array is created when the library is loaded and stays resident on every
-// GPU that loads it until the process exits.
+// CUDA driver creates the array when it loads this module on a device: at
+// library load with CUDA_MODULE_LOADING=EAGER, otherwise (lazy loading, the
+// default) at the first call on that device, which therefore should be made
+// at start-up.  The array then stays resident on that GPU until the process
+// exits.  Calls also add to the eigensolver's phase counters
+// (g_eig_phase_cycles, read by stab_eig_phases), like every other solve.
 // ---------------------------------------------------------------------------
 namespace stab {
 
@@ -191,21 +195,28 @@ extern "C" int stab_eigvals_noalloc(const double* a_dev, int32_t m, double* eig_
     if (!su.done) {   // first call on this device: resolve the array's device address with the device current
       void* p = nullptr;
       su.err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      su.ptr = reinterpret_cast<unsigned char*>(p);
-      su.done = true;
+      if (su.err == cudaSuccess && p) {
+        su.ptr = reinterpret_cast<unsigned char*>(p);
+        su.done = true;   // a failed lookup (e.g. inside a stream capture) is retried by the next call
+      } else {
+        cudaGetLastError();
+      }
     }
   }
-  if (su.err != cudaSuccess || !su.ptr) return STAB_ERR_CUDA;
+  if (!su.done || !su.ptr) return STAB_ERR_CUDA;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   NoallocHeader* hdr = reinterpret_cast<NoallocHeader*>(su.ptr);
   zc* H = reinterpret_cast<zc*>(su.ptr + STAB_NOALLOC_HEADER_BYTES);
   k_noalloc_header<<<1, 1, 0, s>>>(hdr, m);   // resets the work counter left by the previous call
   if (cudaGetLastError() != cudaSuccess) return STAB_ERR_CUDA;
   const size_t sm = eig_plain_smem(m);
-  if (cudaFuncSetAttribute(k_eig_plain<zc>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+  // one instance: the 512-thread variant, as the batched launcher picks for
+  // a few instances (lower latency than the 128-thread batch kernel)
+  if (cudaFuncSetAttribute(k_eig_plain_wide<zc>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+      cudaSuccess)
     return STAB_ERR_CUDA;
-  k_eig_plain<zc><<<1, HQ_T, sm, s>>>(1, &hdr->m, const_cast<zc*>(reinterpret_cast<const zc*>(a_dev)), &hdr->a_off, H,
-                                  &hdr->h_off, reinterpret_cast<zc*>(eig_dev), &hdr->eig_off, status_dev,
-                                  &hdr->counter, nullptr, nullptr);
+  k_eig_plain_wide<zc><<<1, HQ_WIDE, sm, s>>>(1, &hdr->m, const_cast<zc*>(reinterpret_cast<const zc*>(a_dev)),
+                                              &hdr->a_off, H, &hdr->h_off, reinterpret_cast<zc*>(eig_dev),
+                                              &hdr->eig_off, status_dev, &hdr->counter, nullptr, nullptr);
   return cudaGetLastError() == cudaSuccess ? STAB_OK : STAB_ERR_CUDA;
 }

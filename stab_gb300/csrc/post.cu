@@ -175,23 +175,32 @@ __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const 
   for (int q = threadIdx.x; q < d.m; q += blockDim.x) best_out[o + q] = out[o + q];
 }
 
-// After the rounds: the best pair becomes the result (done = 1); instances
-// without any converged pair get done = 0 for the FP64 fallback.
+// After the rounds: the best pair becomes the result.  It is final (done = 1)
+// only where a candidate resolved by the seed spectrum was quick-accepted
+// (final_[k]): then the coarse spectrum held the least-stable mode and the
+// polish landed on it.  A kept pair from the caller's seed round (best_src
+// == seed_src) without that is kept as unverified (done = unverified);
+// every other instance gets done = 0 and goes to the fallback chain, as do
+// instances without any converged pair.
 __global__ void k_take_best(int count, const InstDesc* __restrict__ desc, const int32_t* __restrict__ have,
                             const zc* __restrict__ best_theta, const double* __restrict__ best_err,
                             const int32_t* __restrict__ best_iters, const zc* __restrict__ best_out,
                             const int64_t* __restrict__ out_off, zc* __restrict__ theta, int32_t* __restrict__ done,
-                            double* __restrict__ err, int32_t* __restrict__ iters, zc* __restrict__ out) {
+                            double* __restrict__ err, int32_t* __restrict__ iters, zc* __restrict__ out,
+                            const int32_t* __restrict__ final_, const int32_t* __restrict__ best_src, int seed_src,
+                            int unverified) {
   const int k = blockIdx.x;
   if (k >= count) return;
   const InstDesc d = desc[k];
-  if (!have[k]) {
+  int dn = have[k] ? 1 : 0;
+  if (dn && !final_[k]) dn = (best_src[k] == seed_src) ? unverified : 0;
+  if (!dn) {
     if (threadIdx.x == 0) done[k] = 0;
     return;
   }
   if (threadIdx.x == 0) {
     theta[k] = best_theta[k];
-    done[k] = 1;
+    done[k] = dn;
     err[k] = best_err[k];
     iters[k] = best_iters[k];
   }

@@ -174,13 +174,12 @@ def test_batch_coarse_seeded_matches_oracle(ctx):
                           b=float(rng.uniform(0, 0.3))) for _ in range(4)]
     eig, err, iters, status, vecs = ctx.solve_batch([H.stab_params(d) for d, _ in cases],
                                                     [p for _, p in cases], sg.MODE_COARSE)
-    ok = 0
+    # every instance: the oracle's least-stable mode, with a trusted status
     for k, (d, prof) in enumerate(cases):
         es = H.oracle_solve(d, prof, want_vectors=False)
         w = es.eig[H.select_least(es.eig, d)]
-        if status[k] == sg.ST_OK and abs(eig[k] - w) / abs(w) < EIG_REL:
-            ok += 1
-    assert ok >= 3
+        assert status[k] in (sg.ST_OK, sg.ST_FELLBACK), (k, status[k])
+        assert abs(eig[k] - w) / abs(w) < EIG_REL, (k, eig[k], w)
 
 
 def test_batch_outliving_its_context_is_safe():

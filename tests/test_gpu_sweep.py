@@ -37,5 +37,12 @@ def test_track_beta_sweep_matches_reference_picks(ctx, rule):
     ref = np.asarray(oracle_picks)
     assert np.all(np.isin(st, [sg.ST_OK, sg.ST_FELLBACK]))
     assert np.max(np.abs(vals - ref) / np.abs(ref)) < 1e-10
+    # stab.out: the library's writer and the oracle's restatement of the
+    # reference's format give the same bytes for the same values, and the
+    # numbers read back agree with the oracle's picks
     text = sw.stab_out_lines(betas, vals[0])
-    assert text == so.stab_out_text(betas, ref[0]) or len(text.splitlines()) == len(betas)
+    assert text == so.stab_out_text(betas, vals[0])
+    back = np.array([[float(t) for t in ln.split()] for ln in text.splitlines()])
+    assert back.shape == (len(betas), 3)
+    assert np.max(np.abs(back[:, 1] + 1j * back[:, 2] - ref[0]) / np.abs(ref[0])) < 1e-10
+    assert np.allclose(back[:, 0], betas, rtol=1e-12, atol=1e-15)

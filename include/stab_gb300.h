@@ -121,13 +121,22 @@ int stab_reset_kernel_stats(stab_ctx* ctx);
  *   STAB_STAGE_RETRY_LU   LU and solves of the complex128 inverse-iteration
  *                         retry of the polish (residuals and eigenvalue
  *                         updates stay FP64); default STAB_ARITH_DOUBLE_WORD.
+ *   STAB_STAGE_POLISH_LU  the complex64 LUs of the polish (shift and bordered
+ *                         Jacobian): STAB_ARITH_TF32_SPLIT (default) or
+ *                         STAB_ARITH_FP32.
  * STAB_ARITH_DOUBLE_WORD is float-float pairs (about 48 significant bits)
  * run on the FP32 pipe. */
 #define STAB_STAGE_SEED_EIG 0
 #define STAB_STAGE_PLAIN_EIG 1
 #define STAB_STAGE_RETRY_LU 2
+#define STAB_STAGE_POLISH_LU 3
 #define STAB_ARITH_FP64 0
 #define STAB_ARITH_DOUBLE_WORD 1
+#define STAB_ARITH_FP32 2          /* complex64 on the CUDA cores                   */
+#define STAB_ARITH_TF32_SPLIT 3    /* complex64 with the trailing update on the     *
+                                    * tensor cores: each FP32 operand split into     *
+                                    * three TF32 parts, six part products, FP32      *
+                                    * accumulation in TMEM                           */
 int stab_set_arithmetic(stab_ctx* ctx, int32_t stage, int32_t arithmetic);
 /* N of the seed spectrum that STAB_MODE_COARSE and STAB_MODE_SURROGATE
  * take their candidate shifts from (16 <= ny < 48; default 32).  Applies to
@@ -172,6 +181,15 @@ int stab_autotune(stab_ctx* ctx, const int32_t* orders, int32_t norders, int32_t
  */
 int stab_lu_cluster_check(stab_ctx* ctx, int32_t n, int32_t count, int32_t complex128, double* max_diff,
                           int32_t* piv_diff);
+
+/*
+ * Self-check of the tensor-core LU: count test matrices of order n factored
+ * in complex64 on the CUDA cores and with the tensor-core trailing update.
+ * bwd_tc / bwd_simt: largest backward error max|P A - L U| / max|A| of
+ * either path (computed on the host in FP64); piv_diff: number of differing
+ * pivots.  No reference counterpart (the reference calls LAPACK's ZGETRF).
+ */
+int stab_lu_tc_check(stab_ctx* ctx, int32_t n, int32_t count, double* bwd_tc, double* bwd_simt, int32_t* piv_diff);
 
 /* ---- full spectrum (plain FP64 path) --------------------------------- */
 /*

@@ -29,8 +29,8 @@ LIB_PATH = os.path.join(HERE, "libstab_gb300.so")
 
 MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE, MODE_TRACK = 0, 1, 2, 3, 4
 # arithmetic per stage (stab_set_arithmetic)
-STAGE_SEED_EIG, STAGE_PLAIN_EIG, STAGE_RETRY_LU = 0, 1, 2
-ARITH_FP64, ARITH_DOUBLE_WORD = 0, 1
+STAGE_SEED_EIG, STAGE_PLAIN_EIG, STAGE_RETRY_LU, STAGE_POLISH_LU = 0, 1, 2, 3
+ARITH_FP64, ARITH_DOUBLE_WORD, ARITH_FP32, ARITH_TF32_SPLIT = 0, 1, 2, 3
 ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE, ST_UNVERIFIED = 0, 1, 2, 3, 4, 5, 6
 
 EXPORTED = (
@@ -42,7 +42,7 @@ EXPORTED = (
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
-    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_set_arithmetic", "stab_set_seed_size",
+    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_lu_tc_check", "stab_set_arithmetic", "stab_set_seed_size",
 )
 
 
@@ -158,6 +158,7 @@ def load(path: str = LIB_PATH):
     lib.stab_set_arithmetic.argtypes = [vp, i32, i32]
     lib.stab_set_seed_size.argtypes = [vp, i32]
     lib.stab_lu_cluster_check.argtypes = [vp, i32, i32, i32, P(dbl), P(i32)]
+    lib.stab_lu_tc_check.argtypes = [vp, i32, i32, P(dbl), P(dbl), P(i32)]
     _lib = lib
     return lib
 
@@ -399,12 +400,22 @@ class Context:
                                                    ctypes.byref(pd)))
         return md.value, pd.value
 
+    def lu_tc_check(self, n: int, count: int):
+        """(backward error with the tensor-core update, backward error on the
+        CUDA cores, differing pivots) of count complex64 test LUs of order n
+        (stab_lu_tc_check)."""
+        bt, bs, pd = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        self._check(self.lib.stab_lu_tc_check(self.h, n, count, ctypes.byref(bt), ctypes.byref(bs),
+                                              ctypes.byref(pd)))
+        return bt.value, bs.value, pd.value
+
     DEFAULT_ARITHMETIC = {STAGE_SEED_EIG: ARITH_DOUBLE_WORD, STAGE_PLAIN_EIG: ARITH_FP64,
-                          STAGE_RETRY_LU: ARITH_DOUBLE_WORD}
+                          STAGE_RETRY_LU: ARITH_DOUBLE_WORD, STAGE_POLISH_LU: ARITH_TF32_SPLIT}
 
     def set_arithmetic(self, stage: int, arithmetic: int) -> None:
         """Arithmetic of one stage (stab_set_arithmetic): STAGE_SEED_EIG,
-        STAGE_PLAIN_EIG or STAGE_RETRY_LU; ARITH_FP64 or ARITH_DOUBLE_WORD."""
+        STAGE_PLAIN_EIG or STAGE_RETRY_LU with ARITH_FP64 or ARITH_DOUBLE_WORD;
+        STAGE_POLISH_LU with ARITH_FP32 or ARITH_TF32_SPLIT."""
         self._check(self.lib.stab_set_arithmetic(self.h, int(stage), int(arithmetic)))
 
     def set_seed_size(self, ny: int = 32) -> None:

@@ -15,7 +15,7 @@ BIN = os.path.join(HERE, "bin")
 # command-line drop-ins over the C ABI: `stab < input.dat` and `getevec`
 TOOLS = {"stab_gpu": "stab_main.cpp", "getevec_gpu": "getevec_main.cpp"}
 
-CU_SOURCES = ["prep.cu", "assemble.cu", "lu.cu", "hqr.cu", "polish.cu", "post.cu", "mlp.cu", "capi.cu", "fileio.cpp"]
+CU_SOURCES = ["prep.cu", "assemble.cu", "lu.cu", "lu_tc.cu", "hqr.cu", "polish.cu", "post.cu", "mlp.cu", "capi.cu", "fileio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", os.path.join(HERE, "..", "include")]

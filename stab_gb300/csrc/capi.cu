@@ -67,7 +67,7 @@ struct stab_ctx {
   std::vector<stab_mlp*> nets;     // networks, released by stab_destroy
   std::map<std::pair<int, int>, int> lu_nb;   // (complex128?, size class) -> tuned LU panel width
   // arithmetic per stage (STAB_STAGE_*)
-  int arith[3] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD};
+  int arith[4] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD, STAB_ARITH_TF32_SPLIT};
   int seed_ny = 32;        // N of the seed spectrum of STAB_MODE_COARSE / SURROGATE
 };
 
@@ -771,6 +771,13 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
                                   b->rsc.as<float>(), b->csc.as<float>(), b->off_nof.as<int64_t>(), s, skip);
       });
       if (e != cudaSuccess) return e;
+    }
+    if (c64 && c->arith[STAB_STAGE_POLISH_LU] == STAB_ARITH_TF32_SPLIT && lu_tc_fits(b->nmax)) {
+      return timed(c, "k_lu_tc", [&] {
+        return launch_lu_tc(b->count, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
+                            b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
+                            b->order.as<int32_t>());
+      });
     }
     return timed(c, n_lu, [&] {
       return launch_lu<T>(b->count, D, b->nsz.as<int32_t>(), b->nmax, MP, b->off_n2.as<int64_t>(),
@@ -1547,7 +1554,92 @@ static int lu_cluster_check(stab_ctx* c, int n, int count, double* max_diff, int
   return 0;
 }
 
+// Factor the same complex64 test matrices on the CUDA cores and with the
+// tensor-core update; backward errors of both on the host in FP64.
+static int lu_tc_check(stab_ctx* c, int n, int count, double* bwd_tc, double* bwd_simt, int32_t* piv_diff) {
+  cudaStream_t s = c->stream;
+  DevBuf A1, A2, piv1, piv2, info, nsz, moff, poff;
+  const size_t elems = (size_t)count * n * n;
+  CK(c, A1.ensure(sizeof(cc) * elems, s));
+  CK(c, A2.ensure(sizeof(cc) * elems, s));
+  CK(c, piv1.ensure(sizeof(int32_t) * (size_t)count * n, s));
+  CK(c, piv2.ensure(sizeof(int32_t) * (size_t)count * n, s));
+  CK(c, info.ensure(sizeof(int32_t) * count, s));
+  std::vector<int32_t> ns(count, n);
+  std::vector<int64_t> mo(count), po(count);
+  for (int k = 0; k < count; ++k) {
+    mo[k] = (int64_t)k * n * n;
+    po[k] = (int64_t)k * n;
+  }
+  CK(c, upload(nsz, ns, s));
+  CK(c, upload(moff, mo, s));
+  CK(c, upload(poff, po, s));
+  CK(c, launch_tune_matrix<cc>(count, n, A1.as<cc>(), s));
+  std::vector<cc> h0(elems), h1(elems), h2(elems);
+  CK(c, cudaMemcpyAsync(h0.data(), A1.p, sizeof(cc) * elems, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(A2.p, A1.p, sizeof(cc) * elems, cudaMemcpyDeviceToDevice, s));
+  CK(c, launch_lu<cc>(count, nullptr, nsz.as<int32_t>(), n, A1.as<cc>(), moff.as<int64_t>(), piv1.as<int32_t>(),
+                      poff.as<int64_t>(), info.as<int32_t>(), s, nullptr, 16, nullptr, 1));
+  CK(c, launch_lu_tc(count, nsz.as<int32_t>(), n, A2.as<cc>(), moff.as<int64_t>(), piv2.as<int32_t>(),
+                     poff.as<int64_t>(), info.as<int32_t>(), s));
+  std::vector<int32_t> p1((size_t)count * n), p2((size_t)count * n), inf(count);
+  CK(c, cudaMemcpyAsync(h1.data(), A1.p, sizeof(cc) * elems, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(h2.data(), A2.p, sizeof(cc) * elems, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(p1.data(), piv1.p, sizeof(int32_t) * p1.size(), cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(p2.data(), piv2.p, sizeof(int32_t) * p2.size(), cudaMemcpyDeviceToHost, s));
+  CK(c, cudaMemcpyAsync(inf.data(), info.p, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaStreamSynchronize(s));
+  // max |P A - L U| / max |A| per matrix, P A formed by applying the swaps
+  auto bwd = [&](const std::vector<cc>& F, const std::vector<int32_t>& pv, int k) {
+    const cc* a = h0.data() + (size_t)k * n * n;
+    const cc* f = F.data() + (size_t)k * n * n;
+    std::vector<zc> pa((size_t)n * n);
+    double amax = 0.0;
+    for (size_t q = 0; q < pa.size(); ++q) {
+      pa[q] = zmk(a[q].x, a[q].y);
+      amax = std::max(amax, std::fabs((double)a[q].x) + std::fabs((double)a[q].y));
+    }
+    for (int j = 0; j < n; ++j) {
+      const int p = pv[(size_t)k * n + j];
+      if (p != j)
+        for (int col = 0; col < n; ++col) std::swap(pa[(size_t)col * n + j], pa[(size_t)col * n + p]);
+    }
+    double emax = 0.0;
+    for (int col = 0; col < n; ++col)
+      for (int r = 0; r < n; ++r) {
+        zc acc = zmk(0.0, 0.0);
+        const int lim = std::min(r, col);
+        for (int t = 0; t <= lim; ++t) {
+          const cc l = (t == r) ? cmk(1.f, 0.f) : f[(size_t)t * n + r];
+          const cc u = f[(size_t)col * n + t];
+          acc = zfma(zmk(l.x, l.y), zmk(u.x, u.y), acc);
+        }
+        const zc d = zsub(pa[(size_t)col * n + r], acc);
+        emax = std::max(emax, std::fabs(d.x) + std::fabs(d.y));
+      }
+    return amax > 0 ? emax / amax : emax;
+  };
+  double e1 = 0.0, e2 = 0.0;
+  int32_t pd = 0;
+  for (int k = 0; k < count; ++k) {
+    e1 = std::max(e1, bwd(h1, p1, k));
+    e2 = std::max(e2, inf[k] < 0 ? INFINITY : bwd(h2, p2, k));
+    for (int j = 0; j < n; ++j) pd += (p1[(size_t)k * n + j] != p2[(size_t)k * n + j]) ? 1 : 0;
+  }
+  *bwd_simt = e1;
+  *bwd_tc = e2;
+  *piv_diff = pd;
+  return 0;
+}
+
 extern "C" {
+
+int stab_lu_tc_check(stab_ctx* c, int32_t n, int32_t count, double* bwd_tc, double* bwd_simt, int32_t* piv_diff) {
+  if (!c || !bwd_tc || !bwd_simt || !piv_diff || n < 2 || count < 1 || count > 64) return STAB_ERR_ARG;
+  if (!lu_tc_fits(n)) return set_err(c, STAB_ERR_ARG, "order too large for the tensor-core LU's shared memory");
+  cudaSetDevice(c->device);
+  return lu_tc_check(c, n, count, bwd_tc, bwd_simt, piv_diff);
+}
 
 int stab_lu_cluster_check(stab_ctx* c, int32_t n, int32_t count, int32_t complex128, double* max_diff,
                           int32_t* piv_diff) {
@@ -1579,10 +1671,14 @@ int stab_autotune(stab_ctx* c, const int32_t* orders, int32_t norders, int32_t* 
 
 int stab_set_arithmetic(stab_ctx* c, int32_t stage, int32_t arithmetic) {
   if (!c) return STAB_ERR_ARG;
-  if (stage < STAB_STAGE_SEED_EIG || stage > STAB_STAGE_RETRY_LU)
+  if (stage < STAB_STAGE_SEED_EIG || stage > STAB_STAGE_POLISH_LU)
     return set_err(c, STAB_ERR_ARG, "stage must be one of STAB_STAGE_*");
-  if (arithmetic != STAB_ARITH_FP64 && arithmetic != STAB_ARITH_DOUBLE_WORD)
+  if (stage == STAB_STAGE_POLISH_LU) {
+    if (arithmetic != STAB_ARITH_FP32 && arithmetic != STAB_ARITH_TF32_SPLIT)
+      return set_err(c, STAB_ERR_ARG, "the polish LU takes STAB_ARITH_FP32 or STAB_ARITH_TF32_SPLIT");
+  } else if (arithmetic != STAB_ARITH_FP64 && arithmetic != STAB_ARITH_DOUBLE_WORD) {
     return set_err(c, STAB_ERR_ARG, "arithmetic must be STAB_ARITH_FP64 or STAB_ARITH_DOUBLE_WORD");
+  }
   c->arith[stage] = arithmetic;
   return STAB_OK;
 }

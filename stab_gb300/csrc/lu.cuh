@@ -30,4 +30,13 @@ cudaError_t launch_getrs(int count, const int32_t* nsz, int nmax, const T* LU, c
 // at rs/cs + sc_off[k]); pass the same rs/cs to launch_getrs.
 cudaError_t launch_equilibrate(int count, const int32_t* nsz, cc* A, const int64_t* mat_off, float* rs, float* cs,
                                const int64_t* sc_off, cudaStream_t s, const int32_t* skip = nullptr);
+// Complex64 LU with the trailing update on the tensor cores (lu_tc.cu):
+// same inputs, outputs and pivot order as launch_lu<cc> with panel width 16.
+// info[k] = -1 marks an instance whose MMA completion was not seen.
+cudaError_t launch_lu_tc(int count, const int32_t* nsz, int nmax, cc* A, const int64_t* mat_off, int32_t* piv,
+                         const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip = nullptr,
+                         const int32_t* order = nullptr);
+// dynamic shared memory of k_lu_tc for order nmax, and whether it fits
+size_t lu_tc_smem(int nmax);
+bool lu_tc_fits(int nmax);
 }  // namespace stab

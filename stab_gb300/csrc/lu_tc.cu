@@ -1,0 +1,228 @@
+// Complex64 batched LU with the trailing-matrix update on the tensor cores
+// (tcgen05, kind::tf32): the factorisation of A - s B in the mixed-precision
+// polish (the LU of ZGESV, temporal.f90:774, and of ZGETRF,
+// spatial.f90:978, in the precision of the shift-invert polish).
+//
+// One CTA of 256 threads per matrix, as k_lu: the panel (n x 16) is factored
+// in shared memory by the CUDA cores (lu_panel of lu_body.cuh: pivot search,
+// row swaps, U12 = L11^-1 A12).  The update A22 -= L21 U12 runs per tile of
+// 128 rows x 64 complex columns:
+//   - the panel rows of the tile (L21) and the U12 columns are split into
+//     TF32 parts (tc.cuh) and written to shared memory in the canonical
+//     K-major layout: A planes -Lr and Li (3 parts each, 128 x 16),
+//     B planes [Ur | Ui] and [Ui | -Ur] (3 parts each, 128 x 16), so one
+//     MMA of N = 128 produces the real part in TMEM columns 0-63 and the
+//     imaginary part in columns 64-127;
+//   - thread 0 issues 2 K-steps x 6 part products x 2 operand pairs = 24
+//     MMAs of 128 x 128 x 8 into one float32 TMEM accumulator and commits
+//     them to an mbarrier;
+//   - all eight warps read the accumulator back (tcgen05.ld, warp w owns
+//     TMEM lanes 32 (w mod 4) and half of the columns) and add it to the
+//     tile of A22 in global memory, coalesced along the column.
+// Six part products keep about 2^-33 relative error per product, so the
+// factors carry complex64 (FP32) accuracy; the polish's Newton-chord steps
+// form their residuals in FP64 (polish.cu).
+//
+// Every wait on the MMA mbarrier is bounded; a wait that gives up marks the
+// instance (info = -1), waits once more (bounded) for the MMAs in flight,
+// frees the TMEM and ends the factorisation.
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+#include "dw.cuh"
+#include "lu.cuh"
+#include "tc.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace stab {
+
+#include "lu_body.cuh"
+
+namespace {
+constexpr int kTcNB = 16;                       // panel width = MMA K extent per tile
+constexpr int kTcRows = 128;                    // tile rows (MMA M)
+constexpr int kTcCols = 64;                     // tile complex columns (MMA N = 128 reals)
+constexpr uint32_t kPlane = kTcRows * kTcNB * 4;   // bytes of one TF32 plane (128 x 16)
+constexpr uint32_t kSbo = kTcNB * 32;           // 8-row group stride of a plane
+constexpr uint32_t kLbo = 128;                  // K-adjacent core matrices
+constexpr uint32_t kWaitLimit = 1u << 22;       // polls of the MMA mbarrier before giving up
+constexpr uint32_t kTmemCols = 128;
+
+__device__ __forceinline__ void put_split(unsigned char* base, uint32_t off, float v) {
+  float p0, p1, p2;
+  tc::tf32_split3(v, p0, p1, p2);
+  *reinterpret_cast<float*>(base + off) = p0;
+  *reinterpret_cast<float*>(base + kPlane + off) = p1;
+  *reinterpret_cast<float*>(base + 2 * kPlane + off) = p2;
+}
+}  // namespace
+
+size_t lu_tc_smem(int nmax) {
+  const size_t panel = ((size_t)nmax * kTcNB * sizeof(cc) + 1023) & ~(size_t)1023;
+  return 1024 + panel + 12 * (size_t)kPlane;   // alignment slack, panel, 6 A planes, 6 B planes
+}
+
+// A22 -= L21 U12 for the panel at k0 on the tensor cores.  Returns false if
+// an MMA completion was not seen within the wait limit.
+__device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, const cc* P, unsigned char* Apl,
+                                             unsigned char* Bpl, uint32_t tm, uint64_t* mbar, uint32_t& phase) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c1 = k0 + kTcNB;
+  const int m2 = n - c1;
+  const uint32_t idesc = tc::idesc_tf32(128, 128, false);
+  const uint32_t a_s = tc::smem_u32(Apl), b_s = tc::smem_u32(Bpl);
+  bool ok = true;
+  for (int rb0 = 0; rb0 < m2; rb0 += kTcRows) {
+    const int nrow = min(kTcRows, m2 - rb0);
+    // A planes: -Lr (parts 0..2) then Li (parts 0..2); row r of the tile is
+    // panel row kTcNB + rb0 + r
+    for (int q = tid; q < kTcRows * kTcNB; q += blockDim.x) {
+      const int r = q & (kTcRows - 1), j = q >> 7;
+      const cc v = (r < nrow) ? P[(size_t)j * n + kTcNB + rb0 + r] : cmk(0.f, 0.f);
+      const uint32_t off = tc::plane_off(r, j, kTcNB);
+      put_split(Apl, off, -v.x);
+      put_split(Apl + 3 * kPlane, off, v.y);
+    }
+    for (int cb0 = 0; cb0 < m2; cb0 += kTcCols) {
+      const int ncol = min(kTcCols, m2 - cb0);
+      // B planes: [Ur | Ui] (parts 0..2) then [Ui | -Ur]; B row c is U12
+      // column c1 + cb0 + c, K index j its row k0 + j
+      for (int q = tid; q < kTcCols * kTcNB; q += blockDim.x) {
+        const int j = q & (kTcNB - 1), c = q >> 4;
+        const cc u = (c < ncol) ? M[(size_t)(c1 + cb0 + c) * n + k0 + j] : cmk(0.f, 0.f);
+        const uint32_t o_lo = tc::plane_off(c, j, kTcNB), o_hi = tc::plane_off(kTcCols + c, j, kTcNB);
+        put_split(Bpl, o_lo, u.x);
+        put_split(Bpl, o_hi, u.y);
+        put_split(Bpl + 3 * kPlane, o_lo, u.y);
+        put_split(Bpl + 3 * kPlane, o_hi, -u.x);
+      }
+      tc::fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        // part pairs (a, b) with a + b <= 2
+        const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+        uint32_t acc = 0;
+#pragma unroll
+        for (int ks = 0; ks < kTcNB / 8; ++ks) {
+#pragma unroll
+          for (int t = 0; t < 6; ++t) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {   // h = 0: (-Lr, [Ur | Ui]); h = 1: (Li, [Ui | -Ur])
+              const uint64_t ad = tc::sdesc(a_s + (3 * h + pa[t]) * kPlane + ks * 256, kLbo, kSbo);
+              const uint64_t bd = tc::sdesc(b_s + (3 * h + pb[t]) * kPlane + ks * 256, kLbo, kSbo);
+              tc::mma_tf32(tm, ad, bd, idesc, acc);
+              acc = 1;
+            }
+          }
+        }
+        tc::mma_commit(mbar);
+      }
+      __syncwarp();
+      const bool got = tc::mbar_wait(mbar, phase, kWaitLimit);
+      phase ^= 1u;
+      tc::fence_after_sync();
+      if (!got) {
+        ok = false;
+      } else {
+        // epilogue: warp w reads TMEM lanes 32 (w mod 4) + lane = tile rows,
+        // complex columns [32 (w / 4), +32)
+        const int r = 32 * (warp & 3) + lane;
+        const int ch = 32 * (warp >> 2);
+        const uint32_t trow = tm + ((uint32_t)(32 * (warp & 3)) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 16) {
+          float re[16], im[16];
+          tc::tmem_ld16(trow + (uint32_t)(ch + c0), re);
+          tc::tmem_ld16(trow + (uint32_t)(kTcCols + ch + c0), im);
+          tc::tmem_wait_ld();
+          if (r < nrow) {
+            cc* col = M + (size_t)(c1 + cb0 + ch + c0) * n + c1 + rb0 + r;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              if (ch + c0 + i < ncol) {
+                cc a = col[(size_t)i * n];
+                a.x += re[i];
+                a.y += im[i];
+                col[(size_t)i * n] = a;
+              }
+            }
+          }
+        }
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+      if (!__syncthreads_and(ok)) return false;
+    }
+  }
+  return ok;
+}
+
+__global__ void __launch_bounds__(256, 1) k_lu_tc(int count, const int32_t* __restrict__ nsz, cc* __restrict__ A,
+                                                  const int64_t* __restrict__ mat_off, int32_t* __restrict__ piv,
+                                                  const int64_t* __restrict__ piv_off, int32_t* __restrict__ info,
+                                                  const int32_t* __restrict__ skip, const int32_t* __restrict__ order,
+                                                  int nmax) {
+  extern __shared__ unsigned char smraw_tc[];
+  __shared__ float red_v[256 / 32];
+  __shared__ int red_i[256 / 32];
+  __shared__ int s_piv;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const int k = order ? order[blockIdx.x] : (int)blockIdx.x;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  // 1024-aligned panel, then the planes
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smraw_tc) + 1023) & ~(uintptr_t)1023);
+  cc* P = reinterpret_cast<cc*>(base);
+  const size_t panel = ((size_t)nmax * kTcNB * sizeof(cc) + 1023) & ~(size_t)1023;
+  unsigned char* Apl = base + panel;
+  unsigned char* Bpl = Apl + 6 * kPlane;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_slot, kTmemCols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) tc::mbar_init(&mbar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tmem_slot;
+  const int n = nsz[k];
+  cc* Mk = A + mat_off[k];
+  int32_t* ip = piv + piv_off[k];
+  int first_zero = 0;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int k0 = 0; k0 < n; k0 += kTcNB) {
+    if (!lu_panel<cc, kTcNB, 1>(k0, 0, n, Mk, ip, P, red_v, red_i, s_piv, first_zero)) break;
+    if (!lu_update_tc(k0, n, Mk, P, Apl, Bpl, tm, &mbar, phase)) {
+      ok = false;
+      break;
+    }
+  }
+  if (!ok && tid == 0) (void)tc::mbar_wait(&mbar, phase, kWaitLimit);   // drain what may still be in flight
+  if (tid == 0) info[k] = ok ? first_zero : -1;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
+  if (tid == 0) tc::mbar_inval(&mbar);
+}
+
+cudaError_t launch_lu_tc(int count, const int32_t* nsz, int nmax, cc* A, const int64_t* mat_off, int32_t* piv,
+                         const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip,
+                         const int32_t* order) {
+  if (count <= 0) return cudaSuccess;
+  const size_t sm = lu_tc_smem(nmax);
+  cudaError_t e = cudaFuncSetAttribute(k_lu_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_lu_tc<<<count, 256, sm, s>>>(count, nsz, A, mat_off, piv, piv_off, info, skip, order, nmax);
+  return cudaGetLastError();
+}
+
+bool lu_tc_fits(int nmax) { return nmax >= 2 && lu_tc_smem(nmax) <= 227 * 1024; }
+
+}  // namespace stab

@@ -27,3 +27,15 @@ def test_autotune_picks_a_feasible_width_and_keeps_results(ctx):
 def test_cluster_lu_matches_single_cta(ctx, n, z):
     md, pd = ctx.lu_cluster_check(n, 8, complex128=z)
     assert pd == 0 and md == 0.0
+
+
+@pytest.mark.parametrize("n", [40, 200, 320, 640])
+def test_tensor_core_lu_backward_error(ctx, n):
+    """The complex64 LU with the trailing update on the tensor cores (TF32
+    parts, six part products) against the CUDA-core LU on the same matrices:
+    backward error max|PA - LU| / max|A| at most 4x the CUDA-core one and
+    below 1e-5 (complex64 working accuracy, n up to 640)."""
+    bt, bs, pd = ctx.lu_tc_check(n, 4)
+    assert np.isfinite(bt)
+    assert bt < 1e-5, (bt, bs, pd)
+    assert bt <= 4.0 * bs + 1e-7, (bt, bs, pd)

@@ -45,20 +45,27 @@ extern "C" {
 #define STAB_ST_NAN 3         /* non-finite value in the inputs or results      */
 #define STAB_ST_FELLBACK 4    /* polish did not converge; plain FP64 path used   */
 #define STAB_ST_NOMODE 5      /* no eigenvalue passed the least-stable filter    */
-#define STAB_ST_UNVERIFIED 6  /* STAB_MODE_SURROGATE: a converged eigenpair from *
-                               * the caller's seed that no resolved spectrum     *
-                               * confirmed as the least-stable mode              */
+#define STAB_ST_UNVERIFIED 6  /* a converged eigenpair that no resolved seed     *
+                               * spectrum confirmed as the least-stable mode     *
+                               * (STAB_MODE_COARSE / STAB_MODE_SURROGATE)        */
 
 /* solve modes for stab_batch_run / stab_solve_batch */
 #define STAB_MODE_PLAIN 0     /* FP64 full spectrum + least-stable eigenvector   */
 #define STAB_MODE_SEEDED 1    /* mixed-precision polish from caller seeds        */
 #define STAB_MODE_COARSE 2    /* seeds from a full spectrum at N = 32, then the  *
                                * mixed-precision polish.  STAB_ST_OK only where  *
-                               * a seed candidate (in selection order) polished  *
-                               * to within 1e-7 of itself: the seed spectrum     *
-                               * resolved the mode.  Every other instance takes  *
-                               * seeds from N = 48 under the same rule, then the *
-                               * plain FP64 path (STAB_ST_FELLBACK)              */
+                               * the seed spectrum's most unstable candidate     *
+                               * polished to within 1e-7 of itself (the seed     *
+                               * spectrum resolved it).  Every other instance    *
+                               * takes seeds from N = 48 under the same rule     *
+                               * (STAB_ST_FELLBACK); where that does not settle  *
+                               * it either, the least-stable converged pair is   *
+                               * kept with STAB_ST_UNVERIFIED, and instances     *
+                               * without one take the plain FP64 path            *
+                               * (STAB_ST_FELLBACK).  A discrete mode that the   *
+                               * seed spectrum misplaces below its top candidate *
+                               * can still be missed: the check costs no fine    *
+                               * spectrum, so it cannot rule that out            */
 #define STAB_MODE_TRACK 4     /* polish from caller guesses; where it fails, the *
                                * FP64 spectrum's eigenvalue nearest the guess    *
                                * (the pick of getab.f90:185-192)                 */

@@ -1218,7 +1218,8 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
                                   b->best_err.as<double>(), b->best_iters.as<int32_t>(), b->best_out.as<zc>(),
                                   b->off_mof.as<int64_t>(), b->theta.as<zc>(), b->done.as<int32_t>(),
                                   b->err.as<double>(), b->iters.as<int32_t>(), b->outvec.as<zc>(), fin,
-                                  b->best_src.as<int32_t>(), kShiftCandidates, kDoneUnverified);
+                                  b->best_src.as<int32_t>(), kShiftCandidates, kDoneUnverified,
+                                  b->coarse_ny >= kMediumNy ? 1 : 0);
     return cudaGetLastError();
   }));
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
@@ -1284,7 +1285,7 @@ static int run_fallback(stab_batch* b, bool track = false) {
     b->fb_vec = std::move(vecs);
     for (int q = 0; q < nf; ++q) {
       b->fb_val[q] = zmk(eig[2 * q], eig[2 * q + 1]);
-      b->fb_status[q] = (st[q] == STAB_ST_OK) ? STAB_ST_FELLBACK : st[q];
+      b->fb_status[q] = (st[q] == STAB_ST_OK) ? STAB_ST_FELLBACK : st[q];   // UNVERIFIED stays
     }
     return 0;
   }

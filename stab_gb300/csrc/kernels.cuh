@@ -63,7 +63,8 @@ __global__ void k_fold_best(int count, const InstDesc* desc, const zc* sigma, co
 __global__ void k_take_best(int count, const InstDesc* desc, const int32_t* have, const zc* best_theta,
                             const double* best_err, const int32_t* best_iters, const zc* best_out,
                             const int64_t* out_off, zc* theta, int32_t* done, double* err, int32_t* iters, zc* out,
-                            const int32_t* final_, const int32_t* best_src, int seed_src, int unverified);
+                            const int32_t* final_, const int32_t* best_src, int seed_src, int unverified,
+                            int keep_unverified);
 __global__ void k_temporal_vec(int count, const InstDesc* desc, const zc* vec, int slot, zc* out,
                                const int64_t* out_off, const int32_t* skip);
 

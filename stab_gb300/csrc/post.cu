@@ -165,7 +165,8 @@ __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const 
         if (best_src) best_src[k] = src;
         s_take = 1;
       }
-      if (quick && zabs(zsub(t, sigma[k])) <= quick_tol * zabs(sigma[k])) final_[k] = 1;
+      // quick accept: final_ = 1 + the candidate's index (1: the top candidate)
+      if (quick && zabs(zsub(t, sigma[k])) <= quick_tol * zabs(sigma[k])) final_[k] = 1 + src;
     }
     if (skip64 && final_[k]) skip64[k] = 1;
   }
@@ -175,25 +176,28 @@ __global__ void k_fold_best(int count, const InstDesc* __restrict__ desc, const 
   for (int q = threadIdx.x; q < d.m; q += blockDim.x) best_out[o + q] = out[o + q];
 }
 
-// After the rounds: the best pair becomes the result.  It is final (done = 1)
-// only where a candidate resolved by the seed spectrum was quick-accepted
-// (final_[k]): then the coarse spectrum held the least-stable mode and the
-// polish landed on it.  A kept pair from the caller's seed round (best_src
-// == seed_src) without that is kept as unverified (done = unverified);
-// every other instance gets done = 0 and goes to the fallback chain, as do
-// instances without any converged pair.
+// After the rounds: the best pair becomes the result.  It is trusted
+// (done = 1) only where the top candidate of the seed spectrum (the most
+// unstable one after the selection filter) polished to within the quick-
+// accept distance of itself (final_[k] == 1): the seed spectrum resolved its
+// most unstable mode and the polish landed on it.  Otherwise a mode the seed
+// spectrum did not resolve may be more unstable than the kept pair: the
+// instance gets done = 0 and goes to the fallback chain, unless
+// keep_unverified is set (the last seed level) or the pair came from the
+// caller's seed round (best_src == seed_src), which keep it with done =
+// unverified.  Instances without any converged pair get done = 0.
 __global__ void k_take_best(int count, const InstDesc* __restrict__ desc, const int32_t* __restrict__ have,
                             const zc* __restrict__ best_theta, const double* __restrict__ best_err,
                             const int32_t* __restrict__ best_iters, const zc* __restrict__ best_out,
                             const int64_t* __restrict__ out_off, zc* __restrict__ theta, int32_t* __restrict__ done,
                             double* __restrict__ err, int32_t* __restrict__ iters, zc* __restrict__ out,
                             const int32_t* __restrict__ final_, const int32_t* __restrict__ best_src, int seed_src,
-                            int unverified) {
+                            int unverified, int keep_unverified) {
   const int k = blockIdx.x;
   if (k >= count) return;
   const InstDesc d = desc[k];
   int dn = have[k] ? 1 : 0;
-  if (dn && !final_[k]) dn = (best_src[k] == seed_src) ? unverified : 0;
+  if (dn && final_[k] != 1) dn = (best_src[k] == seed_src || keep_unverified) ? unverified : 0;
   if (!dn) {
     if (threadIdx.x == 0) done[k] = 0;
     return;

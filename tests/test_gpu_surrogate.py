@@ -57,6 +57,11 @@ def test_network_gain_over_coarse_seeds(ctx):
     counts = b.counts()
     b.close()
     sur.close()
+    any_c = (np.abs(e_c - truth) / np.abs(truth) <= 1e-10) & (tst == 0)
+    any_s = (np.abs(e_s - truth) / np.abs(truth) <= 1e-10) & (tst == 0)
+    print(f"surrogate region: coarse trusted-right {int(ok_c.sum())} any-right {int(any_c.sum())} "
+          f"status {np.unique(s_c, return_counts=True)}; surrogate trusted-right {int(ok_s.sum())} "
+          f"any-right {int(any_s.sum())} status {np.unique(s_s, return_counts=True)} counts {counts}")
     assert np.sum(ok_c & ~ok_s) <= 2
     assert np.sum(ok_s & ~ok_c) >= 8, (int(ok_c.sum()), int(ok_s.sum()), counts)
     assert counts["surrogate_seed"] >= 1

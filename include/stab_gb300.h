@@ -244,6 +244,50 @@ int stab_eigenvectors(stab_ctx* ctx, const stab_params* p, int32_t nym, const do
 int stab_parse_input(const char* text, stab_params* p, char* msg, size_t msg_cap);
 /* "profile.<ind>" (makename, getmean.f90:27-28). */
 int stab_profile_name(int32_t ind, char* out, size_t cap);
+
+/*
+ * The multi-point drivers of `stab < input.dat` (stab.f90:85-90): itype 7
+ * (mtemporal, an alpha x beta sweep on profile.0) and itype 8 (mspatial,
+ * stations of delta.dat x omega x beta, each station on its own
+ * profile.<ind>).  Every point's eigensystem goes to eig.<iver>, iver = 1, 2,
+ * ... in loop order.
+ */
+typedef struct stab_sweep {
+  int32_t itype;                   /* 7 or 8 (0 after a single-point input)       */
+  int32_t dtype;                   /* itype 8: 0 Chebyshev collocation            */
+  int32_t ind1, ind2, ind_inc;     /* itype 8: 1-based rows of delta.dat          */
+  double p_min, p_max, p_inc;      /* alpha (itype 7) or omega (itype 8) range    */
+  double b_min, b_max, b_inc;      /* beta range                                  */
+} stab_sweep;
+/* stab_parse_input that also takes itypes 7 and 8: after the common input it
+ * reads the driver's ranges (mtemporal.f90:20-23; mspatial.f90:20-27, where
+ * dtype 1, the finite-difference solver, returns STAB_ERR_ARG).  p->itype is
+ * set to the solver's itype (1 or 2) and sw->itype to 7 or 8; for itypes 1
+ * and 2, sw->itype is 0 and the result equals stab_parse_input's. */
+int stab_parse_sweep_input(const char* text, stab_params* p, stab_sweep* sw, char* msg, size_t msg_cap);
+/* delta.dat (mspatial.f90:29-63): records not starting with '#' hold
+ * "xb delta".  xb, delta may be NULL (count only). */
+int stab_read_delta(const char* path, int32_t cap, double* xb, double* delta, int32_t* nbody);
+/* body.dat of the post-processors (getab.f90:73-86): "index xb" records. */
+int stab_read_body(const char* path, int32_t cap, double* xb, int32_t* nbody);
+/* "eig.<iver>" (makename, mtemporal.f90:53-76). */
+int stab_eig_name(int32_t iver, char* out, size_t cap);
+/* One line of the post-processors' output (no newline): "p Re Im" in
+ * 3(1x,1pe20.13) (stab.out of getab, getab.f90:211) or, with with_ind,
+ * "ind p Re Im" in i4,3(1x,1pe20.13) (stab.out of getax, getax.f90:214;
+ * parm.new of getalpha, getalpha.f90:167).  Returns the length. */
+int stab_stab_out_line(int32_t with_ind, int32_t ind, double p, double vr, double vi, char* out, size_t cap);
+/*
+ * The solves of a sweep in the reference's loop order, each a copy of base
+ * with the swept values set: itype 7 (mtemporal.f90:25-39) alpha outer, beta
+ * inner, na = max(nint((amax - amin) / ainc), 1) points in alpha (amax is not
+ * reached); itype 8 (mspatial.f90:65-96) station outer, then omega, then beta,
+ * zero increments replaced by one, nint(range / inc) + 1 points each, with
+ * x = xb(ind), Yi = 2 delta(ind) and ind the station (profile.<ind>).
+ * points may be NULL (count only); xb / delta (nbody rows) only for itype 8.
+ */
+int stab_sweep_points(const stab_params* base, const stab_sweep* sw, int32_t nbody, const double* xb,
+                      const double* delta, int32_t cap, stab_params* points, int32_t* count);
 /*
  * Read profile.<ind> (getmean.f90:27-80): rows "y rho u v w T", records that
  * start with '#' skipped.  rows == NULL counts only; else up to cap_rows rows

@@ -16,6 +16,8 @@ scipy's bundled LAPACK:
   PIKSR2          stable ascending sort carrying an index
   getevec         getevec.f90:154-227 (selection, real-scale quirk, format)
   makename        mtemporal.f90:53-76
+  sweep drivers   mtemporal.f90:25-39, mspatial.f90:29-96 (loops, delta.dat)
+  post-processors getab.f90:161-201, getax.f90:161-201, getalpha.f90:120-146
 
 Parity pins: ``tests/test_oracle_golden.py`` checks this restatement against
 the reference's golden files (test/space.1, TStest/README.md,
@@ -1117,6 +1119,78 @@ def track_pick(spectra, param, start, rule):
             g = e1 + (e2 - e1) / (p2 - p1) * (param[j] - p1)
         d = np.abs(np.asarray(ev) - g)
         picks.append(complex(ev[int(np.argmin(d))]))
+    return picks
+
+
+def mtemporal_points(amin, amax, ainc, bmin, bmax, binc):
+    """(alpha, beta) of the solves of the temporal driver, in loop order
+    (mtemporal.f90:25-39): na = max(nint((amax-amin)/ainc), 1), beta inner."""
+    na = max(_nint((amax - amin) / ainc), 1)
+    nb = max(_nint((bmax - bmin) / binc), 1)
+    return [(amin + float(ia - 1) * ainc, bmin + float(ib - 1) * binc)
+            for ia in range(1, na + 1) for ib in range(1, nb + 1)]
+
+
+def mspatial_points(omin, omax, oinc, bmin, bmax, binc, ind1, ind2, ind_inc, xb, delta):
+    """(ind, x, Yi, omega, beta) of the spatial driver's solves in loop order
+    (mspatial.f90:65-96): zero increments become one, nint(range/inc) + 1
+    values each, x = xb(ind), Yi = 2 delta(ind)."""
+    oinc = 1.0 if oinc == 0.0 else oinc
+    binc = 1.0 if binc == 0.0 else binc
+    ind_inc = 1 if ind_inc == 0 else ind_inc
+    no = _nint((omax - omin) / oinc) + 1
+    nb = _nint((bmax - bmin) / binc) + 1
+    out = []
+    for ind in range(ind1, ind2 + (1 if ind_inc > 0 else -1), ind_inc):
+        for io in range(1, no + 1):
+            for ib in range(1, nb + 1):
+                out.append((ind, xb[ind - 1], 2.0 * delta[ind - 1], omin + float(io - 1) * oinc,
+                            bmin + float(ib - 1) * binc))
+    return out
+
+
+def _nint(v: float) -> int:
+    """Fortran NINT: nearest integer, halves away from zero."""
+    return int(math.floor(abs(v) + 0.5)) * (1 if v >= 0 else -1)
+
+
+def read_delta(text: str):
+    """delta.dat (mspatial.f90:29-63): rows not starting with '#' hold xb, delta."""
+    xb, de = [], []
+    for ln in text.splitlines():
+        if ln.startswith("#") or not ln.strip():
+            continue
+        f = ln.replace(",", " ").split()
+        xb.append(float(f[0].replace("d", "e").replace("D", "e")))
+        de.append(float(f[1].replace("d", "e").replace("D", "e")))
+    return xb, de
+
+
+def getab_picks(spectra, param, first):
+    """getab / getax (getab.f90:161-201): the first two picks are the
+    eigenvalues nearest the user's values `first` (the -v mode), then the
+    eigenvalue nearest the linear extrapolation through the two previous
+    picks; nearest = first minimum of a strict '<' scan."""
+    picks = []
+    for j, ev in enumerate(spectra):
+        ev = np.asarray(ev)
+        if j < 2:
+            g = complex(first[j])
+        else:
+            e1, p1 = picks[j - 1], param[j - 1]
+            e2, p2 = picks[j - 2], param[j - 2]
+            g = e1 + (e2 - e1) / (p2 - p1) * (param[j] - p1)
+        picks.append(complex(ev[int(np.argmin(np.abs(ev - g)))]))
+    return picks
+
+
+def getalpha_picks(spectra, jloc):
+    """getalpha (getalpha.f90:120-146): the first pick by 1-based index jloc,
+    then the eigenvalue nearest the previous pick."""
+    picks = [complex(np.asarray(spectra[0])[jloc - 1])]
+    for ev in spectra[1:]:
+        ev = np.asarray(ev)
+        picks.append(complex(ev[int(np.argmin(np.abs(ev - picks[-1])))]))
     return picks
 
 

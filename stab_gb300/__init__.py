@@ -19,7 +19,8 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-__all__ = ["StabParams", "EvecHeader", "Context", "Network", "load", "LIB_PATH", "parse_input", "profile_name",
+__all__ = ["StabParams", "Sweep", "parse_sweep_input", "read_delta", "read_body", "eig_name", "stab_out_line",
+           "sweep_points", "EvecHeader", "Context", "Network", "load", "LIB_PATH", "parse_input", "profile_name",
            "read_profile", "grid", "write_evec", "read_evec", "getevec_select", "eigfunction_text", "MODE_PLAIN", "MODE_SEEDED", "MODE_COARSE", "MODE_SURROGATE", "MODE_TRACK",
            "ST_OK", "ST_SINGULAR", "ST_NOCONV", "ST_NAN", "ST_FELLBACK", "ST_NOMODE", "ST_UNVERIFIED",
            "StabError"]
@@ -38,7 +39,8 @@ EXPORTED = (
     "stab_set_profiling", "stab_kernel_stats", "stab_reset_kernel_stats", "stab_assemble",
     "stab_full_spectrum", "stab_batch_create", "stab_batch_set_seeds", "stab_batch_run",
     "stab_batch_results", "stab_batch_work", "stab_batch_destroy", "stab_solve_batch",
-    "stab_eigvals_noalloc", "stab_eigenvectors", "stab_parse_input", "stab_profile_name", "stab_read_profile",
+    "stab_eigvals_noalloc", "stab_eigenvectors", "stab_parse_input", "stab_parse_sweep_input",
+    "stab_read_delta", "stab_read_body", "stab_eig_name", "stab_stab_out_line", "stab_sweep_points", "stab_profile_name", "stab_read_profile",
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
@@ -94,6 +96,16 @@ class StabParams(ctypes.Structure):
         return self.n() if self.itype == 1 else 2 * self.n()
 
 
+class Sweep(ctypes.Structure):
+    """Mirror of ``stab_sweep``: the ranges of the multi-point drivers
+    (itype 7: mtemporal.f90:20-23; itype 8: mspatial.f90:20-27)."""
+
+    _fields_ = [("itype", ctypes.c_int32), ("dtype", ctypes.c_int32), ("ind1", ctypes.c_int32),
+                ("ind2", ctypes.c_int32), ("ind_inc", ctypes.c_int32), ("p_min", ctypes.c_double),
+                ("p_max", ctypes.c_double), ("p_inc", ctypes.c_double), ("b_min", ctypes.c_double),
+                ("b_max", ctypes.c_double), ("b_inc", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -131,6 +143,13 @@ def load(path: str = LIB_PATH):
                                      P(i32), P(P(dbl))]
     lib.stab_eigenvectors.argtypes = [vp, P(StabParams), i32, P(dbl), i32, P(dbl), P(dbl), P(i32)]
     lib.stab_parse_input.argtypes = [ctypes.c_char_p, P(StabParams), ctypes.c_char_p, ctypes.c_size_t]
+    lib.stab_parse_sweep_input.argtypes = [ctypes.c_char_p, P(StabParams), P(Sweep), ctypes.c_char_p,
+                                           ctypes.c_size_t]
+    lib.stab_read_delta.argtypes = [ctypes.c_char_p, i32, P(dbl), P(dbl), P(i32)]
+    lib.stab_read_body.argtypes = [ctypes.c_char_p, i32, P(dbl), P(i32)]
+    lib.stab_eig_name.argtypes = [i32, ctypes.c_char_p, ctypes.c_size_t]
+    lib.stab_stab_out_line.argtypes = [i32, i32, dbl, dbl, dbl, ctypes.c_char_p, ctypes.c_size_t]
+    lib.stab_sweep_points.argtypes = [P(StabParams), P(Sweep), i32, P(dbl), P(dbl), i32, P(StabParams), P(i32)]
     lib.stab_profile_name.argtypes = [i32, ctypes.c_char_p, ctypes.c_size_t]
     lib.stab_read_profile.argtypes = [ctypes.c_char_p, i32, P(dbl), P(i32)]
     lib.stab_grid.argtypes = [i32, dbl, dbl, P(dbl), P(dbl), P(dbl), P(dbl)]
@@ -499,6 +518,77 @@ def parse_input(text: str) -> StabParams:
     if rc:
         raise StabError(f"input: {msg.value.decode()}")
     return p
+
+
+def parse_sweep_input(text: str):
+    """The stdin protocol including the multi-point drivers (itypes 7, 8):
+    (StabParams, Sweep) (stab_parse_sweep_input)."""
+    lib = load()
+    p, sw = StabParams(), Sweep()
+    msg = ctypes.create_string_buffer(256)
+    rc = lib.stab_parse_sweep_input(text.encode(), ctypes.byref(p), ctypes.byref(sw), msg, 256)
+    if rc:
+        raise StabError(f"input: {msg.value.decode()}")
+    return p, sw
+
+
+def read_delta(path: str):
+    """delta.dat rows (xb, delta) (mspatial.f90:29-63)."""
+    lib = load()
+    n = ctypes.c_int32()
+    if lib.stab_read_delta(path.encode(), 0, None, None, ctypes.byref(n)):
+        raise StabError(f"cannot read {path}")
+    xb, de = np.zeros(n.value), np.zeros(n.value)
+    if lib.stab_read_delta(path.encode(), n.value, _dptr(xb), _dptr(de), ctypes.byref(n)):
+        raise StabError(f"cannot read {path}")
+    return xb, de
+
+
+def read_body(path: str) -> np.ndarray:
+    """body.dat stations xb (getab.f90:73-86)."""
+    lib = load()
+    n = ctypes.c_int32()
+    if lib.stab_read_body(path.encode(), 0, None, ctypes.byref(n)):
+        raise StabError(f"cannot read {path}")
+    xb = np.zeros(n.value)
+    if lib.stab_read_body(path.encode(), n.value, _dptr(xb), ctypes.byref(n)):
+        raise StabError(f"cannot read {path}")
+    return xb
+
+
+def eig_name(iver: int) -> str:
+    buf = ctypes.create_string_buffer(64)
+    if load().stab_eig_name(iver, buf, 64):
+        raise StabError("iver out of range")
+    return buf.value.decode()
+
+
+def stab_out_line(p: float, value: complex, ind=None) -> str:
+    """One stab.out / parm.new line (stab_stab_out_line)."""
+    buf = ctypes.create_string_buffer(160)
+    v = complex(value)
+    rc = load().stab_stab_out_line(0 if ind is None else 1, 0 if ind is None else int(ind), float(p), v.real, v.imag,
+                                   buf, 160)
+    if rc < 0:
+        raise StabError("line does not fit")
+    return buf.value.decode()
+
+
+def sweep_points(base: StabParams, sw: Sweep, xb=None, delta=None):
+    """The solves of a sweep in the reference's loop order (stab_sweep_points)."""
+    lib = load()
+    nb = 0 if xb is None else len(xb)
+    xa = None if xb is None else np.ascontiguousarray(xb, dtype=np.float64)
+    da = None if delta is None else np.ascontiguousarray(delta, dtype=np.float64)
+    n = ctypes.c_int32()
+    if lib.stab_sweep_points(ctypes.byref(base), ctypes.byref(sw), nb, _dptr(xa) if xa is not None else None,
+                             _dptr(da) if da is not None else None, 0, None, ctypes.byref(n)):
+        raise StabError("invalid sweep")
+    pts = (StabParams * max(n.value, 1))()
+    if lib.stab_sweep_points(ctypes.byref(base), ctypes.byref(sw), nb, _dptr(xa) if xa is not None else None,
+                             _dptr(da) if da is not None else None, n.value, pts, ctypes.byref(n)):
+        raise StabError("invalid sweep")
+    return [pts[k] for k in range(n.value)]
 
 
 def profile_name(ind: int) -> str:

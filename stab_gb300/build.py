@@ -12,8 +12,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libstab_gb300.so")
 BIN = os.path.join(HERE, "bin")
-# command-line drop-ins over the C ABI: `stab < input.dat` and `getevec`
-TOOLS = {"stab_gpu": "stab_main.cpp", "getevec_gpu": "getevec_main.cpp"}
+# command-line drop-ins over the C ABI: `stab < input.dat` (with the sweep
+# drivers), `getevec` and the sweep post-processors getab, getax, getalpha
+TOOLS = {"stab_gpu": "stab_main.cpp", "getevec_gpu": "getevec_main.cpp", "getab_gpu": "post_main.cpp",
+         "getax_gpu": "post_main.cpp", "getalpha_gpu": "post_main.cpp"}
 
 CU_SOURCES = ["prep.cu", "assemble.cu", "lu.cu", "lu_tc.cu", "hqr.cu", "polish.cu", "post.cu", "mlp.cu", "capi.cu", "fileio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -2,6 +2,13 @@
 //
 //   stab_parse_input       stdin of `stab < input.dat`: input.f90:15-123 and the
 //                          index / x reads of stab.f90:46-55
+//   stab_parse_sweep_input the same with the multi-point drivers (itype 7,
+//                          mtemporal.f90:20-23; itype 8, mspatial.f90:20-27)
+//   stab_sweep_points      the drivers' loops (mtemporal.f90:25-39,
+//                          mspatial.f90:65-96) as a list of solves
+//   stab_read_delta        delta.dat (mspatial.f90:29-63)
+//   stab_read_body         body.dat (getab.f90:73-86, getalpha.f90:36-53)
+//   stab_eig_name          eig.<iver> (makename, mtemporal.f90:53-76)
 //   stab_read_profile      profile.<ind>: rows "y rho u v w T", records that
 //                          start with '#' skipped (getmean.f90:27-80)
 //   stab_grid              Gauss-Lobatto points and the algebraic maps
@@ -17,6 +24,7 @@
 //                          only the real part of the running pick is kept)
 //
 // Nothing here touches the GPU; these run wherever the library loads.
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -166,11 +174,12 @@ bool get_record(std::FILE* f, std::vector<unsigned char>& rec) {
 
 }  // namespace
 
-extern "C" {
-
-int stab_parse_input(const char* text, stab_params* p, char* msg, size_t msg_cap) {
+// The stdin protocol shared by stab_parse_input (itypes 1 and 2) and
+// stab_parse_sweep_input (also the multi-point drivers, itypes 7 and 8).
+static int parse_protocol(const char* text, stab_params* p, stab_sweep* sw, char* msg, size_t msg_cap) {
   if (!text || !p) return STAB_ERR_ARG;
   std::memset(p, 0, sizeof(*p));
+  if (sw) std::memset(sw, 0, sizeof(*sw));
   ListReader rd(text);
   std::vector<std::string> v;
   // a read cut short by '/' leaves the remaining items as they were
@@ -228,10 +237,39 @@ int stab_parse_input(const char* text, stab_params* p, char* msg, size_t msg_cap
   do {
     if (!ints(1, &p->itype, "itype")) return STAB_ERR_ARG;
   } while (p->itype < 1 || p->itype > 9);
+  if (sw && (p->itype == 7 || p->itype == 8)) {
+    // stab.f90:85-90: the drivers run with ind = 0 and itype 1 / 2; input.f90
+    // reads no wavenumbers for them (input.f90:104-115)
+    sw->itype = p->itype;
+    p->itype = (sw->itype == 7) ? 1 : 2;
+    double r[3];
+    // mtemporal.f90:20-23 / mspatial.f90:20-23
+    if (!reals(3, r, sw->itype == 7 ? "alpha_min, alpha_max, alpha_inc" : "omega_min, omega_max, omega_inc"))
+      return STAB_ERR_ARG;
+    sw->p_min = r[0]; sw->p_max = r[1]; sw->p_inc = r[2];
+    if (!reals(3, r, "beta_min, beta_max, beta_inc")) return STAB_ERR_ARG;
+    sw->b_min = r[0]; sw->b_max = r[1]; sw->b_inc = r[2];
+    if (sw->itype == 8) {
+      int32_t ii[3];
+      if (!ints(3, ii, "ind1, ind2, ind_inc")) return STAB_ERR_ARG;   // mspatial.f90:24-25
+      sw->ind1 = ii[0]; sw->ind2 = ii[1]; sw->ind_inc = ii[2];
+      if (!ints(1, &sw->dtype, "dtype")) return STAB_ERR_ARG;         // mspatial.f90:26-27
+      if (sw->dtype != 0) {
+        set_msg(msg, msg_cap, "dtype 1 (finite-difference spatial solver) is outside the Chebyshev path");
+        return STAB_ERR_ARG;
+      }
+    }
+    if (p->ny < 2) {
+      set_msg(msg, msg_cap, "ny < 2");
+      return STAB_ERR_ARG;
+    }
+    return STAB_OK;
+  }
   if (p->itype != 1 && p->itype != 2) {
     set_msg(msg, msg_cap, "itype " + std::to_string(p->itype) +
-                              " (finite-difference, Stokes, bump or multi-point driver) is outside the Chebyshev "
-                              "temporal/spatial path");
+                              (sw ? " (finite-difference, Stokes or bump solver)" :
+                                    " (finite-difference, Stokes, bump or multi-point driver)") +
+                              " is outside the Chebyshev temporal/spatial path");
     return STAB_ERR_ARG;
   }
   if (p->itype == 1) {
@@ -245,6 +283,157 @@ int stab_parse_input(const char* text, stab_params* p, char* msg, size_t msg_cap
   if (p->ny < 2) {
     set_msg(msg, msg_cap, "ny < 2");
     return STAB_ERR_ARG;
+  }
+  return STAB_OK;
+}
+
+extern "C" {
+
+int stab_parse_input(const char* text, stab_params* p, char* msg, size_t msg_cap) {
+  return parse_protocol(text, p, nullptr, msg, msg_cap);
+}
+
+int stab_parse_sweep_input(const char* text, stab_params* p, stab_sweep* sw, char* msg, size_t msg_cap) {
+  if (!sw) return STAB_ERR_ARG;
+  return parse_protocol(text, p, sw, msg, msg_cap);
+}
+
+int stab_read_delta(const char* path, int32_t cap, double* xb, double* delta, int32_t* nbody) {
+  // mspatial.f90:29-63: every record that does not start with '#' holds
+  // "xb delta" (list-directed; further items ignored)
+  if (!path || !nbody) return STAB_ERR_ARG;
+  std::FILE* f = std::fopen(path, "r");
+  if (!f) return STAB_ERR_IO;
+  int32_t n = 0;
+  char line[4096];
+  int rc = STAB_OK;
+  while (std::fgets(line, sizeof(line), f)) {
+    if (line[0] == '#') continue;
+    ListReader rd(line);
+    std::vector<std::string> v;
+    double a = 0.0, b = 0.0;
+    if (rd.read(2, v) < 2 || !to_real(v[0], a) || !to_real(v[1], b)) {
+      rc = STAB_ERR_IO;
+      break;
+    }
+    if (xb && delta) {
+      if (n >= cap) { rc = STAB_ERR_ARG; break; }
+      xb[n] = a;
+      delta[n] = b;
+    }
+    ++n;
+  }
+  std::fclose(f);
+  *nbody = n;
+  return rc;
+}
+
+int stab_read_body(const char* path, int32_t cap, double* xb, int32_t* nbody) {
+  // getab.f90:73-86, getalpha.f90:36-53: one record per station, "index xb"
+  if (!path || !nbody) return STAB_ERR_ARG;
+  std::FILE* f = std::fopen(path, "r");
+  if (!f) return STAB_ERR_IO;
+  int32_t n = 0;
+  char line[4096];
+  int rc = STAB_OK;
+  while (std::fgets(line, sizeof(line), f)) {
+    ListReader rd(line);
+    std::vector<std::string> v;
+    if (rd.read(2, v) == 0) break;   // the reference's counting read stops at the end of the data
+    int32_t it = 0;
+    double a = 0.0;
+    if (v.size() < 2 || !to_int(v[0], it) || !to_real(v[1], a)) {
+      rc = STAB_ERR_IO;
+      break;
+    }
+    if (xb) {
+      if (n >= cap) { rc = STAB_ERR_ARG; break; }
+      xb[n] = a;
+    }
+    ++n;
+  }
+  std::fclose(f);
+  *nbody = n;
+  return rc;
+}
+
+int stab_stab_out_line(int32_t with_ind, int32_t ind, double p, double vr, double vi, char* out, size_t cap) {
+  // getab.f90:211 format 60: 3(1x,1pe20.13); getax.f90:214 / getalpha.f90:167
+  // format 50: i4,3(1x,1pe20.13)
+  if (!out || cap == 0) return STAB_ERR_ARG;
+  std::string s;
+  if (with_ind) {
+    char b[32];
+    std::snprintf(b, sizeof(b), "%4d", (int)ind);
+    s = (std::strlen(b) > 4) ? std::string(4, '*') : std::string(b);
+  }
+  for (double x : {p, vr, vi}) s += " " + fortran_e(x, 20, 13, 0);
+  if (s.size() + 1 > cap) return STAB_ERR_ARG;
+  std::memcpy(out, s.c_str(), s.size() + 1);
+  return (int)s.size();
+}
+
+int stab_eig_name(int32_t iver, char* out, size_t cap) {
+  // makename (mtemporal.f90:53-76): "eig." + iver in I1..I4
+  if (!out || iver < 0 || iver > 9999) return STAB_ERR_ARG;
+  std::snprintf(out, cap, "eig.%d", (int)iver);
+  return STAB_OK;
+}
+
+int stab_sweep_points(const stab_params* base, const stab_sweep* sw, int32_t nbody, const double* xb,
+                      const double* delta, int32_t cap, stab_params* points, int32_t* count) {
+  if (!base || !sw || !count) return STAB_ERR_ARG;
+  std::vector<stab_params> pts;
+  if (sw->itype == 7) {
+    // mtemporal.f90:25-39: na = max(nint((amax-amin)/ainc), 1) (amax itself
+    // is not reached), beta innermost, profile.0
+    if (sw->p_inc == 0.0 || sw->b_inc == 0.0) return STAB_ERR_ARG;
+    const int na = std::max((int)std::lround((sw->p_max - sw->p_min) / sw->p_inc), 1);
+    const int nb = std::max((int)std::lround((sw->b_max - sw->b_min) / sw->b_inc), 1);
+    for (int ia = 1; ia <= na; ++ia)
+      for (int ib = 1; ib <= nb; ++ib) {
+        stab_params q = *base;
+        q.itype = 1;
+        q.ind = 0;
+        q.alpha[0] = sw->p_min + (double)(ia - 1) * sw->p_inc;
+        q.alpha[1] = 0.0;
+        q.beta[0] = sw->b_min + (double)(ib - 1) * sw->b_inc;
+        q.beta[1] = 0.0;
+        pts.push_back(q);
+      }
+  } else if (sw->itype == 8) {
+    // mspatial.f90:65-96: zero increments become one, no = nint(...) + 1,
+    // stations ind1..ind2 step ind_inc with x = xb(ind), Yi = 2 delta(ind)
+    if (!xb || !delta) return STAB_ERR_ARG;
+    const int i1 = sw->ind1, i2 = sw->ind2;
+    if (i1 < 1 || i2 > nbody) return STAB_ERR_ARG;
+    const double oinc = (sw->p_inc == 0.0) ? 1.0 : sw->p_inc;
+    const double binc = (sw->b_inc == 0.0) ? 1.0 : sw->b_inc;
+    const int inc = (sw->ind_inc == 0) ? 1 : sw->ind_inc;
+    const int no = (int)std::lround((sw->p_max - sw->p_min) / oinc) + 1;
+    const int nb = (int)std::lround((sw->b_max - sw->b_min) / binc) + 1;
+    for (int ind = i1; inc > 0 ? ind <= i2 : ind >= i2; ind += inc)
+      for (int io = 1; io <= no; ++io)
+        for (int ib = 1; ib <= nb; ++ib) {
+          stab_params q = *base;
+          q.itype = 2;
+          q.ind = ind;
+          q.x = xb[ind - 1];
+          q.yi = 2.0 * delta[ind - 1];
+          q.omega[0] = sw->p_min + (double)(io - 1) * oinc;
+          q.omega[1] = 0.0;
+          q.beta[0] = sw->b_min + (double)(ib - 1) * binc;
+          q.beta[1] = 0.0;
+          q.alpha[0] = q.alpha[1] = 0.0;
+          pts.push_back(q);
+        }
+  } else {
+    return STAB_ERR_ARG;
+  }
+  *count = (int32_t)pts.size();
+  if (points) {
+    if ((int32_t)pts.size() > cap) return STAB_ERR_ARG;
+    std::memcpy(points, pts.data(), sizeof(stab_params) * pts.size());
   }
   return STAB_OK;
 }

@@ -2,6 +2,10 @@
 // reference's stdin protocol (input.f90:15-123, stab.f90:46-55), the mean
 // flow from profile.<ind> in the working directory, solves on the GPU and
 // writes evec.dat as temporal.f90:883-890 / spatial.f90:1120-1126 do.
+// The multi-point drivers (itype 7, mtemporal.f90; itype 8, mspatial.f90
+// with delta.dat) solve every sweep point in one batch and write each
+// point's eigensystem to eig.<iver>, as the drivers' temporal('eig.<iver>')
+// / spatial('eig.<iver>') calls do.
 //
 //   stab_gpu [-d device] [-o evec.dat] < input.dat
 //
@@ -24,6 +28,119 @@ static int fail(const char* what, int rc, stab_ctx* ctx) {
   return 1;
 }
 
+static bool load_profile(int32_t ind, std::vector<double>& prof, int32_t& nym) {
+  char pname[64];
+  stab_profile_name(ind, pname, sizeof(pname));
+  nym = 0;
+  if (stab_read_profile(pname, 0, nullptr, &nym)) {
+    std::fprintf(stderr, "stab_gpu: cannot read %s\n", pname);
+    return false;
+  }
+  prof.assign(6 * (size_t)nym, 0.0);
+  if (stab_read_profile(pname, nym, prof.data(), &nym)) {
+    std::fprintf(stderr, "stab_gpu: cannot read %s\n", pname);
+    return false;
+  }
+  return true;
+}
+
+// itype 7 / 8: every point of the sweep in one batch of the plain FP64
+// path, then each point's eigensystem to eig.<iver>
+static int run_sweep(const stab_params& base, const stab_sweep& sw, int device) {
+  std::vector<double> xb, delta;
+  int32_t nbody = 0;
+  if (sw.itype == 8) {
+    if (stab_read_delta("delta.dat", 0, nullptr, nullptr, &nbody) || nbody < 1) {
+      std::fprintf(stderr, "stab_gpu: cannot read delta.dat\n");
+      return 1;
+    }
+    xb.resize(nbody);
+    delta.resize(nbody);
+    stab_read_delta("delta.dat", nbody, xb.data(), delta.data(), &nbody);
+    if (sw.ind1 < 1 || sw.ind2 > nbody) {
+      std::fprintf(stderr, "ERROR: illegal index...check delta.dat\n");   // mspatial.f90:45-49
+      return 1;
+    }
+  }
+  int32_t np = 0;
+  if (stab_sweep_points(&base, &sw, nbody, xb.data(), delta.data(), 0, nullptr, &np) || np < 1) {
+    std::fprintf(stderr, "stab_gpu: empty or invalid sweep\n");
+    return 1;
+  }
+  std::vector<stab_params> pts(np);
+  stab_sweep_points(&base, &sw, nbody, xb.data(), delta.data(), np, pts.data(), &np);
+  // one profile per distinct index
+  std::vector<std::vector<double>> profs;
+  std::vector<int32_t> pind, pnym;
+  std::vector<const double*> pp(np);
+  std::vector<int32_t> nyms(np);
+  for (int k = 0; k < np; ++k) {
+    int slot = -1;
+    for (size_t q = 0; q < pind.size(); ++q)
+      if (pind[q] == pts[k].ind) slot = (int)q;
+    if (slot < 0) {
+      std::vector<double> pr;
+      int32_t nym = 0;
+      if (!load_profile(pts[k].ind, pr, nym)) return 1;
+      profs.push_back(std::move(pr));
+      pind.push_back(pts[k].ind);
+      pnym.push_back(nym);
+      slot = (int)profs.size() - 1;
+    }
+    nyms[k] = pnym[slot];
+  }
+  for (int k = 0; k < np; ++k)
+    for (size_t q = 0; q < pind.size(); ++q)
+      if (pind[q] == pts[k].ind) pp[k] = profs[q].data();
+  stab_ctx* ctx = nullptr;
+  int rc = stab_create(&ctx, device);
+  if (rc) return fail("stab_create", rc, nullptr);
+  stab_batch* b = nullptr;
+  rc = stab_batch_create(ctx, np, pts.data(), nyms.data(), pp.data(), &b);
+  if (rc) return fail("stab_batch_create", rc, ctx);
+  rc = stab_batch_run(b, STAB_MODE_PLAIN);
+  if (rc) return fail("stab_batch_run", rc, ctx);
+  std::vector<std::vector<double>> eig(np);
+  std::vector<double*> ep(np);
+  for (int k = 0; k < np; ++k) {
+    eig[k].assign(2 * (size_t)(pts[k].itype == 1 ? 5 : 10) * pts[k].ny, 0.0);
+    ep[k] = eig[k].data();
+  }
+  rc = stab_batch_spectra(b, ep.data());
+  if (rc) return fail("stab_batch_spectra", rc, ctx);
+  std::vector<double> least(2 * (size_t)np);
+  std::vector<int32_t> st(np);
+  rc = stab_batch_results(b, least.data(), nullptr, nullptr, st.data(), nullptr);
+  if (rc) return fail("stab_batch_results", rc, ctx);
+  stab_batch_destroy(b);
+  for (int k = 0; k < np; ++k) {
+    const stab_params& q = pts[k];
+    const int64_t m = (int64_t)(q.itype == 1 ? 5 : 10) * q.ny;
+    std::vector<double> vec;
+    const bool want_vec = (q.itype == 1 || q.ievec == 1);
+    if (want_vec) {
+      vec.resize(2 * m * m);
+      std::vector<int32_t> vs(m);
+      rc = stab_eigenvectors(ctx, &q, nyms[k], pp[k], (int32_t)m, eig[k].data(), vec.data(), vs.data());
+      if (rc) return fail("stab_eigenvectors", rc, ctx);
+    }
+    char name[64];
+    stab_eig_name(k + 1, name, sizeof(name));
+    rc = stab_write_evec(name, &q, eig[k].data(), want_vec ? vec.data() : nullptr);
+    if (rc) return fail("stab_write_evec", rc, ctx);
+    if (q.itype == 1)
+      std::printf("%4d  alpha = (%.6e, %.6e)  beta = (%.6e, %.6e)  least-stable omega = (%.15e, %.15e)  status %d  "
+                  "-> %s\n", k + 1, q.alpha[0], q.alpha[1], q.beta[0], q.beta[1], least[2 * k], least[2 * k + 1],
+                  st[k], name);
+    else
+      std::printf("%4d  ind %d  x = %.6e  Yi = %.6e  omega = (%.6e, %.6e)  beta = (%.6e, %.6e)  least-stable alpha = "
+                  "(%.15e, %.15e)  status %d  -> %s\n", k + 1, q.ind, q.x, q.yi, q.omega[0], q.omega[1], q.beta[0],
+                  q.beta[1], least[2 * k], least[2 * k + 1], st[k], name);
+  }
+  stab_destroy(ctx);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   int device = 0;
   std::string out = "evec.dat";
@@ -39,12 +156,14 @@ int main(int argc, char** argv) {
   }
   std::string text((std::istreambuf_iterator<char>(std::cin)), std::istreambuf_iterator<char>());
   stab_params p;
+  stab_sweep sw;
   char msg[256] = {0};
-  int rc = stab_parse_input(text.c_str(), &p, msg, sizeof(msg));
+  int rc = stab_parse_sweep_input(text.c_str(), &p, &sw, msg, sizeof(msg));
   if (rc) {
     std::fprintf(stderr, "stab_gpu: input: %s\n", msg);
     return 1;
   }
+  if (sw.itype == 7 || sw.itype == 8) return run_sweep(p, sw, device);
   char pname[64];
   stab_profile_name(p.ind, pname, sizeof(pname));
   int32_t nym = 0;

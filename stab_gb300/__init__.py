@@ -32,6 +32,7 @@ MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE, MODE_TRACK = 0, 1, 2, 3, 4
 # arithmetic per stage (stab_set_arithmetic)
 STAGE_SEED_EIG, STAGE_PLAIN_EIG, STAGE_RETRY_LU, STAGE_POLISH_LU = 0, 1, 2, 3
 ARITH_FP64, ARITH_DOUBLE_WORD, ARITH_FP32, ARITH_TF32_SPLIT = 0, 1, 2, 3
+OPT_SEED_QR_SHARED = 1
 ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE, ST_UNVERIFIED = 0, 1, 2, 3, 4, 5, 6
 
 EXPORTED = (
@@ -44,7 +45,7 @@ EXPORTED = (
     "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
-    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_lu_tc_check", "stab_set_arithmetic", "stab_set_seed_size",
+    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_lu_tc_check", "stab_set_option", "stab_set_arithmetic", "stab_set_seed_size",
 )
 
 
@@ -178,6 +179,7 @@ def load(path: str = LIB_PATH):
     lib.stab_set_seed_size.argtypes = [vp, i32]
     lib.stab_lu_cluster_check.argtypes = [vp, i32, i32, i32, P(dbl), P(i32)]
     lib.stab_lu_tc_check.argtypes = [vp, i32, i32, P(dbl), P(dbl), P(i32)]
+    lib.stab_set_option.argtypes = [vp, i32, i32]
     _lib = lib
     return lib
 
@@ -418,6 +420,10 @@ class Context:
         self._check(self.lib.stab_lu_cluster_check(self.h, n, count, 1 if complex128 else 0, ctypes.byref(md),
                                                    ctypes.byref(pd)))
         return md.value, pd.value
+
+    def set_option(self, option: int, value: int) -> None:
+        """stab_set_option: OPT_SEED_QR_SHARED (1 default, 0 off)."""
+        self._check(self.lib.stab_set_option(self.h, int(option), int(value)))
 
     def lu_tc_check(self, n: int, count: int):
         """(backward error with the tensor-core update, backward error on the

@@ -69,6 +69,7 @@ struct stab_ctx {
   // arithmetic per stage (STAB_STAGE_*)
   int arith[4] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD, STAB_ARITH_TF32_SPLIT};
   int seed_ny = 32;        // N of the seed spectrum of STAB_MODE_COARSE / SURROGATE
+  int seed_qr_shared = 1;  // STAB_OPT_SEED_QR_SHARED
 };
 
 // size class of an LU order for the tuned panel-width table
@@ -703,7 +704,8 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
                             b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
                             b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
                             b->flops.as<double>(), grid, s,
-                            c->arith[seed ? STAB_STAGE_SEED_EIG : STAB_STAGE_PLAIN_EIG] == STAB_ARITH_DOUBLE_WORD);
+                            c->arith[seed ? STAB_STAGE_SEED_EIG : STAB_STAGE_PLAIN_EIG] == STAB_ARITH_DOUBLE_WORD,
+                            seed && c->seed_qr_shared);
   }));
   CK(c, timed(c, "k_post_spectrum", [&] {
     size_t sm = sizeof(zc) * b->mmax;
@@ -1682,6 +1684,15 @@ int stab_set_arithmetic(stab_ctx* c, int32_t stage, int32_t arithmetic) {
   }
   c->arith[stage] = arithmetic;
   return STAB_OK;
+}
+
+int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
+  if (!c) return STAB_ERR_ARG;
+  if (option == STAB_OPT_SEED_QR_SHARED) {
+    c->seed_qr_shared = value ? 1 : 0;
+    return STAB_OK;
+  }
+  return set_err(c, STAB_ERR_ARG, "unknown option");
 }
 
 int stab_set_seed_size(stab_ctx* c, int32_t ny) {

@@ -7,10 +7,14 @@
 #pragma once
 
 // dynamic shared memory of eig_plain_body: the active flags and the active
-// list (m ints each, rounded up to 16 bytes), then the vectors v, w, z, vn
-inline size_t eig_plain_smem_bytes(int mmax) {
+// list (m ints each, rounded up to 16 bytes), then the vectors v, w, z, vn;
+// with the QR in shared memory (qr_smem) that region also holds the packed
+// Hessenberg matrix of the QR phase
+inline size_t eig_plain_smem_bytes(int mmax, bool qr_smem = false) {
   const size_t head = ((2 * (size_t)mmax * sizeof(int) + 15) / 16) * 16;
-  return head + 4 * (size_t)mmax * sizeof(zc);
+  size_t vec = 4 * (size_t)mmax;
+  if (qr_smem) vec = std::max(vec, (size_t)hess_packed_size(mmax));
+  return head + vec * sizeof(zc);
 }
 
 // The eigensolver of one CTA over a persistent queue of instances; it runs
@@ -20,7 +24,10 @@ inline size_t eig_plain_smem_bytes(int mmax) {
 // by a power of two that brings its largest entry near 1 (the float exponent
 // range is narrow), again after balancing, and the QR eigenvalues are scaled
 // back; the isolated eigenvalues come straight from the FP64 input.
-template <class C>
+// QS: the QR phase runs on a packed copy of the Hessenberg matrix in shared
+// memory (the kernel's dynamic shared memory was sized with qr_smem), the
+// other phases on the working matrix in global memory as before.
+template <class C, bool QS = false>
 __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restrict__ msz, zc* __restrict__ A,
                                                const int64_t* __restrict__ a_off, zc* __restrict__ Hp,
                                                const int64_t* __restrict__ h_off, zc* __restrict__ eig,
@@ -336,20 +343,32 @@ __device__ __forceinline__ void eig_plain_body(int count, const int32_t* __restr
     }
     phase(3);
     // ---- 5. QR iteration on the packed matrix ---------------------------------
-    // in-place repack of H (ld = mp) to the column-packed layout: a packed
-    // offset never exceeds the unpacked one, so moving column by column in
-    // increasing order through shared memory is safe
-    for (int c = 0; c < mp; ++c) {
-      const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
-      for (int r = tid; r <= rmax; r += NTH) v[r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : ew<C>::zero();
+    C* Hq = Hg;
+    if constexpr (QS) {
+      // packed copy in shared memory (the vectors' region, no longer needed)
+      Hq = zs;
+      for (int c = 0; c < mp; ++c) {
+        const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
+        const int64_t o = hess_coff(c, mp);
+        for (int r = tid; r <= rmax; r += NTH) Hq[o + r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : ew<C>::zero();
+      }
       __syncthreads();
-      const int64_t o = hess_coff(c, mp);
-      for (int r = tid; r <= rmax; r += NTH) Hg[o + r] = v[r];
-      __syncthreads();
+    } else {
+      // in-place repack of H (ld = mp) to the column-packed layout: a packed
+      // offset never exceeds the unpacked one, so moving column by column in
+      // increasing order through shared memory is safe
+      for (int c = 0; c < mp; ++c) {
+        const int rmax = (c + 2 < mp - 1) ? c + 2 : mp - 1;
+        for (int r = tid; r <= rmax; r += NTH) v[r] = (r <= c + 1) ? Hg[(size_t)c * ld + r] : ew<C>::zero();
+        __syncthreads();
+        const int64_t o = hess_coff(c, mp);
+        for (int r = tid; r <= rmax; r += NTH) Hg[o + r] = v[r];
+        __syncthreads();
+      }
     }
     phase(4);
     long long upd = 0;   // 2-element reflector applications (24 flops each), thread 0
-    int st = qr_eigs<C, true>(SAcc<C>{Hg, mp}, mp, ev, s, s.refl, upd);
+    int st = qr_eigs<C, true>(SAcc<C>{Hq, mp}, mp, ev, s, s.refl, upd);
     flops += 24.0 * (double)upd;
     if (unscale != 1.0)
       for (int q = tid; q < mp; q += NTH) ev[q] = zscale(ev[q], unscale);

@@ -33,6 +33,7 @@
 //
 // Every loop has an iteration cap; an instance that hits it gets status
 // STAB_ST_NOCONV and NaN for the missing values.
+#include <algorithm>
 #include <mutex>
 #include <type_traits>
 
@@ -77,6 +78,20 @@ __global__ void __launch_bounds__(HQ_WIDE, 1) k_eig_plain_wide(EIG_PLAIN_ARGS) {
 }
 
 
+// The seed batches (order m <= 160 at N = 32): one 512-thread CTA per SM,
+// the QR phase on the packed Hessenberg matrix in shared memory.  With one
+// instance per SM the working matrices of the reduction (152 x 410 KB in
+// double-word form) stay in L2, and the QR's bulge steps read and write
+// shared memory instead of L2 / HBM.
+template <class C>
+__global__ void __launch_bounds__(HQ_WIDE, 1) k_eig_plain_sq(EIG_PLAIN_ARGS) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ HqrSmem<C> s;
+  __shared__ int s_inst;
+  eig_plain_body<C, true>(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw,
+                          s, s_inst);
+}
+
 cudaError_t eig_phase_cycles(unsigned long long* out, bool reset) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_eig_phase_cycles, sizeof(unsigned long long) * 6);
   if (e != cudaSuccess || !reset) return e;
@@ -90,7 +105,7 @@ template <class C>
 static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
                                 const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
                                 int32_t* work_counter, const int32_t* order, double* flops, int grid,
-                                cudaStream_t s) {
+                                cudaStream_t s, bool qr_smem) {
   size_t sm = eig_plain_smem(mmax);
   cudaError_t e = cudaFuncSetAttribute(k_eig_plain<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -99,6 +114,16 @@ static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, 
   int dev = 0, sms = 1, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t sm_q = eig_plain_smem_bytes(mmax, true) + sizeof(HqrSmem<C>) + 64;
+  if (qr_smem && count * 2 > sms && sm_q <= 227 * 1024) {
+    const size_t dyn = eig_plain_smem_bytes(mmax, true);
+    e = cudaFuncSetAttribute(k_eig_plain_sq<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    const int g = std::min(count, sms);
+    k_eig_plain_sq<C><<<g, HQ_WIDE, dyn, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
+                                              order, flops);
+    return cudaGetLastError();
+  }
   if (count * 2 <= sms) {
     // a few instances: one wide CTA each, so every phase spreads over 16 warps
     e = cudaFuncSetAttribute(k_eig_plain_wide<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -121,12 +146,12 @@ static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, 
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
                              const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
                              int32_t* work_counter, const int32_t* order, double* flops, int grid,
-                             cudaStream_t s, bool double_word) {
+                             cudaStream_t s, bool double_word, bool qr_smem) {
   if (count <= 0) return cudaSuccess;
   return double_word ? launch_eig_t<dz>(count, mmax, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
-                                        order, flops, grid, s)
+                                        order, flops, grid, s, qr_smem)
                      : launch_eig_t<zc>(count, mmax, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
-                                        order, flops, grid, s);
+                                        order, flops, grid, s, qr_smem);
 }
 
 }  // namespace stab

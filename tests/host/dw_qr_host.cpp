@@ -67,10 +67,10 @@ static std::vector<zc> run_qr(const std::vector<zc>& Hd, int mp, int& st, long l
   return ev;
 }
 
-template <class C>
+template <class C, bool QS = false>
 static std::vector<zc> run_body(const std::vector<zc>& A, int m, int& st, long long& upd) {
   std::vector<zc> M(A), Hw((size_t)m * m), ev(m);
-  std::vector<unsigned char> smraw(eig_plain_smem_bytes(m));
+  std::vector<unsigned char> smraw(eig_plain_smem_bytes(m, QS));
   const int32_t msz = m;
   const int64_t off = 0;
   int32_t status = -1, counter = 0;
@@ -78,8 +78,8 @@ static std::vector<zc> run_body(const std::vector<zc>& A, int m, int& st, long l
   static HqrSmem<C> s;
   static int s_inst;
   run_block([&](int) {
-    eig_plain_body<C>(1, &msz, M.data(), &off, Hw.data(), &off, ev.data(), &off, &status, &counter, nullptr, &flops,
-                      smraw.data(), s, s_inst);
+    eig_plain_body<C, QS>(1, &msz, M.data(), &off, Hw.data(), &off, ev.data(), &off, &status, &counter, nullptr,
+                          &flops, smraw.data(), s, s_inst);
   });
   st = status;
   upd = (long long)flops;
@@ -108,6 +108,9 @@ int main(int argc, char** argv) {
   } else if (mode == "body") {
     if (!dw_only) e1 = run_body<zc>(H, m, st1, u1);
     e2 = run_body<dz>(H, m, st2, u2);
+  } else if (mode == "bodyq") {   // the QR phase on the packed copy in (shared) scratch memory
+    if (!dw_only) e1 = run_body<zc, true>(H, m, st1, u1);
+    e2 = run_body<dz, true>(H, m, st2, u2);
   } else {
     return 2;
   }

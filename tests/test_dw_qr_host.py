@@ -110,16 +110,17 @@ def test_double_word_qr_matches_numpy(harness, itype, seed, N):
     assert max(np.min(np.abs(edw - r)) for r in ref) < 1e-9
 
 
-def _run(exe, d, tag, X, threads=32):
+def _run(exe, d, tag, X, threads=32, mode="body"):
     """Whole kernel body on X with a block of `threads` (32: one warp; 128:
-    the four warps of the batch kernel)."""
+    the four warps of the batch kernel); mode "bodyq" runs the QR phase on
+    the packed copy in the shared-memory scratch (k_eig_plain_sq)."""
     m = X.shape[0]
-    fin, fout = os.path.join(d, f"b{tag}.bin"), os.path.join(d, f"bo{tag}.bin")
+    fin, fout = os.path.join(d, f"b{tag}.bin"), os.path.join(d, f"bo{tag}{mode}.bin")
     with open(fin, "wb") as f:
         f.write(np.int32(m).tobytes())
         f.write(np.asfortranarray(X).astype(np.complex128).tobytes(order="F"))
     env = dict(os.environ, HOST_BLOCK_THREADS=str(threads))
-    subprocess.run([exe, "body", fin, fout], check=True, timeout=600, env=env)
+    subprocess.run([exe, mode, fin, fout], check=True, timeout=600, env=env)
     raw = open(fout, "rb").read()
     st64, stdw = np.frombuffer(raw[:8], np.int32)
     ev = np.frombuffer(raw[24:], np.complex128)
@@ -187,3 +188,17 @@ def test_kernel_body_memory_safe_under_asan():
             assert st64 == 0 and stdw == 0
     finally:
         shutil.rmtree(d, ignore_errors=True)
+
+
+@pytest.mark.parametrize("itype,N,M,threads", [(1, 12, 0.5, 32), (2, 10, 0.01, 128)])
+def test_shared_memory_qr_variant_is_bit_identical(harness, itype, N, M, threads):
+    """The variant with the QR phase on a packed copy in shared memory (the
+    seed kernel k_eig_plain_sq) computes the same operations on the same
+    values as the in-place repack: eigenvalues equal bit for bit, in FP64 and
+    double-word form."""
+    exe, d = harness
+    X = _operator(itype, 0, N, M)
+    a = _run(exe, d, f"q{itype}_{N}_{threads}", X, threads, "body")
+    b = _run(exe, d, f"q{itype}_{N}_{threads}", X, threads, "bodyq")
+    assert a[0] == b[0] == 0 and a[1] == b[1] == 0
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])

@@ -83,7 +83,9 @@ typedef struct stab_params {
     int32_t mattyp;   /* 0 constant mu, 1 Sutherland                         */
     int32_t ny;       /* collocation points N (polynomial degree N-1)        */
     int32_t ievec;    /* 1: eigenvectors wanted                              */
-    int32_t ider;     /* 1: internal derivatives (the only supported value) */
+    int32_t ider;     /* 1: mean derivatives by the collocation matrices;   *
+                       * 0: from tables (getmean2.f90): profile rows then  *
+                       * hold 18 values, the three tables side by side     */
     int32_t top;      /* spatial free-stream BC: 0 rho=0, 1 continuity       */
     int32_t wall;     /* carried through to evec.dat                         */
     int32_t wallt;    /* 0 isothermal, 2 adiabatic wall                      */
@@ -172,7 +174,12 @@ int stab_eig_phases(stab_ctx* ctx, uint64_t* cycles_out, int32_t reset);
  *   itype 2: mats_out = [C0 | C1 | C2], three n x n complex matrices
  *            (spatial.f90:677-959; (C0 + alpha C1 + alpha^2 C2) phi = 0).
  * profile: nym rows of (y, rho, u, v, w, T), row-major, as profile.<ind>
- * (getmean.f90:40-80; v is forced to zero).
+ * (getmean.f90:40-80; v is forced to zero).  With p->ider = 0 each row holds
+ * 18 values: the profile row, then the row of the first y-derivative table
+ * (first.<ind>) and of the second (second.<ind>), each "y f1..f5"
+ * (getmean2.f90:99-175: the tables are splined on their own y and taken as
+ * the mean derivatives without the map's chain rule).  The same holds for
+ * every entry point that takes profiles.
  * Replaces the inline assembly of temporal.f90:95-752 / spatial.f90:96-959.
  */
 int stab_assemble(stab_ctx* ctx, const stab_params* p, int32_t nym, const double* profile,

@@ -8,7 +8,8 @@ reference's own LAPACK calls (ZGESV, ZGETRF, ZGETRS, ZGEEV) taken from
 scipy's bundled LAPACK:
 
   grid            sgengrid.f90:2-45       (algebraic maps only)
-  mean profile    getmean.f90:2-122, spline.f90:2-75 (SPLINE / SPEVAL)
+  mean profile    getmean.f90:2-122, spline.f90:2-75 (SPLINE / SPEVAL);
+                  getmean2.f90:2-195 (ider = 0: derivative tables)
   materials       getmat.f90:2-37, input.f90:19-43 (incl. Te = T0 quirk)
   derivative mat  chebyd.f90:2-60 (CHEBYD, brute-force Lagrange form)
   temporal        temporal.f90:88-890
@@ -253,6 +254,28 @@ def getmean(ym: np.ndarray, vt: np.ndarray, y: np.ndarray) -> np.ndarray:
     return vm
 
 
+def getmean2(ym, vt, first, second, y):
+    """getmean2.f90:24-175 (ider = 0): the mean field as getmean, and its
+    first and second y-derivatives from their own tables (rows y f1..f5, the
+    mean's row count, v forced to zero), splined on the tables' own y and
+    clamped to each table's last row where y exceeds the MEAN profile's last
+    y (ymaxm is taken before the derivative reads overwrite ym).
+    Returns vm, g2vm, g22vm (ny, 5)."""
+    vm = getmean(ym, vt, y)
+    ymaxm = ym[-1]
+    out = []
+    for tab in (first, second):
+        ty = np.asarray(tab[:, 0], dtype=np.float64)
+        tv = np.asarray(tab[:, 1:6], dtype=np.float64).copy()
+        tv[:, 2] = 0.0
+        fdp = spline(ty, tv)
+        g = np.zeros((y.shape[0], NDOF))
+        for j, yy in enumerate(y):
+            g[j] = speval(ty, tv, fdp, yy) if yy <= ymaxm else tv[-1]
+        out.append(g)
+    return vm, out[0], out[1]
+
+
 def getmat(t, p: StabParams):
     """getmat.f90:2-37.  Returns (rmu, rlm, con, dmu, d2mu, dlm, d2lm, dcon, d2con)."""
     c0, c1, c2 = p.datmat()
@@ -308,12 +331,18 @@ class MeanState:
     g22vm: np.ndarray
 
 
-def mean_state(p: StabParams, ym: np.ndarray, vt: np.ndarray) -> MeanState:
+def mean_state(p: StabParams, ym: np.ndarray, vt: np.ndarray, first=None, second=None) -> MeanState:
     """Grid + mean flow + derivative matrices + mapped mean derivatives
-    (temporal.f90:95-179, spatial.f90:96-163)."""
+    (temporal.f90:95-179, spatial.f90:96-163).  With p.ider == 0 the mean
+    derivatives come from the tables `first` and `second` (getmean2) and
+    skip the collocation derivatives and the chain rule
+    (temporal.f90:149-179)."""
     ny = p.ny
     y, eta, deta, d2eta = sgengrid(ny, p.yi, p.ymax)
-    vm = getmean(ym, vt, y)
+    if not p.ider:
+        vm, g2, g22 = getmean2(ym, vt, first, second, y)
+    else:
+        vm = getmean(ym, vt, y)
     D1 = chebyd(ny - 1)
     D2 = D1 @ D1
     if p.wallt == 2:
@@ -322,10 +351,11 @@ def mean_state(p: StabParams, ym: np.ndarray, vt: np.ndarray) -> MeanState:
         Dt2 = D1 @ Dt1
     else:
         Dt1, Dt2 = D1, D2
-    g2 = D1 @ vm
-    g22 = D2 @ vm
-    g22 = g22 * (deta ** 2)[:, None] + g2 * d2eta[:, None]
-    g2 = g2 * deta[:, None]
+    if p.ider:
+        g2 = D1 @ vm
+        g22 = D2 @ vm
+        g22 = g22 * (deta ** 2)[:, None] + g2 * d2eta[:, None]
+        g2 = g2 * deta[:, None]
     return MeanState(y, eta, deta, d2eta, D1, D2, Dt1, Dt2, vm, g2, g22)
 
 
@@ -947,8 +977,8 @@ def spatial_solve(p: StabParams, ms: MeanState, want_vectors=True) -> Eigensyste
     return Eigensystem(p, ms, alp, evec)
 
 
-def solve(p: StabParams, ym, vt, want_vectors=True) -> Eigensystem:
-    ms = mean_state(p, ym, vt)
+def solve(p: StabParams, ym, vt, want_vectors=True, first=None, second=None) -> Eigensystem:
+    ms = mean_state(p, ym, vt, first, second)
     if p.itype == 1:
         return temporal_solve(p, ms, want_vectors)
     if p.itype == 2:

@@ -194,8 +194,9 @@ def _iptr(a: np.ndarray):
 
 def _prof(profile) -> np.ndarray:
     a = np.ascontiguousarray(profile, dtype=np.float64)
-    if a.ndim != 2 or a.shape[1] != 6:
-        raise ValueError("profile must be (nym, 6): y rho u v w T")
+    if a.ndim != 2 or a.shape[1] not in (6, 18):
+        raise ValueError("profile must be (nym, 6): y rho u v w T, or (nym, 18) with the derivative tables "
+                         "(ider = 0)")
     return a
 
 

@@ -283,7 +283,7 @@ static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDes
   if (q.itype != 1 && q.itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal) or 2 (spatial)");
   if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
   if (q.curve != 0) return set_err(c, STAB_ERR_ARG, "curve != 0 (curved walls) is not supported");
-  if (q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider = 0 (external derivatives) is not supported");
+  if (q.ider != 0 && q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider must be 0 or 1");
   if (q.wallt != 0 && q.wallt != 2) return set_err(c, STAB_ERR_ARG, "Illegal value of wallt");
   if (q.yi == 0.0) return set_err(c, STAB_ERR_ARG, "Yi = 0 (tanh map) is not supported");
   if (q.mattyp != 0 && q.mattyp != 1) return set_err(c, STAB_ERR_ARG, "mattyp must be 0 or 1");
@@ -310,6 +310,7 @@ static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDes
   d.nym = pd.nym;
   d.off_prof = pd.off_prof;
   d.off_spl = pd.off_spl;
+  d.ider = q.ider;
   return 0;
 }
 
@@ -429,31 +430,52 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return p[a].itype < p[bb].itype; });
   b->perm = idx;
   // profiles: dedupe by pointer; copied straight from caller memory in
-  // contiguous runs (validated on the device by k_spline)
+  // contiguous runs (validated on the device by k_spline).  With ider = 0 a
+  // row holds three tables side by side (mean, first and second
+  // y-derivatives, 6 values each): they become three consecutive profile
+  // entries, separated on the host.
   std::map<const double*, int> pidx;
   std::vector<ProfDesc> pds;
   std::vector<std::pair<const double*, int64_t>> runs;   // (source, doubles)
+  std::vector<std::vector<double>> staged;                // de-interleaved ider = 0 tables
   int64_t prof_off = 0, spl_off = 0;
   for (int i = 0; i < count; ++i) {
     const double* pp = profiles[i];
     if (!pp) return set_err(c, STAB_ERR_ARG, "null profile pointer");
     if (nym[i] < 4) return set_err(c, STAB_ERR_ARG, "profile needs at least 4 rows");
+    const int ntab = (p[i].ider == 0) ? 3 : 1;
     auto it = pidx.find(pp);
     if (it != pidx.end()) {
       if (pds[it->second].nym != nym[i]) return set_err(c, STAB_ERR_ARG, "same profile pointer with different nym");
+      if ((pds[it->second].three != 0) != (ntab == 3))
+        return set_err(c, STAB_ERR_ARG, "same profile pointer with different ider");
       continue;
     }
-    ProfDesc pd{};
-    pd.off_prof = prof_off;
-    pd.off_spl = spl_off;
-    pd.nym = nym[i];
-    const int64_t len = (int64_t)nym[i] * 6;
-    if (!runs.empty() && runs.back().first + runs.back().second == pp) runs.back().second += len;
-    else runs.push_back({pp, len});
-    prof_off += len;
-    spl_off += len;
     pidx[pp] = (int)pds.size();
-    pds.push_back(pd);
+    const int64_t len = (int64_t)nym[i] * 6;
+    for (int t = 0; t < ntab; ++t) {
+      ProfDesc pd{};
+      pd.off_prof = prof_off;
+      pd.off_spl = spl_off;
+      pd.nym = nym[i];
+      pd.three = (ntab == 3) ? 1 : 0;
+      const double* src = pp;
+      if (ntab == 3) {
+        std::vector<double> tab((size_t)len);
+        for (int64_t r = 0; r < nym[i]; ++r)
+          for (int f = 0; f < 6; ++f) tab[(size_t)(6 * r + f)] = pp[18 * r + 6 * t + f];
+        staged.push_back(std::move(tab));
+        src = staged.back().data();
+        runs.push_back({src, len});
+      } else if (!runs.empty() && runs.back().first + runs.back().second == pp) {
+        runs.back().second += len;
+      } else {
+        runs.push_back({pp, len});
+      }
+      prof_off += len;
+      spl_off += len;
+      pds.push_back(pd);
+    }
   }
   b->nprof = (int)pds.size();
   for (int k = 0; k < count; ++k) {
@@ -462,6 +484,14 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
     InstDesc d;
     int rc = make_desc(c, p[u], ip, pds[ip], d);
     if (rc) return rc;
+    if (d.ider == 0) {
+      d.iprof_d1 = ip + 1;
+      d.iprof_d2 = ip + 2;
+      d.off_prof_d1 = pds[ip + 1].off_prof;
+      d.off_spl_d1 = pds[ip + 1].off_spl;
+      d.off_prof_d2 = pds[ip + 2].off_prof;
+      d.off_spl_d2 = pds[ip + 2].off_spl;
+    }
     b->P.push_back(p[u]);
     b->Pin.push_back(p[u]);
     b->hd.push_back(d);
@@ -519,6 +549,12 @@ static int batch_build_child(stab_batch* parent, const std::vector<int>& ks, int
     InstDesc d;
     int rc = make_desc(c, pq, pd0.iprof, pd, d);
     if (rc) return rc;
+    d.iprof_d1 = pd0.iprof_d1;
+    d.iprof_d2 = pd0.iprof_d2;
+    d.off_prof_d1 = pd0.off_prof_d1;
+    d.off_spl_d1 = pd0.off_spl_d1;
+    d.off_prof_d2 = pd0.off_prof_d2;
+    d.off_spl_d2 = pd0.off_spl_d2;
     b->perm.push_back(q);
     b->P.push_back(pq);
     b->Pin.push_back(parent->Pin[k]);

@@ -112,7 +112,7 @@ struct InstDesc {
   int32_t dmat;           // index of the (D1, D2) table for this ny
   int32_t m;              // order of the standard eigenproblem: n (temporal), 2n (spatial)
   int32_t iprof;          // index of the mean profile (ProfDesc)
-  int32_t pad_;
+  int32_t ider;           // 1: mean derivatives by the collocation matrices; 0: from tables (getmean2)
   double Ma, Re, Pr, Te, yi, ymax;
   double ar, ai, br, bi, wr, wi;  // alpha, beta, omega
   int64_t off_prof;       // profile pool (doubles): nym*6, row-major y rho u v w T
@@ -122,6 +122,10 @@ struct InstDesc {
   int64_t off_mat;        // dense complex128 matrix pool (elements)
   int64_t off_mat32;      // dense complex64 matrix pool (elements)
   int64_t off_vec;        // vector pool (complex128 elements): VEC_SLOTS*n
+  // ider = 0: the first and second y-derivative tables of the profile
+  // (getmean2.f90:99-175), profile entries like the mean's
+  int32_t iprof_d1, iprof_d2;
+  int64_t off_prof_d1, off_spl_d1, off_prof_d2, off_spl_d2;
 };
 #define VEC_SLOTS 10
 
@@ -129,7 +133,8 @@ struct InstDesc {
 struct ProfDesc {
   int64_t off_prof;       // profile pool (doubles): nym*6
   int64_t off_spl;        // spline pool (doubles): nym*6
-  int32_t nym, pad_;
+  int32_t nym;
+  int32_t three;          // 1: one of the three tables of an ider = 0 profile row
 };
 
 // node pool layout per node (doubles): y eta deta d2eta vm[5] g2[5] g22[5]

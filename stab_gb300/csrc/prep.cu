@@ -7,7 +7,8 @@
 //   spline.f90:2-49        k_spline (SPLINE, cantilever end condition, lambda = 1)
 //   sgengrid.f90:2-45      node_grid (algebraic maps)
 //   spline.f90:52-75 +     k_nodes (SPEVAL; getmean clamps above the last row,
-//   getmean.f90:95-112               getmean.f90:103-108)
+//   getmean.f90:95-112               getmean.f90:103-108; with ider = 0 the
+//   getmean2.f90:99-175              derivative tables too)
 //   temporal.f90:148-179   k_meanderiv (D1 v, D2 v and the map chain rule)
 //   temporal.f90:206-598   k_blocks (materials, coefficient blocks), and
 //   spatial.f90:138-673    the h = 1 spatial variant
@@ -165,26 +166,11 @@ __device__ __forceinline__ void node_grid(const InstDesc& d, int i, double& y, d
 // The interval search returns the first I with y <= X(I+1) like SPEVAL's
 // linear scan; the profile abscissae are strictly ascending, so a binary
 // search gives the same interval.
-__global__ void k_nodes(int count, const InstDesc* __restrict__ desc, const double* __restrict__ prof,
-                        const double* __restrict__ spl, double* __restrict__ node, const int32_t* __restrict__ bad,
-                        int32_t* __restrict__ flags) {
-  int k = blockIdx.y;
-  if (k >= count) return;
-  const InstDesc d = desc[k];
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ny) return;
-  if (i == 0 && bad[d.iprof]) atomicOr(flags + k, 2);
-  double y, eta, deta, d2eta;
-  node_grid(d, i, y, eta, deta, d2eta);
-  const double* P = prof + d.off_prof;
-  const double* S = spl + d.off_spl;
-  const int n = d.nym;
-  double* out = node + d.off_node + (size_t)NODE_STRIDE * i;
-  out[NODE_Y] = y;
-  out[NODE_ETA] = eta;
-  out[NODE_DETA] = deta;
-  out[NODE_D2ETA] = d2eta;
-  if (y <= P[6 * (n - 1)]) {
+// SPEVAL (spline.f90:52-75) of the five fields of a table (rows y f1..f5,
+// v = 0) at y; above ymaxm the table's last row.
+__device__ __forceinline__ void table_eval(const double* __restrict__ P, const double* __restrict__ S, int n,
+                                           double y, double ymaxm, double* __restrict__ out) {
+  if (y <= ymaxm) {
     int lo = 0, hi = n - 2;  // find first I in [0, n-2] with y <= X(I+1)
     while (lo < hi) {
       int mid = (lo + hi) >> 1;
@@ -198,12 +184,40 @@ __global__ void k_nodes(int count, const InstDesc* __restrict__ desc, const doub
       double y0 = (f == 2) ? 0.0 : P[6 * I + 1 + f];
       double y1 = (f == 2) ? 0.0 : P[6 * (I + 1) + 1 + f];
       double f0 = S[6 * I + f], f1 = S[6 * (I + 1) + f];
-      out[NODE_VM + f] = f0 * dxp * (dxp * dxp / del - del) / 6.0 + f1 * dxm * (dxm * dxm / del - del) / 6.0 +
-                         y0 * dxp / del + y1 * dxm / del;
+      out[f] = f0 * dxp * (dxp * dxp / del - del) / 6.0 + f1 * dxm * (dxm * dxm / del - del) / 6.0 +
+               y0 * dxp / del + y1 * dxm / del;
     }
   } else {
 #pragma unroll
-    for (int f = 0; f < 5; ++f) out[NODE_VM + f] = (f == 2) ? 0.0 : P[6 * (n - 1) + 1 + f];
+    for (int f = 0; f < 5; ++f) out[f] = (f == 2) ? 0.0 : P[6 * (n - 1) + 1 + f];
+  }
+}
+
+__global__ void k_nodes(int count, const InstDesc* __restrict__ desc, const double* __restrict__ prof,
+                        const double* __restrict__ spl, double* __restrict__ node, const int32_t* __restrict__ bad,
+                        int32_t* __restrict__ flags) {
+  int k = blockIdx.y;
+  if (k >= count) return;
+  const InstDesc d = desc[k];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ny) return;
+  if (i == 0 && (bad[d.iprof] || (d.ider == 0 && (bad[d.iprof_d1] || bad[d.iprof_d2])))) atomicOr(flags + k, 2);
+  double y, eta, deta, d2eta;
+  node_grid(d, i, y, eta, deta, d2eta);
+  const double* P = prof + d.off_prof;
+  const int n = d.nym;
+  double* out = node + d.off_node + (size_t)NODE_STRIDE * i;
+  out[NODE_Y] = y;
+  out[NODE_ETA] = eta;
+  out[NODE_DETA] = deta;
+  out[NODE_D2ETA] = d2eta;
+  // nodes above the mean profile's last row take each table's last row
+  // (getmean.f90:103-108, getmean2.f90:84-97, 127-140, 163-176)
+  const double ymaxm = P[6 * (n - 1)];
+  table_eval(P, spl + d.off_spl, n, y, ymaxm, out + NODE_VM);
+  if (d.ider == 0) {
+    table_eval(prof + d.off_prof_d1, spl + d.off_spl_d1, n, y, ymaxm, out + NODE_G2);
+    table_eval(prof + d.off_prof_d2, spl + d.off_spl_d2, n, y, ymaxm, out + NODE_G22);
   }
 }
 
@@ -213,6 +227,7 @@ __global__ void k_meanderiv(int count, const InstDesc* __restrict__ desc, const 
   int k = blockIdx.y;
   if (k >= count) return;
   const InstDesc d = desc[k];
+  if (d.ider == 0) return;   // derivatives from the tables (temporal.f90:149-179 skip with ider false)
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= d.ny * 5) return;
   int i = t / 5, f = t % 5;

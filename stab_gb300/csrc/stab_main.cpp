@@ -28,19 +28,46 @@ static int fail(const char* what, int rc, stab_ctx* ctx) {
   return 1;
 }
 
-static bool load_profile(int32_t ind, std::vector<double>& prof, int32_t& nym) {
+static bool read_table(const std::string& name, std::vector<double>& rows, int32_t& nym) {
+  nym = 0;
+  if (stab_read_profile(name.c_str(), 0, nullptr, &nym)) {
+    std::fprintf(stderr, "stab_gpu: cannot read %s\n", name.c_str());
+    return false;
+  }
+  rows.assign(6 * (size_t)nym, 0.0);
+  if (stab_read_profile(name.c_str(), nym, rows.data(), &nym)) {
+    std::fprintf(stderr, "stab_gpu: cannot read %s\n", name.c_str());
+    return false;
+  }
+  return true;
+}
+
+// profile.<ind>; with ider = 0 also first.<ind> and second.<ind>
+// (getmean2.f90:27, 103, 146: nym rows each, the profile's count), packed
+// as rows of 18 values
+static bool load_profile(int32_t ind, int32_t ider, std::vector<double>& prof, int32_t& nym) {
   char pname[64];
   stab_profile_name(ind, pname, sizeof(pname));
-  nym = 0;
-  if (stab_read_profile(pname, 0, nullptr, &nym)) {
-    std::fprintf(stderr, "stab_gpu: cannot read %s\n", pname);
-    return false;
+  if (!read_table(pname, prof, nym)) return false;
+  if (ider != 0) return true;
+  std::vector<double> t[2];
+  for (int q = 0; q < 2; ++q) {
+    int32_t n2 = 0;
+    const std::string name = std::string(q == 0 ? "first." : "second.") + std::to_string(ind);
+    if (!read_table(name, t[q], n2)) return false;
+    if (n2 < nym) {
+      std::fprintf(stderr, "stab_gpu: %s has %d rows, the profile %d\n", name.c_str(), n2, nym);
+      return false;
+    }
   }
-  prof.assign(6 * (size_t)nym, 0.0);
-  if (stab_read_profile(pname, nym, prof.data(), &nym)) {
-    std::fprintf(stderr, "stab_gpu: cannot read %s\n", pname);
-    return false;
-  }
+  std::vector<double> rows(18 * (size_t)nym);
+  for (int32_t r = 0; r < nym; ++r)
+    for (int f = 0; f < 6; ++f) {
+      rows[18 * (size_t)r + f] = prof[6 * (size_t)r + f];
+      rows[18 * (size_t)r + 6 + f] = t[0][6 * (size_t)r + f];
+      rows[18 * (size_t)r + 12 + f] = t[1][6 * (size_t)r + f];
+    }
+  prof.swap(rows);
   return true;
 }
 
@@ -81,7 +108,7 @@ static int run_sweep(const stab_params& base, const stab_sweep& sw, int device) 
     if (slot < 0) {
       std::vector<double> pr;
       int32_t nym = 0;
-      if (!load_profile(pts[k].ind, pr, nym)) return 1;
+      if (!load_profile(pts[k].ind, pts[k].ider, pr, nym)) return 1;
       profs.push_back(std::move(pr));
       pind.push_back(pts[k].ind);
       pnym.push_back(nym);
@@ -164,20 +191,9 @@ int main(int argc, char** argv) {
     return 1;
   }
   if (sw.itype == 7 || sw.itype == 8) return run_sweep(p, sw, device);
-  char pname[64];
-  stab_profile_name(p.ind, pname, sizeof(pname));
   int32_t nym = 0;
-  rc = stab_read_profile(pname, 0, nullptr, &nym);
-  if (rc) {
-    std::fprintf(stderr, "stab_gpu: cannot read %s\n", pname);
-    return 1;
-  }
-  std::vector<double> prof(6 * (size_t)nym);
-  rc = stab_read_profile(pname, nym, prof.data(), &nym);
-  if (rc) {
-    std::fprintf(stderr, "stab_gpu: cannot read %s\n", pname);
-    return 1;
-  }
+  std::vector<double> prof;
+  if (!load_profile(p.ind, p.ider, prof, nym)) return 1;
   stab_ctx* ctx = nullptr;
   rc = stab_create(&ctx, device);
   if (rc) return fail("stab_create", rc, nullptr);

@@ -23,6 +23,13 @@ def cases() -> dict:
 
 def stab_params(d: dict):
     import stab_gb300
+    q = _stab_params(d)
+    q.ider = int(d.get("ider", 1))
+    return q
+
+
+def _stab_params(d: dict):
+    import stab_gb300
     return stab_gb300.StabParams.make(
         itype=d["itype"], ny=d["ny"], Ma=d["Ma"], Re=d["Re"], Pr=d["Pr"], mattyp=d["mattyp"], T0=d["T0"],
         yi=d["yi"], ymax=d["ymax"], alpha=complex(*d["alpha"]), beta=complex(*d["beta"]),
@@ -31,7 +38,8 @@ def stab_params(d: dict):
 
 def oracle_params(d: dict) -> so.StabParams:
     return so.StabParams(mattyp=d["mattyp"], T0=d["T0"], Ma=d["Ma"], Re=d["Re"], Pr=d["Pr"], ny=d["ny"],
-                         yi=d["yi"], ymax=d["ymax"], ievec=d["ievec"], ider=1, top=d["top"], wall=d["wall"],
+                         yi=d["yi"], ymax=d["ymax"], ievec=d["ievec"], ider=int(d.get("ider", 1)), top=d["top"],
+                         wall=d["wall"],
                          wallt=d["wallt"], curve=0, itype=d["itype"], alpha=complex(*d["alpha"]),
                          beta=complex(*d["beta"]), omega=complex(*d["omega"]))
 
@@ -45,11 +53,44 @@ def synth_case(itype, N, M, Re, a=0.0, b=0.0, w=0.0, ymax=50.0, yi=1.0 / 23.0, c
     return d, prof
 
 
+def derivative_tables(prof: np.ndarray, M: float, width=2.0, crossflow=False) -> np.ndarray:
+    """Rows of 18 values for ider = 0: the synthetic profile row (y rho u v w
+    T), then the exact first and second y-derivatives of its fields on the
+    same y (U = erf(y/s), T by Crocco-Busemann, rho = 1/T, W the crossflow
+    profile), each table "y f1..f5" as first.<ind> / second.<ind>."""
+    import math
+    y = prof[:, 0]
+    s = width
+    U = prof[:, 2]
+    T = prof[:, 5]
+    U1 = 2.0 / (s * math.sqrt(math.pi)) * np.exp(-(y / s) ** 2)
+    U2 = -2.0 * y / s ** 2 * U1
+    Tw = 1.0 + 0.2 * math.sqrt(0.72) * M ** 2
+    c = 0.2 * M ** 2
+    T1 = ((1.0 - Tw) + c * (1.0 - 2.0 * U)) * U1
+    T2 = ((1.0 - Tw) + c * (1.0 - 2.0 * U)) * U2 - 2.0 * c * U1 ** 2
+    r1 = -T1 / T ** 2
+    r2 = -T2 / T ** 2 + 2.0 * T1 ** 2 / T ** 3
+    if crossflow:
+        e = np.exp(1.0 - y / 1.5)
+        W1 = 0.08 / 1.5 * e * (1.0 - y / 1.5)
+        W2 = -0.08 / 1.5 / 1.5 * e * (2.0 - y / 1.5)
+    else:
+        W1 = W2 = np.zeros_like(y)
+    z = np.zeros_like(y)
+    first = np.column_stack([y, r1, U1, z, W1, T1])
+    second = np.column_stack([y, r2, U2, z, W2, T2])
+    return np.hstack([prof, first, second])
+
+
 def oracle_solve(d: dict, prof: np.ndarray, want_vectors=True):
     p = oracle_params(d)
     ym = prof[:, 0].copy()
     vt = prof[:, 1:6].copy()
     vt[:, 2] = 0.0
+    if prof.shape[1] == 18:   # ider = 0: the derivative tables ride along
+        p.ider = 0
+        return so.solve(p, ym, vt, want_vectors, first=prof[:, 6:12], second=prof[:, 12:18])
     return so.solve(p, ym, vt, want_vectors)
 
 

@@ -290,3 +290,33 @@ def test_double_word_retry_lu_matches_fp64(ctx):
     both = (s64 == sg.ST_OK) & (sdw == sg.ST_OK)
     assert np.array_equal(s64 == sg.ST_OK, sdw == sg.ST_OK)
     assert np.max(np.abs(edw[both] - e64[both]) / np.abs(e64[both])) < 1e-10
+
+
+@pytest.mark.parametrize("itype", [1, 2])
+def test_external_derivatives_ider0_match_oracle(ctx, itype):
+    """ider = 0 (getmean2.f90): the mean derivatives from first/second
+    tables instead of the collocation matrices.  Operators within 1e-12 of
+    the oracle's largest entry; least-stable eigenvalue within 1e-10 and its
+    eigenvector within 1e-8; the same instance with ider = 1 on the same
+    profile agrees to 1e-6 (the tables are the profile's exact derivatives)."""
+    if itype == 1:
+        d, prof = H.synth_case(1, 32, 0.8, 1500.0, a=0.2, b=0.05)
+    else:
+        d, prof = H.synth_case(2, 32, 0.8, 2000.0, w=0.05, b=0.1, crossflow=True)
+    tab = H.derivative_tables(prof, d["Ma"], crossflow=(itype == 2))
+    d0 = dict(d, ider=0)
+    mats = ctx.assemble(H.stab_params(d0), tab)
+    p = H.oracle_params(d0)
+    vt = np.where(np.arange(5) == 2, 0.0, prof[:, 1:6])
+    ms = so.mean_state(p, prof[:, 0], vt, tab[:, 6:12], tab[:, 12:18])
+    ref = so.temporal_pencil(p, ms) if itype == 1 else so.spatial_operators(p, ms)
+    for a, b in zip(mats, ref):
+        assert _mat_close(a, b) < 1e-12
+    eig, vec, li, st = ctx.full_spectrum(H.stab_params(d0), tab, want_vector=True)
+    es = H.oracle_solve(d0, tab)
+    jo = H.select_least(es.eig, d0)
+    assert st == sg.ST_OK and li >= 0 and jo >= 0
+    assert abs(eig[li] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    assert np.max(np.abs(H.phase_normalize(vec) - H.phase_normalize(es.evec[:, jo]))) < VEC_ABS
+    e1, _, l1, _ = ctx.full_spectrum(H.stab_params(d), prof, want_vector=False)
+    assert abs(e1[l1] - eig[li]) / abs(eig[li]) < 1e-6

@@ -50,3 +50,18 @@ def test_evec_dat_record_layout():
     n1 = struct.unpack("<i", raw[:4])[0]
     assert n1 == 40
     assert struct.unpack("<10i", raw[4:44])[:4] == (0, 8, 5, 1)
+
+
+def test_oracle_external_derivatives_agree_with_internal():
+    """getmean2 (ider = 0) restated: with the profile's exact derivative
+    tables the least-stable eigenvalue equals the ider = 1 one (collocation
+    derivatives of the splined profile) to 1e-6 relative (N = 32)."""
+    from tests import helpers as H
+    for itype, kw in ((1, dict(a=0.2, b=0.05)), (2, dict(w=0.05, b=0.1, crossflow=True))):
+        d, prof = H.synth_case(itype, 32, 0.8, 1500.0, **kw)
+        tab = H.derivative_tables(prof, 0.8, crossflow=kw.get("crossflow", False))
+        e1 = H.oracle_solve(d, prof, want_vectors=False).eig
+        d0 = dict(d, ider=0)
+        e0 = H.oracle_solve(d0, tab, want_vectors=False).eig
+        j1, j0 = H.select_least(e1, d), H.select_least(e0, d0)
+        assert abs(e1[j1] - e0[j0]) / abs(e1[j1]) < 1e-6

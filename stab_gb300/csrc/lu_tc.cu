@@ -8,7 +8,8 @@
 // row swaps, U12 = L11^-1 A12).  The update A22 -= L21 U12 runs per tile of
 // 128 rows x 64 complex columns:
 //   - the panel rows of the tile (L21) and the U12 columns are split into
-//     TF32 parts (tc.cuh) and written to shared memory in the canonical
+//     TF32 parts (tc.cuh) and written to shared memory (over the panel's,
+//     L21 re-read from global memory / L2) in the canonical
 //     K-major layout: A planes -Lr and Li (3 parts each, 128 x 16),
 //     B planes [Ur | Ui] and [Ui | -Ur] (3 parts each, 128 x 16), so one
 //     MMA of N = 128 produces the real part in TMEM columns 0-63 and the
@@ -26,6 +27,7 @@
 // Every wait on the MMA mbarrier is bounded; a wait that gives up marks the
 // instance (info = -1), waits once more (bounded) for the MMAs in flight,
 // frees the TMEM and ends the factorisation.
+#include <algorithm>
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -58,14 +60,19 @@ __device__ __forceinline__ void put_split(unsigned char* base, uint32_t off, flo
 }
 }  // namespace
 
+// The panel (steps 1-3) and the TF32 planes (step 4) are never live at the
+// same time: the planes reuse the panel's shared memory, and the update
+// reads L21 from global memory, where lu_panel has just written it back (L2).
+// For n <= 640 that is 97 KB, so two CTAs share an SM and one's panel
+// factorisation overlaps the other's update.
 size_t lu_tc_smem(int nmax) {
   const size_t panel = ((size_t)nmax * kTcNB * sizeof(cc) + 1023) & ~(size_t)1023;
-  return 1024 + panel + 12 * (size_t)kPlane;   // alignment slack, panel, 6 A planes, 6 B planes
+  return 1024 + std::max(panel, 12 * (size_t)kPlane);   // alignment slack, panel or 6 A + 6 B planes
 }
 
 // A22 -= L21 U12 for the panel at k0 on the tensor cores.  Returns false if
 // an MMA completion was not seen within the wait limit.
-__device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, const cc* P, unsigned char* Apl,
+__device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, unsigned char* Apl,
                                              unsigned char* Bpl, uint32_t tm, uint64_t* mbar, uint32_t& phase) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c1 = k0 + kTcNB;
@@ -76,10 +83,10 @@ __device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, 
   for (int rb0 = 0; rb0 < m2; rb0 += kTcRows) {
     const int nrow = min(kTcRows, m2 - rb0);
     // A planes: -Lr (parts 0..2) then Li (parts 0..2); row r of the tile is
-    // panel row kTcNB + rb0 + r
+    // row c1 + rb0 + r of L21 (panel column k0 + j, in global memory)
     for (int q = tid; q < kTcRows * kTcNB; q += blockDim.x) {
       const int r = q & (kTcRows - 1), j = q >> 7;
-      const cc v = (r < nrow) ? P[(size_t)j * n + kTcNB + rb0 + r] : cmk(0.f, 0.f);
+      const cc v = (r < nrow) ? M[(size_t)(k0 + j) * n + c1 + rb0 + r] : cmk(0.f, 0.f);
       const uint32_t off = tc::plane_off(r, j, kTcNB);
       put_split(Apl, off, -v.x);
       put_split(Apl + 3 * kPlane, off, v.y);
@@ -131,24 +138,23 @@ __device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, 
         const int r = 32 * (warp & 3) + lane;
         const int ch = 32 * (warp >> 2);
         const uint32_t trow = tm + ((uint32_t)(32 * (warp & 3)) << 16);
+#pragma unroll 1
+        for (int c0 = 0; c0 < 32; c0 += 8) {
+          // the 8 A22 entries are loaded before any store, so their global
+          // latencies overlap each other and the TMEM reads
+          cc a[8];
+          cc* col = M + (size_t)(c1 + cb0 + ch + c0) * n + c1 + rb0 + r;
+          const bool row_ok = r < nrow;
 #pragma unroll
-        for (int c0 = 0; c0 < 32; c0 += 16) {
-          float re[16], im[16];
-          tc::tmem_ld16(trow + (uint32_t)(ch + c0), re);
-          tc::tmem_ld16(trow + (uint32_t)(kTcCols + ch + c0), im);
+          for (int i = 0; i < 8; ++i)
+            a[i] = (row_ok && ch + c0 + i < ncol) ? col[(size_t)i * n] : cmk(0.f, 0.f);
+          float re[8], im[8];
+          tc::tmem_ld8(trow + (uint32_t)(ch + c0), re);             // real parts
+          tc::tmem_ld8(trow + (uint32_t)(kTcCols + ch + c0), im);   // imaginary parts
           tc::tmem_wait_ld();
-          if (r < nrow) {
-            cc* col = M + (size_t)(c1 + cb0 + ch + c0) * n + c1 + rb0 + r;
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-              if (ch + c0 + i < ncol) {
-                cc a = col[(size_t)i * n];
-                a.x += re[i];
-                a.y += im[i];
-                col[(size_t)i * n] = a;
-              }
-            }
-          }
+          for (int i = 0; i < 8; ++i)
+            if (row_ok && ch + c0 + i < ncol) col[(size_t)i * n] = cmk(a[i].x + re[i], a[i].y + im[i]);
         }
       }
       tc::fence_before_sync();
@@ -159,7 +165,7 @@ __device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, 
   return ok;
 }
 
-__global__ void __launch_bounds__(256, 1) k_lu_tc(int count, const int32_t* __restrict__ nsz, cc* __restrict__ A,
+__global__ void __launch_bounds__(256, 2) k_lu_tc(int count, const int32_t* __restrict__ nsz, cc* __restrict__ A,
                                                   const int64_t* __restrict__ mat_off, int32_t* __restrict__ piv,
                                                   const int64_t* __restrict__ piv_off, int32_t* __restrict__ info,
                                                   const int32_t* __restrict__ skip, const int32_t* __restrict__ order,
@@ -176,9 +182,8 @@ __global__ void __launch_bounds__(256, 1) k_lu_tc(int count, const int32_t* __re
   // 1024-aligned panel, then the planes
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smraw_tc) + 1023) & ~(uintptr_t)1023);
-  cc* P = reinterpret_cast<cc*>(base);
-  const size_t panel = ((size_t)nmax * kTcNB * sizeof(cc) + 1023) & ~(size_t)1023;
-  unsigned char* Apl = base + panel;
+  cc* P = reinterpret_cast<cc*>(base);           // steps 1-3
+  unsigned char* Apl = base;                      // step 4, over the panel
   unsigned char* Bpl = Apl + 6 * kPlane;
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) {
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(256, 1) k_lu_tc(int count, const int32_t* __re
   bool ok = true;
   for (int k0 = 0; k0 < n; k0 += kTcNB) {
     if (!lu_panel<cc, kTcNB, 1>(k0, 0, n, Mk, ip, P, red_v, red_i, s_piv, first_zero)) break;
-    if (!lu_update_tc(k0, n, Mk, P, Apl, Bpl, tm, &mbar, phase)) {
+    if (!lu_update_tc(k0, n, Mk, Apl, Bpl, tm, &mbar, phase)) {
       ok = false;
       break;
     }

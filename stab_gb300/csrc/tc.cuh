@@ -7,8 +7,8 @@
 // Complex product on real tensor cores (real split).  With L = Lr + i Li and
 // U = Ur + i Ui, the update C -= L U is
 //   Cr -= Lr Ur - Li Ui,   Ci -= Lr Ui + Li Ur,
-// four real products accumulated in two TMEM regions, the signs taken from
-// the MMA's operand-negate bit.  Each real operand x is split into three TF32
+// four real products accumulated in two TMEM regions, the signs carried by
+// the operand planes (-Lr, and a B plane [Ui | -Ur] next to [Ur | Ui]).  Each real operand x is split into three TF32
 // parts x = x0 + x1 + x2 (x0 = tf32(x), x1 = tf32(x - x0), x2 = tf32(x - x0 -
 // x1)); a product keeps the six terms whose part indices sum to at most 2,
 // x0y0 + x0y1 + x1y0 + x0y2 + x1y1 + x2y0, which leaves a relative error of
@@ -143,6 +143,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
       : "r"(taddr));
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+// 8 consecutive float32 columns, as tmem_ld16
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 

@@ -387,6 +387,8 @@ def main():
     ap.add_argument("--cpu-sample-threaded", type=int, default=16,
                     help="instances of the one-process multi-threaded CPU mode")
     ap.add_argument("--plain-reps", type=int, default=3, help="timed passes of the plain FP64 path")
+    ap.add_argument("--variants", type=int, default=1, help="1: also time the pass with each stage's other "
+                    "implementation (polish LU on CUDA cores, seed QR in global memory)")
     ap.add_argument("--ref-sample", type=int, default=48)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--surrogate", type=int, default=1, help="1: also run the surrogate-seeded leg")
@@ -500,6 +502,33 @@ def main():
     stats = {k: v for k, v in stats.items() if not k.startswith("stage:")}
     launches_per_step = sum(v[0] for v in stats.values())
 
+    # the same pass with a stage switched to its other implementation (CUDA
+    # events, two passes each after one untimed pass), for the design notes
+    def variant_ms(setter, reset):
+        setter()
+        try:
+            batch.run(sg.MODE_COARSE)
+            torch.cuda.synchronize()
+            v0, v1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            v0.record(stream)
+            for _ in range(2):
+                batch.run(sg.MODE_COARSE)
+            v1.record(stream)
+            torch.cuda.synchronize()
+            return v0.elapsed_time(v1) / 2
+        finally:
+            reset()
+            batch.run(sg.MODE_COARSE)   # re-capture the default graph
+    variants = None
+    if args.variants:
+        variants = {
+            "default_ms": ms_local,
+            "polish_lu_cuda_cores_ms": variant_ms(lambda: ctx.set_arithmetic(sg.STAGE_POLISH_LU, sg.ARITH_FP32),
+                                                  ctx.reset_arithmetic),
+            "seed_qr_global_memory_ms": variant_ms(lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 0),
+                                                   lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 1)),
+        }
+
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None
     single = single_instance_leg(ctx, stream, cpu=args.cpu_sample > 0) if rank == 0 else None
     serving = serving_leg(ctx, args) if (rank == 0 and args.serve_seconds > 0) else None
@@ -584,6 +613,7 @@ def main():
                                                                                key=lambda kv: -kv[1][1])},
         "gpu_launches": int(launches_per_step * args.steps),
         "round_ms": stages,
+        "variants": variants,
         "eig_phase_share": {k: round(v / max(1, sum(phases.values())), 4) for k, v in phases.items()},
         "autotune_lu_panel": {str(n): {"c64": v["c64"][0], "c128": v["c128"][0]} for n, v in tune.items()},
         "cuda_graph": "device part of each timed pass replayed from a captured CUDA graph",

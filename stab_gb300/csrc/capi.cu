@@ -70,6 +70,7 @@ struct stab_ctx {
   int arith[4] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD, STAB_ARITH_TF32_SPLIT};
   int seed_ny = 32;        // N of the seed spectrum of STAB_MODE_COARSE / SURROGATE
   int seed_qr_shared = 1;  // STAB_OPT_SEED_QR_SHARED
+  int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
 // size class of an LU order for the tuned panel-width table
@@ -240,6 +241,7 @@ struct stab_batch {
   DevBuf startc;
   DevBuf seed_raw, best_src;                  // STAB_MODE_SURROGATE: the extra candidate, winner per instance
   int graph_mode = -1;                        // mode of the captured graph
+  int graph_epoch = -1;                       // context settings the graph was captured under
   int coarse_ny = 32;                         // N of the seed spectrum of STAB_MODE_COARSE
   std::vector<zc> fb_val;
   std::vector<int32_t> fb_status;
@@ -1419,8 +1421,9 @@ static int run_coarse_device(stab_batch* b, bool extra) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   const int gmode = extra ? STAB_MODE_SURROGATE : STAB_MODE_COARSE;
+  if (b->graph_epoch != c->epoch) b->coarse_runs = 0;   // new settings: one eager pass first
   const bool graphable = !c->profiling && s != nullptr && b->coarse_runs > 0 && b->graph_mode == gmode;
-  if (b->coarse_graph && (b->graph_stream != s || b->graph_mode != gmode)) {
+  if (b->coarse_graph && (b->graph_stream != s || b->graph_mode != gmode || b->graph_epoch != c->epoch)) {
     cudaGraphExecDestroy(b->coarse_graph);
     b->coarse_graph = nullptr;
   }
@@ -1432,6 +1435,7 @@ static int run_coarse_device(stab_batch* b, bool extra) {
       if (rc == 0 && e == cudaSuccess && g) {
         if (cudaGraphInstantiate(&b->coarse_graph, g, 0) != cudaSuccess) b->coarse_graph = nullptr;
         b->graph_stream = s;
+        b->graph_epoch = c->epoch;
       }
       if (g) cudaGraphDestroy(g);
       cudaGetLastError();   // a failed capture leaves no sticky error: run eagerly below
@@ -1439,6 +1443,7 @@ static int run_coarse_device(stab_batch* b, bool extra) {
   }
   b->coarse_runs = (b->graph_mode == gmode) ? b->coarse_runs + 1 : 1;
   b->graph_mode = gmode;
+  b->graph_epoch = c->epoch;
   if (graphable && b->coarse_graph) {
     CK(c, cudaGraphLaunch(b->coarse_graph, s));
     return 0;
@@ -1701,6 +1706,7 @@ int stab_autotune(stab_ctx* c, const int32_t* orders, int32_t norders, int32_t* 
       const int rc = z ? tune_lu_one<zc>(c, n, reps, &nb, &ms) : tune_lu_one<cc>(c, n, reps, &nb, &ms);
       if (rc) return rc;
       c->lu_nb[{z, lu_class(n)}] = nb;
+      c->epoch += 1;
       if (nb_out) nb_out[2 * q + z] = nb;
       if (ms_out) ms_out[2 * q + z] = ms;
     }
@@ -1719,6 +1725,7 @@ int stab_set_arithmetic(stab_ctx* c, int32_t stage, int32_t arithmetic) {
     return set_err(c, STAB_ERR_ARG, "arithmetic must be STAB_ARITH_FP64 or STAB_ARITH_DOUBLE_WORD");
   }
   c->arith[stage] = arithmetic;
+  c->epoch += 1;
   return STAB_OK;
 }
 
@@ -1726,6 +1733,7 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   if (!c) return STAB_ERR_ARG;
   if (option == STAB_OPT_SEED_QR_SHARED) {
     c->seed_qr_shared = value ? 1 : 0;
+    c->epoch += 1;
     return STAB_OK;
   }
   return set_err(c, STAB_ERR_ARG, "unknown option");

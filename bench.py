@@ -388,7 +388,7 @@ def main():
                     help="instances of the one-process multi-threaded CPU mode")
     ap.add_argument("--plain-reps", type=int, default=3, help="timed passes of the plain FP64 path")
     ap.add_argument("--variants", type=int, default=1, help="1: also time the pass with each stage's other "
-                    "implementation (polish LU on CUDA cores, seed QR in global memory)")
+                    "implementation (polish LU on CUDA cores, seed QR in shared memory)")
     ap.add_argument("--ref-sample", type=int, default=48)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--surrogate", type=int, default=1, help="1: also run the surrogate-seeded leg")
@@ -525,8 +525,8 @@ def main():
             "default_ms": ms_local,
             "polish_lu_cuda_cores_ms": variant_ms(lambda: ctx.set_arithmetic(sg.STAGE_POLISH_LU, sg.ARITH_FP32),
                                                   ctx.reset_arithmetic),
-            "seed_qr_global_memory_ms": variant_ms(lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 0),
-                                                   lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 1)),
+            "seed_qr_shared_memory_ms": variant_ms(lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 1),
+                                                   lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 0)),
         }
 
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None

@@ -153,11 +153,12 @@ int stab_set_arithmetic(stab_ctx* ctx, int32_t stage, int32_t arithmetic);
  * as N^3) and resolves fewer least-stable modes.  No reference counterpart. */
 int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
 /* Execution options (no reference counterpart):
- *   STAB_OPT_SEED_QR_SHARED  1 (default): seed spectra whose packed
- *     Hessenberg matrix fits in shared memory (order <= 160, the N = 32
- *     temporal seeds) run one 512-thread CTA per SM with the QR phase in
- *     shared memory; 0: the 128-thread batch kernel, everything in global
- *     memory.  Same algorithm and arithmetic either way. */
+ *   STAB_OPT_SEED_QR_SHARED  1: seed spectra whose packed Hessenberg matrix
+ *     fits in shared memory (order <= 160, the N = 32 temporal seeds) run
+ *     one 512-thread CTA per SM with the QR phase in shared memory; 0
+ *     (default, measured faster on the 4096-instance sweep): the 128-thread
+ *     batch kernel, four CTAs per SM, everything in global memory.  Same
+ *     algorithm and arithmetic, bit-identical eigenvalues either way. */
 #define STAB_OPT_SEED_QR_SHARED 1
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every

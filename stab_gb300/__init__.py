@@ -423,7 +423,7 @@ class Context:
         return md.value, pd.value
 
     def set_option(self, option: int, value: int) -> None:
-        """stab_set_option: OPT_SEED_QR_SHARED (1 default, 0 off)."""
+        """stab_set_option: OPT_SEED_QR_SHARED (0 default, 1 on)."""
         self._check(self.lib.stab_set_option(self.h, int(option), int(value)))
 
     def lu_tc_check(self, n: int, count: int):

@@ -69,7 +69,7 @@ struct stab_ctx {
   // arithmetic per stage (STAB_STAGE_*)
   int arith[4] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD, STAB_ARITH_TF32_SPLIT};
   int seed_ny = 32;        // N of the seed spectrum of STAB_MODE_COARSE / SURROGATE
-  int seed_qr_shared = 1;  // STAB_OPT_SEED_QR_SHARED
+  int seed_qr_shared = 0;  // STAB_OPT_SEED_QR_SHARED
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 

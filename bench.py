@@ -44,6 +44,16 @@ UNIT = "modes/s"
 TOL = 1e-10
 T0_SUTH = 110.4 / 0.3815
 FP64_PEAK_TFLOPS = 1.19   # FMA probe on a GB300 (profiles/fp64_fp32_peak_probe.md)
+HBM_FALLBACK_GBS = 6800.0  # used only when MEASURED_PEAKS.json is absent
+
+
+def hbm_peak():
+    """(GB/s, source) of the HBM copy bandwidth measured on this machine."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback 6.8 TB/s"
 FP32_PEAK_TFLOPS = 69.9
 COARSE_TRAFFIC_PER_INSTANCE = (25.59e9 + 21.59e9) / 512
 # kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
@@ -53,6 +63,10 @@ KERNEL_WORK = {
                            "default), run in double-word arithmetic"),
     "k_eig_plain_fallback": ("eig_fp64", "fp64", "FP64 flops counted by the kernel on the fallback instances"),
     "k_lu_c": ("lu_c64", "fp32", "8/3 n^3 real flops per complex64 LU, per factorisation run"),
+    "k_lu_tc": ("lu_c64", "hbm", "trailing-matrix traffic of the complex64 LU with 16-column panels: every "
+                "panel step reads and writes A22, sum over steps of (n - k)^2 x 16 bytes = n^3 / 3 bytes per LU "
+                "(work lu_c64 / 8)"),
+    "k_lu_tc_tma": ("lu_c64", "hbm", "as k_lu_tc (n^3 / 3 bytes per LU)"),
     "k_lu_z": ("lu_c128", "fp64", "8/3 n^3 real flops per complex128 LU, per factorisation run"),
     "k_lu_dz": ("lu_c128", "dw", "8/3 n^3 real flops per double-word complex LU, per factorisation run"),
 }
@@ -525,6 +539,8 @@ def main():
             "default_ms": ms_local,
             "polish_lu_cuda_cores_ms": variant_ms(lambda: ctx.set_arithmetic(sg.STAGE_POLISH_LU, sg.ARITH_FP32),
                                                   ctx.reset_arithmetic),
+            "polish_lu_tensor_no_tma_ms": variant_ms(lambda: ctx.set_option(sg.OPT_POLISH_LU_TMA, 0),
+                                                     lambda: ctx.set_option(sg.OPT_POLISH_LU_TMA, 1)),
             "seed_qr_shared_memory_ms": variant_ms(lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 1),
                                                    lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 0)),
         }
@@ -562,6 +578,13 @@ def main():
         if kname not in KERNEL_WORK or kms <= 0:
             continue
         wkey, bound, note = KERNEL_WORK[kname]
+        if bound == "hbm":
+            hp, hsrc = hbm_peak()
+            ach = work[wkey] / 8.0 / (kms / 1000.0) / 1e9   # bytes over the same launches
+            rooflines[kname] = {"bound": "hbm", "achieved": ach, "peak": hp, "unit": "GB/s", "frac": ach / hp,
+                                "traffic": None, "kernel": kname, "launches": kl, "ms": kms, "algorithmic": note,
+                                "peak_source": hsrc}
+            continue
         # double-word kernels: a double-word multiply-add (2 flops) is 15 FP32
         # instructions, so their flop peak is the FP32 instruction rate * 2 / 15
         peak = {"fp64": FP64_PEAK_TFLOPS, "fp32": FP32_PEAK_TFLOPS, "dw": FP32_PEAK_TFLOPS / 15.0}[bound]

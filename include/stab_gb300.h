@@ -160,6 +160,13 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     batch kernel, four CTAs per SM, everything in global memory.  Same
  *     algorithm and arithmetic, bit-identical eigenvalues either way. */
 #define STAB_OPT_SEED_QR_SHARED 1
+/*   STAB_OPT_POLISH_LU_TMA  1 (default): the tensor-core LU moves each
+ *     128 x 64 tile of the trailing matrix between global and shared memory
+ *     with tensor (TMA) loads and stores, overlapped with the operand
+ *     staging and the MMAs (batches whose orders are all even; odd orders
+ *     take the other form); 0: the epilogue reads and writes the tile from
+ *     the registers.  Same arithmetic either way. */
+#define STAB_OPT_POLISH_LU_TMA 2
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,
@@ -207,7 +214,8 @@ int stab_lu_cluster_check(stab_ctx* ctx, int32_t n, int32_t count, int32_t compl
 
 /*
  * Self-check of the tensor-core LU: count test matrices of order n factored
- * in complex64 on the CUDA cores and with the tensor-core trailing update.
+ * in complex64 on the CUDA cores and with the tensor-core trailing update
+ * (in the form STAB_OPT_POLISH_LU_TMA selects).
  * bwd_tc / bwd_simt: largest backward error max|P A - L U| / max|A| of
  * either path (computed on the host in FP64); piv_diff: number of differing
  * pivots.  No reference counterpart (the reference calls LAPACK's ZGETRF).

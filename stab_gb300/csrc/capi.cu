@@ -70,6 +70,7 @@ struct stab_ctx {
   int arith[4] = {STAB_ARITH_DOUBLE_WORD, STAB_ARITH_FP64, STAB_ARITH_DOUBLE_WORD, STAB_ARITH_TF32_SPLIT};
   int seed_ny = 32;        // N of the seed spectrum of STAB_MODE_COARSE / SURROGATE
   int seed_qr_shared = 0;  // STAB_OPT_SEED_QR_SHARED
+  int lu_tma = 1;          // STAB_OPT_POLISH_LU_TMA
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -240,6 +241,8 @@ struct stab_batch {
   bool use_start = false;
   DevBuf startc;
   DevBuf seed_raw, best_src;                  // STAB_MODE_SURROGATE: the extra candidate, winner per instance
+  DevBuf tmaps;                               // tensor maps of the complex64 matrices (TMA tiles of the LU)
+  int tmaps_state = 0;                        // 0 not built, 1 built, -1 not possible (odd order)
   int graph_mode = -1;                        // mode of the captured graph
   int graph_epoch = -1;                       // context settings the graph was captured under
   int coarse_ny = 32;                         // N of the seed spectrum of STAB_MODE_COARSE
@@ -259,7 +262,7 @@ struct stab_batch {
                      &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
                      &bad, &flops, &rsc, &csc, &cand, &accepted, &skip64, &lus32, &lus64, &have, &best_key, &best_theta, &best_err,
                      &best_iters, &best_out, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
-                     &done, &err, &iters, &status, &counter, &startc, &seed_raw, &best_src};
+                     &done, &err, &iters, &status, &counter, &startc, &seed_raw, &best_src, &tmaps};
     for (DevBuf* d : all) {
       if (d->p) cudaFreeAsync(d->p, d->st);
       d->p = nullptr;
@@ -813,10 +816,24 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
       if (e != cudaSuccess) return e;
     }
     if (c64 && c->arith[STAB_STAGE_POLISH_LU] == STAB_ARITH_TF32_SPLIT && lu_tc_fits(b->nmax)) {
-      return timed(c, "k_lu_tc", [&] {
+      const CUtensorMap* tm = nullptr;
+      if (c->lu_tma && lu_tc_fits(b->nmax, true)) {
+        if (b->tmaps_state == 0) {
+          std::vector<CUtensorMap> maps;
+          if (lu_tc_tensor_maps(b->count, b->hn.data(), b->h_n2.data(), b->M32.as<cc>(), maps)) {
+            cudaError_t e = upload(b->tmaps, maps, s);
+            if (e != cudaSuccess) return e;
+            b->tmaps_state = 1;
+          } else {
+            b->tmaps_state = -1;
+          }
+        }
+        if (b->tmaps_state == 1) tm = b->tmaps.as<CUtensorMap>();
+      }
+      return timed(c, tm ? "k_lu_tc_tma" : "k_lu_tc", [&] {
         return launch_lu_tc(b->count, b->nsz.as<int32_t>(), b->nmax, b->M32.as<cc>(), b->off_n2.as<int64_t>(),
                             b->piv.as<int32_t>(), b->off_nof.as<int64_t>(), b->info.as<int32_t>(), s, skip,
-                            b->order.as<int32_t>());
+                            b->order.as<int32_t>(), tm);
       });
     }
     return timed(c, n_lu, [&] {
@@ -1624,8 +1641,18 @@ static int lu_tc_check(stab_ctx* c, int n, int count, double* bwd_tc, double* bw
   CK(c, cudaMemcpyAsync(A2.p, A1.p, sizeof(cc) * elems, cudaMemcpyDeviceToDevice, s));
   CK(c, launch_lu<cc>(count, nullptr, nsz.as<int32_t>(), n, A1.as<cc>(), moff.as<int64_t>(), piv1.as<int32_t>(),
                       poff.as<int64_t>(), info.as<int32_t>(), s, nullptr, 16, nullptr, 1));
+  DevBuf tmaps;
+  const CUtensorMap* tm = nullptr;
+  if (c->lu_tma && lu_tc_fits(n, true)) {
+    std::vector<CUtensorMap> maps;
+    std::vector<int32_t> ns2(count, n);
+    if (lu_tc_tensor_maps(count, ns2.data(), mo.data(), A2.as<cc>(), maps)) {
+      CK(c, upload(tmaps, maps, s));
+      tm = tmaps.as<CUtensorMap>();
+    }
+  }
   CK(c, launch_lu_tc(count, nsz.as<int32_t>(), n, A2.as<cc>(), moff.as<int64_t>(), piv2.as<int32_t>(),
-                     poff.as<int64_t>(), info.as<int32_t>(), s));
+                     poff.as<int64_t>(), info.as<int32_t>(), s, nullptr, nullptr, tm));
   std::vector<int32_t> p1((size_t)count * n), p2((size_t)count * n), inf(count);
   CK(c, cudaMemcpyAsync(h1.data(), A1.p, sizeof(cc) * elems, cudaMemcpyDeviceToHost, s));
   CK(c, cudaMemcpyAsync(h2.data(), A2.p, sizeof(cc) * elems, cudaMemcpyDeviceToHost, s));
@@ -1733,6 +1760,11 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   if (!c) return STAB_ERR_ARG;
   if (option == STAB_OPT_SEED_QR_SHARED) {
     c->seed_qr_shared = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_POLISH_LU_TMA) {
+    c->lu_tma = value ? 1 : 0;
     c->epoch += 1;
     return STAB_OK;
   }

@@ -1,5 +1,7 @@
 // Host launchers of the batched LU / triangular-solve kernels (lu.cu).
 #pragma once
+#include <vector>
+#include <cuda.h>
 #include "common.cuh"
 
 namespace stab {
@@ -33,10 +35,15 @@ cudaError_t launch_equilibrate(int count, const int32_t* nsz, cc* A, const int64
 // Complex64 LU with the trailing update on the tensor cores (lu_tc.cu):
 // same inputs, outputs and pivot order as launch_lu<cc> with panel width 16.
 // info[k] = -1 marks an instance whose MMA completion was not seen.
+// tmaps (device, one per instance, or null): tensor maps of the matrices
+// (lu_tc_tensor_maps) for the TMA tile path.
 cudaError_t launch_lu_tc(int count, const int32_t* nsz, int nmax, cc* A, const int64_t* mat_off, int32_t* piv,
                          const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip = nullptr,
-                         const int32_t* order = nullptr);
+                         const int32_t* order = nullptr, const CUtensorMap* tmaps = nullptr);
 // dynamic shared memory of k_lu_tc for order nmax, and whether it fits
-size_t lu_tc_smem(int nmax);
-bool lu_tc_fits(int nmax);
+size_t lu_tc_smem(int nmax, bool tma = false);
+bool lu_tc_fits(int nmax, bool tma = false);
+// host: the tensor maps of count matrices at base + off[k] (orders n[k]);
+// false if any order or offset is odd or the encoder is unavailable
+bool lu_tc_tensor_maps(int count, const int32_t* n, const int64_t* off, cc* base, std::vector<CUtensorMap>& out);
 }  // namespace stab

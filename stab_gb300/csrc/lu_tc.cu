@@ -28,7 +28,9 @@
 // instance (info = -1), waits once more (bounded) for the MMAs in flight,
 // frees the TMEM and ends the factorisation.
 #include <algorithm>
+#include <vector>
 #include <cooperative_groups.h>
+#include <cudaTypedefs.h>
 
 #include "common.cuh"
 #include "dw.cuh"
@@ -65,15 +67,28 @@ __device__ __forceinline__ void put_split(unsigned char* base, uint32_t off, flo
 // reads L21 from global memory, where lu_panel has just written it back (L2).
 // For n <= 640 that is 97 KB, so two CTAs share an SM and one's panel
 // factorisation overlaps the other's update.
-size_t lu_tc_smem(int nmax) {
+__host__ __device__ __forceinline__ size_t lu_tc_region(int nmax) {
   const size_t panel = ((size_t)nmax * kTcNB * sizeof(cc) + 1023) & ~(size_t)1023;
-  return 1024 + std::max(panel, 12 * (size_t)kPlane);   // alignment slack, panel or 6 A + 6 B planes
+  const size_t planes = 12 * (size_t)kPlane;
+  return panel > planes ? panel : planes;   // panel, or 6 A + 6 B planes
+}
+// With TMA the A22 tile buffer (64 KB) follows, and one CTA fits per SM.
+size_t lu_tc_smem(int nmax, bool tma) {
+  return 1024 + lu_tc_region(nmax) + (tma ? (size_t)kTcRows * kTcCols * sizeof(cc) : 0);
 }
 
 // A22 -= L21 U12 for the panel at k0 on the tensor cores.  Returns false if
-// an MMA completion was not seen within the wait limit.
+// an MMA (or tile-load) completion was not seen within the wait limit.
+// TMA: the A22 tile goes through shared memory (Cs, 128 x 64 complex,
+// column-major): thread 0 starts its tensor load before the B planes are
+// staged, so the load overlaps the staging and the MMAs; the epilogue adds
+// the accumulator to the tile in shared memory and thread 0 stores it back
+// with a tensor store that overlaps the next tile's staging.  Without TMA the
+// epilogue reads and writes A22 in global memory from the registers.
+template <bool TMA>
 __device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, unsigned char* Apl,
-                                             unsigned char* Bpl, uint32_t tm, uint64_t* mbar, uint32_t& phase) {
+                                             unsigned char* Bpl, cc* Cs, const void* tmap, uint32_t tm,
+                                             uint64_t* mbar, uint32_t& phase, uint64_t* tbar, uint32_t& tphase) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c1 = k0 + kTcNB;
   const int m2 = n - c1;
@@ -93,6 +108,15 @@ __device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, 
     }
     for (int cb0 = 0; cb0 < m2; cb0 += kTcCols) {
       const int ncol = min(kTcCols, m2 - cb0);
+      if constexpr (TMA) {
+        // the tile's rows start at c1 + rb0, a multiple of 16 (16-byte aligned
+        // for 8-byte elements); the previous tile's store has read Cs
+        if (tid == 0) {
+          tc::bulk_wait_read();
+          tc::mbar_arrive_expect_tx(tbar, kTcRows * kTcCols * (uint32_t)sizeof(cc));
+          tc::tma_load_2d(Cs, tmap, c1 + rb0, c1 + cb0, tbar);
+        }
+      }
       // B planes: [Ur | Ui] (parts 0..2) then [Ui | -Ur]; B row c is U12
       // column c1 + cb0 + c, K index j its row k0 + j
       for (int q = tid; q < kTcCols * kTcNB; q += blockDim.x) {
@@ -127,8 +151,12 @@ __device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, 
         tc::mma_commit(mbar);
       }
       __syncwarp();
-      const bool got = tc::mbar_wait(mbar, phase, kWaitLimit);
+      bool got = tc::mbar_wait(mbar, phase, kWaitLimit);
       phase ^= 1u;
+      if constexpr (TMA) {
+        got = tc::mbar_wait(tbar, tphase, kWaitLimit) && got;
+        tphase ^= 1u;
+      }
       tc::fence_after_sync();
       if (!got) {
         ok = false;
@@ -138,59 +166,102 @@ __device__ __forceinline__ bool lu_update_tc(int k0, int n, cc* __restrict__ M, 
         const int r = 32 * (warp & 3) + lane;
         const int ch = 32 * (warp >> 2);
         const uint32_t trow = tm + ((uint32_t)(32 * (warp & 3)) << 16);
+        if constexpr (TMA) {
 #pragma unroll 1
-        for (int c0 = 0; c0 < 32; c0 += 8) {
-          // the 8 A22 entries are loaded before any store, so their global
-          // latencies overlap each other and the TMEM reads
-          cc a[8];
-          cc* col = M + (size_t)(c1 + cb0 + ch + c0) * n + c1 + rb0 + r;
-          const bool row_ok = r < nrow;
+          for (int c0 = 0; c0 < 32; c0 += 8) {
+            float re[8], im[8];
+            tc::tmem_ld8(trow + (uint32_t)(ch + c0), re);
+            tc::tmem_ld8(trow + (uint32_t)(kTcCols + ch + c0), im);
+            tc::tmem_wait_ld();
 #pragma unroll
-          for (int i = 0; i < 8; ++i)
-            a[i] = (row_ok && ch + c0 + i < ncol) ? col[(size_t)i * n] : cmk(0.f, 0.f);
-          float re[8], im[8];
-          tc::tmem_ld8(trow + (uint32_t)(ch + c0), re);             // real parts
-          tc::tmem_ld8(trow + (uint32_t)(kTcCols + ch + c0), im);   // imaginary parts
-          tc::tmem_wait_ld();
+            for (int i = 0; i < 8; ++i) {
+              cc* e = Cs + (size_t)(ch + c0 + i) * kTcRows + r;   // rows and columns outside A22 are not stored
+              *e = cmk(e->x + re[i], e->y + im[i]);
+            }
+          }
+        } else {
+#pragma unroll 1
+          for (int c0 = 0; c0 < 32; c0 += 8) {
+            // the 8 A22 entries are loaded before any store, so their global
+            // latencies overlap each other and the TMEM reads
+            cc a[8];
+            cc* col = M + (size_t)(c1 + cb0 + ch + c0) * n + c1 + rb0 + r;
+            const bool row_ok = r < nrow;
 #pragma unroll
-          for (int i = 0; i < 8; ++i)
-            if (row_ok && ch + c0 + i < ncol) col[(size_t)i * n] = cmk(a[i].x + re[i], a[i].y + im[i]);
+            for (int i = 0; i < 8; ++i)
+              a[i] = (row_ok && ch + c0 + i < ncol) ? col[(size_t)i * n] : cmk(0.f, 0.f);
+            float re[8], im[8];
+            tc::tmem_ld8(trow + (uint32_t)(ch + c0), re);             // real parts
+            tc::tmem_ld8(trow + (uint32_t)(kTcCols + ch + c0), im);   // imaginary parts
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+              if (row_ok && ch + c0 + i < ncol) col[(size_t)i * n] = cmk(a[i].x + re[i], a[i].y + im[i]);
+          }
         }
       }
+      if constexpr (TMA) tc::fence_async_smem();   // Cs writes visible to the tensor store
       tc::fence_before_sync();
       __syncthreads();
       if (!__syncthreads_and(ok)) return false;
+      if constexpr (TMA) {
+        if (tid == 0) {
+          tc::tma_store_2d(tmap, c1 + rb0, c1 + cb0, Cs);
+          tc::bulk_commit();
+        }
+      }
     }
+  }
+  if constexpr (TMA) {
+    // the next panel reads A22 with ordinary loads
+    if (tid == 0) {
+      tc::bulk_wait_all();
+      tc::fence_async_global();
+    }
+    __syncthreads();
   }
   return ok;
 }
 
-__global__ void __launch_bounds__(256, 2) k_lu_tc(int count, const int32_t* __restrict__ nsz, cc* __restrict__ A,
-                                                  const int64_t* __restrict__ mat_off, int32_t* __restrict__ piv,
-                                                  const int64_t* __restrict__ piv_off, int32_t* __restrict__ info,
-                                                  const int32_t* __restrict__ skip, const int32_t* __restrict__ order,
-                                                  int nmax) {
+template <bool TMA>
+__global__ void __launch_bounds__(256, TMA ? 1 : 2) k_lu_tc(int count, const int32_t* __restrict__ nsz,
+                                                            cc* __restrict__ A, const int64_t* __restrict__ mat_off,
+                                                            int32_t* __restrict__ piv,
+                                                            const int64_t* __restrict__ piv_off,
+                                                            int32_t* __restrict__ info,
+                                                            const int32_t* __restrict__ skip,
+                                                            const int32_t* __restrict__ order, int nmax,
+                                                            const CUtensorMap* __restrict__ tmaps) {
   extern __shared__ unsigned char smraw_tc[];
   __shared__ float red_v[256 / 32];
   __shared__ int red_i[256 / 32];
   __shared__ int s_piv;
   __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t tbar;
   __shared__ uint32_t tmem_slot;
   const int k = order ? order[blockIdx.x] : (int)blockIdx.x;
   if (k >= count) return;
   if (skip && skip[k]) return;
-  // 1024-aligned panel, then the planes
+  // 1024-aligned panel, then (TMA) the A22 tile buffer
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smraw_tc) + 1023) & ~(uintptr_t)1023);
   cc* P = reinterpret_cast<cc*>(base);           // steps 1-3
   unsigned char* Apl = base;                      // step 4, over the panel
   unsigned char* Bpl = Apl + 6 * kPlane;
+  cc* Cs = reinterpret_cast<cc*>(base + lu_tc_region(nmax));
+  const void* tmap = TMA ? (const void*)(tmaps + k) : nullptr;
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) {
     tc::tmem_alloc(&tmem_slot, kTmemCols);
     tc::tmem_relinquish();
   }
-  if (tid == 0) tc::mbar_init(&mbar, 1);
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    if (TMA) {
+      tc::mbar_init(&tbar, 1);
+      tc::tmap_acquire(tmap);
+    }
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -199,35 +270,83 @@ __global__ void __launch_bounds__(256, 2) k_lu_tc(int count, const int32_t* __re
   cc* Mk = A + mat_off[k];
   int32_t* ip = piv + piv_off[k];
   int first_zero = 0;
-  uint32_t phase = 0;
+  uint32_t phase = 0, tphase = 0;
   bool ok = true;
   for (int k0 = 0; k0 < n; k0 += kTcNB) {
     if (!lu_panel<cc, kTcNB, 1>(k0, 0, n, Mk, ip, P, red_v, red_i, s_piv, first_zero)) break;
-    if (!lu_update_tc(k0, n, Mk, Apl, Bpl, tm, &mbar, phase)) {
+    if (!lu_update_tc<TMA>(k0, n, Mk, Apl, Bpl, Cs, tmap, tm, &mbar, phase, &tbar, tphase)) {
       ok = false;
       break;
     }
   }
-  if (!ok && tid == 0) (void)tc::mbar_wait(&mbar, phase, kWaitLimit);   // drain what may still be in flight
+  if (!ok && tid == 0) {   // drain what may still be in flight
+    (void)tc::mbar_wait(&mbar, phase, kWaitLimit);
+    if (TMA) {
+      (void)tc::mbar_wait(&tbar, tphase, kWaitLimit);
+      tc::bulk_wait_all();
+    }
+  }
   if (tid == 0) info[k] = ok ? first_zero : -1;
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
-  if (tid == 0) tc::mbar_inval(&mbar);
+  if (tid == 0) {
+    tc::mbar_inval(&mbar);
+    if (TMA) tc::mbar_inval(&tbar);
+  }
 }
 
 cudaError_t launch_lu_tc(int count, const int32_t* nsz, int nmax, cc* A, const int64_t* mat_off, int32_t* piv,
                          const int64_t* piv_off, int32_t* info, cudaStream_t s, const int32_t* skip,
-                         const int32_t* order) {
+                         const int32_t* order, const CUtensorMap* tmaps) {
   if (count <= 0) return cudaSuccess;
-  const size_t sm = lu_tc_smem(nmax);
-  cudaError_t e = cudaFuncSetAttribute(k_lu_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  k_lu_tc<<<count, 256, sm, s>>>(count, nsz, A, mat_off, piv, piv_off, info, skip, order, nmax);
+  const bool tma = tmaps != nullptr;
+  const size_t sm = lu_tc_smem(nmax, tma);
+  if (tma) {
+    cudaError_t e = cudaFuncSetAttribute(k_lu_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_lu_tc<true><<<count, 256, sm, s>>>(count, nsz, A, mat_off, piv, piv_off, info, skip, order, nmax, tmaps);
+  } else {
+    cudaError_t e = cudaFuncSetAttribute(k_lu_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_lu_tc<false><<<count, 256, sm, s>>>(count, nsz, A, mat_off, piv, piv_off, info, skip, order, nmax, nullptr);
+  }
   return cudaGetLastError();
 }
 
-bool lu_tc_fits(int nmax) { return nmax >= 2 && lu_tc_smem(nmax) <= 227 * 1024; }
+bool lu_tc_fits(int nmax, bool tma) { return nmax >= 2 && lu_tc_smem(nmax, tma) <= 227 * 1024; }
+
+// Tensor maps of the complex64 matrices for the tile loads and stores: per
+// instance a 2D tensor of 8-byte elements, n rows (contiguous) x n columns,
+// boxes of 128 x 64.  Needs 16-byte aligned bases and strides, so every
+// order n must be even and every offset even; returns false (nothing
+// encoded) otherwise or when the driver entry point is missing.
+bool lu_tc_tensor_maps(int count, const int32_t* n, const int64_t* off, cc* base, std::vector<CUtensorMap>& out) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      cudaGetLastError();
+      return false;
+    }
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  out.assign(count, CUtensorMap{});
+  for (int k = 0; k < count; ++k) {
+    if ((n[k] & 1) || (off[k] & 1)) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)n[k], (cuuint64_t)n[k]};
+    const cuuint64_t strides[1] = {(cuuint64_t)n[k] * sizeof(cc)};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcRows, (cuuint32_t)kTcCols};
+    const cuuint32_t estr[2] = {1, 1};
+    if (encode(&out[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, base + off[k], dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
+}
 
 }  // namespace stab

@@ -29,13 +29,20 @@ def test_cluster_lu_matches_single_cta(ctx, n, z):
     assert pd == 0 and md == 0.0
 
 
-@pytest.mark.parametrize("n", [40, 200, 320, 640])
-def test_tensor_core_lu_backward_error(ctx, n):
+@pytest.mark.parametrize("tma", [1, 0])
+@pytest.mark.parametrize("n", [40, 201, 320, 640])
+def test_tensor_core_lu_backward_error(ctx, n, tma):
     """The complex64 LU with the trailing update on the tensor cores (TF32
-    parts, six part products) against the CUDA-core LU on the same matrices:
-    backward error max|PA - LU| / max|A| at most 4x the CUDA-core one and
-    below 1e-5 (complex64 working accuracy, n up to 640)."""
-    bt, bs, pd = ctx.lu_tc_check(n, 4)
+    parts, six part products), with the A22 tiles moved by tensor (TMA)
+    loads and stores or through the registers, against the CUDA-core LU on
+    the same matrices: backward error max|PA - LU| / max|A| at most 4x the
+    CUDA-core one and below 1e-5 (complex64 working accuracy, n up to 640;
+    the odd order takes the register form in both settings)."""
+    ctx.set_option(sg.OPT_POLISH_LU_TMA, tma)
+    try:
+        bt, bs, pd = ctx.lu_tc_check(n, 4)
+    finally:
+        ctx.set_option(sg.OPT_POLISH_LU_TMA, 1)
     assert np.isfinite(bt)
     assert bt < 1e-5, (bt, bs, pd)
     assert bt <= 4.0 * bs + 1e-7, (bt, bs, pd)

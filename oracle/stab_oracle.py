@@ -13,7 +13,7 @@ scipy's bundled LAPACK:
   materials       getmat.f90:2-37, input.f90:19-43 (incl. Te = T0 quirk)
   derivative mat  chebyd.f90:2-60 (CHEBYD, brute-force Lagrange form)
   temporal        temporal.f90:88-890
-  spatial         spatial.f90:89-1126 (curve = 0, h = 1)
+  spatial         spatial.f90:89-1126 (curve = 0, and curve = 2 with circh.f90)
   PIKSR2          stable ascending sort carrying an index
   getevec         getevec.f90:154-227 (selection, real-scale quirk, format)
   makename        mtemporal.f90:53-76
@@ -572,13 +572,356 @@ def temporal_blocks(p: StabParams, ms: MeanState):
     return bl
 
 
+INFTY = 1.0e30
+
+
+def circh_scalars(s: float):
+    """The station-independent part of circh (circh.f90:2-188, with xcloc and
+    ycloc, :201-229): the wall of a circle of radius s (the caller's x),
+    evaluated at arc position 0.  Returns dxbds, dybds, dbn1, dbn2, d2xbds2,
+    d2ybds2, d2bn1, d2bn2 (the tangent, the normal's arc derivative and the
+    second arc derivatives), from which circh_metrics forms h and its
+    derivatives at distance r from the wall.  circh also sets its argument
+    (the module's x) to zero (circh.f90:60)."""
+    radius = s
+    # xcloc(0, 0): th1 = atan2(sqrt(R^2 - x1^2), x1), xl = R cos(th1 - ds)
+    th1 = math.atan2(math.sqrt(radius ** 2 - 0.0 ** 2), 0.0)
+    xl = radius * math.cos(th1 - 0.0)
+    yl = math.sqrt(radius ** 2 - xl ** 2)            # ycloc(xl)
+    th = math.atan2(-xl, math.sqrt(radius ** 2 - xl ** 2))
+    bn1 = -math.sin(th)
+    bn2 = math.cos(th)
+    dydx = -INFTY if xl == 0.0 else (-xl) / yl
+    dxbds = 1.0 / math.sqrt(1.0 + dydx ** 2)
+    dxdy = -INFTY if xl == 0.0 else yl / (-xl)
+    dybds = 1.0 / math.sqrt(dxdy ** 2 + 1.0) if xl <= 0.0 else -1.0 / math.sqrt(dxdy ** 2 + 1.0)
+    if yl == 0.0:
+        dx, dy = 0.0, -xl
+        ddxdx, ddydx, ddxdy, ddydy = -INFTY, -1.0, 1.0, 0.0
+        d2dxdx2, d2dydx2, d2dxdy2, d2dydy2 = -INFTY, 0.0, 0.0, (xl ** 2 + yl ** 2) / xl ** 3
+    elif xl == 0.0:
+        dx, dy = yl, 0.0
+        ddxdx, ddydx, ddxdy, ddydy = 0.0, -1.0, 1.0, INFTY
+        d2dxdx2, d2dydx2, d2dxdy2, d2dydy2 = -(yl ** 2 + xl ** 2) / yl ** 3, 0.0, 0.0, INFTY
+    else:
+        dx, dy = yl, -xl
+        ddxdx, ddydx, ddxdy, ddydy = -xl / yl, -1.0, 1.0, yl / xl
+        d2dxdx2, d2dydx2, d2dxdy2, d2dydy2 = (-(yl ** 2 + xl ** 2) / yl ** 3, 0.0, 0.0,
+                                              (xl ** 2 + yl ** 2) / xl ** 3)
+    q = dx ** 2 + dy ** 2
+    if abs(bn1) > abs(bn2):
+        dbn1 = (-ddydy / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * dybds
+        dbn2 = (ddxdy / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * dybds
+    else:
+        dbn1 = (-ddydx / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * dxbds
+        dbn2 = (ddxdx / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * dxbds
+    if abs(bn1) > abs(bn2):
+        d2xdy2 = -(xl ** 2 + yl ** 2) / xl ** 3
+        if xl <= 0:
+            d2ybds2 = -(1.0 + dxdy ** 2) ** (-1.5) * dxdy * d2xdy2 * dybds
+        else:
+            d2ybds2 = (1.0 + dxdy ** 2) ** (-1.5) * dxdy * d2xdy2 * dybds
+        d2xbds2 = d2xdy2 * dybds ** 2 + dxdy * d2ybds2
+    else:
+        d2ydx2 = -(xl ** 2 + yl ** 2) / yl ** 3
+        d2xbds2 = -(1.0 + dydx ** 2) ** (-1.5) * dydx * d2ydx2 * dxbds
+        d2ybds2 = d2ydx2 * dxbds ** 2 + dydx * d2xbds2
+    if abs(bn1) > abs(bn2):
+        t1 = dy * ddxdy - dx * ddydy
+        t2 = dx * ddxdy + dy * ddydy
+        d2bn1 = (((ddxdy * t1 + dx * (dy * d2dxdy2 - dx * d2dydy2)) / q ** 1.5
+                  - (3.0 * dx * t1 * t2) / q ** 2.5) * dybds ** 2
+                 + (-ddydy / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * d2ybds2)
+        d2bn2 = (((ddydy * t1 + dy * (dy * d2dxdy2 - dx * d2dydy2)) / q ** 1.5
+                  - (3.0 * dy * t1 * t2) / q ** 2.5) * dybds ** 2
+                 + (ddxdy / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * d2ybds2)
+    else:
+        t1 = dy * ddxdx - dx * ddydx
+        t2 = dx * ddxdx + dy * ddydx
+        d2bn1 = (((ddxdx * t1 + dx * (dy * d2dxdx2 - dx * d2dydx2)) / q ** 1.5
+                  - (3.0 * dx * t1 * t2) / q ** 2.5) * dxbds ** 2
+                 + (-ddydx / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * d2xbds2)
+        d2bn2 = (((ddydx * t1 + dy * (dy * d2dxdx2 - dx * d2dydx2)) / q ** 1.5
+                  - (3.0 * dy * t1 * t2) / q ** 2.5) * dxbds ** 2
+                 + (ddxdx / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * d2xbds2)
+    if xl == 0.0:
+        d2bn1 = 0.0
+    return dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2
+
+
+def circh_metrics(sc, r):
+    """h, dh/ds, dh/dr, d2h/dsdr, d2h/dr2 at distances r from the wall
+    (circh.f90:190-199) from the scalars of circh_scalars."""
+    dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2 = sc
+    r = np.asarray(r, dtype=np.float64)
+    a = dxbds + r * dbn1
+    b = dybds + r * dbn2
+    h = np.sqrt(a ** 2 + b ** 2)
+    dads = d2xbds2 + r * d2bn1
+    dbds = d2ybds2 + r * d2bn2
+    dhds = (a * dads + b * dbds) / h
+    dhdr = (a * dbn1 + b * dbn2) / h
+    dhdrr = (-dhdr ** 2 + dbn1 ** 2 + dbn2 ** 2) / h
+    dhdsr = -dhds / h ** 2 * (a * dbn1 + b * dbn2) + (dads * dbn1 + a * d2bn1 + dbds * dbn2 + b * d2bn2) / h
+    return h, dhds, dhdr, dhdsr, dhdrr
+
+
+def wall_metrics(p: StabParams, y):
+    """The wall metrics of spatial.f90:110-125: curve = 2 a circle of radius
+    x (circh), curve = 0 a flat wall (h = 1).  curve = 1 (calch, a parabola
+    located with Numerical Recipes' rtflsp, which the reference does not
+    ship) is not restated."""
+    ny = len(y)
+    if p.curve == 0:
+        return np.ones(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny)
+    if p.curve == 2:
+        if p.x == -1.0:   # circh.f90:46-53: curvature turned off
+            return np.ones(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny)
+        return circh_metrics(circh_scalars(p.x), y)
+    raise ValueError("curve = 1 (calch) needs Numerical Recipes' rtflsp, absent from the reference")
+
+
+def spatial_blocks_curved(p: StabParams, ms: MeanState, met):
+    """Coefficient blocks of the spatial operator on a curved wall,
+    spatial.f90:230-673 term by term, with the metric h(y) of the wall and
+    its derivatives (met = h, dhds, dhdr, dhdsr, dhdrr).  The parallel mean
+    flow has u2m = 0 and no streamwise or spanwise gradients
+    (spatial.f90:147, 167-185)."""
+    h, dhds, dhdr, dhdsr, dhdrr = met
+    ny = p.ny
+    vm = ms.vm
+    rhom, u1m, _, u3m, tm = (vm[:, k] for k in range(5))
+    u2m = np.zeros(ny)
+    z = np.zeros(ny)
+    g2vm, g22vm = ms.g2vm, ms.g22vm
+    g1vm = g3vm = np.zeros((ny, 5))
+    g11vm = g12vm = g13vm = g23vm = g33vm = np.zeros((ny, 5))
+    gum = np.zeros((ny, 3, 3))
+    for i, k in enumerate((1, 2, 3)):
+        gum[:, i, 0] = g1vm[:, k]
+        gum[:, i, 1] = g2vm[:, k]
+        gum[:, i, 2] = g3vm[:, k]
+    divum = (gum[:, 0, 0] + u2m * dhdr) / h + gum[:, 1, 1] + gum[:, 2, 2]
+    grhom = np.stack([g1vm[:, 0], g2vm[:, 0], g3vm[:, 0]], axis=1)
+    gtm = np.stack([g1vm[:, 4], g2vm[:, 4], g3vm[:, 4]], axis=1)
+    g1divum = (-dhds / h ** 3 * (gum[:, 0, 0] + u2m * dhdr)
+               + 1.0 / h ** 2 * (g11vm[:, 1] + gum[:, 1, 0] * dhdr + u2m * dhdsr)
+               + 1.0 / h * (g12vm[:, 2] + g13vm[:, 3]))
+    g2divum = (-dhdr / h ** 2 * (gum[:, 0, 0] + u2m * dhdr)
+               + 1.0 / h * (g12vm[:, 1] + gum[:, 1, 1] * dhdr + u2m * dhdrr) + (g22vm[:, 2] + g23vm[:, 3]))
+    g3divum = 1.0 / h * (g13vm[:, 1] + gum[:, 1, 2] * dhdr) + g23vm[:, 2] + g33vm[:, 3]
+    S = np.zeros((ny, 3, 3))
+    S[:, 0, 0] = (gum[:, 0, 0] + u2m * dhdr) / h
+    S[:, 0, 1] = 0.5 * ((gum[:, 1, 0] - u1m * dhdr) / h + gum[:, 0, 1])
+    S[:, 0, 2] = 0.5 * (gum[:, 2, 0] / h + gum[:, 0, 2])
+    S[:, 1, 0] = S[:, 0, 1]
+    S[:, 1, 1] = gum[:, 1, 1]
+    S[:, 1, 2] = 0.5 * (gum[:, 2, 1] + gum[:, 1, 2])
+    S[:, 2, 0] = S[:, 0, 2]
+    S[:, 2, 1] = S[:, 1, 2]
+    S[:, 2, 2] = gum[:, 2, 2]
+    S1jj = (-0.5 * (dhdr ** 2 + dhdrr * h) / h ** 2 * u1m + 0.5 * dhdr * gum[:, 0, 1] / h + 0.5 * g22vm[:, 1]
+            - dhds * gum[:, 0, 0] / h ** 3 + g11vm[:, 1] / h ** 2 + 0.5 * g33vm[:, 1]
+            + (h * dhdsr - dhdr * dhds) / h ** 3 * u2m + 3.0 * dhdr * gum[:, 1, 0] / (2.0 * h ** 2)
+            + 0.5 * g12vm[:, 2] / h + 0.5 * g13vm[:, 3] / h)
+    S2jj = (0.5 * (dhdr * dhds - h * dhdsr) / h ** 3 * u1m - 3.0 * dhdr * gum[:, 0, 0] / (2.0 * h ** 2)
+            + 0.5 * g12vm[:, 1] / h - dhdr ** 2 * u2m / h ** 2 + dhdr * gum[:, 1, 1] / h + g22vm[:, 2]
+            - 0.5 * dhds * gum[:, 1, 0] / h ** 3 + 0.5 * g11vm[:, 2] / h ** 2 + 0.5 * g33vm[:, 2]
+            + 0.5 * g23vm[:, 3])
+    S3jj = (0.5 * g13vm[:, 1] / h + 0.5 * g23vm[:, 2] + 0.5 * dhdr * gum[:, 1, 2] / h
+            + 0.5 * dhdr * gum[:, 2, 1] / h + 0.5 * g22vm[:, 3] + 0.5 * g11vm[:, 3] / h ** 2 + g33vm[:, 3]
+            - 0.5 * dhds * gum[:, 2, 0] / h ** 3)
+    LapT = 1.0 / h * (-dhds / h ** 2 * gtm[:, 0] + 1.0 / h * g11vm[:, 4] + h * g22vm[:, 4] + gtm[:, 1] * dhdr
+                      + h * g33vm[:, 4])
+    m = _materials(p, tm)
+    rmu, rlm, con = m["rmu"], m["rlm"], m["con"]
+    dmu, d2mu, dlm, d2lm, dcon, d2con = m["dmu"], m["d2mu"], m["dlm"], m["d2lm"], m["dcon"], m["d2con"]
+    g1mu, g2mu, g3mu = (dmu * gtm[:, k] for k in range(3))
+    g1dmu, g2dmu, g3dmu = (d2mu * gtm[:, k] for k in range(3))
+    g1con, g2con, g3con = (dcon * gtm[:, k] for k in range(3))
+    g1dcon, g2dcon, g3dcon = (d2con * gtm[:, k] for k in range(3))
+    g1lm, g2lm, g3lm = (dlm * gtm[:, k] for k in range(3))
+    g1dlm, g2dlm, g3dlm = (d2lm * gtm[:, k] for k in range(3))
+    rlme, rmue = m["rlme"], m["rmue"]
+    gM2 = GAMMA * p.Ma ** 2
+    nav = p.navier()
+    Re, Pr, Ma = p.Re, p.Pr, p.Ma
+
+    bl = _zero_blocks(ny)
+    G, A, B, C, D = bl["G"], bl["A"], bl["B"], bl["C"], bl["D"]
+    Vxx, Vxy, Vyy, Vxz, Vyz, Vzz = (bl[k] for k in ("Vxx", "Vxy", "Vyy", "Vxz", "Vyz", "Vzz"))
+    # continuity (spatial.f90:356-371)
+    G[:, 0, 0] = 1.0
+    A[:, 0, 0] = u1m / h; A[:, 0, 1] = rhom / h
+    B[:, 0, 0] = u2m; B[:, 0, 2] = rhom
+    C[:, 0, 0] = u3m; C[:, 0, 3] = rhom
+    D[:, 0, 0] = divum; D[:, 0, 1] = grhom[:, 0] / h; D[:, 0, 2] = grhom[:, 1] + rhom * dhdr / h
+    D[:, 0, 3] = grhom[:, 2]
+    # x_1 momentum (spatial.f90:375-455)
+    G[:, 1, 1] = rhom
+    A[:, 1, 0] = tm / (h * gM2); A[:, 1, 1] = rhom * u1m / h; A[:, 1, 4] = rhom / (h * gM2)
+    B[:, 1, 1] = rhom * u2m
+    C[:, 1, 1] = rhom * u3m
+    D[:, 1, 0] = (u1m / h * (gum[:, 0, 0] + u2m * dhdr) + u2m * gum[:, 0, 1] + u3m * gum[:, 0, 2]
+                  + gtm[:, 0] / (h * gM2))
+    D[:, 1, 1] = rhom * (gum[:, 0, 0] + u2m * dhdr) / h
+    D[:, 1, 2] = rhom * (gum[:, 0, 1] + u1m * dhdr / h)
+    D[:, 1, 3] = rhom * gum[:, 0, 2]
+    D[:, 1, 4] = grhom[:, 0] / (h * gM2)
+    if nav:
+        f = rlme / (rmue * Re)
+        A[:, 1, 1] -= f * (g1lm / h ** 2 - rlm / h ** 3 * dhds)
+        A[:, 1, 2] -= f * rlm / h ** 2 * dhdr
+        A[:, 1, 4] -= f * dlm * divum / h
+        B[:, 1, 2] -= f * (g1lm / h)
+        C[:, 1, 3] -= f * (g1lm / h)
+        D[:, 1, 2] -= f * (g1lm * dhdr / h ** 2 - rlm / h ** 3 * dhds * dhdr + rlm / h ** 2 * dhdsr)
+        D[:, 1, 4] -= f * (g1dlm * divum / h + dlm * g1divum)
+        Vxx[:, 1, 1] = f * rlm / h ** 2
+        Vxy[:, 1, 2] = f * rlm / h
+        Vxz[:, 1, 3] = f * rlm / h
+        f = 1.0 / Re
+        A[:, 1, 1] -= f * (2.0 * g1mu / h ** 2 - 2.0 * rmu * dhds / h ** 3)
+        A[:, 1, 2] -= f * (g2mu / h + rmu * 3.0 * dhdr / h ** 2)
+        A[:, 1, 3] -= f * g3mu / h
+        A[:, 1, 4] -= f * dmu * 2.0 * S[:, 0, 0] / h
+        B[:, 1, 1] -= f * (g2mu + rmu * dhdr / h)
+        B[:, 1, 4] -= f * dmu * 2.0 * S[:, 0, 1]
+        C[:, 1, 1] -= f * g3mu
+        C[:, 1, 4] -= f * dmu * 2.0 * S[:, 0, 2]
+        D[:, 1, 1] -= f * (g2mu / h * (-dhdr) - rmu * (dhdr ** 2 + dhdrr * h) / h ** 2)
+        D[:, 1, 2] -= f * (2.0 * g1mu / h ** 2 * dhdr + 2.0 * rmu * (dhdsr * h - dhds * dhdr) / h ** 3)
+        D[:, 1, 4] -= f * 2.0 * (g1dmu / h * S[:, 0, 0] + g2dmu * S[:, 0, 1] + g3dmu * S[:, 0, 2] + dmu * S1jj)
+        Vxx[:, 1, 1] += f * 2.0 * rmu / h ** 2
+        Vxy[:, 1, 2] += f * rmu / h
+        Vyy[:, 1, 1] += f * rmu
+        Vxz[:, 1, 3] += f * rmu / h
+        Vzz[:, 1, 1] += f * rmu
+    # x_2 momentum (spatial.f90:459-541)
+    G[:, 2, 2] = rhom
+    A[:, 2, 2] = rhom * u1m / h
+    B[:, 2, 0] = tm / gM2; B[:, 2, 2] = rhom * u2m; B[:, 2, 4] = rhom / gM2
+    C[:, 2, 2] = rhom * u3m
+    D[:, 2, 0] = u1m / h * (gum[:, 1, 0] - u1m * dhdr) + u2m * gum[:, 1, 1] + u3m * gum[:, 1, 2] + gtm[:, 1] / gM2
+    D[:, 2, 1] = rhom * (gum[:, 1, 0] - 2.0 * u1m * dhdr) / h
+    D[:, 2, 2] = rhom * gum[:, 1, 1]
+    D[:, 2, 3] = rhom * gum[:, 1, 2]
+    D[:, 2, 4] = grhom[:, 1] / gM2
+    if nav:
+        f = rlme / (rmue * Re)
+        A[:, 2, 1] -= f * (g2lm / h - rlm * dhdr / h ** 2)
+        B[:, 2, 2] -= f * (g2lm + rlm * dhdr / h)
+        B[:, 2, 4] -= f * dlm * divum
+        C[:, 2, 3] -= f * g2lm
+        D[:, 2, 2] -= f * (g2lm / h * dhdr - rlm * dhdr / h ** 2 * dhdr + rlm / h * dhdrr)
+        D[:, 2, 4] -= f * (g2dlm * divum + dlm * g2divum)
+        Vxy[:, 2, 1] = f * rlm / h
+        Vyy[:, 2, 2] = f * rlm
+        Vyz[:, 2, 3] = f * rlm
+        f = 1.0 / Re
+        A[:, 2, 1] += f * rmu * 3.0 * dhdr / h ** 2
+        A[:, 2, 2] -= f * (g1mu / h ** 2 - rmu * dhds / h ** 3)
+        A[:, 2, 4] -= f * dmu * 2.0 * S[:, 1, 0] / h
+        B[:, 2, 1] -= f * g1mu / h
+        B[:, 2, 2] -= f * (2.0 * g2mu + 2.0 * rmu * dhdr / h)
+        B[:, 2, 3] -= f * g3mu
+        B[:, 2, 4] -= f * dmu * 2.0 * S[:, 1, 1]
+        C[:, 2, 2] -= f * g3mu
+        C[:, 2, 4] -= f * dmu * 2.0 * S[:, 1, 2]
+        D[:, 2, 1] -= f * (g1mu / h ** 2 * (-dhdr) + rmu * (dhds * dhdr - h * dhdsr) / h ** 3)
+        D[:, 2, 2] += f * 2.0 * rmu * dhdr ** 2 / h ** 2
+        D[:, 2, 4] -= f * 2.0 * (g1dmu / h * S[:, 1, 0] + g2dmu * S[:, 1, 1] + g3dmu * S[:, 1, 2] + dmu * S2jj)
+        Vxx[:, 2, 2] += f * rmu / h ** 2
+        Vxy[:, 2, 1] += f * rmu / h
+        Vyy[:, 2, 2] += f * 2.0 * rmu
+        Vyz[:, 2, 3] += f * rmu
+        Vzz[:, 2, 2] += f * rmu
+    # x_3 momentum (spatial.f90:545-597)
+    G[:, 3, 3] = rhom
+    A[:, 3, 3] = rhom * u1m / h
+    B[:, 3, 3] = rhom * u2m
+    C[:, 3, 0] = tm / gM2; C[:, 3, 3] = rhom * u3m; C[:, 3, 4] = rhom / gM2
+    D[:, 3, 0] = u1m * gum[:, 2, 0] / h + u2m * gum[:, 2, 1] + u3m * gum[:, 2, 2] + gtm[:, 2] / gM2
+    D[:, 3, 1] = rhom * gum[:, 2, 0] / h
+    D[:, 3, 2] = rhom * gum[:, 2, 1]
+    D[:, 3, 3] = rhom * gum[:, 2, 2]
+    D[:, 3, 4] = grhom[:, 2] / gM2
+    if nav:
+        f = rlme / (rmue * Re)
+        A[:, 3, 1] -= f * g3lm / h
+        B[:, 3, 2] -= f * g3lm
+        C[:, 3, 3] -= f * g3lm
+        C[:, 3, 2] -= f * rlm / h * dhdr
+        C[:, 3, 4] -= f * dlm * divum
+        D[:, 3, 2] -= f * (g2lm / h * dhdr)
+        D[:, 3, 4] -= f * (g3dlm * divum + dlm * g3divum)
+        Vxz[:, 3, 1] = f * rlm / h
+        Vyz[:, 3, 2] = f * rlm
+        Vzz[:, 3, 3] = f * rlm
+        f = 1.0 / Re
+        A[:, 3, 3] -= f * (g1mu / h ** 2 - rmu * dhds / h ** 3)
+        A[:, 3, 4] -= f * dmu * 2.0 * S[:, 2, 0] / h
+        B[:, 3, 3] -= f * (g2mu + rmu * dhdr / h)
+        B[:, 3, 4] -= f * dmu * 2.0 * S[:, 2, 1]
+        C[:, 3, 1] -= f * g1mu / h
+        C[:, 3, 2] -= f * (g2mu + rmu * dhdr / h)
+        C[:, 3, 3] -= f * 2.0 * g3mu
+        C[:, 3, 4] -= f * dmu * 2.0 * S[:, 2, 2]
+        D[:, 3, 4] -= f * 2.0 * (g1dmu / h * S[:, 2, 0] + g2dmu * S[:, 2, 1] + g3dmu * S[:, 2, 2] + dmu * S3jj)
+        Vxx[:, 3, 3] += f * rmu / h ** 2
+        Vyy[:, 3, 3] += f * rmu
+        Vxz[:, 3, 1] += f * rmu / h
+        Vyz[:, 3, 2] += f * rmu
+        Vzz[:, 3, 3] += f * 2.0 * rmu
+    # energy (spatial.f90:601-673)
+    G[:, 4, 4] = rhom
+    A[:, 4, 1] = rhom * GAMMA1 * tm / h; A[:, 4, 4] = rhom * u1m / h
+    B[:, 4, 2] = rhom * GAMMA1 * tm; B[:, 4, 4] = rhom * u2m
+    C[:, 4, 3] = rhom * GAMMA1 * tm; C[:, 4, 4] = rhom * u3m
+    D[:, 4, 0] = u1m / h * gtm[:, 0] + u2m * gtm[:, 1] + u3m * gtm[:, 2] + GAMMA1 * tm * divum
+    D[:, 4, 1] = rhom * gtm[:, 0] / h
+    D[:, 4, 2] = rhom * gtm[:, 1] + rhom * GAMMA1 * tm * dhdr / h
+    D[:, 4, 3] = rhom * gtm[:, 2]
+    D[:, 4, 4] = rhom * GAMMA1 * divum
+    if nav:
+        f = GAMMA / (Pr * Re)
+        A[:, 4, 4] -= f * (g1con / h ** 2 + dcon * gtm[:, 0] / h ** 2 - con * dhds / h ** 3)
+        B[:, 4, 4] -= f * (g2con + dcon * gtm[:, 1] + con * dhdr / h)
+        C[:, 4, 4] -= f * (g3con + dcon * gtm[:, 2])
+        D[:, 4, 4] -= f * (g1dcon * gtm[:, 0] / h ** 2 + g2dcon * gtm[:, 1] + g3dcon * gtm[:, 2] + dcon * LapT)
+        Vxx[:, 4, 4] = f * con / h ** 2
+        Vyy[:, 4, 4] = f * con
+        Vzz[:, 4, 4] = f * con
+        f = GAMMA * GAMMA1 * Ma ** 2 * rlme / (Re * rmue)
+        A[:, 4, 1] -= f * 2.0 * rlm * divum / h
+        B[:, 4, 2] -= f * 2.0 * rlm * divum
+        C[:, 4, 3] -= f * 2.0 * rlm * divum
+        D[:, 4, 2] -= f * 2.0 * rlm * divum * dhdr / h
+        D[:, 4, 4] -= f * dlm * divum * divum
+        f = GAMMA * GAMMA1 * Ma ** 2 / Re
+        A[:, 4, 1] -= f * 4.0 * rmu * S[:, 0, 0] / h
+        A[:, 4, 2] -= f * 4.0 * rmu * S[:, 1, 0] / h
+        A[:, 4, 3] -= f * 4.0 * rmu * S[:, 2, 0] / h
+        B[:, 4, 1] -= f * 4.0 * rmu * S[:, 0, 1]
+        B[:, 4, 2] -= f * 4.0 * rmu * S[:, 1, 1]
+        B[:, 4, 3] -= f * 4.0 * rmu * S[:, 2, 1]
+        C[:, 4, 1] -= f * 4.0 * rmu * S[:, 0, 2]
+        C[:, 4, 2] -= f * 4.0 * rmu * S[:, 1, 2]
+        C[:, 4, 3] -= f * 4.0 * rmu * S[:, 2, 2]
+        D[:, 4, 1] += f * 4.0 * rmu * S[:, 1, 0] * dhdr / h
+        D[:, 4, 2] -= f * 4.0 * rmu * S[:, 0, 0] * dhdr / h
+        D[:, 4, 4] -= f * 2.0 * dmu * (S ** 2).sum(axis=(1, 2))
+    return bl
+
+
 def spatial_blocks(p: StabParams, ms: MeanState):
     """Coefficient blocks of the spatial operator for a flat wall (curve=0,
-    h=1), spatial.f90:138-673.  The spatial solver zeroes u2m
+    h=1), spatial.f90:138-673; curved walls (curve = 2) go through
+    spatial_blocks_curved.  The spatial solver zeroes u2m
     (spatial.f90:147) and uses the gamma-multiplied energy equation
     (spatial.f90:599-673)."""
     if p.curve != 0:
-        raise ValueError("curvature (curve != 0) is outside this path")
+        return spatial_blocks_curved(p, ms, wall_metrics(p, ms.y))
     ny = p.ny
     vm = ms.vm
     rhom, u1m, _, u3m, tm = (vm[:, k] for k in range(5))

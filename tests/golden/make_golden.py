@@ -15,6 +15,9 @@ inputs and outputs for the Chebyshev path into small files:
   thesis_space.ref    thesis/TStest/space.ref (spatial N=96 eigenfunction)
   *.inp               the stdin files of those runs, verbatim: test/input.dat,
                       TStest/input.dat, thesis/TStest/temporal.inp, spatial.inp
+  cf_*, fsc_*         CFtest and FSCtest (curved wall, curve = 2): input.dat,
+                      profile.0 (as .npy), space.ref, and their eigenvalues
+                      (CFtest/README.md, the header of FSCtest/space.ref)
 """
 import json
 import os
@@ -78,6 +81,27 @@ def main(ref):
     c["golden"] = [2.2804739411180E-01, -6.5163146952626E-03]
     c["eigfunction"] = "thesis_space.ref"
     cases["thesis_spatial_n96"] = c
+    # curved-wall crossflow and Falkner-Skan-Cooke cases (curve = 2, circh):
+    # their own profiles; eigenvalues from CFtest/README.md (SGI at N = 64,
+    # MacOS at N = 96) and the header of FSCtest/space.ref
+    for tag, sub, gold in (("cf", "CFtest", {64: [-3.7392297537875E+001, -2.9982641664422E-001],
+                                              96: [-3.7392546274473E+001, -2.9977113927779E-001]}),
+                           ("fsc", "FSCtest", {64: [-4.6108596548503E-001, -7.0050272583092E-003]})):
+        rows = []
+        for ln in open(os.path.join(ref, sub, "profile.0")):
+            if ln[:1] == "#" or not ln.split():
+                continue
+            rows.append([float(t.replace("D", "E").replace("d", "e")) for t in ln.split()[:6]])
+        np.save(os.path.join(HERE, f"{tag}_profile.npy"), np.asarray(rows, dtype=np.float64))
+        shutil.copyfile(os.path.join(ref, sub, "input.dat"), os.path.join(HERE, f"{tag}_input.inp"))
+        shutil.copyfile(os.path.join(ref, sub, "space.ref"), os.path.join(HERE, f"{tag}_space.ref"))
+        c = read_input(os.path.join(ref, sub, "input.dat"))
+        c["x"] = 500.0          # the station read after the index (the circle's radius for curve = 2)
+        for ny, g in gold.items():
+            e = dict(c, ny=ny, golden=g, profile=f"{tag}_profile.npy")
+            if ny == 64:
+                e["eigfunction_rows"] = f"{tag}_space.ref"
+            cases[f"{tag}test_spatial_n{ny}"] = e
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1)
     for src, dst in [("test/input.dat", "test_input.inp"), ("TStest/input.dat", "tstest_input.inp"),

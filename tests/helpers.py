@@ -25,7 +25,14 @@ def stab_params(d: dict):
     import stab_gb300
     q = _stab_params(d)
     q.ider = int(d.get("ider", 1))
+    q.curve = int(d.get("curve", 0))
+    q.x = float(d.get("x", 0.0))
     return q
+
+
+def case_profile(c: dict) -> np.ndarray:
+    """The profile rows of a golden case (the TStest profile unless named)."""
+    return np.load(os.path.join(GOLDEN, c.get("profile", "ts_profile.npy")))
 
 
 def _stab_params(d: dict):
@@ -39,8 +46,8 @@ def _stab_params(d: dict):
 def oracle_params(d: dict) -> so.StabParams:
     return so.StabParams(mattyp=d["mattyp"], T0=d["T0"], Ma=d["Ma"], Re=d["Re"], Pr=d["Pr"], ny=d["ny"],
                          yi=d["yi"], ymax=d["ymax"], ievec=d["ievec"], ider=int(d.get("ider", 1)), top=d["top"],
-                         wall=d["wall"],
-                         wallt=d["wallt"], curve=0, itype=d["itype"], alpha=complex(*d["alpha"]),
+                         wall=d["wall"], wallt=d["wallt"], curve=int(d.get("curve", 0)), x=float(d.get("x", 0.0)),
+                         itype=d["itype"], alpha=complex(*d["alpha"]),
                          beta=complex(*d["beta"]), omega=complex(*d["omega"]))
 
 

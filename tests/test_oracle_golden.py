@@ -65,3 +65,35 @@ def test_oracle_external_derivatives_agree_with_internal():
         e0 = H.oracle_solve(d0, tab, want_vectors=False).eig
         j1, j0 = H.select_least(e1, d), H.select_least(e0, d0)
         assert abs(e1[j1] - e0[j0]) / abs(e1[j1]) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["cftest_spatial_n64", "cftest_spatial_n96", "fsctest_spatial_n64"])
+def test_oracle_curved_wall_matches_reference(name):
+    """Curved walls (curve = 2, the circle of circh.f90 with radius x = 500):
+    the crossflow case CFtest (N = 64 on SGI and N = 96 on MacOS, its README)
+    and the Falkner-Skan-Cooke case FSCtest (N = 64, the header of its
+    space.ref).  Eigenvalue within 1e-10 relative; at N = 64 the eigenfunction
+    rows of space.ref (the first 5N entries of the companion eigenvector),
+    matched by y and divided by their largest-modulus entry, within 1e-8."""
+    c = H.cases()[name]
+    prof = H.case_profile(c)
+    es = H.oracle_solve(c, prof, want_vectors="eigfunction_rows" in c)
+    g = complex(*c["golden"])
+    j = so.getevec_select(es.eig, g)
+    assert abs(es.eig[j] - g) / abs(g) < EIG_REL
+    if "eigfunction_rows" in c:
+        ref = np.loadtxt(H.GOLDEN + "/" + c["eigfunction_rows"], comments="#")
+        ny = c["ny"]
+        v = es.evec[:5 * ny, j].reshape(ny, 5)
+        ys = es.ms.y
+        assert ref.shape == (ny, 11)
+        # rows matched by y (the files list them wall first or free stream first)
+        order = [int(np.argmin(np.abs(ys - yr))) for yr in ref[:, 0]]
+        assert len(set(order)) == ny
+        assert np.allclose(ys[order], ref[:, 0], rtol=1e-10, atol=1e-12)
+        got = v[order]
+        want = ref[:, 1::2] + 1j * ref[:, 2::2]
+        kg = np.unravel_index(np.argmax(np.abs(got)), got.shape)
+        kw = np.unravel_index(np.argmax(np.abs(want)), want.shape)
+        assert kg == kw
+        assert np.max(np.abs(got / got[kg] - want / want[kw])) < NDIFF_ABS

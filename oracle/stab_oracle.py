@@ -1325,7 +1325,12 @@ def solve(p: StabParams, ym, vt, want_vectors=True, first=None, second=None) -> 
     if p.itype == 1:
         return temporal_solve(p, ms, want_vectors)
     if p.itype == 2:
-        return spatial_solve(p, ms, want_vectors)
+        es = spatial_solve(p, ms, want_vectors)
+        if p.curve == 2 and p.x != -1.0:
+            # circh sets its argument, the module's x, to zero (circh.f90:60);
+            # evec.dat records that x
+            es.params = dataclasses.replace(p, x=0.0)
+        return es
     raise ValueError("itype must be 1 or 2")
 
 

@@ -282,12 +282,74 @@ struct stab_batch {
 
 stab_batch::~stab_batch() { delete coarse; }
 
+// The station-independent scalars of circh (circh.f90:2-188, with xcloc and
+// ycloc, :201-229): the wall of a circle of radius s at arc position 0.
+// out = dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2; h(y) and
+// its derivatives follow in k_blocks (circh.f90:190-199).
+static void circh_scalars(double s, double out[8]) {
+  const double infty = 1.0e30;
+  const double radius = s;
+  const double th1 = std::atan2(std::sqrt(radius * radius - 0.0), 0.0);   // xcloc(0, 0)
+  const double xl = radius * std::cos(th1 - 0.0);
+  const double yl = std::sqrt(radius * radius - xl * xl);                   // ycloc(xl)
+  const double th = std::atan2(-xl, std::sqrt(radius * radius - xl * xl));
+  const double bn1 = -std::sin(th), bn2 = std::cos(th);
+  const double dydx = (xl == 0.0) ? -infty : (-xl) / yl;
+  const double dxbds = 1.0 / std::sqrt(1.0 + dydx * dydx);
+  const double dxdy = (xl == 0.0) ? -infty : yl / (-xl);
+  const double dybds = (xl <= 0.0) ? 1.0 / std::sqrt(dxdy * dxdy + 1.0) : -1.0 / std::sqrt(dxdy * dxdy + 1.0);
+  double dx, dy, ddxdx, ddydx, ddxdy, ddydy, d2dxdx2, d2dydx2, d2dxdy2, d2dydy2;
+  if (yl == 0.0) {
+    dx = 0.0; dy = -xl; ddxdx = -infty; ddydx = -1.0; ddxdy = 1.0; ddydy = 0.0;
+    d2dxdx2 = -infty; d2dydx2 = 0.0; d2dxdy2 = 0.0; d2dydy2 = (xl * xl + yl * yl) / (xl * xl * xl);
+  } else if (xl == 0.0) {
+    dx = yl; dy = 0.0; ddxdx = 0.0; ddydx = -1.0; ddxdy = 1.0; ddydy = infty;
+    d2dxdx2 = -(yl * yl + xl * xl) / (yl * yl * yl); d2dydx2 = 0.0; d2dxdy2 = 0.0; d2dydy2 = infty;
+  } else {
+    dx = yl; dy = -xl; ddxdx = -xl / yl; ddydx = -1.0; ddxdy = 1.0; ddydy = yl / xl;
+    d2dxdx2 = -(yl * yl + xl * xl) / (yl * yl * yl); d2dydx2 = 0.0; d2dxdy2 = 0.0;
+    d2dydy2 = (xl * xl + yl * yl) / (xl * xl * xl);
+  }
+  const double q = dx * dx + dy * dy;
+  const double q05 = std::pow(q, 0.5), q15 = std::pow(q, 1.5), q25 = std::pow(q, 2.5);
+  const bool nflat = std::fabs(bn1) > std::fabs(bn2);
+  // derivatives along the arc through y (nflat) or through x
+  const double ddx = nflat ? ddxdy : ddxdx, ddy = nflat ? ddydy : ddydx;
+  const double d2dx = nflat ? d2dxdy2 : d2dxdx2, d2dy = nflat ? d2dydy2 : d2dydx2;
+  const double dsd = nflat ? dybds : dxbds;
+  const double dbn1 = (-ddy / q05 + 0.5 * dy * (2.0 * dx * ddx + 2.0 * dy * ddy) / q15) * dsd;
+  const double dbn2 = (ddx / q05 - 0.5 * dx * (2.0 * dx * ddx + 2.0 * dy * ddy) / q15) * dsd;
+  double d2xbds2, d2ybds2;
+  if (nflat) {
+    const double d2xdy2 = -(xl * xl + yl * yl) / (xl * xl * xl);
+    d2ybds2 = (xl <= 0 ? -1.0 : 1.0) * std::pow(1.0 + dxdy * dxdy, -1.5) * dxdy * d2xdy2 * dybds;
+    d2xbds2 = d2xdy2 * dybds * dybds + dxdy * d2ybds2;
+  } else {
+    const double d2ydx2 = -(xl * xl + yl * yl) / (yl * yl * yl);
+    d2xbds2 = -std::pow(1.0 + dydx * dydx, -1.5) * dydx * d2ydx2 * dxbds;
+    d2ybds2 = d2ydx2 * dxbds * dxbds + dydx * d2xbds2;
+  }
+  const double d2s = nflat ? d2ybds2 : d2xbds2;
+  const double t1 = dy * ddx - dx * ddy, t2 = dx * ddx + dy * ddy;
+  double d2bn1 = ((ddx * t1 + dx * (dy * d2dx - dx * d2dy)) / q15 - (3.0 * dx * t1 * t2) / q25) * dsd * dsd +
+                 (-ddy / q05 + 0.5 * dy * (2.0 * dx * ddx + 2.0 * dy * ddy) / q15) * d2s;
+  const double d2bn2 = ((ddy * t1 + dy * (dy * d2dx - dx * d2dy)) / q15 - (3.0 * dy * t1 * t2) / q25) * dsd * dsd +
+                       (ddx / q05 - 0.5 * dx * (2.0 * dx * ddx + 2.0 * dy * ddy) / q15) * d2s;
+  if (xl == 0.0) d2bn1 = 0.0;
+  const double v[8] = {dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2};
+  for (int i = 0; i < 8; ++i) out[i] = v[i];
+}
+
 // Descriptor of one instance from its run parameters (validated) and the
 // entry of its mean profile in the profile pools.
 static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDesc& pd, InstDesc& d) {
   if (q.itype != 1 && q.itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal) or 2 (spatial)");
   if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
-  if (q.curve != 0) return set_err(c, STAB_ERR_ARG, "curve != 0 (curved walls) is not supported");
+  if (q.itype == 2 && q.curve == 1)
+    return set_err(c, STAB_ERR_ARG, "curve = 1 (calch: a parabola located with Numerical Recipes' rtflsp, which the "
+                                    "reference does not ship) is not supported; curve = 2 (circle) is");
+  if (q.itype == 2 && q.curve != 0 && q.curve != 1 && q.curve != 2)
+    return set_err(c, STAB_ERR_ARG, "curve must be 0, 1 or 2");
   if (q.ider != 0 && q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider must be 0 or 1");
   if (q.wallt != 0 && q.wallt != 2) return set_err(c, STAB_ERR_ARG, "Illegal value of wallt");
   if (q.yi == 0.0) return set_err(c, STAB_ERR_ARG, "Yi = 0 (tanh map) is not supported");
@@ -316,6 +378,10 @@ static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDes
   d.off_prof = pd.off_prof;
   d.off_spl = pd.off_spl;
   d.ider = q.ider;
+  // spatial.f90:110-125: the temporal solver has no wall metric; circh with
+  // x = -1 turns curvature off (circh.f90:46-53)
+  d.curved = (q.itype == 2 && q.curve == 2 && q.x != -1.0) ? 1 : 0;
+  if (d.curved) circh_scalars(q.x, d.cw);
   return 0;
 }
 

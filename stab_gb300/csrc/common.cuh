@@ -126,6 +126,11 @@ struct InstDesc {
   // (getmean2.f90:99-175), profile entries like the mean's
   int32_t iprof_d1, iprof_d2;
   int64_t off_prof_d1, off_spl_d1, off_prof_d2, off_spl_d2;
+  // curved wall (spatial, curve = 2): 1, and the arc-position scalars of the
+  // circle's metric (dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1,
+  // d2bn2) from which h(y) and its derivatives follow (circh.f90:190-199)
+  int32_t curved, pad2_;
+  double cw[8];
 };
 #define VEC_SLOTS 10
 

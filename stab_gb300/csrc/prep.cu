@@ -11,7 +11,8 @@
 //   getmean2.f90:99-175              derivative tables too)
 //   temporal.f90:148-179   k_meanderiv (D1 v, D2 v and the map chain rule)
 //   temporal.f90:206-598   k_blocks (materials, coefficient blocks), and
-//   spatial.f90:138-673    the h = 1 spatial variant
+//   spatial.f90:138-673    the spatial variant: h = 1 (node_blocks), or the
+//                          circular wall of circh.f90 (node_blocks_curved)
 //   temporal.f90:604-662   temporal operator blocks (Dh, Bh, mapping, B0)
 //   spatial.f90:677-959    spatial operator blocks (C0, C1, C2)
 #include "common.cuh"
@@ -408,6 +409,228 @@ __device__ void node_blocks(const InstDesc& d, const double* nd, bool spatial, B
   }
 }
 
+// The spatial blocks on a curved wall, spatial.f90:230-673 term by term,
+// with the metric h of the wall at this node and its derivatives
+// (dh/ds, dh/dr, d2h/dsdr, d2h/dr2).  The parallel mean has u2m = 0 and no
+// streamwise or spanwise gradients (spatial.f90:147, 167-185), so of the
+// reference's mean-gradient arrays only the y derivatives survive.
+__device__ void node_blocks_curved(const InstDesc& d, const double* nd, double h, double dhds, double dhdr,
+                                   double dhdsr, double dhdrr, Blocks& b) {
+  const double gamma = 1.4, gamma1 = 0.4, cp = 1003.1, pt66 = 6.6666666666666666666e-1;
+  const double Ma = d.Ma, Re = d.Re, Pr = d.Pr, Te = d.Te;
+  const double rhom = nd[NODE_VM + 0], u1m = nd[NODE_VM + 1], u3m = nd[NODE_VM + 3], tm = nd[NODE_VM + 4];
+  const double u2m = 0.0;
+  // gum[i][j] = d u_i / d x_j: only j = y (index 1) of u and w
+  double gum[3][3] = {{0.0, nd[NODE_G2 + 1], 0.0}, {0.0, nd[NODE_G2 + 2], 0.0}, {0.0, nd[NODE_G2 + 3], 0.0}};
+  const double g22u = nd[NODE_G22 + 1], g22v = nd[NODE_G22 + 2], g22w = nd[NODE_G22 + 3], g22t = nd[NODE_G22 + 4];
+  const double grhom[3] = {0.0, nd[NODE_G2 + 0], 0.0}, gtm[3] = {0.0, nd[NODE_G2 + 4], 0.0};
+  const double h2 = h * h, h3 = h2 * h;
+  const double divum = (gum[0][0] + u2m * dhdr) / h + gum[1][1] + gum[2][2];
+  const double g1divum = -dhds / h3 * (gum[0][0] + u2m * dhdr) + 1.0 / h2 * (gum[1][0] * dhdr + u2m * dhdsr);
+  const double g2divum = -dhdr / h2 * (gum[0][0] + u2m * dhdr) + 1.0 / h * (gum[1][1] * dhdr + u2m * dhdrr) + g22v;
+  const double g3divum = 1.0 / h * (gum[1][2] * dhdr);
+  double S[3][3];
+  S[0][0] = (gum[0][0] + u2m * dhdr) / h;
+  S[0][1] = 0.5 * ((gum[1][0] - u1m * dhdr) / h + gum[0][1]);
+  S[0][2] = 0.5 * (gum[2][0] / h + gum[0][2]);
+  S[1][0] = S[0][1];
+  S[1][1] = gum[1][1];
+  S[1][2] = 0.5 * (gum[2][1] + gum[1][2]);
+  S[2][0] = S[0][2];
+  S[2][1] = S[1][2];
+  S[2][2] = gum[2][2];
+  const double S1jj = -0.5 * (dhdr * dhdr + dhdrr * h) / h2 * u1m + 0.5 * dhdr * gum[0][1] / h + 0.5 * g22u -
+                      dhds * gum[0][0] / h3 + (h * dhdsr - dhdr * dhds) / h3 * u2m +
+                      3.0 * dhdr * gum[1][0] / (2.0 * h2);
+  const double S2jj = 0.5 * (dhdr * dhds - h * dhdsr) / h3 * u1m - 3.0 * dhdr * gum[0][0] / (2.0 * h2) -
+                      dhdr * dhdr * u2m / h2 + dhdr * gum[1][1] / h + g22v - 0.5 * dhds * gum[1][0] / h3;
+  const double S3jj = 0.5 * dhdr * gum[1][2] / h + 0.5 * dhdr * gum[2][1] / h + 0.5 * g22w -
+                      0.5 * dhds * gum[2][0] / h3;
+  const double LapT = 1.0 / h * (-dhds / h2 * gtm[0] + h * g22t + gtm[1] * dhdr);
+  double mue, dmue, d2mue;
+  material(d.mattyp, Te, mue, dmue, d2mue);
+  const double rmue = mue, cone = mue * cp / Pr, rlme = -pt66 * mue;
+  double mu, dmu0, d2mu0;
+  material(d.mattyp, tm * Te, mu, dmu0, d2mu0);
+  const double rmu = mu / rmue, dmu = dmu0 * Te / rmue, d2mu = d2mu0 * Te * Te / rmue;
+  const double con = mu * cp / Pr / cone, dcon = dmu0 * cp / Pr * Te / cone, d2con = d2mu0 * cp / Pr * Te * Te / cone;
+  const double rlm = -pt66 * mu / rlme, dlm = -pt66 * dmu0 * Te / rlme, d2lm = -pt66 * d2mu0 * Te * Te / rlme;
+  double g1mu = dmu * gtm[0], g2mu = dmu * gtm[1], g3mu = dmu * gtm[2];
+  double g1dmu = d2mu * gtm[0], g2dmu = d2mu * gtm[1], g3dmu = d2mu * gtm[2];
+  double g1con = dcon * gtm[0], g2con = dcon * gtm[1], g3con = dcon * gtm[2];
+  double g1dcon = d2con * gtm[0], g2dcon = d2con * gtm[1], g3dcon = d2con * gtm[2];
+  double g1lm = dlm * gtm[0], g2lm = dlm * gtm[1], g3lm = dlm * gtm[2];
+  double g1dlm = d2lm * gtm[0], g2dlm = d2lm * gtm[1], g3dlm = d2lm * gtm[2];
+  const double gM2 = gamma * Ma * Ma;
+  const bool nav = !(Re >= 1.0e98 || Re == 0.0);
+  double* all = &b.G[0][0];
+  for (int q = 0; q < 11 * 25; ++q) all[q] = 0.0;
+  auto &G = b.G, &A = b.A, &B = b.B, &C = b.C, &D = b.D;
+  auto &Vxx = b.Vxx, &Vxy = b.Vxy, &Vyy = b.Vyy, &Vxz = b.Vxz, &Vyz = b.Vyz, &Vzz = b.Vzz;
+  // continuity (spatial.f90:356-371)
+  G[0][0] = 1.0;
+  A[0][0] = u1m / h; A[0][1] = rhom / h;
+  B[0][0] = u2m; B[0][2] = rhom;
+  C[0][0] = u3m; C[0][3] = rhom;
+  D[0][0] = divum; D[0][1] = grhom[0] / h; D[0][2] = grhom[1] + rhom * dhdr / h; D[0][3] = grhom[2];
+  // x_1 momentum (spatial.f90:375-455)
+  G[1][1] = rhom;
+  A[1][0] = tm / (h * gM2); A[1][1] = rhom * u1m / h; A[1][4] = rhom / (h * gM2);
+  B[1][1] = rhom * u2m;
+  C[1][1] = rhom * u3m;
+  D[1][0] = u1m / h * (gum[0][0] + u2m * dhdr) + u2m * gum[0][1] + u3m * gum[0][2] + gtm[0] / (h * gM2);
+  D[1][1] = rhom * (gum[0][0] + u2m * dhdr) / h;
+  D[1][2] = rhom * (gum[0][1] + u1m * dhdr / h);
+  D[1][3] = rhom * gum[0][2];
+  D[1][4] = grhom[0] / (h * gM2);
+  if (nav) {
+    double f = rlme / (rmue * Re);
+    A[1][1] -= f * (g1lm / h2 - rlm / h3 * dhds);
+    A[1][2] -= f * rlm / h2 * dhdr;
+    A[1][4] -= f * dlm * divum / h;
+    B[1][2] -= f * (g1lm / h);
+    C[1][3] -= f * (g1lm / h);
+    D[1][2] -= f * (g1lm * dhdr / h2 - rlm / h3 * dhds * dhdr + rlm / h2 * dhdsr);
+    D[1][4] -= f * (g1dlm * divum / h + dlm * g1divum);
+    Vxx[1][1] = f * rlm / h2;
+    Vxy[1][2] = f * rlm / h;
+    Vxz[1][3] = f * rlm / h;
+    f = 1.0 / Re;
+    A[1][1] -= f * (2.0 * g1mu / h2 - 2.0 * rmu * dhds / h3);
+    A[1][2] -= f * (g2mu / h + rmu * 3.0 * dhdr / h2);
+    A[1][3] -= f * g3mu / h;
+    A[1][4] -= f * dmu * 2.0 * S[0][0] / h;
+    B[1][1] -= f * (g2mu + rmu * dhdr / h);
+    B[1][4] -= f * dmu * 2.0 * S[0][1];
+    C[1][1] -= f * g3mu;
+    C[1][4] -= f * dmu * 2.0 * S[0][2];
+    D[1][1] -= f * (g2mu / h * (-dhdr) - rmu * (dhdr * dhdr + dhdrr * h) / h2);
+    D[1][2] -= f * (2.0 * g1mu / h2 * dhdr + 2.0 * rmu * (dhdsr * h - dhds * dhdr) / h3);
+    D[1][4] -= f * 2.0 * (g1dmu / h * S[0][0] + g2dmu * S[0][1] + g3dmu * S[0][2] + dmu * S1jj);
+    Vxx[1][1] += f * 2.0 * rmu / h2;
+    Vxy[1][2] += f * rmu / h;
+    Vyy[1][1] += f * rmu;
+    Vxz[1][3] += f * rmu / h;
+    Vzz[1][1] += f * rmu;
+  }
+  // x_2 momentum (spatial.f90:459-541)
+  G[2][2] = rhom;
+  A[2][2] = rhom * u1m / h;
+  B[2][0] = tm / gM2; B[2][2] = rhom * u2m; B[2][4] = rhom / gM2;
+  C[2][2] = rhom * u3m;
+  D[2][0] = u1m / h * (gum[1][0] - u1m * dhdr) + u2m * gum[1][1] + u3m * gum[1][2] + gtm[1] / gM2;
+  D[2][1] = rhom * (gum[1][0] - 2.0 * u1m * dhdr) / h;
+  D[2][2] = rhom * gum[1][1];
+  D[2][3] = rhom * gum[1][2];
+  D[2][4] = grhom[1] / gM2;
+  if (nav) {
+    double f = rlme / (rmue * Re);
+    A[2][1] -= f * (g2lm / h - rlm * dhdr / h2);
+    B[2][2] -= f * (g2lm + rlm * dhdr / h);
+    B[2][4] -= f * dlm * divum;
+    C[2][3] -= f * g2lm;
+    D[2][2] -= f * (g2lm / h * dhdr - rlm * dhdr / h2 * dhdr + rlm / h * dhdrr);
+    D[2][4] -= f * (g2dlm * divum + dlm * g2divum);
+    Vxy[2][1] = f * rlm / h;
+    Vyy[2][2] = f * rlm;
+    Vyz[2][3] = f * rlm;
+    f = 1.0 / Re;
+    A[2][1] += f * rmu * 3.0 * dhdr / h2;
+    A[2][2] -= f * (g1mu / h2 - rmu * dhds / h3);
+    A[2][4] -= f * dmu * 2.0 * S[1][0] / h;
+    B[2][1] -= f * g1mu / h;
+    B[2][2] -= f * (2.0 * g2mu + 2.0 * rmu * dhdr / h);
+    B[2][3] -= f * g3mu;
+    B[2][4] -= f * dmu * 2.0 * S[1][1];
+    C[2][2] -= f * g3mu;
+    C[2][4] -= f * dmu * 2.0 * S[1][2];
+    D[2][1] -= f * (g1mu / h2 * (-dhdr) + rmu * (dhds * dhdr - h * dhdsr) / h3);
+    D[2][2] += f * 2.0 * rmu * dhdr * dhdr / h2;
+    D[2][4] -= f * 2.0 * (g1dmu / h * S[1][0] + g2dmu * S[1][1] + g3dmu * S[1][2] + dmu * S2jj);
+    Vxx[2][2] += f * rmu / h2;
+    Vxy[2][1] += f * rmu / h;
+    Vyy[2][2] += f * 2.0 * rmu;
+    Vyz[2][3] += f * rmu;
+    Vzz[2][2] += f * rmu;
+  }
+  // x_3 momentum (spatial.f90:545-597)
+  G[3][3] = rhom;
+  A[3][3] = rhom * u1m / h;
+  B[3][3] = rhom * u2m;
+  C[3][0] = tm / gM2; C[3][3] = rhom * u3m; C[3][4] = rhom / gM2;
+  D[3][0] = u1m * gum[2][0] / h + u2m * gum[2][1] + u3m * gum[2][2] + gtm[2] / gM2;
+  D[3][1] = rhom * gum[2][0] / h;
+  D[3][2] = rhom * gum[2][1];
+  D[3][3] = rhom * gum[2][2];
+  D[3][4] = grhom[2] / gM2;
+  if (nav) {
+    double f = rlme / (rmue * Re);
+    A[3][1] -= f * g3lm / h;
+    B[3][2] -= f * g3lm;
+    C[3][3] -= f * g3lm;
+    C[3][2] -= f * rlm / h * dhdr;
+    C[3][4] -= f * dlm * divum;
+    D[3][2] -= f * (g2lm / h * dhdr);
+    D[3][4] -= f * (g3dlm * divum + dlm * g3divum);
+    Vxz[3][1] = f * rlm / h;
+    Vyz[3][2] = f * rlm;
+    Vzz[3][3] = f * rlm;
+    f = 1.0 / Re;
+    A[3][3] -= f * (g1mu / h2 - rmu * dhds / h3);
+    A[3][4] -= f * dmu * 2.0 * S[2][0] / h;
+    B[3][3] -= f * (g2mu + rmu * dhdr / h);
+    B[3][4] -= f * dmu * 2.0 * S[2][1];
+    C[3][1] -= f * g1mu / h;
+    C[3][2] -= f * (g2mu + rmu * dhdr / h);
+    C[3][3] -= f * 2.0 * g3mu;
+    C[3][4] -= f * dmu * 2.0 * S[2][2];
+    D[3][4] -= f * 2.0 * (g1dmu / h * S[2][0] + g2dmu * S[2][1] + g3dmu * S[2][2] + dmu * S3jj);
+    Vxx[3][3] += f * rmu / h2;
+    Vyy[3][3] += f * rmu;
+    Vxz[3][1] += f * rmu / h;
+    Vyz[3][2] += f * rmu;
+    Vzz[3][3] += f * 2.0 * rmu;
+  }
+  // energy (spatial.f90:601-673)
+  G[4][4] = rhom;
+  A[4][1] = rhom * gamma1 * tm / h; A[4][4] = rhom * u1m / h;
+  B[4][2] = rhom * gamma1 * tm; B[4][4] = rhom * u2m;
+  C[4][3] = rhom * gamma1 * tm; C[4][4] = rhom * u3m;
+  D[4][0] = u1m / h * gtm[0] + u2m * gtm[1] + u3m * gtm[2] + gamma1 * tm * divum;
+  D[4][1] = rhom * gtm[0] / h;
+  D[4][2] = rhom * gtm[1] + rhom * gamma1 * tm * dhdr / h;
+  D[4][3] = rhom * gtm[2];
+  D[4][4] = rhom * gamma1 * divum;
+  if (nav) {
+    double f = gamma / (Pr * Re);
+    A[4][4] -= f * (g1con / h2 + dcon * gtm[0] / h2 - con * dhds / h3);
+    B[4][4] -= f * (g2con + dcon * gtm[1] + con * dhdr / h);
+    C[4][4] -= f * (g3con + dcon * gtm[2]);
+    D[4][4] -= f * (g1dcon * gtm[0] / h2 + g2dcon * gtm[1] + g3dcon * gtm[2] + dcon * LapT);
+    Vxx[4][4] = f * con / h2;
+    Vyy[4][4] = f * con;
+    Vzz[4][4] = f * con;
+    f = gamma * gamma1 * Ma * Ma * rlme / (Re * rmue);
+    A[4][1] -= f * 2.0 * rlm * divum / h;
+    B[4][2] -= f * 2.0 * rlm * divum;
+    C[4][3] -= f * 2.0 * rlm * divum;
+    D[4][2] -= f * 2.0 * rlm * divum * dhdr / h;
+    D[4][4] -= f * dlm * divum * divum;
+    f = gamma * gamma1 * Ma * Ma / Re;
+    for (int c = 0; c < 3; ++c) {
+      A[4][1 + c] -= f * 4.0 * rmu * S[c][0] / h;
+      B[4][1 + c] -= f * 4.0 * rmu * S[c][1];
+      C[4][1 + c] -= f * 4.0 * rmu * S[c][2];
+    }
+    D[4][1] += f * 4.0 * rmu * S[1][0] * dhdr / h;
+    D[4][2] -= f * 4.0 * rmu * S[0][0] * dhdr / h;
+    double ss = 0.0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) ss += S[i][j] * S[i][j];
+    D[4][4] -= f * 2.0 * dmu * ss;
+  }
+}
+
 // 5x5 complex inverse by Gauss-Jordan with partial pivoting (B0 blocks)
 __device__ bool inv5(const zc in[5][5], zc out[5][5]) {
   zc a[5][10];
@@ -456,7 +679,22 @@ __global__ void k_blocks(int count, const InstDesc* __restrict__ desc, const dou
   const double* D1 = dtab[2 * d.dmat];
   const double dww = D1[(size_t)(ny - 1) * ny + (ny - 1)];   // D1(wall, wall), for the adiabatic row
   Blocks b;
-  node_blocks(d, nd, spatial, b);
+  if (spatial && d.curved) {
+    // the circle's metric at this node's distance r = y from the wall
+    // (circh.f90:190-199)
+    const double r = nd[NODE_Y];
+    const double* w = d.cw;
+    const double a = w[0] + r * w[2], bb = w[1] + r * w[3];
+    const double h = sqrt(a * a + bb * bb);
+    const double dads = w[4] + r * w[6], dbds = w[5] + r * w[7];
+    const double dhds = (a * dads + bb * dbds) / h;
+    const double dhdr = (a * w[2] + bb * w[3]) / h;
+    const double dhdrr = (-dhdr * dhdr + w[2] * w[2] + w[3] * w[3]) / h;
+    const double dhdsr = -dhds / (h * h) * (a * w[2] + bb * w[3]) + (dads * w[2] + a * w[6] + dbds * w[3] + bb * w[7]) / h;
+    node_blocks_curved(d, nd, h, dhds, dhdr, dhdsr, dhdrr, b);
+  } else {
+    node_blocks(d, nd, spatial, b);
+  }
   const zc I = zmk(0.0, 1.0);
   const bool top_node = (i == 0), wall_node = (i == ny - 1);
   zc* out = blk + d.off_blk + (size_t)BLK_STRIDE * i;

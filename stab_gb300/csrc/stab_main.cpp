@@ -153,7 +153,9 @@ static int run_sweep(const stab_params& base, const stab_sweep& sw, int device) 
     }
     char name[64];
     stab_eig_name(k + 1, name, sizeof(name));
-    rc = stab_write_evec(name, &q, eig[k].data(), want_vec ? vec.data() : nullptr);
+    stab_params qw = q;
+    if (qw.itype == 2 && qw.curve == 2 && qw.x != -1.0) qw.x = 0.0;   // circh.f90:60
+    rc = stab_write_evec(name, &qw, eig[k].data(), want_vec ? vec.data() : nullptr);
     if (rc) return fail("stab_write_evec", rc, ctx);
     if (q.itype == 1)
       std::printf("%4d  alpha = (%.6e, %.6e)  beta = (%.6e, %.6e)  least-stable omega = (%.15e, %.15e)  status %d  "
@@ -210,6 +212,7 @@ int main(int argc, char** argv) {
     rc = stab_eigenvectors(ctx, &p, nym, prof.data(), (int32_t)m, eig.data(), vec.data(), st.data());
     if (rc) return fail("stab_eigenvectors", rc, ctx);
   }
+  if (p.itype == 2 && p.curve == 2 && p.x != -1.0) p.x = 0.0;   // circh zeroes the module's x (circh.f90:60)
   rc = stab_write_evec(out.c_str(), &p, eig.data(), want_vec ? vec.data() : nullptr);
   if (rc) return fail("stab_write_evec", rc, ctx);
   if (least >= 0)

@@ -65,3 +65,4 @@ def test_settings_reject_null_context(lib):
     assert lib.stab_set_arithmetic(None, sg.STAGE_SEED_EIG, sg.ARITH_FP64) != 0
     assert lib.stab_set_seed_size(None, 32) != 0
     assert lib.stab_set_profiling(None, 1) != 0
+

@@ -320,3 +320,75 @@ def test_external_derivatives_ider0_match_oracle(ctx, itype):
     assert np.max(np.abs(H.phase_normalize(vec) - H.phase_normalize(es.evec[:, jo]))) < VEC_ABS
     e1, _, l1, _ = ctx.full_spectrum(H.stab_params(d), prof, want_vector=False)
     assert abs(e1[l1] - eig[li]) / abs(eig[li]) < 1e-6
+
+
+def test_assemble_curved_wall_matches_oracle(ctx):
+    """curve = 2 (the circle of circh.f90, radius x): C0, C1, C2 within
+    1e-12 of the oracle's largest entry, on the CFtest case at N = 24 and
+    with a small radius where the metric departs far from 1."""
+    for name, x in (("cftest_spatial_n64", 500.0), ("fsctest_spatial_n64", 2.0)):
+        c = dict(H.cases()[name], ny=24, x=x)
+        prof = H.case_profile(c)
+        mats = ctx.assemble(H.stab_params(c), prof)
+        p = H.oracle_params(c)
+        ms = so.mean_state(p, prof[:, 0], np.where(np.arange(5) == 2, 0.0, prof[:, 1:6]))
+        for a, b in zip(mats, so.spatial_operators(p, ms)):
+            assert _mat_close(a, b) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["cftest_spatial_n64", "cftest_spatial_n96", "fsctest_spatial_n64"])
+def test_curved_wall_golden_eigenvalues(ctx, name):
+    """The curved-wall golden cases (CFtest, FSCtest; curve = 2): the polish
+    from the reference's eigenvalue lands on it within 1e-9 relative (the
+    reference platforms' band) and on the oracle's within 1e-10."""
+    c = H.cases()[name]
+    prof = H.case_profile(c)
+    g = complex(*c["golden"])
+    eig, err, iters, status, vecs = ctx.solve_batch([H.stab_params(c)], [prof], sg.MODE_SEEDED, seeds=[g],
+                                                    want_vectors=True)
+    assert status[0] == sg.ST_OK, (status, err, iters)
+    es = H.oracle_solve(c, prof, want_vectors=False)
+    jo = so.getevec_select(es.eig, g)
+    assert abs(eig[0] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    assert abs(eig[0] - g) / abs(g) < 1e-9
+    if "eigfunction_rows" in c:
+        # space.ref rows (wall first or free stream first), matched by y
+        ny = c["ny"]
+        ref = np.loadtxt(H.GOLDEN + "/" + c["eigfunction_rows"], comments="#")
+        rows = H.eigfunction_rows(vecs[0], ny, es.ms.y)
+        order = [int(np.argmin(np.abs(rows[:, 0] - yr))) for yr in ref[:, 0]]
+        assert len(set(order)) == ny
+        got = rows[order][:, 1::2] + 1j * rows[order][:, 2::2]
+        want = ref[:, 1::2] + 1j * ref[:, 2::2]
+        kg = np.unravel_index(np.argmax(np.abs(got)), got.shape)
+        kw = np.unravel_index(np.argmax(np.abs(want)), want.shape)
+        assert kg == kw
+        assert np.max(np.abs(got / got[kg] - want / want[kw])) < NDIFF_ABS
+
+
+def test_curved_wall_full_spectrum_fsctest(ctx):
+    """FSCtest at N = 64 (companion order 640, curve = 2): the full FP64
+    spectrum holds the reference's eigenvalue within 1e-9 and the oracle's
+    within 1e-10."""
+    c = H.cases()["fsctest_spatial_n64"]
+    prof = H.case_profile(c)
+    eig, vec, li, st = ctx.full_spectrum(H.stab_params(c), prof, want_vector=False)
+    g = complex(*c["golden"])
+    j = so.getevec_select(eig, g)
+    es = H.oracle_solve(c, prof, want_vectors=False)
+    jo = so.getevec_select(es.eig, g)
+    assert abs(eig[j] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    assert abs(eig[j] - g) / abs(g) < 1e-9
+
+
+def test_curve1_and_unknown_curves_are_rejected(ctx):
+    """curve = 1 (calch: a parabola located with a root finder the reference
+    does not ship) and curve values outside 0..2 are refused with
+    STAB_ERR_ARG before any device work; the context stays usable."""
+    c = dict(H.cases()["cftest_spatial_n64"], ny=16)
+    prof = H.case_profile(c)
+    for curve in (1, 3):
+        with pytest.raises(sg.StabError):
+            ctx.full_spectrum(H.stab_params(dict(c, curve=curve)), prof, want_vector=False)
+    eig, _, _, st = ctx.full_spectrum(H.stab_params(c), prof, want_vector=False)
+    assert eig.size == 160

@@ -89,10 +89,13 @@ typedef struct stab_params {
     int32_t top;      /* spatial free-stream BC: 0 rho=0, 1 continuity       */
     int32_t wall;     /* carried through to evec.dat                         */
     int32_t wallt;    /* 0 isothermal, 2 adiabatic wall                      */
-    int32_t curve;    /* spatial only: 0 flat; 2 wall on a circle of radius *
-                       * x (circh.f90; x = -1 keeps the wall flat, and the *
-                       * x written to evec.dat is 0, as circh leaves it);  *
-                       * 1 (calch's parabola) is rejected with STAB_ERR_ARG */
+    int32_t curve;    /* spatial only: 0 flat; 1 parabolic cylinder       *
+                       * y = sqrt(2x) at arc length x from its nose       *
+                       * (calch.f90; STAB_ERR_ARG where its false-position *
+                       * search stops without a root, e.g. x in (.02,.9)); *
+                       * 2 circle of radius x (circh.f90; the x written to *
+                       * evec.dat is 0, as circh leaves it); x = -1 keeps  *
+                       * the wall flat in both                             */
     int32_t itype;    /* 1 temporal, 2 spatial                               */
     int32_t ind;      /* profile index (profile.<ind>)                       */
     double T0, Ma, Re, Pr, yi, ymax, x;

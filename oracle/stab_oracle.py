@@ -649,6 +649,106 @@ def circh_scalars(s: float):
     return dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2
 
 
+def parabola_arc(x1: float, x2: float) -> float:
+    """Arc length of the parabolic cylinder y = sqrt(2 x) from x1 to x2
+    (calch.f90, function arc)."""
+    def f(x):
+        xi = math.sqrt(x)
+        t = math.sqrt(1.0 + 2.0 * xi ** 2)
+        return math.sqrt(2.0) * 0.5 * xi * t + 0.5 * math.log(math.sqrt(2.0) * xi + t)
+    return f(x2) - f(x1)
+
+
+def false_position(func, x1: float, x2: float, xacc: float, maxit: int = 30) -> float:
+    """Root of func in [x1, x2] by the method of false position as published
+    in Numerical Recipes (Press, Teukolsky, Vetterling, Flannery, 2nd ed.
+    1992, section 9.2, routine rtflsp), which calch.f90's xloc calls and the
+    reference does not ship: keep the endpoint with func < 0 and the one with
+    func >= 0, replace the one on the side of the secant root, stop when the
+    replaced endpoint moved less than xacc or func is exactly zero, and give
+    up after maxit (30) secant steps.  Raises ValueError where that routine
+    stops the program (no bracket, no convergence)."""
+    fl, fh = func(x1), func(x2)
+    if fl * fh > 0.0:
+        raise ValueError("false position: root not bracketed")
+    if fl < 0.0:
+        lo, hi = x1, x2
+    else:
+        lo, hi = x2, x1
+        fl, fh = fh, fl
+    for _ in range(maxit):
+        if fl == fh:
+            raise ValueError("false position: flat secant")
+        x = lo + (hi - lo) * fl / (fl - fh)
+        f = func(x)
+        if f < 0.0:
+            moved = lo - x
+            lo, fl = x, f
+        else:
+            moved = hi - x
+            hi, fh = x, f
+        if abs(moved) < xacc or f == 0.0:
+            return x
+    raise ValueError("false position: no convergence in %d steps" % maxit)
+
+
+def calch_scalars(s: float):
+    """The station-independent part of calch (calch.f90:31-148): the wall of
+    the parabolic cylinder y = sqrt(2 x), at the point whose arc length from
+    the nose is s (the caller's x), located by xloc (calch.f90:170-184) with
+    false position on [0, 2 s] to 1e-12.  Returns the same eight scalars as
+    circh_scalars; circh_metrics (the same closing formulas, calch.f90:
+    152-167) forms h and its derivatives from them."""
+    xl = false_position(lambda x: s - parabola_arc(0.0, x), 0.0, 0.0 + 2.0 * s, 1.0e-12)
+    yl = math.sqrt(2.0 * xl)
+    th = math.atan2(1.0, yl)
+    bn1 = -math.sin(th)
+    bn2 = math.cos(th)
+    dydx = INFTY if xl == 0.0 else 1.0 / math.sqrt(2.0 * xl)
+    dxbds = 1.0 / math.sqrt(1.0 + dydx ** 2)
+    dxdy = 0.0 if xl == 0.0 else math.sqrt(2.0 * xl)
+    dybds = 1.0 / math.sqrt(dxdy ** 2 + 1.0)
+    if xl == 0.0:
+        dx, dy = 0.0, 1.0
+        ddxdx, ddydx, ddxdy, ddydy = INFTY, 0.0, 1.0, 0.0
+        d2dxdx2 = INFTY
+    else:
+        dx, dy = yl, 1.0
+        ddxdx, ddydx, ddxdy, ddydy = 1.0 / yl, 0.0, 1.0, 0.0
+        d2dxdx2 = -math.sqrt(2.0) / (2.0 ** 2 * xl ** 1.5)
+    d2dydx2 = d2dxdy2 = d2dydy2 = 0.0
+    q = dx ** 2 + dy ** 2
+    if abs(bn1) > abs(bn2):
+        dbn1 = (-ddydy / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * dybds
+        dbn2 = (ddxdy / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * dybds
+        d2xdy2 = 1.0
+        d2ybds2 = -(1.0 + dxdy ** 2) ** (-1.5) * dxdy * d2xdy2 * dybds
+        d2xbds2 = d2xdy2 * dybds ** 2 + dxdy * d2ybds2
+        t1 = dy * ddxdy - dx * ddydy
+        t2 = dx * ddxdy + dy * ddydy
+        d2bn1 = (((ddxdy * t1 + dx * (dy * d2dxdy2 - dx * d2dydy2)) / q ** 1.5
+                  - (3.0 * dx * t1 * t2) / q ** 2.5) * dybds ** 2
+                 + (-ddydy / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * d2ybds2)
+        d2bn2 = (((ddydy * t1 + dy * (dy * d2dxdy2 - dx * d2dydy2)) / q ** 1.5
+                  - (3.0 * dy * t1 * t2) / q ** 2.5) * dybds ** 2
+                 + (ddxdy / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q ** 1.5) * d2ybds2)
+    else:
+        dbn1 = (-ddydx / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * dxbds
+        dbn2 = (ddxdx / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * dxbds
+        d2ydx2 = -1.0 / (2.0 * math.sqrt(2.0) * xl ** 1.5)
+        d2xbds2 = -(1.0 + dydx ** 2) ** (-1.5) * dydx * d2ydx2 * dxbds
+        d2ybds2 = d2ydx2 * dxbds ** 2 + dydx * d2xbds2
+        t1 = dy * ddxdx - dx * ddydx
+        t2 = dx * ddxdx + dy * ddydx
+        d2bn1 = (((ddxdx * t1 + dx * (dy * d2dxdx2 - dx * d2dydx2)) / q ** 1.5
+                  - (3.0 * dx * t1 * t2) / q ** 2.5) * dxbds ** 2
+                 + (-ddydx / q ** 0.5 + 0.5 * dy * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * d2xbds2)
+        d2bn2 = (((ddydx * t1 + dy * (dy * d2dxdx2 - dx * d2dydx2)) / q ** 1.5
+                  - (3.0 * dy * t1 * t2) / q ** 2.5) * dxbds ** 2
+                 + (ddxdx / q ** 0.5 - 0.5 * dx * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q ** 1.5) * d2xbds2)
+    return dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2
+
+
 def circh_metrics(sc, r):
     """h, dh/ds, dh/dr, d2h/dsdr, d2h/dr2 at distances r from the wall
     (circh.f90:190-199) from the scalars of circh_scalars."""
@@ -667,18 +767,21 @@ def circh_metrics(sc, r):
 
 
 def wall_metrics(p: StabParams, y):
-    """The wall metrics of spatial.f90:110-125: curve = 2 a circle of radius
-    x (circh), curve = 0 a flat wall (h = 1).  curve = 1 (calch, a parabola
-    located with Numerical Recipes' rtflsp, which the reference does not
-    ship) is not restated."""
+    """The wall metrics of spatial.f90:110-125: curve = 1 the parabolic
+    cylinder of calch at arc length x from its nose, curve = 2 a circle of
+    radius x (circh), curve = 0 a flat wall (h = 1).  x = -1 turns the
+    curvature off in both (calch.f90:31-39, circh.f90:46-53)."""
     ny = len(y)
-    if p.curve == 0:
-        return np.ones(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny)
+    flat = (np.ones(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny))
+    if p.curve == 0 or (p.curve in (1, 2) and p.x == -1.0):
+        return flat
+    if p.curve == 1:
+        if not p.x > 0.0:
+            raise ValueError("curve = 1 needs an arc length x > 0 (or -1)")
+        return circh_metrics(calch_scalars(p.x), y)
     if p.curve == 2:
-        if p.x == -1.0:   # circh.f90:46-53: curvature turned off
-            return np.ones(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny), np.zeros(ny)
         return circh_metrics(circh_scalars(p.x), y)
-    raise ValueError("curve = 1 (calch) needs Numerical Recipes' rtflsp, absent from the reference")
+    raise ValueError("curve must be 0, 1 or 2")
 
 
 def spatial_blocks_curved(p: StabParams, ms: MeanState, met):

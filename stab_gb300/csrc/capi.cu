@@ -340,16 +340,115 @@ static void circh_scalars(double s, double out[8]) {
   for (int i = 0; i < 8; ++i) out[i] = v[i];
 }
 
+// Arc length of the parabolic cylinder y = sqrt(2 x) from x1 to x2
+// (calch.f90, function arc).
+static double parabola_arc(double x1, double x2) {
+  auto f = [](double x) {
+    const double xi = std::sqrt(x), t = std::sqrt(1.0 + 2.0 * xi * xi);
+    return std::sqrt(2.0) * 0.5 * xi * t + 0.5 * std::log(std::sqrt(2.0) * xi + t);
+  };
+  return f(x2) - f(x1);
+}
+
+// The method of false position as published in Numerical Recipes (Press,
+// Teukolsky, Vetterling, Flannery, 2nd ed. 1992, section 9.2, routine
+// rtflsp), which calch.f90's xloc calls and the reference does not ship:
+// the endpoints with f < 0 and f >= 0 are kept, the one on the side of the
+// secant root is replaced, and the search ends when the replaced endpoint
+// moved less than xacc or f is exactly zero; 30 secant steps at most.
+// Returns false where that routine stops the program (no bracket, no
+// convergence).
+template <class F>
+static bool false_position(F f, double x1, double x2, double xacc, double& root) {
+  double fl = f(x1), fh = f(x2);
+  if (fl * fh > 0.0) return false;
+  double lo = x1, hi = x2;
+  if (!(fl < 0.0)) {
+    std::swap(lo, hi);
+    std::swap(fl, fh);
+  }
+  for (int it = 0; it < 30; ++it) {
+    if (fl == fh) return false;
+    const double x = lo + (hi - lo) * fl / (fl - fh);
+    const double fx = f(x);
+    double moved;
+    if (fx < 0.0) {
+      moved = lo - x;
+      lo = x;
+      fl = fx;
+    } else {
+      moved = hi - x;
+      hi = x;
+      fh = fx;
+    }
+    if (std::fabs(moved) < xacc || fx == 0.0) {
+      root = x;
+      return true;
+    }
+  }
+  return false;
+}
+
+// The station-independent scalars of calch (calch.f90:31-148): the wall of
+// the parabolic cylinder y = sqrt(2 x) at arc length s from its nose, the
+// point located by xloc (calch.f90:170-184): false position on [0, 2 s] to
+// 1e-12.  Same outputs as circh_scalars; h(y) and its derivatives follow in
+// k_blocks with the closing formulas both routines share (calch.f90:152-167).
+static bool calch_scalars(double s, double out[8]) {
+  const double infty = 1.0e30;
+  double xl = 0.0;
+  if (!false_position([s](double x) { return s - parabola_arc(0.0, x); }, 0.0, 0.0 + 2.0 * s, 1.0e-12, xl))
+    return false;
+  const double yl = std::sqrt(2.0 * xl);
+  const double th = std::atan2(1.0, yl);
+  const double bn1 = -std::sin(th), bn2 = std::cos(th);
+  const double dydx = (xl == 0.0) ? infty : 1.0 / std::sqrt(2.0 * xl);
+  const double dxbds = 1.0 / std::sqrt(1.0 + dydx * dydx);
+  const double dxdy = (xl == 0.0) ? 0.0 : std::sqrt(2.0 * xl);
+  const double dybds = 1.0 / std::sqrt(dxdy * dxdy + 1.0);
+  const double dx = (xl == 0.0) ? 0.0 : yl, dy = 1.0;
+  const double ddxdx = (xl == 0.0) ? infty : 1.0 / yl, ddydx = 0.0, ddxdy = 1.0, ddydy = 0.0;
+  const double d2dxdx2 = (xl == 0.0) ? infty : -std::sqrt(2.0) / (4.0 * std::pow(xl, 1.5));
+  const double d2dydx2 = 0.0, d2dxdy2 = 0.0, d2dydy2 = 0.0;
+  const double q = dx * dx + dy * dy, q05 = std::sqrt(q), q15 = std::pow(q, 1.5), q25 = std::pow(q, 2.5);
+  double dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2;
+  if (std::fabs(bn1) > std::fabs(bn2)) {   // the wall leans toward the y axis: derivatives through y
+    dbn1 = (-ddydy / q05 + 0.5 * dy * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q15) * dybds;
+    dbn2 = (ddxdy / q05 - 0.5 * dx * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q15) * dybds;
+    const double d2xdy2 = 1.0;
+    d2ybds2 = -std::pow(1.0 + dxdy * dxdy, -1.5) * dxdy * d2xdy2 * dybds;
+    d2xbds2 = d2xdy2 * (dybds * dybds) + dxdy * d2ybds2;
+    const double t1 = dy * ddxdy - dx * ddydy, t2 = dx * ddxdy + dy * ddydy;
+    d2bn1 = ((ddxdy * t1 + dx * (dy * d2dxdy2 - dx * d2dydy2)) / q15 - (3.0 * dx * t1 * t2) / q25) * (dybds * dybds) +
+            (-ddydy / q05 + 0.5 * dy * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q15) * d2ybds2;
+    d2bn2 = ((ddydy * t1 + dy * (dy * d2dxdy2 - dx * d2dydy2)) / q15 - (3.0 * dy * t1 * t2) / q25) * (dybds * dybds) +
+            (ddxdy / q05 - 0.5 * dx * (2.0 * dx * ddxdy + 2.0 * dy * ddydy) / q15) * d2ybds2;
+  } else {                                  // through x
+    dbn1 = (-ddydx / q05 + 0.5 * dy * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q15) * dxbds;
+    dbn2 = (ddxdx / q05 - 0.5 * dx * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q15) * dxbds;
+    const double d2ydx2 = -1.0 / (2.0 * std::sqrt(2.0) * std::pow(xl, 1.5));
+    d2xbds2 = -std::pow(1.0 + dydx * dydx, -1.5) * dydx * d2ydx2 * dxbds;
+    d2ybds2 = d2ydx2 * (dxbds * dxbds) + dydx * d2xbds2;
+    const double t1 = dy * ddxdx - dx * ddydx, t2 = dx * ddxdx + dy * ddydx;
+    d2bn1 = ((ddxdx * t1 + dx * (dy * d2dxdx2 - dx * d2dydx2)) / q15 - (3.0 * dx * t1 * t2) / q25) * (dxbds * dxbds) +
+            (-ddydx / q05 + 0.5 * dy * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q15) * d2xbds2;
+    d2bn2 = ((ddydx * t1 + dy * (dy * d2dxdx2 - dx * d2dydx2)) / q15 - (3.0 * dy * t1 * t2) / q25) * (dxbds * dxbds) +
+            (ddxdx / q05 - 0.5 * dx * (2.0 * dx * ddxdx + 2.0 * dy * ddydx) / q15) * d2xbds2;
+  }
+  const double v[8] = {dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1, d2bn2};
+  for (int i = 0; i < 8; ++i) out[i] = v[i];
+  return true;
+}
+
 // Descriptor of one instance from its run parameters (validated) and the
 // entry of its mean profile in the profile pools.
 static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDesc& pd, InstDesc& d) {
   if (q.itype != 1 && q.itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal) or 2 (spatial)");
   if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
-  if (q.itype == 2 && q.curve == 1)
-    return set_err(c, STAB_ERR_ARG, "curve = 1 (calch: a parabola located with Numerical Recipes' rtflsp, which the "
-                                    "reference does not ship) is not supported; curve = 2 (circle) is");
   if (q.itype == 2 && q.curve != 0 && q.curve != 1 && q.curve != 2)
     return set_err(c, STAB_ERR_ARG, "curve must be 0, 1 or 2");
+  if (q.itype == 2 && q.curve == 1 && q.x != -1.0 && !(q.x > 0.0))
+    return set_err(c, STAB_ERR_ARG, "curve = 1 needs an arc length x > 0 (or -1, no curvature)");
   if (q.ider != 0 && q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider must be 0 or 1");
   if (q.wallt != 0 && q.wallt != 2) return set_err(c, STAB_ERR_ARG, "Illegal value of wallt");
   if (q.yi == 0.0) return set_err(c, STAB_ERR_ARG, "Yi = 0 (tanh map) is not supported");
@@ -378,10 +477,13 @@ static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDes
   d.off_prof = pd.off_prof;
   d.off_spl = pd.off_spl;
   d.ider = q.ider;
-  // spatial.f90:110-125: the temporal solver has no wall metric; circh with
-  // x = -1 turns curvature off (circh.f90:46-53)
-  d.curved = (q.itype == 2 && q.curve == 2 && q.x != -1.0) ? 1 : 0;
-  if (d.curved) circh_scalars(q.x, d.cw);
+  // spatial.f90:110-125: the temporal solver has no wall metric; x = -1
+  // turns curvature off (calch.f90:31-39, circh.f90:46-53)
+  d.curved = (q.itype == 2 && (q.curve == 1 || q.curve == 2) && q.x != -1.0) ? 1 : 0;
+  if (d.curved && q.curve == 2) circh_scalars(q.x, d.cw);
+  if (d.curved && q.curve == 1 && !calch_scalars(q.x, d.cw))
+    return set_err(c, STAB_ERR_ARG, "curve = 1: false position found no wall point in 30 steps (the reference's "
+                                    "xloc stops there too)");
   return 0;
 }
 

@@ -381,14 +381,36 @@ def test_curved_wall_full_spectrum_fsctest(ctx):
     assert abs(eig[j] - g) / abs(g) < 1e-9
 
 
-def test_curve1_and_unknown_curves_are_rejected(ctx):
-    """curve = 1 (calch: a parabola located with a root finder the reference
-    does not ship) and curve values outside 0..2 are refused with
+def test_curve1_parabola_matches_oracle(ctx):
+    """curve = 1 (calch.f90, the parabolic cylinder y = sqrt(2x) at arc
+    length x from its nose): operators within 1e-12 of the oracle's largest
+    entry and the least-stable eigenvalue within 1e-10, eigenvector within
+    1e-8, near the nose (x = 2, strong curvature) and downstream (x = 50).
+    Unpinned by the reference: its tests hold no curve = 1 case."""
+    for x in (2.0, 50.0):
+        c, prof = H.synth_case(2, 32, 0.8, 2000.0, w=0.05, b=0.1, crossflow=True)
+        c.update(curve=1, x=x)
+        mats = ctx.assemble(H.stab_params(c), prof)
+        p = H.oracle_params(c)
+        ms = so.mean_state(p, prof[:, 0], np.where(np.arange(5) == 2, 0.0, prof[:, 1:6]))
+        for a, b in zip(mats, so.spatial_operators(p, ms)):
+            assert _mat_close(a, b) < 1e-12
+        eig, vec, li, st = ctx.full_spectrum(H.stab_params(c), prof, want_vector=True)
+        es = H.oracle_solve(c, prof)
+        jo = H.select_least(es.eig, c)
+        assert st == sg.ST_OK and li >= 0 and jo >= 0
+        assert abs(eig[li] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+        assert np.max(np.abs(H.phase_normalize(vec) - H.phase_normalize(es.evec[:, jo]))) < VEC_ABS
+
+
+def test_bad_curves_are_rejected(ctx):
+    """curve values outside 0..2, and curve = 1 where false position finds
+    no wall point in 30 steps (x = 0.5) or x <= 0, are refused with
     STAB_ERR_ARG before any device work; the context stays usable."""
     c = dict(H.cases()["cftest_spatial_n64"], ny=16)
     prof = H.case_profile(c)
-    for curve in (1, 3):
+    for curve, x in ((3, 500.0), (1, 0.5), (1, 0.0), (1, -2.0)):
         with pytest.raises(sg.StabError):
-            ctx.full_spectrum(H.stab_params(dict(c, curve=curve)), prof, want_vector=False)
+            ctx.full_spectrum(H.stab_params(dict(c, curve=curve, x=x)), prof, want_vector=False)
     eig, _, _, st = ctx.full_spectrum(H.stab_params(c), prof, want_vector=False)
     assert eig.size == 160

@@ -97,3 +97,38 @@ def test_oracle_curved_wall_matches_reference(name):
         kw = np.unravel_index(np.argmax(np.abs(want)), want.shape)
         assert kg == kw
         assert np.max(np.abs(got / got[kg] - want / want[kw])) < NDIFF_ABS
+
+
+def test_oracle_calch_scalars_follow_the_parabola():
+    """curve = 1 (calch.f90): the eight wall scalars against central
+    differences of the geometry itself, the wall point located to full
+    precision by bisection on the arc length (independent of the
+    false-position search calch uses).  Agreement to 1e-5 relative (the
+    difference step's error); x = 0.5 is where calch's search gives up."""
+    import math
+
+    def wall(s):
+        lo, hi = 0.0, 2.0 * s + 1.0
+        for _ in range(200):
+            mid = 0.5 * (lo + hi)
+            if so.parabola_arc(0.0, mid) < s:
+                lo = mid
+            else:
+                hi = mid
+        x = 0.5 * (lo + hi)
+        th = math.atan2(1.0, math.sqrt(2.0 * x))
+        return np.array([x, math.sqrt(2.0 * x), -math.sin(th), math.cos(th)])
+
+    for s in (1.0, 2.0, 5.0, 50.0):
+        h = 1e-3 * max(1.0, s)
+        a, c, b = wall(s - h), wall(s), wall(s + h)
+        d1 = (b - a) / (2 * h)
+        d2 = (b - 2 * c + a) / h ** 2
+        sc = so.calch_scalars(s)
+        want = [d1[0], d1[1], d1[2], d1[3], d2[0], d2[1], d2[2], d2[3]]
+        for got, w in zip(sc, want):
+            assert abs(got - w) <= 1e-5 * max(abs(w), 1e-3), (s, sc, want)
+    with pytest.raises(ValueError):
+        so.calch_scalars(0.5)
+    p = so.StabParams(curve=1, x=-1.0, itype=2, ny=8)
+    assert np.array_equal(so.wall_metrics(p, np.linspace(0, 1, 8))[0], np.ones(8))

@@ -544,6 +544,10 @@ def main():
             "seed_qr_shared_memory_ms": variant_ms(lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 1),
                                                    lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 0)),
         }
+        # batch eigensolver with k instances in flight per SM (default: the occupancy's four)
+        for k in (1, 2, 3):
+            variants["eig_resident_%d_per_sm_ms" % k] = variant_ms(
+                lambda k=k: ctx.set_option(sg.OPT_EIG_RESIDENT, k), lambda: ctx.set_option(sg.OPT_EIG_RESIDENT, 0))
 
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None
     single = single_instance_leg(ctx, stream, cpu=args.cpu_sample > 0) if rank == 0 else None

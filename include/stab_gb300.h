@@ -51,7 +51,11 @@ extern "C" {
 
 /* solve modes for stab_batch_run / stab_solve_batch */
 #define STAB_MODE_PLAIN 0     /* FP64 full spectrum + least-stable eigenvector   */
-#define STAB_MODE_SEEDED 1    /* mixed-precision polish from caller seeds        */
+#define STAB_MODE_SEEDED 1    /* mixed-precision polish from caller seeds; where *
+                               * complex64 factors do not converge, complex128   *
+                               * inverse iteration at the seed; where that fails *
+                               * too, the FP64 spectrum's least-stable mode      *
+                               * (STAB_ST_FELLBACK)                              */
 #define STAB_MODE_COARSE 2    /* seeds from a full spectrum at N = 32, then the  *
                                * mixed-precision polish.  STAB_ST_OK only where  *
                                * the seed spectrum's most unstable candidate     *
@@ -66,9 +70,10 @@ extern "C" {
                                * seed spectrum misplaces below its top candidate *
                                * can still be missed: the check costs no fine    *
                                * spectrum, so it cannot rule that out            */
-#define STAB_MODE_TRACK 4     /* polish from caller guesses; where it fails, the *
-                               * FP64 spectrum's eigenvalue nearest the guess    *
-                               * (the pick of getab.f90:185-192)                 */
+#define STAB_MODE_TRACK 4     /* polish from caller guesses (complex64, then     *
+                               * complex128 inverse iteration); where both fail, *
+                               * the FP64 spectrum's eigenvalue nearest the      *
+                               * guess (the pick of getab.f90:185-192)           */
 #define STAB_MODE_SURROGATE 3 /* STAB_MODE_COARSE plus the caller's predicted    *
                                * seed (and start vector, stab_batch_set_start)   *
                                * as one more candidate round                     */
@@ -173,6 +178,13 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     take the other form); 0: the epilogue reads and writes the tile from
  *     the registers.  Same arithmetic either way. */
 #define STAB_OPT_POLISH_LU_TMA 2
+/*   STAB_OPT_EIG_RESIDENT  k >= 1: the batch eigensolver (seed and plain
+ *     spectra of batches larger than half the SM count) keeps at most k
+ *     instances in flight per SM, so that their working matrices can stay
+ *     in L2 (each CTA takes the next instance from a work counter when it
+ *     finishes one); 0 (default): as many as the occupancy allows (four).
+ *     Bit-identical eigenvalues for every value. */
+#define STAB_OPT_EIG_RESIDENT 3
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,

@@ -32,7 +32,7 @@ MODE_PLAIN, MODE_SEEDED, MODE_COARSE, MODE_SURROGATE, MODE_TRACK = 0, 1, 2, 3, 4
 # arithmetic per stage (stab_set_arithmetic)
 STAGE_SEED_EIG, STAGE_PLAIN_EIG, STAGE_RETRY_LU, STAGE_POLISH_LU = 0, 1, 2, 3
 ARITH_FP64, ARITH_DOUBLE_WORD, ARITH_FP32, ARITH_TF32_SPLIT = 0, 1, 2, 3
-OPT_SEED_QR_SHARED, OPT_POLISH_LU_TMA = 1, 2
+OPT_SEED_QR_SHARED, OPT_POLISH_LU_TMA, OPT_EIG_RESIDENT = 1, 2, 3
 ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE, ST_UNVERIFIED = 0, 1, 2, 3, 4, 5, 6
 
 EXPORTED = (
@@ -423,7 +423,8 @@ class Context:
         return md.value, pd.value
 
     def set_option(self, option: int, value: int) -> None:
-        """stab_set_option: OPT_SEED_QR_SHARED (0 default, 1 on), OPT_POLISH_LU_TMA (1 default, 0 off)."""
+        """stab_set_option: OPT_SEED_QR_SHARED (0 default, 1 on), OPT_POLISH_LU_TMA (1 default, 0 off),
+        OPT_EIG_RESIDENT (0 default: occupancy; k: k instances per SM)."""
         self._check(self.lib.stab_set_option(self.h, int(option), int(value)))
 
     def lu_tc_check(self, n: int, count: int):

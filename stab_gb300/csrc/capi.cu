@@ -71,6 +71,7 @@ struct stab_ctx {
   int seed_ny = 32;        // N of the seed spectrum of STAB_MODE_COARSE / SURROGATE
   int seed_qr_shared = 0;  // STAB_OPT_SEED_QR_SHARED
   int lu_tma = 1;          // STAB_OPT_POLISH_LU_TMA
+  int eig_resident = 0;    // STAB_OPT_EIG_RESIDENT
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -908,7 +909,13 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
     }));
   }
   CK(c, timed(c, eig_name, [&] {
-    int grid = 0;   // sized by occupancy in the launcher
+    int grid = 0;   // sized by occupancy in the launcher, or capped per SM
+    if (c->eig_resident > 0) {
+      int dev = 0, sms = 1;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      grid = sms * c->eig_resident;
+    }
     return launch_eig_plain(b->count, b->mmax, b->msz.as<int32_t>(), b->Abig.as<zc>(), b->off_m2.as<int64_t>(),
                             b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
                             b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
@@ -1451,6 +1458,33 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
   return 0;
 }
 
+// Seeded modes: the instances whose complex64 Newton-chord did not converge
+// (operators whose scales complex64 factors do not resolve, such as the
+// 1/(gamma M^2) pressure terms at M = 0.001) take the complex128 inverse
+// iteration at their seed before the full-spectrum fallback.
+static int retry_seeded(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const int n = b->count;
+  std::vector<int32_t> dn(n);
+  CK(c, cudaMemcpyAsync(dn.data(), b->done.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  CK(c, cudaStreamSynchronize(s));
+  if (std::all_of(dn.begin(), dn.end(), [](int32_t d) { return d == 1; })) return 0;
+  CK(c, b->skip64.ensure(sizeof(int32_t) * n, s));
+  int32_t* mask = b->skip64.as<int32_t>();
+  CK(c, timed(c, "k_converged_mask", [&] {
+    k_converged_mask<<<(n + 255) / 256, 256, 0, s>>>(n, b->done.as<int32_t>(), mask, 0);
+    return cudaGetLastError();
+  }));
+  int rc = run_polish64_ii(b, true, mask);
+  if (rc) return rc;
+  CK(c, timed(c, "k_converged_mask", [&] {
+    k_converged_mask<<<(n + 255) / 256, 256, 0, s>>>(n, b->done.as<int32_t>(), mask, 1);
+    return cudaGetLastError();
+  }));
+  return 0;
+}
+
 // Re-solve, with the plain FP64 path, every instance whose polish did not
 // converge (or had no accepted shift); results are kept on the host for
 // stab_batch_results.
@@ -1672,8 +1706,11 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
   }
   int rc = batch_run(b, mode);
   if (rc) return rc;
-  if (mode == STAB_MODE_SEEDED) return run_fallback(b);
-  if (mode == STAB_MODE_TRACK) return run_fallback(b, true);
+  if (mode == STAB_MODE_SEEDED || mode == STAB_MODE_TRACK) {
+    rc = retry_seeded(b);
+    if (rc) return rc;
+    return run_fallback(b, mode == STAB_MODE_TRACK);
+  }
   b->counts[0] = b->count;
   b->counts[1] = b->counts[2] = 0;
   return STAB_OK;
@@ -1933,6 +1970,12 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   }
   if (option == STAB_OPT_POLISH_LU_TMA) {
     c->lu_tma = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_EIG_RESIDENT) {
+    if (value < 0 || value > 64) return set_err(c, STAB_ERR_ARG, "resident instances per SM must be in [0, 64]");
+    c->eig_resident = value;
     c->epoch += 1;
     return STAB_OK;
   }

@@ -6,6 +6,7 @@
 //   k_take_candidate,  seed rounds of the coarse-shift mode
 //   k_fold_best,
 //   k_take_best
+//   k_converged_mask   complex128 retry of the seeded modes
 //   k_post_spectrum    alpha = 1/lambda with lambda = 0 -> 0
 //                      (spatial.f90:1065-1069), ascending stable sort on the
 //                      imaginary part (the PIKSR2 call, temporal.f90:844-855,
@@ -116,6 +117,16 @@ __global__ void k_post_spectrum(int count, const InstDesc* __restrict__ desc, co
       break;
     }
   }
+}
+
+// Retry bookkeeping of the seeded modes: mask[k] = (done[k] == 1) before the
+// complex128 inverse iteration, which marks the instances it skips done = 4;
+// with `restore` the converged instances get done = 1 back afterwards.
+__global__ void k_converged_mask(int count, int32_t* __restrict__ done, int32_t* __restrict__ mask, int restore) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  if (!restore) mask[k] = (done[k] == 1) ? 1 : 0;
+  else if (mask[k]) done[k] = 1;
 }
 
 // sigma[k] <- candidate j of instance k

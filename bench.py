@@ -43,8 +43,16 @@ METRIC = "converged least-stable modes/sec at |d omega|<=1e-10 (seeded+mixed vs 
 UNIT = "modes/s"
 TOL = 1e-10
 T0_SUTH = 110.4 / 0.3815
-FP64_PEAK_TFLOPS = 1.19   # FMA probe on a GB300 (profiles/fp64_fp32_peak_probe.md)
 HBM_FALLBACK_GBS = 6800.0  # used only when MEASURED_PEAKS.json is absent
+
+
+def bf16_peak():
+    """(TFLOP/s, source) of the cuBLAS bf16 burst measured on this machine, or None."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (measured)"
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 def hbm_peak():
@@ -54,7 +62,6 @@ def hbm_peak():
             return float(json.load(fh)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
     except (OSError, KeyError, ValueError):
         return HBM_FALLBACK_GBS, "fallback 6.8 TB/s"
-FP32_PEAK_TFLOPS = 69.9
 COARSE_TRAFFIC_PER_INSTANCE = (25.59e9 + 21.59e9) / 512
 # kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
 KERNEL_WORK = {
@@ -453,6 +460,9 @@ def main():
     batch = ctx.batch(sp, profiles)
     # LU panel widths for the orders of this workload and of the N = 32 seeds
     tune = ctx.autotune(sorted({5 * d["ny"] for d in params} | {160}))
+    # FP32 / FP64 / double-word multiply-add rates of this GPU, measured now:
+    # the denominators of the kernels bound by those pipes
+    peaks = ctx.peak_rates()
 
     # reference result: plain FP64 full spectrum on every instance; one
     # untimed pass (pool growth, first-use costs), then args.plain_reps timed
@@ -589,14 +599,17 @@ def main():
                                 "traffic": None, "kernel": kname, "launches": kl, "ms": kms, "algorithmic": note,
                                 "peak_source": hsrc}
             continue
-        # double-word kernels: a double-word multiply-add (2 flops) is 15 FP32
-        # instructions, so their flop peak is the FP32 instruction rate * 2 / 15
-        peak = {"fp64": FP64_PEAK_TFLOPS, "fp32": FP32_PEAK_TFLOPS, "dw": FP32_PEAK_TFLOPS / 15.0}[bound]
+        # pipe-bound kernels: the multiply-add rate of their arithmetic,
+        # measured in this run (stab_peak_rates)
+        peak = {"fp64": peaks["fp64"], "fp32": peaks["fp32"], "dw": peaks["double_word_complex"]}[bound]
         ach = work[wkey] / (kms / 1000.0) / 1e12    # flops and time of the same launches
         rooflines[kname] = {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                             "frac": ach / peak, "traffic": None, "kernel": kname, "launches": kl,
                             "ms": kms, "algorithmic": note,
-                            "peak_source": "FMA probe on a GB300 of the same kind (profiles/fp64_fp32_peak_probe.md)"}
+                            "peak_source": "measured in this run: independent multiply-add chains on every SM "
+                                           "(stab_peak_rates, %s)" % {"fp64": "FP64 FMA", "fp32": "FP32 FMA",
+                                                                     "dw": "double-word complex"}[bound],
+                            "frac_of_bf16_tensor_peak": ach / bf16_peak()[0] if bf16_peak() else None}
     if "k_eig_plain_coarse" in rooflines:
         # DRAM bytes per launch from the committed ncu capture of the same kernel
         # (profiles/k_eig_plain_coarse_n32_512.md: 47.18 GB for 512 instances),
@@ -636,6 +649,7 @@ def main():
                        "speedup_seeded_over_plain": value / (total / (plain_ms / 1000.0))},
         "roofline": roof,
         "kernel_rooflines": rooflines,
+        "pipe_peaks_tflops": peaks,
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in sorted(stats.items(),
                                                                                key=lambda kv: -kv[1][1])},
         "gpu_launches": int(launches_per_step * args.steps),

@@ -101,7 +101,11 @@ typedef struct stab_params {
                        * 2 circle of radius x (circh.f90; the x written to *
                        * evec.dat is 0, as circh leaves it); x = -1 keeps  *
                        * the wall flat in both                             */
-    int32_t itype;    /* 1 temporal, 2 spatial                               */
+    int32_t itype;    /* 1 temporal, 2 spatial, 3 temporal by finite         *
+                       * differences (fd_temporal.f90: fourth-order        *
+                       * stencils with Carpenter's closures on ogengrid's  *
+                       * uniform eta, wall first; needs ymax > 2 yi and    *
+                       * ny >= 10; evec.dat records itype 1)               */
     int32_t ind;      /* profile index (profile.<ind>)                       */
     double T0, Ma, Re, Pr, yi, ymax, x;
     double alpha[2];  /* temporal: streamwise wavenumber                     */
@@ -240,6 +244,16 @@ int stab_lu_cluster_check(stab_ctx* ctx, int32_t n, int32_t count, int32_t compl
  */
 int stab_lu_tc_check(stab_ctx* ctx, int32_t n, int32_t count, double* bwd_tc, double* bwd_simt, int32_t* piv_diff);
 
+/*
+ * Measured multiply-add throughput of this device, in TFLOP/s: out[0] FP32
+ * FMA, out[1] FP64 FMA (2 flops each), out[2] double-word complex
+ * multiply-add (8 flops each, the unit of stab_batch_work and the kernels'
+ * flop counts).  Independent chains on every SM, timed with CUDA events
+ * after a warm-up launch: the roofline denominators of the kernels bound by
+ * these pipes.  No reference counterpart.
+ */
+int stab_peak_rates(stab_ctx* ctx, double* out);
+
 /* ---- full spectrum (plain FP64 path) --------------------------------- */
 /*
  * All eigenvalues of one instance, sorted ascending by imaginary part with
@@ -338,6 +352,9 @@ int stab_sweep_points(const stab_params* base, const stab_sweep* sw, int32_t nbo
 int stab_read_profile(const char* path, int32_t cap_rows, double* rows, int32_t* nym);
 /* Collocation grid y, eta, d eta/dy, d2 eta/dy2 (sgengrid.f90:18-45). */
 int stab_grid(int32_t ny, double yi, double ymax, double* y, double* eta, double* deta, double* d2eta);
+/* Grid of the finite-difference solver (ogengrid.f90:20-44): uniform eta on
+ * [0, 1] from the wall, y = a eta / (b - eta); needs ymax > 2 yi. */
+int stab_fd_grid(int32_t ny, double yi, double ymax, double* y, double* eta, double* deta, double* d2eta);
 /*
  * Write evec.dat as gfortran writes it (temporal.f90:883-890,
  * spatial.f90:1120-1126): sequential unformatted records with 4-byte

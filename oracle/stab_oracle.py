@@ -1356,6 +1356,184 @@ def piksr2_order(keys: np.ndarray) -> np.ndarray:
     return np.argsort(keys, kind="stable")
 
 
+# ---------------------------------------------------------------------------
+# finite-difference temporal solver (fd_temporal.f90, itype = 3)
+# ---------------------------------------------------------------------------
+# stencils.f90:9-120, the reference's coefficient table (values as written there)
+FD_GA = (8.333333333333333333333E-02, -6.666666666666666666667E-01, 6.666666666666666666667E-01,
+         -8.333333333333333333333E-02)
+FD_GG = (-1.87603205562073772290017534999, 3.18538322557789286703668141674, -1.81454567943752757247830550034,
+         0.59165824105260274421658150053, -0.101052068000505624644095417028, 0.0145883364282753087693133500917)
+FD_GH = (-0.384254232677925402043233692192, -0.290638947767348681070279077173, 0.67176478451531541138011989728,
+         0.071081659837399872713651693126, -0.073630718761724245070378308432, 0.0056774548542830440901194873933)
+FD_GI = (0.182885278686826206583549109115, -1.08001475417455516433881053795, 0.65787289649662525818641772732,
+         0.1776170486891931456381189546, 0.076779836395827558602005515075, -0.0151403060939170046712807681567)
+FD_GJ = (-0.0341837103365291857798396404953, 0.224829025740103121729831613399, -0.89081233292845396245426338198,
+         0.165299947710035014782196870489, 0.61343955208752529977826815383, -0.078572482272680288056193615249)
+FD_DA = (-8.333333333333333333333E-02, 1.333333333333333333333E+00, -2.500000000000000000000E+00,
+         1.333333333333333333333E+00, -8.333333333333333333333E-02)
+FD_DB = (9.166666666666666666667E-01, -1.666666666666666666667E+00, 5.000000000000000000000E-01,
+         3.333333333333333333333E-01, -8.333333333333333333333E-02)
+FD_DD = (2.916666666666666666667E+00, -8.666666666666666666667E+00, 9.500000000000000000000E+00,
+         -4.666666666666666666667E+00, 9.166666666666666666667E-01)
+
+
+def ogengrid(ny: int, yi: float, ymax: float):
+    """ogengrid.f90:14-44: uniform eta = (j-1)/(ny-1) on [0, 1], wall first,
+    y = a eta / (b - eta) with a = ymax yi / (ymax - 2 yi), b = 1 + a / ymax.
+    The Mahesh map (yi = 0) reads its parameters interactively and is not
+    supported.  Returns y, eta, deta, d2eta and the eta spacing."""
+    if yi == 0.0:
+        raise ValueError("Mahesh map (Yi = 0) reads dymin, b, yc interactively; not supported")
+    dy = 1.0 / float(ny - 1)
+    aa = ymax * yi / (ymax - 2.0 * yi)
+    bb = 1.0 + aa / ymax
+    eta = np.arange(ny, dtype=np.float64) * dy
+    y = aa * eta / (bb - eta)
+    deta = (bb - eta) ** 2 / (aa * bb)
+    d2eta = -2.0 * (bb - eta) ** 3 / (aa * bb) ** 2
+    return y, eta, deta, d2eta, dy
+
+
+def fd_grad_matrix(ny: int, dy: float) -> np.ndarray:
+    """The y-gradient of grad.f90:62-86 as a matrix: fourth-order one-sided
+    and biased five-point stencils at the two end rows on each side, the
+    central stencil inside, each divided by 12 dy."""
+    G = np.zeros((ny, ny))
+    G[0, 0:5] = (-25.0, 48.0, -36.0, 16.0, -3.0)
+    G[1, 0:5] = (-3.0, -10.0, 18.0, -6.0, 1.0)
+    for i in range(2, ny - 2):
+        G[i, i - 2:i + 3] = (1.0, -8.0, 0.0, 8.0, -1.0)
+    G[ny - 2, ny - 5:ny] = -np.array((1.0, -6.0, 18.0, -10.0, -3.0))
+    G[ny - 1, ny - 5:ny] = -np.array((-3.0, 16.0, -36.0, 48.0, -25.0))
+    return G / (12.0 * dy)
+
+
+def fd_operator_tables(ny: int, dy: float):
+    """Per-row stencils of the finite-difference operator (fd_temporal.f90:
+    636-895), as matrices multiplying Bh (first derivative, F1) and Vyy
+    (second derivative, F2), with node 0 the wall:
+      row 0        Carpenter's one-sided gg / the one-sided dd (wall rows);
+      rows 1, 2, 3 Carpenter's biased gh, gi, gj / db, da, da;
+      rows 4..ny-5 the central ga (no centre entry) / da;
+      rows ny-4, ny-3, ny-2 the mirrored gj, gi, gh with a minus sign, and
+                   the second-derivative signs exactly as the reference
+                   writes them (+da4, +da5 on row ny-4; +da4 on row ny-3);
+      row ny-1     zero (the free-stream rows are B0 = i I, A0 = 0)."""
+    F1 = np.zeros((ny, ny))
+    F2 = np.zeros((ny, ny))
+    F1[0, 0:6] = FD_GG
+    F2[0, 0:5] = FD_DD
+    F1[1, 0:6] = FD_GH
+    F2[1, 0:5] = FD_DB
+    F1[2, 0:6] = FD_GI
+    F2[2, 0:5] = FD_DA
+    F1[3, 0:6] = FD_GJ
+    F2[3, 1:6] = FD_DA
+    for i in range(4, ny - 4):
+        F1[i, i - 2] = FD_GA[0]
+        F1[i, i - 1] = FD_GA[1]
+        F1[i, i + 1] = FD_GA[2]
+        F1[i, i + 2] = FD_GA[3]
+        F2[i, i - 2:i + 3] = FD_DA
+    i = ny - 4
+    F1[i, i - 2:i + 4] = [-FD_GJ[5], -FD_GJ[4], -FD_GJ[3], -FD_GJ[2], -FD_GJ[1], -FD_GJ[0]]
+    F2[i, i - 2:i + 3] = [FD_DA[0], FD_DA[1], FD_DA[2], -FD_DA[3], -FD_DA[4]]
+    i = ny - 3
+    F1[i, i - 3:i + 3] = [-FD_GI[5], -FD_GI[4], -FD_GI[3], -FD_GI[2], -FD_GI[1], -FD_GI[0]]
+    F2[i, i - 2:i + 3] = [FD_DA[0], FD_DA[1], FD_DA[2], -FD_DA[3], FD_DA[4]]
+    i = ny - 2
+    F1[i, i - 4:i + 2] = [-FD_GH[5], -FD_GH[4], -FD_GH[3], -FD_GH[2], -FD_GH[1], -FD_GH[0]]
+    F2[i, i - 3:i + 2] = [FD_DB[4], FD_DB[3], FD_DB[2], FD_DB[1], FD_DB[0]]
+    return F1 / dy, F2 / (dy * dy)
+
+
+def fd_mean_state(p: StabParams, ym: np.ndarray, vt: np.ndarray, first=None, second=None) -> MeanState:
+    """Grid, mean flow and mean derivatives of fd_temporal.f90:92-152: the
+    ogengrid grid, getmean's spline at its nodes, then grad applied once and
+    twice in eta and mapped (g22 = G(G v) deta^2 + (G v) d2eta, g2 = (G v)
+    deta); with ider = 0 the derivatives come from getmean2's tables.  D1, D2
+    hold the operator's stencil tables (fd_operator_tables)."""
+    ny = p.ny
+    y, eta, deta, d2eta, dy = ogengrid(ny, p.yi, p.ymax)
+    if not p.ider:
+        vm, g2, g22 = getmean2(ym, vt, first, second, y)
+    else:
+        vm = getmean(ym, vt, y)
+        G = fd_grad_matrix(ny, dy)
+        g2 = G @ vm
+        g22 = G @ g2
+        g22 = g22 * (deta ** 2)[:, None] + g2 * d2eta[:, None]
+        g2 = g2 * deta[:, None]
+    F1, F2 = fd_operator_tables(ny, dy)
+    return MeanState(y, eta, deta, d2eta, F1, F2, F1, F2, vm, g2, g22)
+
+
+def fd_temporal_pencil(p: StabParams, ms: MeanState, bl=None):
+    """A0, B0 of the finite-difference temporal problem (fd_temporal.f90:
+    581-895).  Node 0 is the wall: its continuity row is Dh + F1 Bh, its
+    energy row Dh + F1 Bh - F2 Vyy with the temperature column's Bh term
+    left out (the "adiabatic constraint", :693-708), and its momentum rows
+    are B0 = i, A0 = 0; the free-stream node has B0 = i I, A0 = 0 (the
+    zero-disturbance rows).  The wall temperature option is not read."""
+    if bl is None:
+        bl = temporal_blocks(p, ms)
+    ny = p.ny
+    a, b = p.alpha, p.beta
+    im = 1j
+    Dh = bl["D"] + im * a * bl["A"] + im * b * bl["C"] + a ** 2 * bl["Vxx"] + a * b * bl["Vxz"] + b ** 2 * bl["Vzz"]
+    Bh = bl["B"] - im * a * bl["Vxy"] - im * b * bl["Vyz"]
+    Bh = Bh * ms.deta[:, None, None] - bl["Vyy"] * ms.d2eta[:, None, None]
+    Vyy = bl["Vyy"] * (ms.deta ** 2)[:, None, None]
+    mask = np.zeros((ny, NDOF))
+    mask[1:ny - 1, :] = 1.0
+    A0 = _dense(Bh, Vyy, mask, ms.D1, ms.D2, Dh)
+    # wall continuity row: Dh + F1 Bh
+    mc = np.zeros((ny, NDOF))
+    mc[0, 0] = 1.0
+    A0 += _dense(Bh, np.zeros_like(Vyy), mc, ms.D1, ms.D2, Dh)
+    # wall energy row: Dh + F1 Bh - F2 Vyy, no Bh term in the temperature column
+    me = np.zeros((ny, NDOF))
+    me[0, 4] = 1.0
+    Bw = Bh.copy()
+    Bw[0, 4, 4] = 0.0
+    A0 += _dense(Bw, Vyy, me, ms.D1, ms.D2, Dh)
+    n = ny * NDOF
+    B0 = np.zeros((n, n), dtype=complex)
+    for e in range(NDOF - 1):
+        B0[e, e] = 1j
+    B0[4, 0:NDOF] = 1j * bl["G"][0, 4, :]
+    for i in range(1, ny - 1):
+        B0[i * NDOF:(i + 1) * NDOF, i * NDOF:(i + 1) * NDOF] = 1j * bl["G"][i]
+    i = ny - 1
+    for e in range(NDOF):
+        B0[i * NDOF + e, i * NDOF + e] = 1j
+    return A0, B0
+
+
+def fd_temporal_solve(p: StabParams, ms: MeanState, want_vectors=True) -> Eigensystem:
+    """fd_temporal.f90:970-1042: ZGESV(B0, A0), ZGEEV('N','V'), PIKSR2 on
+    Im(omega), columns scaled by their max-modulus entry."""
+    lp = _lapack()
+    A0, B0 = fd_temporal_pencil(p, ms)
+    lu, piv, X, info = lp.zgesv(B0, A0)
+    if info != 0:
+        raise RuntimeError(f"ZGESV info={info}")
+    w, vl, vr, info = lp.zgeev(X, compute_vl=0, compute_vr=1 if want_vectors else 0)
+    if info != 0:
+        raise RuntimeError(f"ZGEEV info={info}")
+    order = piksr2_order(w.imag)
+    w = w[order]
+    evec = None
+    if want_vectors:
+        evec = vr[:, order]
+        idx = np.argmax(np.abs(evec), axis=0)
+        sc = evec[idx, np.arange(evec.shape[1])]
+        nz = sc != 0
+        evec[:, nz] = evec[:, nz] / sc[nz]
+    return Eigensystem(p, ms, w, evec)
+
+
 def _lapack():
     from scipy.linalg import lapack
     return lapack
@@ -1424,6 +1602,11 @@ def spatial_solve(p: StabParams, ms: MeanState, want_vectors=True) -> Eigensyste
 
 
 def solve(p: StabParams, ym, vt, want_vectors=True, first=None, second=None) -> Eigensystem:
+    if p.itype == 3:
+        # stab.f90:56-60: itype becomes 1 before fd_temporal runs, so evec.dat says 1
+        es = fd_temporal_solve(p, fd_mean_state(p, ym, vt, first, second), want_vectors)
+        es.params = dataclasses.replace(p, itype=1)
+        return es
     ms = mean_state(p, ym, vt, first, second)
     if p.itype == 1:
         return temporal_solve(p, ms, want_vectors)

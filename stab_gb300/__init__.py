@@ -42,10 +42,10 @@ EXPORTED = (
     "stab_batch_results", "stab_batch_work", "stab_batch_destroy", "stab_solve_batch",
     "stab_eigvals_noalloc", "stab_eigenvectors", "stab_parse_input", "stab_parse_sweep_input",
     "stab_read_delta", "stab_read_body", "stab_eig_name", "stab_stab_out_line", "stab_sweep_points", "stab_profile_name", "stab_read_profile",
-    "stab_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
+    "stab_grid", "stab_fd_grid", "stab_write_evec", "stab_read_evec", "stab_getevec_select", "stab_eigfunction_text",
     "stab_mlp_create", "stab_mlp_param_count", "stab_mlp_set_params", "stab_mlp_get_params", "stab_mlp_forward",
     "stab_mlp_gradients", "stab_mlp_train_step", "stab_mlp_destroy", "stab_batch_set_start", "stab_batch_counts",
-    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_lu_tc_check", "stab_set_option", "stab_set_arithmetic", "stab_set_seed_size",
+    "stab_batch_spectra", "stab_autotune", "stab_eig_phases", "stab_lu_cluster_check", "stab_lu_tc_check", "stab_peak_rates", "stab_set_option", "stab_set_arithmetic", "stab_set_seed_size",
 )
 
 
@@ -94,7 +94,7 @@ class StabParams(ctypes.Structure):
         return 5 * self.ny
 
     def m(self) -> int:
-        return self.n() if self.itype == 1 else 2 * self.n()
+        return 2 * self.n() if self.itype == 2 else self.n()
 
 
 class Sweep(ctypes.Structure):
@@ -154,6 +154,7 @@ def load(path: str = LIB_PATH):
     lib.stab_profile_name.argtypes = [i32, ctypes.c_char_p, ctypes.c_size_t]
     lib.stab_read_profile.argtypes = [ctypes.c_char_p, i32, P(dbl), P(i32)]
     lib.stab_grid.argtypes = [i32, dbl, dbl, P(dbl), P(dbl), P(dbl), P(dbl)]
+    lib.stab_fd_grid.argtypes = [i32, dbl, dbl, P(dbl), P(dbl), P(dbl), P(dbl)]
     lib.stab_write_evec.argtypes = [ctypes.c_char_p, P(StabParams), P(dbl), P(dbl)]
     lib.stab_read_evec.argtypes = [ctypes.c_char_p, P(EvecHeader), P(dbl), P(dbl), P(dbl)]
     lib.stab_getevec_select.argtypes = [P(dbl), i32, dbl, dbl]
@@ -179,6 +180,7 @@ def load(path: str = LIB_PATH):
     lib.stab_set_seed_size.argtypes = [vp, i32]
     lib.stab_lu_cluster_check.argtypes = [vp, i32, i32, i32, P(dbl), P(i32)]
     lib.stab_lu_tc_check.argtypes = [vp, i32, i32, P(dbl), P(dbl), P(i32)]
+    lib.stab_peak_rates.argtypes = [vp, P(dbl)]
     lib.stab_set_option.argtypes = [vp, i32, i32]
     _lib = lib
     return lib
@@ -422,6 +424,13 @@ class Context:
                                                    ctypes.byref(pd)))
         return md.value, pd.value
 
+    def peak_rates(self) -> dict:
+        """stab_peak_rates: measured FP32 / FP64 FMA and double-word complex
+        multiply-add throughput of this device, TFLOP/s."""
+        out = np.zeros(3)
+        self._check(self.lib.stab_peak_rates(self.h, _dptr(out)))
+        return {"fp32": float(out[0]), "fp64": float(out[1]), "double_word_complex": float(out[2])}
+
     def set_option(self, option: int, value: int) -> None:
         """stab_set_option: OPT_SEED_QR_SHARED (0 default, 1 on), OPT_POLISH_LU_TMA (1 default, 0 off),
         OPT_EIG_RESIDENT (0 default: occupancy; k: k instances per SM)."""
@@ -624,6 +633,15 @@ def grid(ny: int, yi: float, ymax: float):
     """y, eta, deta, d2eta of the collocation grid (sgengrid.f90:18-45)."""
     out = [np.zeros(ny) for _ in range(4)]
     if load().stab_grid(ny, yi, ymax, *[_dptr(a) for a in out]):
+        raise StabError("bad grid arguments")
+    return tuple(out)
+
+
+def fd_grid(ny: int, yi: float, ymax: float):
+    """y, eta, deta, d2eta of the finite-difference grid (ogengrid.f90:20-44),
+    wall first."""
+    out = [np.zeros(ny) for _ in range(4)]
+    if load().stab_fd_grid(ny, yi, ymax, *[_dptr(a) for a in out]):
         raise StabError("bad grid arguments")
     return tuple(out)
 

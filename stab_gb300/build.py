@@ -17,7 +17,7 @@ BIN = os.path.join(HERE, "bin")
 TOOLS = {"stab_gpu": "stab_main.cpp", "getevec_gpu": "getevec_main.cpp", "getab_gpu": "post_main.cpp",
          "getax_gpu": "post_main.cpp", "getalpha_gpu": "post_main.cpp"}
 
-CU_SOURCES = ["prep.cu", "assemble.cu", "lu.cu", "lu_tc.cu", "hqr.cu", "polish.cu", "post.cu", "mlp.cu", "capi.cu", "fileio.cpp"]
+CU_SOURCES = ["prep.cu", "assemble.cu", "lu.cu", "lu_tc.cu", "hqr.cu", "polish.cu", "post.cu", "probe.cu", "mlp.cu", "capi.cu", "fileio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", os.path.join(HERE, "..", "include")]

@@ -57,7 +57,7 @@ struct stab_ctx {
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   std::string err;
-  std::map<int, std::pair<double*, double*>> dtabs;  // ny -> (D1, D2) on the device
+  std::map<int, std::pair<double*, double*>> dtabs;  // table key -> (D1, D2) on the device
   int profiling = 0;
   std::vector<KStat> stats;
   std::vector<PendingEv> pending;
@@ -143,9 +143,98 @@ static void drain_stats(stab_ctx* c) {
   c->pending.clear();
 }
 
-// Chebyshev tables for ny, built once per context
-static int ensure_dtab(stab_ctx* c, int ny) {
-  if (c->dtabs.count(ny)) return 0;
+// Derivative tables, built once per context, by key: ny for the Chebyshev
+// D1 and D1 D1; kFdOpKey + ny for the finite-difference operator's stencil
+// matrices; kFdMeanKey + ny for grad.f90's matrix G and G G.
+static const int kFdOpKey = 1 << 20, kFdMeanKey = 2 << 20;
+
+// stencils.f90:9-120, the reference's coefficient table (values as written there)
+static const double kGa[4] = {8.333333333333333333333E-02, -6.666666666666666666667E-01, 6.666666666666666666667E-01,
+                              -8.333333333333333333333E-02};
+static const double kGg[6] = {-1.87603205562073772290017534999, 3.18538322557789286703668141674,
+                              -1.81454567943752757247830550034, 0.59165824105260274421658150053,
+                              -0.101052068000505624644095417028, 0.0145883364282753087693133500917};
+static const double kGh[6] = {-0.384254232677925402043233692192, -0.290638947767348681070279077173,
+                              0.67176478451531541138011989728, 0.071081659837399872713651693126,
+                              -0.073630718761724245070378308432, 0.0056774548542830440901194873933};
+static const double kGi[6] = {0.182885278686826206583549109115, -1.08001475417455516433881053795,
+                              0.65787289649662525818641772732, 0.1776170486891931456381189546,
+                              0.076779836395827558602005515075, -0.0151403060939170046712807681567};
+static const double kGj[6] = {-0.0341837103365291857798396404953, 0.224829025740103121729831613399,
+                              -0.89081233292845396245426338198, 0.165299947710035014782196870489,
+                              0.61343955208752529977826815383, -0.078572482272680288056193615249};
+static const double kDa[5] = {-8.333333333333333333333E-02, 1.333333333333333333333E+00, -2.500000000000000000000E+00,
+                              1.333333333333333333333E+00, -8.333333333333333333333E-02};
+static const double kDb[5] = {9.166666666666666666667E-01, -1.666666666666666666667E+00, 5.000000000000000000000E-01,
+                              3.333333333333333333333E-01, -8.333333333333333333333E-02};
+static const double kDd[5] = {2.916666666666666666667E+00, -8.666666666666666666667E+00, 9.500000000000000000000E+00,
+                              -4.666666666666666666667E+00, 9.166666666666666666667E-01};
+
+// Row-major ny x ny stencil matrices of the finite-difference solver, node 0
+// at the wall (fd_temporal.f90:636-895): F1 multiplies Bh, F2 multiplies
+// Vyy.  Rows 0-3 the one-sided and biased closures, central rows, the
+// mirrored closures with the signs the reference writes (+da4 and +da5 on
+// row ny-4, +da4 on row ny-3), and a zero free-stream row.
+static void fd_operator_tables(int ny, std::vector<double>& F1, std::vector<double>& F2) {
+  const double dy = 1.0 / (double)(ny - 1);
+  F1.assign((size_t)ny * ny, 0.0);
+  F2.assign((size_t)ny * ny, 0.0);
+  auto f1 = [&](int i, int j, double v) { F1[(size_t)i * ny + j] = v / dy; };
+  auto f2 = [&](int i, int j, double v) { F2[(size_t)i * ny + j] = v / (dy * dy); };
+  for (int t = 0; t < 6; ++t) { f1(0, t, kGg[t]); f1(1, t, kGh[t]); f1(2, t, kGi[t]); f1(3, t, kGj[t]); }
+  for (int t = 0; t < 5; ++t) { f2(0, t, kDd[t]); f2(1, t, kDb[t]); f2(2, t, kDa[t]); f2(3, 1 + t, kDa[t]); }
+  for (int i = 4; i < ny - 4; ++i) {
+    f1(i, i - 2, kGa[0]); f1(i, i - 1, kGa[1]); f1(i, i + 1, kGa[2]); f1(i, i + 2, kGa[3]);
+    for (int t = 0; t < 5; ++t) f2(i, i - 2 + t, kDa[t]);
+  }
+  int i = ny - 4;
+  for (int t = 0; t < 6; ++t) f1(i, i - 2 + t, -kGj[5 - t]);
+  for (int t = 0; t < 5; ++t) f2(i, i - 2 + t, t < 3 ? kDa[t] : -kDa[t]);
+  i = ny - 3;
+  for (int t = 0; t < 6; ++t) f1(i, i - 3 + t, -kGi[5 - t]);
+  for (int t = 0; t < 5; ++t) f2(i, i - 2 + t, t == 3 ? -kDa[t] : kDa[t]);
+  i = ny - 2;
+  for (int t = 0; t < 6; ++t) f1(i, i - 4 + t, -kGh[5 - t]);
+  for (int t = 0; t < 5; ++t) f2(i, i - 3 + t, kDb[4 - t]);
+}
+
+// grad.f90:62-86 as a matrix G (fourth-order five-point stencils, one-sided
+// and biased at both ends, over 12 deta), and G G.
+static void fd_mean_tables(int ny, std::vector<double>& G, std::vector<double>& GG) {
+  const double dy = 1.0 / (double)(ny - 1);
+  G.assign((size_t)ny * ny, 0.0);
+  auto g = [&](int i, int j, double v) { G[(size_t)i * ny + j] = v / (12.0 * dy); };
+  const double r0[5] = {-25.0, 48.0, -36.0, 16.0, -3.0}, r1[5] = {-3.0, -10.0, 18.0, -6.0, 1.0};
+  for (int t = 0; t < 5; ++t) { g(0, t, r0[t]); g(1, t, r1[t]); }
+  const double c[5] = {1.0, -8.0, 0.0, 8.0, -1.0};
+  for (int i = 2; i < ny - 2; ++i)
+    for (int t = 0; t < 5; ++t) if (c[t] != 0.0) g(i, i - 2 + t, c[t]);
+  for (int t = 0; t < 5; ++t) { g(ny - 2, ny - 1 - t, -r1[t]); g(ny - 1, ny - 1 - t, -r0[t]); }
+  GG.assign((size_t)ny * ny, 0.0);
+  for (int i = 0; i < ny; ++i)
+    for (int k = 0; k < ny; ++k) {
+      const double a = G[(size_t)i * ny + k];
+      if (a == 0.0) continue;
+      for (int j = 0; j < ny; ++j) GG[(size_t)i * ny + j] += a * G[(size_t)k * ny + j];
+    }
+}
+
+static int ensure_dtab(stab_ctx* c, int key) {
+  if (c->dtabs.count(key)) return 0;
+  if (key >= kFdOpKey) {
+    const int ny = key & (kFdOpKey - 1);
+    std::vector<double> T1, T2;
+    if (key >= kFdMeanKey) fd_mean_tables(ny, T1, T2);
+    else fd_operator_tables(ny, T1, T2);
+    double *D1 = nullptr, *D2 = nullptr;
+    CK(c, cudaMalloc(&D1, sizeof(double) * ny * ny));
+    CK(c, cudaMalloc(&D2, sizeof(double) * ny * ny));
+    CK(c, cudaMemcpy(D1, T1.data(), sizeof(double) * ny * ny, cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(D2, T2.data(), sizeof(double) * ny * ny, cudaMemcpyHostToDevice));
+    c->dtabs[key] = {D1, D2};
+    return 0;
+  }
+  const int ny = key;
   double *D1 = nullptr, *D2 = nullptr, *xa = nullptr;
   CK(c, cudaMalloc(&D1, sizeof(double) * ny * ny));
   CK(c, cudaMalloc(&D2, sizeof(double) * ny * ny));
@@ -159,7 +248,7 @@ static int ensure_dtab(stab_ctx* c, int ny) {
   CK(c, cudaGetLastError());
   CK(c, cudaStreamSynchronize(c->stream));
   cudaFree(xa);
-  c->dtabs[ny] = {D1, D2};
+  c->dtabs[key] = {D1, D2};
   return 0;
 }
 
@@ -444,7 +533,12 @@ static bool calch_scalars(double s, double out[8]) {
 // Descriptor of one instance from its run parameters (validated) and the
 // entry of its mean profile in the profile pools.
 static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDesc& pd, InstDesc& d) {
-  if (q.itype != 1 && q.itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal) or 2 (spatial)");
+  if (q.itype != 1 && q.itype != 2 && q.itype != 3)
+    return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal), 2 (spatial) or 3 (temporal, finite differences)");
+  const bool fd = (q.itype == 3);
+  if (fd && q.ny < 10) return set_err(c, STAB_ERR_ARG, "the finite-difference solver needs ny >= 10");
+  if (fd && !(q.yi != 0.0 && q.ymax > 2.0 * q.yi))
+    return set_err(c, STAB_ERR_ARG, "the finite-difference grid (ogengrid) needs Yi != 0 and Ymax > 2 Yi");
   if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
   if (q.itype == 2 && q.curve != 0 && q.curve != 1 && q.curve != 2)
     return set_err(c, STAB_ERR_ARG, "curve must be 0, 1 or 2");
@@ -458,8 +552,9 @@ static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDes
   d = InstDesc{};
   d.ny = q.ny;
   d.n = 5 * q.ny;
-  d.itype = q.itype;
-  d.m = (q.itype == 1) ? d.n : 2 * d.n;
+  d.itype = fd ? 1 : q.itype;
+  d.fd = fd ? 1 : 0;
+  d.m = (d.itype == 1) ? d.n : 2 * d.n;
   d.wallt = q.wallt;
   d.top = q.top;
   d.mattyp = q.mattyp;
@@ -497,7 +592,9 @@ static int batch_finish(stab_ctx* c, stab_batch* b) {
   int64_t node_off = 0, blk_off = 0, vec_off = 0;
   b->tcount = 0;
   for (auto& d : b->hd) {
-    if (std::find(tab_ny.begin(), tab_ny.end(), d.ny) == tab_ny.end()) tab_ny.push_back(d.ny);
+    const int kop = d.fd ? kFdOpKey + d.ny : d.ny, kmean = d.fd ? kFdMeanKey + d.ny : d.ny;
+    for (int key : {kop, kmean})
+      if (std::find(tab_ny.begin(), tab_ny.end(), key) == tab_ny.end()) tab_ny.push_back(key);
     d.off_node = node_off;
     d.off_blk = blk_off;
     d.off_vec = vec_off;
@@ -517,7 +614,10 @@ static int batch_finish(stab_ctx* c, stab_batch* b) {
     hdt.push_back(kv.second.first);
     hdt.push_back(kv.second.second);
   }
-  for (auto& d : b->hd) d.dmat = tab_index[d.ny];
+  for (auto& d : b->hd) {
+    d.dmat = tab_index[d.fd ? kFdOpKey + d.ny : d.ny];
+    d.dmean = tab_index[d.fd ? kFdMeanKey + d.ny : d.ny];
+  }
   // offsets
   for (auto& d : b->hd) {
     b->hn.push_back(d.n);
@@ -601,7 +701,8 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   b->coarse_ny = c->seed_ny;
   std::vector<int> idx(count);
   for (int i = 0; i < count; ++i) idx[i] = i;
-  std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return p[a].itype < p[bb].itype; });
+  // temporal (itype 1 and 3) before spatial
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return (p[a].itype == 2) < (p[bb].itype == 2); });
   b->perm = idx;
   // profiles: dedupe by pointer; copied straight from caller memory in
   // contiguous runs (validated on the device by k_spline).  With ider = 0 a
@@ -1917,6 +2018,40 @@ int stab_lu_tc_check(stab_ctx* c, int32_t n, int32_t count, double* bwd_tc, doub
   return lu_tc_check(c, n, count, bwd_tc, bwd_simt, piv_diff);
 }
 
+int stab_peak_rates(stab_ctx* c, double* out) {
+  if (!c || !out) return STAB_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  int sms = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  float* sink = nullptr;
+  CK(c, cudaMallocAsync(reinterpret_cast<void**>(&sink), sizeof(float), s));
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int iters[3] = {65536, 2048, 4096};   // a few milliseconds per launch
+  int rc = STAB_OK;
+  for (int kind = 0; kind < 3 && rc == STAB_OK; ++kind) {
+    launch_probe(kind, 4 * sms, iters[kind] / 8, sink, s);   // warm-up
+    cudaEventRecord(a, s);
+    const double flops = launch_probe(kind, 4 * sms, iters[kind], sink, s);
+    cudaEventRecord(b, s);
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e != cudaSuccess) {
+      rc = set_err(c, STAB_ERR_CUDA, cudaGetErrorString(e));
+      break;
+    }
+    out[kind] = flops / (ms * 1e-3) / 1e12;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFreeAsync(sink, s);
+  cudaStreamSynchronize(s);
+  return rc;
+}
+
 int stab_lu_cluster_check(stab_ctx* c, int32_t n, int32_t count, int32_t complex128, double* max_diff,
                           int32_t* piv_diff) {
   if (!c || !max_diff || !piv_diff || n < 2 || n > 1024 || count < 1) return STAB_ERR_ARG;
@@ -2158,9 +2293,9 @@ int stab_assemble(stab_ctx* c, const stab_params* p, int32_t nym, const double* 
   const Range r{0, 1};
   const int kinds_t[2] = {OP_T_A0, OP_T_B0};
   const int kinds_s[3] = {OP_S_C0, OP_S_C1, OP_S_C2};
-  const int nk = (p->itype == 1) ? 2 : 3;
+  const int nk = (p->itype != 2) ? 2 : 3;
   for (int q = 0; q < nk; ++q) {
-    const int kd = (p->itype == 1) ? kinds_t[q] : kinds_s[q];
+    const int kd = (p->itype != 2) ? kinds_t[q] : kinds_s[q];
     rc = node_ops(b, r, kd, kd, nullptr);
     if (rc) return rc;
     rc = dense<zc>(b, r, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z");
@@ -2176,7 +2311,7 @@ int stab_eigenvectors(stab_ctx* c, const stab_params* p, int32_t nym, const doub
                       const double* eig, double* vec_out, int32_t* status_out) {
   if (!c || !p || !profile || !eig || !vec_out || count < 0) return set_err(c, STAB_ERR_ARG, "null argument");
   if (count == 0) return STAB_OK;
-  if (p->itype != 1 && p->itype != 2) return set_err(c, STAB_ERR_ARG, "itype must be 1 or 2");
+  if (p->itype != 1 && p->itype != 2 && p->itype != 3) return set_err(c, STAB_ERR_ARG, "itype must be 1, 2 or 3");
   cudaSetDevice(c->device);
   const bool spatial = (p->itype == 2);
   const int64_t mlen = (int64_t)(spatial ? 10 : 5) * p->ny;

@@ -129,7 +129,12 @@ struct InstDesc {
   // curved wall (spatial, curve = 2): 1, and the arc-position scalars of the
   // circle's metric (dxbds, dybds, dbn1, dbn2, d2xbds2, d2ybds2, d2bn1,
   // d2bn2) from which h(y) and its derivatives follow (circh.f90:190-199)
-  int32_t curved, pad2_;
+  int32_t curved;
+  // finite-difference temporal solver (fd_temporal.f90, input itype 3):
+  // ogengrid nodes on a uniform eta, node 0 at the wall; D tables are its
+  // stencil matrices, and the mean derivatives use grad.f90's matrices
+  int32_t fd;
+  int32_t dmean, pad3_;   // index of the mean-derivative (D1, D2) table (= dmat for Chebyshev)
   double cw[8];
 };
 #define VEC_SLOTS 10

@@ -265,14 +265,16 @@ static int parse_protocol(const char* text, stab_params* p, stab_sweep* sw, char
     }
     return STAB_OK;
   }
-  if (p->itype != 1 && p->itype != 2) {
+  if (p->itype != 1 && p->itype != 2 && p->itype != 3) {
     set_msg(msg, msg_cap, "itype " + std::to_string(p->itype) +
-                              (sw ? " (finite-difference, Stokes or bump solver)" :
-                                    " (finite-difference, Stokes, bump or multi-point driver)") +
-                              " is outside the Chebyshev temporal/spatial path");
+                              (sw ? " (finite-difference spatial, Stokes or bump solver)" :
+                                    " (finite-difference spatial, Stokes, bump or multi-point driver)") +
+                              " is outside the temporal/spatial path");
     return STAB_ERR_ARG;
   }
-  if (p->itype == 1) {
+  // itype 3: the finite-difference temporal solver, same questions as the
+  // Chebyshev one (stab.f90:56-60)
+  if (p->itype == 1 || p->itype == 3) {
     if (!reals(2, p->alpha, "alphar, alphai")) return STAB_ERR_ARG;
   } else {
     if (!reals(2, p->omega, "omegar, omegai")) return STAB_ERR_ARG;
@@ -482,6 +484,21 @@ int stab_read_profile(const char* path, int32_t cap_rows, double* rows, int32_t*
   return rc;
 }
 
+int stab_fd_grid(int32_t ny, double yi, double ymax, double* y, double* eta, double* deta, double* d2eta) {
+  if (ny < 2 || yi == 0.0 || !(ymax > 2.0 * yi) || !y || !eta || !deta || !d2eta) return STAB_ERR_ARG;
+  const double dy = 1.0 / (double)(ny - 1);
+  const double aa = ymax * yi / (ymax - 2.0 * yi);
+  const double bb = 1.0 + aa / ymax;
+  for (int i = 0; i < ny; ++i) {
+    const double e = (double)i * dy, q = bb - e;
+    eta[i] = e;
+    y[i] = aa * e / q;
+    deta[i] = q * q / (aa * bb);
+    d2eta[i] = -2.0 * q * q * q / ((aa * bb) * (aa * bb));
+  }
+  return STAB_OK;
+}
+
 int stab_grid(int32_t ny, double yi, double ymax, double* y, double* eta, double* deta, double* d2eta) {
   if (ny < 2 || yi == 0.0 || !y || !eta || !deta || !d2eta) return STAB_ERR_ARG;
   const double pi = std::acos(-1.0);
@@ -507,17 +524,22 @@ int stab_grid(int32_t ny, double yi, double ymax, double* y, double* eta, double
 
 int stab_write_evec(const char* path, const stab_params* p, const double* eig, const double* vec) {
   if (!path || !p || !eig || p->ny < 2) return STAB_ERR_ARG;
-  if (p->itype != 1 && p->itype != 2) return STAB_ERR_ARG;
+  if (p->itype != 1 && p->itype != 2 && p->itype != 3) return STAB_ERR_ARG;
   const int ny = p->ny;
-  const int64_t nmax = (int64_t)(p->itype == 1 ? 1 : 2) * kNdof * ny;
-  const bool want_vec = (p->itype == 1 || p->ievec == 1);
+  // itype 3 (finite differences) is temporal, recorded as 1 (stab.f90:59),
+  // with ogengrid's grid (fd_temporal.f90:1052-1055)
+  const bool fd = (p->itype == 3);
+  const int32_t itype = fd ? 1 : p->itype;
+  const int64_t nmax = (int64_t)(itype == 1 ? 1 : 2) * kNdof * ny;
+  const bool want_vec = (itype == 1 || p->ievec == 1);
   if (want_vec && !vec) return STAB_ERR_ARG;
   std::vector<double> y(ny), eta(ny), deta(ny), d2eta(ny);
-  int rc = stab_grid(ny, p->yi, p->ymax, y.data(), eta.data(), deta.data(), d2eta.data());
+  int rc = fd ? stab_fd_grid(ny, p->yi, p->ymax, y.data(), eta.data(), deta.data(), d2eta.data())
+              : stab_grid(ny, p->yi, p->ymax, y.data(), eta.data(), deta.data(), d2eta.data());
   if (rc) return rc;
   std::FILE* f = std::fopen(path, "wb");
   if (!f) return STAB_ERR_IO;
-  const int32_t r1[10] = {p->ind, p->ny, kNdof, p->itype, p->ievec, p->curve, p->top, p->wall, p->wallt,
+  const int32_t r1[10] = {p->ind, p->ny, kNdof, itype, p->ievec, p->curve, p->top, p->wall, p->wallt,
                           p->ider ? 1 : 0};
   put_record(f, r1, sizeof(r1));
   const double r2[9] = {p->omega[0], p->omega[1], p->alpha[0], p->alpha[1], p->beta[0], p->beta[1],

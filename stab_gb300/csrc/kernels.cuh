@@ -56,6 +56,9 @@ __global__ void k_spatial_vec(int count, const InstDesc* desc, const zc* theta, 
 // folding of each round into the best pair, final pick
 __global__ void k_take_candidate(int count, const zc* cand, int ncand, int j, zc* sigma);
 __global__ void k_converged_mask(int count, int32_t* done, int32_t* mask, int restore);
+// FMA throughput probes (probe.cu): kind 0 FP32, 1 FP64, 2 double-word
+// complex; returns the flops of the launch
+double launch_probe(int kind, int blocks, int iters, float* out, cudaStream_t s);
 __global__ void k_fold_best(int count, const InstDesc* desc, const zc* sigma, const zc* theta, const int32_t* done,
                             const double* err, const int32_t* iters, const zc* out, const int64_t* out_off,
                             int32_t* final_, int32_t* have, double* best_key, zc* best_theta, double* best_err,

@@ -146,6 +146,19 @@ __global__ void k_spline(int nprof, const ProfDesc* __restrict__ pdesc, const do
 // grid of sgengrid (algebraic maps): eta = cos(pi (i-1)/(ny-1))
 __device__ __forceinline__ void node_grid(const InstDesc& d, int i, double& y, double& eta, double& deta,
                                           double& d2eta) {
+  if (d.fd) {
+    // ogengrid.f90:20-44: eta = i / (ny - 1) on [0, 1], wall first,
+    // y = a eta / (b - eta), a = ymax yi / (ymax - 2 yi), b = 1 + a / ymax
+    const double dy = 1.0 / (double)(d.ny - 1);
+    const double aa = d.ymax * d.yi / (d.ymax - 2.0 * d.yi);
+    const double bb = 1.0 + aa / d.ymax;
+    eta = (double)i * dy;
+    y = aa * eta / (bb - eta);
+    const double q = bb - eta;
+    deta = q * q / (aa * bb);
+    d2eta = -2.0 * q * q * q / ((aa * bb) * (aa * bb));
+    return;
+  }
   const double pi = 3.1415926535897932385;
   double dth = pi / (double)(d.ny - 1);
   eta = cos((double)i * dth);
@@ -222,7 +235,9 @@ __global__ void k_nodes(int count, const InstDesc* __restrict__ desc, const doub
   }
 }
 
-// g2 = deta * D1 v,  g22 = deta^2 * D2 v + d2eta * D1 v; one thread per (node, field)
+// g2 = deta * D1 v,  g22 = deta^2 * D2 v + d2eta * D1 v; one thread per (node, field).
+// D1, D2: the Chebyshev matrices, or for the finite-difference solver
+// grad.f90's fourth-order matrix G and G G (fd_temporal.f90:135-152)
 __global__ void k_meanderiv(int count, const InstDesc* __restrict__ desc, const double* const* __restrict__ dtab,
                             double* __restrict__ node) {
   int k = blockIdx.y;
@@ -233,8 +248,8 @@ __global__ void k_meanderiv(int count, const InstDesc* __restrict__ desc, const 
   if (t >= d.ny * 5) return;
   int i = t / 5, f = t % 5;
   const int ny = d.ny;
-  const double* D1 = dtab[2 * d.dmat];
-  const double* D2 = dtab[2 * d.dmat + 1];
+  const double* D1 = dtab[2 * d.dmean];
+  const double* D2 = dtab[2 * d.dmean + 1];
   double* nb = node + d.off_node;
   double s1 = 0.0, s2 = 0.0;
   for (int j = 0; j < ny; ++j) {
@@ -696,7 +711,9 @@ __global__ void k_blocks(int count, const InstDesc* __restrict__ desc, const dou
     node_blocks(d, nd, spatial, b);
   }
   const zc I = zmk(0.0, 1.0);
-  const bool top_node = (i == 0), wall_node = (i == ny - 1);
+  // Chebyshev nodes run from the free stream to the wall, the
+  // finite-difference ones from the wall
+  const bool top_node = d.fd ? (i == ny - 1) : (i == 0), wall_node = d.fd ? (i == 0) : (i == ny - 1);
   zc* out = blk + d.off_blk + (size_t)BLK_STRIDE * i;
   zc P1[5][5], P2[5][5], P3[5][5];
   const zc z0 = zmk(0.0, 0.0);
@@ -726,7 +743,23 @@ __global__ void k_blocks(int count, const InstDesc* __restrict__ desc, const dou
     zc B0[5][5];
     for (int e = 0; e < 5; ++e)
       for (int v = 0; v < 5; ++v) B0[e][v] = z0;
-    if (top_node || wall_node) {
+    if (d.fd && (top_node || wall_node)) {
+      // fd_temporal.f90:601-708: free stream B0 = i I, A0 = 0; wall
+      // continuity row Dh + F1 Bh, momentum rows B0 = i, A0 = 0, energy row
+      // Dh + F1 Bh - F2 Vyy without the temperature column's Bh term, with
+      // B0's energy row i G (the wall temperature option is not read)
+      for (int e = 0; e < 5; ++e) B0[e][e] = I;
+      if (wall_node) {
+        for (int v = 0; v < 5; ++v) {
+          P1[0][v] = Bh[0][v];
+          P3[0][v] = Dh[0][v];
+          P1[4][v] = (v < 4) ? Bh[4][v] : z0;
+          P2[4][v] = zmk(Vy[4][v], 0.0);
+          P3[4][v] = Dh[4][v];
+          B0[4][v] = zscale(I, b.G[4][v]);
+        }
+      }
+    } else if (top_node || wall_node) {
       // continuity row only, no Vyy D2 term (temporal.f90:664-681, :706-722)
       for (int v = 0; v < 5; ++v) { P1[0][v] = Bh[0][v]; P3[0][v] = Dh[0][v]; }
       for (int e = 0; e < 5; ++e) B0[e][e] = I;

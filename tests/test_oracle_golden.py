@@ -132,3 +132,35 @@ def test_oracle_calch_scalars_follow_the_parabola():
         so.calch_scalars(0.5)
     p = so.StabParams(curve=1, x=-1.0, itype=2, ny=8)
     assert np.array_equal(so.wall_metrics(p, np.linspace(0, 1, 8))[0], np.ones(8))
+
+
+def test_oracle_fd_temporal_converges_to_the_spectral_adiabatic_solution():
+    """Finite-difference temporal solver (itype 3, fd_temporal.f90), thesis
+    TStest fd_temporal.inp (M = 0.3, Re = 1000, Pr = 1, alpha = 0.30862069,
+    Yi = 1, Ymax = 50, constant viscosity).  Its wall energy row is the
+    energy equation with the temperature column's first-derivative term left
+    out, an adiabatic condition whatever wallt says, so it converges to the
+    Chebyshev solver's TS mode with wallt = 2 (pinned to the reference's
+    golden files) rather than to the isothermal golden value of the
+    README.  Fourth-order stencils: at N = 256 within 5e-8 relative, and the
+    error falls by more than 4x from N = 64 to N = 128 (third-order
+    closures at the boundaries)."""
+    prof = H.ts_profile()
+    ym, vt = prof[:, 0].copy(), prof[:, 1:6].copy()
+    vt[:, 2] = 0.0
+    base = dict(mattyp=0, T0=0.0, Ma=0.3, Re=1000.0, Pr=1.0, yi=1.0, ymax=50.0, ievec=1, ider=1, top=0, wall=0,
+                curve=0, alpha=0.308620690 + 0j, beta=0j, omega=0j)
+    spec = so.solve(so.StabParams(ny=96, wallt=2, itype=1, **base), ym, vt, want_vectors=False)
+    g = 1.1467880189410E-001 + 2.3844535276592E-003j        # the isothermal value, to find the mode
+    ref = spec.eig[so.getevec_select(spec.eig, g)]
+    err = {}
+    for N in (64, 128, 256):
+        es = so.solve(so.StabParams(ny=N, wallt=0, itype=3, **base), ym, vt, want_vectors=False)
+        assert es.params.itype == 1                          # stab.f90:59: recorded as temporal
+        w = es.eig[so.getevec_select(es.eig, ref)]
+        err[N] = abs(w - ref) / abs(ref)
+    assert err[256] < 5e-8, err
+    assert err[128] < err[64] / 4, err
+    # the grid: uniform eta from the wall, y(0) = 0, y(1) = ymax
+    y, eta, deta, d2eta, dy = so.ogengrid(33, 1.0, 50.0)
+    assert y[0] == 0.0 and abs(y[-1] - 50.0) < 1e-12 and abs(eta[1] - 1.0 / 32) < 1e-15

@@ -1448,6 +1448,37 @@ def fd_operator_tables(ny: int, dy: float):
     return F1 / dy, F2 / (dy * dy)
 
 
+def fd_spatial_tables(ny: int, dy: float):
+    """Per-row stencils of the finite-difference spatial operator
+    (fd_spatial.f90:668-960), node 0 the wall: rows 0-3 and the interior as
+    in fd_operator_tables, the central rows running to ny-3, row ny-2 the
+    fourth-order biased (-1, 6, -18, 10, 3)/12 with the mirrored db second
+    derivative, and row ny-1 the one-sided (3, -16, 36, -48, 25)/12 first
+    derivative that the free-stream continuity row uses when top = 1."""
+    F1 = np.zeros((ny, ny))
+    F2 = np.zeros((ny, ny))
+    F1[0, 0:6] = FD_GG
+    F2[0, 0:5] = FD_DD
+    F1[1, 0:6] = FD_GH
+    F2[1, 0:5] = FD_DB
+    F1[2, 0:6] = FD_GI
+    F2[2, 0:5] = FD_DA
+    F1[3, 0:6] = FD_GJ
+    F2[3, 1:6] = FD_DA
+    for i in range(4, ny - 2):
+        F1[i, i - 2] = FD_GA[0]
+        F1[i, i - 1] = FD_GA[1]
+        F1[i, i + 1] = FD_GA[2]
+        F1[i, i + 2] = FD_GA[3]
+        F2[i, i - 2:i + 3] = FD_DA
+    i = ny - 2
+    F1[i, i - 3:i + 2] = np.array([-1.0, 6.0, -18.0, 10.0, 3.0]) / 12.0
+    F2[i, i - 3:i + 2] = [FD_DB[4], FD_DB[3], FD_DB[2], FD_DB[1], FD_DB[0]]
+    i = ny - 1
+    F1[i, i - 4:i + 1] = np.array([3.0, -16.0, 36.0, -48.0, 25.0]) / 12.0
+    return F1 / dy, F2 / (dy * dy)
+
+
 def fd_mean_state(p: StabParams, ym: np.ndarray, vt: np.ndarray, first=None, second=None) -> MeanState:
     """Grid, mean flow and mean derivatives of fd_temporal.f90:92-152: the
     ogengrid grid, getmean's spline at its nodes, then grad applied once and
@@ -1465,7 +1496,7 @@ def fd_mean_state(p: StabParams, ym: np.ndarray, vt: np.ndarray, first=None, sec
         g22 = G @ g2
         g22 = g22 * (deta ** 2)[:, None] + g2 * d2eta[:, None]
         g2 = g2 * deta[:, None]
-    F1, F2 = fd_operator_tables(ny, dy)
+    F1, F2 = fd_spatial_tables(ny, dy) if p.itype == 4 else fd_operator_tables(ny, dy)
     return MeanState(y, eta, deta, d2eta, F1, F2, F1, F2, vm, g2, g22)
 
 
@@ -1509,6 +1540,87 @@ def fd_temporal_pencil(p: StabParams, ms: MeanState, bl=None):
     for e in range(NDOF):
         B0[i * NDOF + e, i * NDOF + e] = 1j
     return A0, B0
+
+
+def fd_spatial_operators(p: StabParams, ms: MeanState):
+    """C0, C1, C2 of the finite-difference spatial problem (fd_spatial.f90:
+    106-1170), node 0 the wall.  The coefficient blocks are the spatial
+    solver's; the wall metric is calch's for curve = 1 and flat otherwise
+    (fd_spatial.f90:108-116 has no circle).  Rows as in spatial_operators
+    with the finite-difference stencils, and two quirks kept: the wall
+    energy row of wallt = 2 takes its -i omega G term from the G of node
+    ny-1 (top = 1) or ny-2 (top = 0), the node index the assembly loops leave
+    behind (fd_spatial.f90:917-921), and its temperature column has no
+    first-derivative term in C0 and C1 (the "adiabatic constraint")."""
+    q = p if (p.curve == 1 and p.x != -1.0) else dataclasses.replace(p, curve=0)
+    bl = spatial_blocks(q, ms)
+    ny = p.ny
+    om, b = p.omega, p.beta
+    im = 1j
+    n = ny * NDOF
+    Dh = bl["D"] + im * b * bl["C"] + b ** 2 * bl["Vzz"]
+    Bh = (bl["B"] - im * b * bl["Vyz"]) * ms.deta[:, None, None] - bl["Vyy"] * ms.d2eta[:, None, None]
+    Vyy = bl["Vyy"] * (ms.deta ** 2)[:, None, None]
+    zero = np.zeros_like(Vyy)
+    F1, F2 = ms.D1, ms.D2
+    mask = np.zeros((ny, NDOF))
+    mask[1:ny - 1, :] = 1.0
+    C0 = _dense(Bh, Vyy, mask, F1, F2, Dh)
+    mc = np.zeros((ny, NDOF))
+    mc[0, 0] = 1.0
+    if p.top == 1:
+        mc[ny - 1, 0] = 1.0
+    C0 = C0 + _dense(Bh, zero, mc, F1, F2, Dh)
+    gq = ny - 1 if p.top == 1 else ny - 2
+    if p.wallt == 2:
+        me = np.zeros((ny, NDOF))
+        me[0, 4] = 1.0
+        Bw = Bh.copy()
+        Bw[0, 4, 4] = 0.0
+        C0 = C0 + _dense(Bw, Vyy, me, F1, F2, Dh)
+    # time term and boundary rows (fd_spatial.f90:907-947)
+    C0[0, 0] = C0[0, 0] - im * om
+    for e in (1, 2, 3):
+        C0[e, e] = -1.0
+    if p.wallt == 0:
+        C0[4, 4] = -1.0
+    elif p.wallt == 2:
+        C0[4, 0:NDOF] = C0[4, 0:NDOF] - im * om * bl["G"][gq, 4, :]
+    else:
+        raise ValueError(f"Illegal value of wallt: {p.wallt}")
+    for i in range(1, ny - 1):
+        sl = slice(i * NDOF, (i + 1) * NDOF)
+        C0[sl, sl] = C0[sl, sl] - im * om * bl["G"][i]
+    i0 = (ny - 1) * NDOF
+    if p.top == 1:
+        C0[i0, i0] = C0[i0, i0] - im * om
+    else:
+        C0[i0, i0] = -1.0
+    for e in range(1, NDOF):
+        C0[i0 + e, i0 + e] = -1.0
+    # C1 (fd_spatial.f90:951-1160)
+    Dh1 = im * bl["A"] + b * bl["Vxz"]
+    Bh1 = (-im * bl["Vxy"]) * ms.deta[:, None, None]
+    m1 = np.zeros((ny, NDOF))
+    m1[1:ny - 1, :] = 1.0
+    m1[0, 0] = 1.0
+    if p.top == 1:
+        m1[ny - 1, 0] = 1.0
+    C1 = _dense(Bh1, zero, m1, F1, F2, Dh1)
+    if p.wallt == 2:
+        me = np.zeros((ny, NDOF))
+        me[0, 4] = 1.0
+        Bw1 = Bh1.copy()
+        Bw1[0, 4, 4] = 0.0
+        C1 = C1 + _dense(Bw1, zero, me, F1, F2, Dh1)
+    # C2 (fd_spatial.f90:1164-1180)
+    C2 = np.zeros((n, n), dtype=complex)
+    if p.wallt == 2:
+        C2[4, 0:NDOF] = bl["Vxx"][0, 4, :]
+    for i in range(1, ny - 1):
+        sl = slice(i * NDOF, (i + 1) * NDOF)
+        C2[sl, sl] = bl["Vxx"][i]
+    return C0, C1, C2
 
 
 def fd_temporal_solve(p: StabParams, ms: MeanState, want_vectors=True) -> Eigensystem:
@@ -1570,11 +1682,11 @@ def temporal_solve(p: StabParams, ms: MeanState, want_vectors=True) -> Eigensyst
     return Eigensystem(p, ms, w, evec)
 
 
-def spatial_companion(p: StabParams, ms: MeanState):
-    """spatial.f90:972-1016: ZGETRF(C0), C1 := -C0^{-1} C1, C2 := -C0^{-1} C2,
-    B0 = [[C1, C2], [I, 0]]."""
+def spatial_companion(p: StabParams, ms: MeanState, ops=None):
+    """spatial.f90:972-1016 (fd_spatial.f90:1194-1236): ZGETRF(C0),
+    C1 := -C0^{-1} C1, C2 := -C0^{-1} C2, B0 = [[C1, C2], [I, 0]]."""
     lp = _lapack()
-    C0, C1, C2 = spatial_operators(p, ms)
+    C0, C1, C2 = spatial_operators(p, ms) if ops is None else ops
     lu, piv, info = lp.zgetrf(C0)
     if info < 0:
         raise RuntimeError(f"ZGETRF info={info}")
@@ -1588,11 +1700,11 @@ def spatial_companion(p: StabParams, ms: MeanState):
     return B0
 
 
-def spatial_solve(p: StabParams, ms: MeanState, want_vectors=True) -> Eigensystem:
+def spatial_solve(p: StabParams, ms: MeanState, want_vectors=True, ops=None) -> Eigensystem:
     """spatial.f90:1041-1084: ZGEEV on the companion matrix, alpha = 1/lambda
     (lambda = 0 -> 0), PIKSR2 on Im(alpha).  Eigenvectors are not rescaled."""
     lp = _lapack()
-    B0 = spatial_companion(p, ms)
+    B0 = spatial_companion(p, ms, ops)
     w, vl, vr, info = lp.zgeev(B0, compute_vl=0, compute_vr=1 if want_vectors else 0)
     alp = np.where(w != 0, 1.0 / np.where(w != 0, w, 1.0), 0.0)
     order = piksr2_order(alp.imag)
@@ -1602,6 +1714,12 @@ def spatial_solve(p: StabParams, ms: MeanState, want_vectors=True) -> Eigensyste
 
 
 def solve(p: StabParams, ym, vt, want_vectors=True, first=None, second=None) -> Eigensystem:
+    if p.itype == 4:
+        # stab.f90:61-67: itype becomes 2 before fd_spatial runs
+        ms = fd_mean_state(p, ym, vt, first, second)
+        es = spatial_solve(p, ms, want_vectors, fd_spatial_operators(p, ms))
+        es.params = dataclasses.replace(p, itype=2)
+        return es
     if p.itype == 3:
         # stab.f90:56-60: itype becomes 1 before fd_temporal runs, so evec.dat says 1
         es = fd_temporal_solve(p, fd_mean_state(p, ym, vt, first, second), want_vectors)

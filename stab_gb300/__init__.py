@@ -94,7 +94,7 @@ class StabParams(ctypes.Structure):
         return 5 * self.ny
 
     def m(self) -> int:
-        return 2 * self.n() if self.itype == 2 else self.n()
+        return 2 * self.n() if self.itype in (2, 4) else self.n()
 
 
 class Sweep(ctypes.Structure):
@@ -477,7 +477,7 @@ class Context:
         """Dense operators: [A0, B0] (temporal) or [C0, C1, C2] (spatial)."""
         prof = _prof(profile)
         n = p.n()
-        k = 2 if p.itype == 1 else 3
+        k = 3 if p.itype in (2, 4) else 2
         out = np.zeros(k * n * n, dtype=np.complex128)
         self._check(self.lib.stab_assemble(self.h, ctypes.byref(p), prof.shape[0], _dptr(prof),
                                            _dptr(out.view(np.float64))))

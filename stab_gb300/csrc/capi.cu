@@ -143,10 +143,14 @@ static void drain_stats(stab_ctx* c) {
   c->pending.clear();
 }
 
+// itype 2 (Chebyshev) and 4 (finite differences) are spatial
+static inline bool is_spatial(int itype) { return itype == 2 || itype == 4; }
+
 // Derivative tables, built once per context, by key: ny for the Chebyshev
 // D1 and D1 D1; kFdOpKey + ny for the finite-difference operator's stencil
-// matrices; kFdMeanKey + ny for grad.f90's matrix G and G G.
-static const int kFdOpKey = 1 << 20, kFdMeanKey = 2 << 20;
+// matrices (temporal), kFdSpKey + ny for the spatial ones; kFdMeanKey + ny
+// for grad.f90's matrix G and G G.
+static const int kFdOpKey = 1 << 20, kFdMeanKey = 2 << 20, kFdSpKey = 3 << 20;
 
 // stencils.f90:9-120, the reference's coefficient table (values as written there)
 static const double kGa[4] = {8.333333333333333333333E-02, -6.666666666666666666667E-01, 6.666666666666666666667E-01,
@@ -198,6 +202,29 @@ static void fd_operator_tables(int ny, std::vector<double>& F1, std::vector<doub
   for (int t = 0; t < 5; ++t) f2(i, i - 3 + t, kDb[4 - t]);
 }
 
+// The spatial solver's stencil matrices (fd_spatial.f90:668-1160): rows
+// 0-3 and the central rows as above, the central rows running to ny-3, row
+// ny-2 the biased (-1, 6, -18, 10, 3)/12 with the mirrored db, row ny-1 the
+// one-sided (3, -16, 36, -48, 25)/12 of the top = 1 continuity rows.
+static void fd_spatial_tables(int ny, std::vector<double>& F1, std::vector<double>& F2) {
+  const double dy = 1.0 / (double)(ny - 1);
+  F1.assign((size_t)ny * ny, 0.0);
+  F2.assign((size_t)ny * ny, 0.0);
+  auto f1 = [&](int i, int j, double v) { F1[(size_t)i * ny + j] = v / dy; };
+  auto f2 = [&](int i, int j, double v) { F2[(size_t)i * ny + j] = v / (dy * dy); };
+  for (int t = 0; t < 6; ++t) { f1(0, t, kGg[t]); f1(1, t, kGh[t]); f1(2, t, kGi[t]); f1(3, t, kGj[t]); }
+  for (int t = 0; t < 5; ++t) { f2(0, t, kDd[t]); f2(1, t, kDb[t]); f2(2, t, kDa[t]); f2(3, 1 + t, kDa[t]); }
+  for (int i = 4; i < ny - 2; ++i) {
+    f1(i, i - 2, kGa[0]); f1(i, i - 1, kGa[1]); f1(i, i + 1, kGa[2]); f1(i, i + 2, kGa[3]);
+    for (int t = 0; t < 5; ++t) f2(i, i - 2 + t, kDa[t]);
+  }
+  const double b5[5] = {-1.0, 6.0, -18.0, 10.0, 3.0}, t5[5] = {3.0, -16.0, 36.0, -48.0, 25.0};
+  int i = ny - 2;
+  for (int t = 0; t < 5; ++t) { f1(i, i - 3 + t, b5[t] / 12.0); f2(i, i - 3 + t, kDb[4 - t]); }
+  i = ny - 1;
+  for (int t = 0; t < 5; ++t) f1(i, i - 4 + t, t5[t] / 12.0);
+}
+
 // grad.f90:62-86 as a matrix G (fourth-order five-point stencils, one-sided
 // and biased at both ends, over 12 deta), and G G.
 static void fd_mean_tables(int ny, std::vector<double>& G, std::vector<double>& GG) {
@@ -224,7 +251,8 @@ static int ensure_dtab(stab_ctx* c, int key) {
   if (key >= kFdOpKey) {
     const int ny = key & (kFdOpKey - 1);
     std::vector<double> T1, T2;
-    if (key >= kFdMeanKey) fd_mean_tables(ny, T1, T2);
+    if (key >= kFdSpKey) fd_spatial_tables(ny, T1, T2);
+    else if (key >= kFdMeanKey) fd_mean_tables(ny, T1, T2);
     else fd_operator_tables(ny, T1, T2);
     double *D1 = nullptr, *D2 = nullptr;
     CK(c, cudaMalloc(&D1, sizeof(double) * ny * ny));
@@ -533,16 +561,17 @@ static bool calch_scalars(double s, double out[8]) {
 // Descriptor of one instance from its run parameters (validated) and the
 // entry of its mean profile in the profile pools.
 static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDesc& pd, InstDesc& d) {
-  if (q.itype != 1 && q.itype != 2 && q.itype != 3)
-    return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal), 2 (spatial) or 3 (temporal, finite differences)");
-  const bool fd = (q.itype == 3);
-  if (fd && q.ny < 10) return set_err(c, STAB_ERR_ARG, "the finite-difference solver needs ny >= 10");
+  if (q.itype < 1 || q.itype > 4)
+    return set_err(c, STAB_ERR_ARG, "itype must be 1 (temporal), 2 (spatial), 3 or 4 (the same by finite differences)");
+  const bool fd = (q.itype == 3 || q.itype == 4);
+  const bool spat = (q.itype == 2 || q.itype == 4);
+  if (fd && q.ny < 10) return set_err(c, STAB_ERR_ARG, "the finite-difference solvers need ny >= 10");
   if (fd && !(q.yi != 0.0 && q.ymax > 2.0 * q.yi))
     return set_err(c, STAB_ERR_ARG, "the finite-difference grid (ogengrid) needs Yi != 0 and Ymax > 2 Yi");
   if (q.ny < 4 || q.ny > 400) return set_err(c, STAB_ERR_ARG, "ny out of range [4, 400]");
-  if (q.itype == 2 && q.curve != 0 && q.curve != 1 && q.curve != 2)
+  if (spat && q.curve != 0 && q.curve != 1 && q.curve != 2)
     return set_err(c, STAB_ERR_ARG, "curve must be 0, 1 or 2");
-  if (q.itype == 2 && q.curve == 1 && q.x != -1.0 && !(q.x > 0.0))
+  if (spat && q.curve == 1 && q.x != -1.0 && !(q.x > 0.0))
     return set_err(c, STAB_ERR_ARG, "curve = 1 needs an arc length x > 0 (or -1, no curvature)");
   if (q.ider != 0 && q.ider != 1) return set_err(c, STAB_ERR_ARG, "ider must be 0 or 1");
   if (q.wallt != 0 && q.wallt != 2) return set_err(c, STAB_ERR_ARG, "Illegal value of wallt");
@@ -552,7 +581,7 @@ static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDes
   d = InstDesc{};
   d.ny = q.ny;
   d.n = 5 * q.ny;
-  d.itype = fd ? 1 : q.itype;
+  d.itype = spat ? 2 : 1;
   d.fd = fd ? 1 : 0;
   d.m = (d.itype == 1) ? d.n : 2 * d.n;
   d.wallt = q.wallt;
@@ -575,7 +604,9 @@ static int make_desc(stab_ctx* c, const stab_params& q, int iprof, const ProfDes
   d.ider = q.ider;
   // spatial.f90:110-125: the temporal solver has no wall metric; x = -1
   // turns curvature off (calch.f90:31-39, circh.f90:46-53)
-  d.curved = (q.itype == 2 && (q.curve == 1 || q.curve == 2) && q.x != -1.0) ? 1 : 0;
+  // the finite-difference spatial solver has calch's metric only
+  // (fd_spatial.f90:108-116): curve = 2 is a flat wall there
+  d.curved = (spat && (q.curve == 1 || (q.curve == 2 && !fd)) && q.x != -1.0) ? 1 : 0;
   if (d.curved && q.curve == 2) circh_scalars(q.x, d.cw);
   if (d.curved && q.curve == 1 && !calch_scalars(q.x, d.cw))
     return set_err(c, STAB_ERR_ARG, "curve = 1: false position found no wall point in 30 steps (the reference's "
@@ -592,7 +623,8 @@ static int batch_finish(stab_ctx* c, stab_batch* b) {
   int64_t node_off = 0, blk_off = 0, vec_off = 0;
   b->tcount = 0;
   for (auto& d : b->hd) {
-    const int kop = d.fd ? kFdOpKey + d.ny : d.ny, kmean = d.fd ? kFdMeanKey + d.ny : d.ny;
+    const int kop = d.fd ? (d.itype == 2 ? kFdSpKey : kFdOpKey) + d.ny : d.ny;
+    const int kmean = d.fd ? kFdMeanKey + d.ny : d.ny;
     for (int key : {kop, kmean})
       if (std::find(tab_ny.begin(), tab_ny.end(), key) == tab_ny.end()) tab_ny.push_back(key);
     d.off_node = node_off;
@@ -615,7 +647,7 @@ static int batch_finish(stab_ctx* c, stab_batch* b) {
     hdt.push_back(kv.second.second);
   }
   for (auto& d : b->hd) {
-    d.dmat = tab_index[d.fd ? kFdOpKey + d.ny : d.ny];
+    d.dmat = tab_index[d.fd ? (d.itype == 2 ? kFdSpKey : kFdOpKey) + d.ny : d.ny];
     d.dmean = tab_index[d.fd ? kFdMeanKey + d.ny : d.ny];
   }
   // offsets
@@ -701,8 +733,8 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   b->coarse_ny = c->seed_ny;
   std::vector<int> idx(count);
   for (int i = 0; i < count; ++i) idx[i] = i;
-  // temporal (itype 1 and 3) before spatial
-  std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return (p[a].itype == 2) < (p[bb].itype == 2); });
+  // temporal (itype 1 and 3) before spatial (2 and 4)
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int bb) { return is_spatial(p[a].itype) < is_spatial(p[bb].itype); });
   b->perm = idx;
   // profiles: dedupe by pointer; copied straight from caller memory in
   // contiguous runs (validated on the device by k_spline).  With ider = 0 a
@@ -1260,7 +1292,7 @@ static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullpt
 static void finalize_polish_host(std::vector<zc>& val, std::vector<int32_t>& st, const std::vector<int32_t>& dn,
                                  const std::vector<stab_params>& P) {
   for (size_t k = 0; k < val.size(); ++k) {
-    if (P[k].itype == 2) {
+    if (P[k].itype == 2 || P[k].itype == 4) {
       zc l = val[k];
       double d = l.x * l.x + l.y * l.y;
       val[k] = d > 0 ? zmk(l.x / d, -l.y / d) : zmk(0.0, 0.0);
@@ -1312,7 +1344,7 @@ static int batch_run(stab_batch* b, int32_t mode) {
     for (int k = 0; k < b->count; ++k) {
       const int u = b->perm[k];
       zc a = zmk(b->seeds[2 * u], b->seeds[2 * u + 1]);
-      if (b->P[k].itype == 2) {
+      if (b->P[k].itype == 2 || b->P[k].itype == 4) {
         double d = a.x * a.x + a.y * a.y;
         a = d > 0 ? zmk(a.x / d, -a.y / d) : zmk(0.0, 0.0);
       }
@@ -1674,7 +1706,7 @@ static int run_fallback(stab_batch* b, bool track = false) {
       pidx[q] = j;
       pick_val[q] = e[j];
       zc r = e[j];
-      if (fb->P[q].itype == 2) {
+      if (fb->P[q].itype == 2 || fb->P[q].itype == 4) {
         const double dd = r.x * r.x + r.y * r.y;
         r = dd > 0 ? zmk(r.x / dd, -r.y / dd) : zmk(0.0, 0.0);
       }
@@ -1784,7 +1816,7 @@ int stab_batch_run(stab_batch* b, int32_t mode) {
       for (int k = 0; k < b->count; ++k) {
         const int u = b->perm[k];
         zc a = zmk(b->seeds[2 * u], b->seeds[2 * u + 1]);
-        if (b->P[k].itype == 2) {
+        if (b->P[k].itype == 2 || b->P[k].itype == 4) {
           const double d = a.x * a.x + a.y * a.y;
           a = d > 0 ? zmk(a.x / d, -a.y / d) : zmk(0.0, 0.0);
         }
@@ -2293,9 +2325,9 @@ int stab_assemble(stab_ctx* c, const stab_params* p, int32_t nym, const double* 
   const Range r{0, 1};
   const int kinds_t[2] = {OP_T_A0, OP_T_B0};
   const int kinds_s[3] = {OP_S_C0, OP_S_C1, OP_S_C2};
-  const int nk = (p->itype != 2) ? 2 : 3;
+  const int nk = is_spatial(p->itype) ? 3 : 2;
   for (int q = 0; q < nk; ++q) {
-    const int kd = (p->itype != 2) ? kinds_t[q] : kinds_s[q];
+    const int kd = is_spatial(p->itype) ? kinds_s[q] : kinds_t[q];
     rc = node_ops(b, r, kd, kd, nullptr);
     if (rc) return rc;
     rc = dense<zc>(b, r, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z");
@@ -2311,9 +2343,9 @@ int stab_eigenvectors(stab_ctx* c, const stab_params* p, int32_t nym, const doub
                       const double* eig, double* vec_out, int32_t* status_out) {
   if (!c || !p || !profile || !eig || !vec_out || count < 0) return set_err(c, STAB_ERR_ARG, "null argument");
   if (count == 0) return STAB_OK;
-  if (p->itype != 1 && p->itype != 2 && p->itype != 3) return set_err(c, STAB_ERR_ARG, "itype must be 1, 2 or 3");
+  if (p->itype < 1 || p->itype > 4) return set_err(c, STAB_ERR_ARG, "itype must be 1, 2, 3 or 4");
   cudaSetDevice(c->device);
-  const bool spatial = (p->itype == 2);
+  const bool spatial = is_spatial(p->itype);
   const int64_t mlen = (int64_t)(spatial ? 10 : 5) * p->ny;
   const zc* ev = reinterpret_cast<const zc*>(eig);
   // copies of the instance, one per eigenvalue, in chunks that bound memory

@@ -265,15 +265,14 @@ static int parse_protocol(const char* text, stab_params* p, stab_sweep* sw, char
     }
     return STAB_OK;
   }
-  if (p->itype != 1 && p->itype != 2 && p->itype != 3) {
+  if (p->itype < 1 || p->itype > 4) {
     set_msg(msg, msg_cap, "itype " + std::to_string(p->itype) +
-                              (sw ? " (finite-difference spatial, Stokes or bump solver)" :
-                                    " (finite-difference spatial, Stokes, bump or multi-point driver)") +
+                              (sw ? " (Stokes or bump solver)" : " (Stokes, bump or multi-point driver)") +
                               " is outside the temporal/spatial path");
     return STAB_ERR_ARG;
   }
-  // itype 3: the finite-difference temporal solver, same questions as the
-  // Chebyshev one (stab.f90:56-60)
+  // itypes 3 and 4: the finite-difference solvers, with the questions of
+  // the Chebyshev ones (stab.f90:56-67)
   if (p->itype == 1 || p->itype == 3) {
     if (!reals(2, p->alpha, "alphar, alphai")) return STAB_ERR_ARG;
   } else {
@@ -281,7 +280,7 @@ static int parse_protocol(const char* text, stab_params* p, stab_sweep* sw, char
   }
   if (!reals(2, p->beta, "betar, betai")) return STAB_ERR_ARG;
   if (!ints(1, &p->ind, "index")) return STAB_ERR_ARG;
-  if (p->itype == 2 && !reals(1, &p->x, "x")) return STAB_ERR_ARG;
+  if ((p->itype == 2 || p->itype == 4) && !reals(1, &p->x, "x")) return STAB_ERR_ARG;
   if (p->ny < 2) {
     set_msg(msg, msg_cap, "ny < 2");
     return STAB_ERR_ARG;
@@ -524,12 +523,12 @@ int stab_grid(int32_t ny, double yi, double ymax, double* y, double* eta, double
 
 int stab_write_evec(const char* path, const stab_params* p, const double* eig, const double* vec) {
   if (!path || !p || !eig || p->ny < 2) return STAB_ERR_ARG;
-  if (p->itype != 1 && p->itype != 2 && p->itype != 3) return STAB_ERR_ARG;
+  if (p->itype < 1 || p->itype > 4) return STAB_ERR_ARG;
   const int ny = p->ny;
-  // itype 3 (finite differences) is temporal, recorded as 1 (stab.f90:59),
-  // with ogengrid's grid (fd_temporal.f90:1052-1055)
-  const bool fd = (p->itype == 3);
-  const int32_t itype = fd ? 1 : p->itype;
+  // itypes 3 and 4 (finite differences) are recorded as 1 and 2
+  // (stab.f90:59, :66), with ogengrid's grid (fd_temporal.f90:1052-1055)
+  const bool fd = (p->itype == 3 || p->itype == 4);
+  const int32_t itype = (p->itype == 3) ? 1 : (p->itype == 4 ? 2 : p->itype);
   const int64_t nmax = (int64_t)(itype == 1 ? 1 : 2) * kNdof * ny;
   const bool want_vec = (itype == 1 || p->ievec == 1);
   if (want_vec && !vec) return STAB_ERR_ARG;

@@ -829,7 +829,23 @@ __global__ void k_blocks(int count, const InstDesc* __restrict__ desc, const dou
       for (int v = 0; v < 5; ++v) { P1[0][v] = Bh0[0][v]; P3[0][v] = Dh0[0][v]; Q1[0][v] = Bh1[0][v]; Q3[0][v] = Dh1[0][v]; }
       P3[0][0] = zsub(P3[0][0], iom);
       for (int e = 1; e < 4; ++e) P3[e][e] = zmk(-1.0, 0.0);
-      if (d.wallt == 2) {
+      if (d.fd && d.wallt == 2) {
+        // fd_spatial.f90:697-750, 994-1025, 1164-1171: the wall energy row,
+        // its temperature column without the first-derivative term, and
+        // the -i omega G term taken from the G of the node the assembly
+        // loops leave behind (ny-1 with top = 1, else ny-2, 0-based here)
+        Blocks bq;
+        const int gq = (d.top == 1) ? ny - 1 : ny - 2;
+        node_blocks(d, node + d.off_node + (size_t)NODE_STRIDE * gq, true, bq);
+        for (int v = 0; v < 5; ++v) {
+          P1[4][v] = (v < 4) ? Bh0[4][v] : z0;
+          P2[4][v] = zmk(Vy[4][v], 0.0);
+          P3[4][v] = zsub(Dh0[4][v], zscale(iom, bq.G[4][v]));
+          Q1[4][v] = (v < 4) ? Bh1[4][v] : z0;
+          Q3[4][v] = Dh1[4][v];
+          R3[4][v] = zmk(b.Vxx[4][v], 0.0);
+        }
+      } else if (d.wallt == 2) {
         for (int v = 0; v < 4; ++v) {
           P1[4][v] = Bh0[4][v]; P2[4][v] = zmk(Vy[4][v], 0.0); P3[4][v] = Dh0[4][v];
           Q1[4][v] = Bh1[4][v]; Q3[4][v] = Dh1[4][v];

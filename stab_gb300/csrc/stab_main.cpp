@@ -199,13 +199,14 @@ int main(int argc, char** argv) {
   stab_ctx* ctx = nullptr;
   rc = stab_create(&ctx, device);
   if (rc) return fail("stab_create", rc, nullptr);
-  const int64_t m = (int64_t)(p.itype != 2 ? 5 : 10) * p.ny;
+  const bool spatial = (p.itype == 2 || p.itype == 4);
+  const int64_t m = (int64_t)(spatial ? 10 : 5) * p.ny;
   std::vector<double> eig(2 * m);
   int32_t least = -1, status = 0;
   rc = stab_full_spectrum(ctx, &p, nym, prof.data(), eig.data(), nullptr, &least, &status);
   if (rc) return fail("stab_full_spectrum", rc, ctx);
   std::vector<double> vec;
-  const bool want_vec = (p.itype != 2 || p.ievec == 1);
+  const bool want_vec = (!spatial || p.ievec == 1);
   if (want_vec) {
     vec.resize(2 * m * m);
     std::vector<int32_t> st(m);
@@ -216,7 +217,7 @@ int main(int argc, char** argv) {
   rc = stab_write_evec(out.c_str(), &p, eig.data(), want_vec ? vec.data() : nullptr);
   if (rc) return fail("stab_write_evec", rc, ctx);
   if (least >= 0)
-    std::printf("least-stable %s = (%.15e, %.15e)  index %d of %lld  status %d\n", p.itype != 2 ? "omega" : "alpha",
+    std::printf("least-stable %s = (%.15e, %.15e)  index %d of %lld  status %d\n", spatial ? "alpha" : "omega",
                 eig[2 * least], eig[2 * least + 1], least + 1, (long long)m, status);
   else
     std::printf("no eigenvalue passed the least-stable filter (status %d)\n", status);

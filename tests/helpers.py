@@ -112,7 +112,7 @@ def select_least(eig: np.ndarray, d: dict) -> int:
         if not np.isfinite(x):
             continue
         ax = abs(x)
-        if d["itype"] != 2:
+        if d["itype"] in (1, 3):
             if not ax > 1e-12 or ax > cmax * kabs:
                 continue
             key = x.imag

@@ -65,7 +65,7 @@ def test_parse_input_list_directed_rules():
 
 @pytest.mark.parametrize("text,needle", [
     ("0\n0.3 1000 1\n32 1 0\n1\n1\n0 0 0 0\n5\n0.1 0\n0 0\n0\n", "outside"),
-    ("0\n0.3 1000 1\n32 1 0\n1\n1\n0 0 0 0\n4\n0.1 0\n0 0\n0\n", "outside"),
+    ("0\n0.3 1000 1\n32 1 0\n1\n1\n0 0 0 0\n6\n0.1 0\n0 0\n0\n", "outside"),
     ("0\n0.3 1000 1\n32 1 0\n1\n1\n0 0 0 0\n2\n0.1 0\n", "beta"),
     ("0\n0.3 x 1\n", "bad real"),
 ])
@@ -174,9 +174,12 @@ def test_getevec_tool_on_oracle_system_reproduces_golden(tmp_path):
     assert _ndiff(out, _text("space1.ref"), 1e-8)
 
 
-def test_parse_fd_temporal_input():
-    """itype 3 (the finite-difference temporal solver, stab.f90:56-60) asks
-    the temporal questions: alpha, beta, index."""
+def test_parse_fd_inputs():
+    """itypes 3 and 4 (the finite-difference solvers, stab.f90:56-67) ask
+    the temporal and the spatial questions: alpha or omega, beta, index, and
+    x for the spatial one."""
     p = sg.parse_input("0\n0.3 1000 1\n128 1.0 50.0\n1\n1\n0 0 0 0\n3\n0.30862069, 0\n0 0\n0\n")
     assert p.itype == 3 and p.ny == 128 and p.ind == 0
     assert complex(*p.alpha) == 0.30862069 and complex(*p.beta) == 0
+    p = sg.parse_input("0\n0.3 1000 1\n128 1.0 50.0\n1\n1\n0 0 0 1\n4\n0.08 0\n0 0\n0\n2.5\n")
+    assert p.itype == 4 and p.curve == 1 and p.x == 2.5 and complex(*p.omega) == 0.08

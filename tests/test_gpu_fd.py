@@ -75,7 +75,7 @@ def test_fd_full_spectrum_matches_oracle(ctx, which):
     if which == "ts":
         j, jo = so.getevec_select(eig, TS_GUESS), so.getevec_select(es.eig, TS_GUESS)
         assert abs(eig[j] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
-        assert abs(es.eig[jo] - TS_GUESS) / abs(TS_GUESS) < 1e-6
+        assert abs(es.eig[jo] - TS_GUESS) / abs(TS_GUESS) < 1e-5     # the N = 96 discretisation error
 
 
 def test_fd_polish_and_coarse_modes(ctx):
@@ -124,7 +124,7 @@ def test_fd_cli_writes_evec_and_eigenfunction(tmp_path):
     assert np.array_equal(y, yo)
     es = H.oracle_solve(_ts_case(N), H.ts_profile())
     jo = so.getevec_select(es.eig, TS_GUESS)
-    g = es.eig[jo]
+    g = complex(es.eig[jo])
     r = subprocess.run([os.path.join(BIN, "getevec_gpu"), "-v"], cwd=tmp_path, capture_output=True, text=True,
                        input=f"evec.dat\n{g.real!r} {g.imag!r}\n0 0\n", timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -132,3 +132,68 @@ def test_fd_cli_writes_evec_and_eigenfunction(tmp_path):
     want = [ln.split() for ln in so.eigfunction_text(es, jo).splitlines() if ln.strip() and not ln.startswith("#")]
     assert len(got) == len(want) == N
     assert max(abs(float(a) - float(b)) for u, v in zip(got, want) for a, b in zip(u, v)) <= 1e-8
+
+
+def _ts_spatial(N, **kw):
+    d = _ts_case(N, itype=4, alpha=[0.0, 0.0], omega=[0.08, 0.0])
+    d.update(kw)
+    return d
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(top=1), dict(wallt=2), dict(wallt=2, top=1), dict(curve=1, x=5.0),
+                                dict(curve=2, x=500.0)])
+def test_fd_spatial_assemble_matches_oracle(ctx, kw):
+    """C0, C1, C2 of fd_spatial.f90 for both free-stream conditions, both
+    wall temperature conditions (with the wall energy row's G from another
+    node, as the reference writes it), calch's curvature, and curve = 2,
+    which this solver treats as a flat wall."""
+    d = _ts_spatial(24, **kw)
+    prof = H.ts_profile()
+    mats = ctx.assemble(H.stab_params(d), prof)
+    p = H.oracle_params(d)
+    vt = prof[:, 1:6].copy()
+    vt[:, 2] = 0.0
+    ms = so.fd_mean_state(p, prof[:, 0], vt)
+    for a, b in zip(mats, so.fd_spatial_operators(p, ms)):
+        assert _mat_close(a, b) < 1e-12
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(wallt=2, top=1)])
+def test_fd_spatial_full_spectrum_and_polish(ctx, kw):
+    d = _ts_spatial(64, **kw)
+    prof = H.ts_profile()
+    eig, vec, li, st = ctx.full_spectrum(H.stab_params(d), prof, want_vector=True)
+    es = H.oracle_solve(d, prof)
+    assert eig.size == 10 * d["ny"]
+    g = 2.2804739411185E-001 - 6.5163146952733E-003j
+    j, jo = so.getevec_select(eig, g), so.getevec_select(es.eig, g)
+    assert abs(eig[j] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    lo = H.select_least(es.eig, d)
+    assert li >= 0 and lo >= 0
+    assert abs(eig[li] - es.eig[lo]) / abs(es.eig[lo]) < EIG_REL
+    assert np.max(np.abs(H.phase_normalize(vec) - H.phase_normalize(es.evec[:, lo]))) < VEC_ABS
+    w, err, iters, status, vecs = ctx.solve_batch([H.stab_params(d)], [prof], sg.MODE_SEEDED,
+                                                  seeds=[es.eig[jo] * (1 + 1e-7)], want_vectors=True)
+    assert status[0] == sg.ST_OK, (status, err, iters)
+    assert abs(w[0] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
+    assert np.max(np.abs(H.phase_normalize(vecs[0]) - H.phase_normalize(es.evec[:, jo]))) < VEC_ABS
+
+
+def test_fd_spatial_cli_evec(tmp_path):
+    """stab_gpu < input with itype 4: evec.dat records itype 2, the x read
+    after the index, and ogengrid's grid."""
+    N = 32
+    with open(tmp_path / "profile.0", "w") as fh:
+        for r in H.ts_profile():
+            fh.write(" ".join(repr(float(v)) for v in r) + "\n")
+    text = "0\n0.3 1000 1\n%d 1.0 50.0\n1\n1\n0 0 0 0\n4\n0.08, 0\n0 0\n0\n123.5\n" % N
+    r = subprocess.run([os.path.join(BIN, "stab_gpu")], cwd=tmp_path, input=text, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    h, y, eig, vec = sg.read_evec(str(tmp_path / "evec.dat"))
+    assert h.itype == 2 and h.ny == N and h.x == 123.5
+    assert np.array_equal(y, sg.fd_grid(N, 1.0, 50.0)[0])
+    es = H.oracle_solve(_ts_spatial(N), H.ts_profile(), want_vectors=False)
+    g = 2.2804739411185E-001 - 6.5163146952733E-003j
+    j, jo = so.getevec_select(eig, g), so.getevec_select(es.eig, g)
+    assert abs(eig[j] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL

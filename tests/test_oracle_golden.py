@@ -164,3 +164,32 @@ def test_oracle_fd_temporal_converges_to_the_spectral_adiabatic_solution():
     # the grid: uniform eta from the wall, y(0) = 0, y(1) = ymax
     y, eta, deta, d2eta, dy = so.ogengrid(33, 1.0, 50.0)
     assert y[0] == 0.0 and abs(y[-1] - 50.0) < 1e-12 and abs(eta[1] - 1.0 / 32) < 1e-15
+
+
+def test_oracle_fd_spatial_converges_to_the_spectral_solution():
+    """Finite-difference spatial solver (itype 4, fd_spatial.f90), thesis
+    TStest case at omega = 0.08 (its spatial TS mode, README.md), Ymax = 50:
+    with the isothermal wall (wallt = 0) and either free-stream condition it
+    converges at fourth order to the Chebyshev solver's TS alpha (pinned to
+    the reference's golden files): within 2e-7 at N = 128 and 3e-8 at
+    N = 192, the error falling more than 10x from N = 64 to N = 128.  (With
+    wallt = 2 it does not: its wall energy row takes G from another node, a
+    quirk the restatement keeps.)"""
+    prof = H.ts_profile()
+    ym, vt = prof[:, 0].copy(), prof[:, 1:6].copy()
+    vt[:, 2] = 0.0
+    g = 2.2804739411185E-001 - 6.5163146952733E-003j
+    for top in (0, 1):
+        base = dict(mattyp=0, T0=0.0, Ma=0.3, Re=1000.0, Pr=1.0, yi=1.0, ymax=50.0, ievec=1, ider=1, top=top,
+                    wall=0, wallt=0, curve=0, alpha=0j, beta=0j, omega=0.08 + 0j)
+        spec = so.solve(so.StabParams(ny=96, itype=2, **base), ym, vt, want_vectors=False)
+        ref = spec.eig[so.getevec_select(spec.eig, g)]     # the same TS mode on this grid (Ymax = 50)
+        err = {}
+        for N in (64, 128) if top else (64, 128, 192):
+            es = so.solve(so.StabParams(ny=N, itype=4, **base), ym, vt, want_vectors=False)
+            assert es.params.itype == 2                     # stab.f90:66: recorded as spatial
+            w = es.eig[so.getevec_select(es.eig, ref)]
+            err[N] = abs(w - ref) / abs(ref)
+        assert err[128] < 2.5e-7 and err[128] < err[64] / 10, err
+        if 192 in err:
+            assert err[192] < 3e-8, err

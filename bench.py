@@ -62,7 +62,9 @@ def hbm_peak():
             return float(json.load(fh)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
     except (OSError, KeyError, ValueError):
         return HBM_FALLBACK_GBS, "fallback 6.8 TB/s"
-COARSE_TRAFFIC_PER_INSTANCE = (25.59e9 + 21.59e9) / 512
+# DRAM bytes per instance of the seed eigensolve, ncu at 1024 instances
+# (profiles/k_eig_plain_dw_seed_traffic_1024.md: 47.85 GB read + 41.36 GB written)
+COARSE_TRAFFIC_PER_INSTANCE = (47.85e9 + 41.36e9) / 1024
 # kernel -> (work key of Batch.work(), bound, what the algorithmic count is)
 KERNEL_WORK = {
     "k_eig_plain": ("eig_fp64", "fp64", "FP64 flops counted by the kernel (Householder reduction + QR sweeps)"),
@@ -640,11 +642,10 @@ def main():
                             "frac_of_bf16_tensor_peak": ach / bf16_peak()[0] if bf16_peak() else None}
     if "k_eig_plain_coarse" in rooflines:
         # DRAM bytes per launch from the committed ncu capture of the same kernel
-        # (profiles/k_eig_plain_coarse_n32_512.md: 47.18 GB for 512 instances),
-        # scaled by the instances of this launch (traffic grows with the
-        # resident working matrices, one per instance)
+        # at 1024 instances, scaled by the instances of this launch (the
+        # per-instance traffic is the same at 512 and 1024)
         rooflines["k_eig_plain_coarse"]["traffic"] = COARSE_TRAFFIC_PER_INSTANCE * args.count
-        rooflines["k_eig_plain_coarse"]["traffic_unit"] = "bytes per launch (ncu capture at 512, scaled)"
+        rooflines["k_eig_plain_coarse"]["traffic_unit"] = "bytes per launch (ncu capture at 1024, scaled)"
     roof = rooflines.get(dname, {"bound": "unknown", "kernel": dname, "achieved": None, "peak": None,
                                  "unit": None, "frac": None, "traffic": None})
     h2d = int(prof.nbytes + len(sp) * 120 + len(sp) * 4)

@@ -560,6 +560,9 @@ def main():
         # the occupancy's four (1 and 2 measured slower still)
         variants["eig_resident_3_per_sm_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_RESIDENT, 3),
                                                           lambda: ctx.set_option(sg.OPT_EIG_RESIDENT, 0))
+        # 64-thread eigensolver CTAs, eight per SM
+        variants["eig_64_thread_ctas_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_THREADS, 64),
+                                                       lambda: ctx.set_option(sg.OPT_EIG_THREADS, 128))
         # seed spectra at another N: a batch of its own (the seed size applies
         # to batches created afterwards), timed and checked like the default
         for sny in (28,):

@@ -189,6 +189,11 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     finishes one); 0 (default): as many as the occupancy allows (four).
  *     Bit-identical eigenvalues for every value. */
 #define STAB_OPT_EIG_RESIDENT 3
+/*   STAB_OPT_EIG_THREADS  128 (default): the batch eigensolver runs 128-
+ *     thread CTAs, four per SM; 64: 64-thread CTAs, eight per SM (twice the
+ *     instances in flight).  The same algorithm; block sums run in another
+ *     order, so eigenvalues agree to rounding, not bit for bit. */
+#define STAB_OPT_EIG_THREADS 4
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,

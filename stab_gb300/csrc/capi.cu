@@ -72,6 +72,7 @@ struct stab_ctx {
   int seed_qr_shared = 0;  // STAB_OPT_SEED_QR_SHARED
   int lu_tma = 1;          // STAB_OPT_POLISH_LU_TMA
   int eig_resident = 0;    // STAB_OPT_EIG_RESIDENT
+  int eig_threads = 128;   // STAB_OPT_EIG_THREADS
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -1047,14 +1048,14 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
       int dev = 0, sms = 1;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      grid = sms * c->eig_resident;
+      grid = sms * c->eig_resident * (c->eig_threads == 64 ? 2 : 1);
     }
     return launch_eig_plain(b->count, b->mmax, b->msz.as<int32_t>(), b->Abig.as<zc>(), b->off_m2.as<int64_t>(),
                             b->Hbig.as<zc>(), b->off_m2.as<int64_t>(), b->eigraw.as<zc>(), b->off_mof.as<int64_t>(),
                             b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
                             b->flops.as<double>(), grid, s,
                             c->arith[seed ? STAB_STAGE_SEED_EIG : STAB_STAGE_PLAIN_EIG] == STAB_ARITH_DOUBLE_WORD,
-                            seed && c->seed_qr_shared);
+                            seed && c->seed_qr_shared, c->eig_threads);
   }));
   CK(c, timed(c, "k_post_spectrum", [&] {
     size_t sm = sizeof(zc) * b->mmax;
@@ -2137,6 +2138,12 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   }
   if (option == STAB_OPT_POLISH_LU_TMA) {
     c->lu_tma = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_EIG_THREADS) {
+    if (value != 64 && value != 128) return set_err(c, STAB_ERR_ARG, "eigensolver CTA size must be 64 or 128");
+    c->eig_threads = value;
     c->epoch += 1;
     return STAB_OK;
   }

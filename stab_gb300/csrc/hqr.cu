@@ -68,6 +68,16 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(EIG_PLAIN_ARGS) {
                     s_inst);
 }
 
+// the batch kernel with 64-thread CTAs, eight per SM (more instances in flight)
+template <class C>
+__global__ void __launch_bounds__(HQ_T / 2, 8) k_eig_plain_half(EIG_PLAIN_ARGS) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ HqrSmem<C> s;
+  __shared__ int s_inst;
+  eig_plain_body<C>(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
+                    s_inst);
+}
+
 template <class C>
 __global__ void __launch_bounds__(HQ_WIDE, 1) k_eig_plain_wide(EIG_PLAIN_ARGS) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -105,7 +115,7 @@ template <class C>
 static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
                                 const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
                                 int32_t* work_counter, const int32_t* order, double* flops, int grid,
-                                cudaStream_t s, bool qr_smem) {
+                                cudaStream_t s, bool qr_smem, int threads) {
   size_t sm = eig_plain_smem(mmax);
   cudaError_t e = cudaFuncSetAttribute(k_eig_plain<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -132,6 +142,20 @@ static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, 
                                                    work_counter, order, flops);
     return cudaGetLastError();
   }
+  if (threads == HQ_T / 2) {
+    // persistent grid of 64-thread CTAs
+    e = cudaFuncSetAttribute(k_eig_plain_half<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eig_plain_half<C>, HQ_T / 2, sm) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    const int resident = sms * per_sm;
+    if (grid <= 0 || grid > resident) grid = resident;
+    if (grid > count) grid = count;
+    k_eig_plain_half<C><<<grid, HQ_T / 2, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status,
+                                                  work_counter, order, flops);
+    return cudaGetLastError();
+  }
   // persistent grid: as many CTAs as can be resident at once
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eig_plain<C>, HQ_T, sm) != cudaSuccess || per_sm < 1)
     per_sm = 1;
@@ -146,12 +170,12 @@ static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, 
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
                              const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
                              int32_t* work_counter, const int32_t* order, double* flops, int grid,
-                             cudaStream_t s, bool double_word, bool qr_smem) {
+                             cudaStream_t s, bool double_word, bool qr_smem, int threads) {
   if (count <= 0) return cudaSuccess;
   return double_word ? launch_eig_t<dz>(count, mmax, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
-                                        order, flops, grid, s, qr_smem)
+                                        order, flops, grid, s, qr_smem, threads)
                      : launch_eig_t<zc>(count, mmax, msz, A, a_off, H, h_off, eig, eig_off, status, work_counter,
-                                        order, flops, grid, s, qr_smem);
+                                        order, flops, grid, s, qr_smem, threads);
 }
 
 }  // namespace stab

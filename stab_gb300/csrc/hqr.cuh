@@ -19,5 +19,5 @@ cudaError_t eig_phase_cycles(unsigned long long* out, bool reset);
 cudaError_t launch_eig_plain(int count, int mmax, const int32_t* msz, zc* A, const int64_t* a_off, zc* H,
                              const int64_t* h_off, zc* eig, const int64_t* eig_off, int32_t* status,
                              int32_t* work_counter, const int32_t* order, double* flops, int grid,
-                             cudaStream_t s, bool double_word = false, bool qr_smem = false);
+                             cudaStream_t s, bool double_word = false, bool qr_smem = false, int threads = 0);
 }  // namespace stab

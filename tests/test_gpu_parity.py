@@ -414,3 +414,35 @@ def test_bad_curves_are_rejected(ctx):
             ctx.full_spectrum(H.stab_params(dict(c, curve=curve, x=x)), prof, want_vector=False)
     eig, _, _, st = ctx.full_spectrum(H.stab_params(c), prof, want_vector=False)
     assert eig.size == 160
+
+
+def test_eigensolver_64_thread_ctas_agree(ctx):
+    """STAB_OPT_EIG_THREADS = 64 (eight 64-thread CTAs per SM) gives the same
+    spectra as the default 128-thread CTAs to rounding, FP64 and double-word,
+    and the same coarse-seeded results."""
+    cases = [H.synth_case(1, N, 0.5 + 0.1 * k, 1000.0 + 100 * k, a=0.2)[0] for k, N in enumerate((24, 32, 40))]
+    profs = [H.synth_case(1, c["ny"], c["Ma"], c["Re"], a=0.2)[1] for c in cases]
+    sp = [H.stab_params(c) for c in cases] * 60          # enough instances for the persistent batch grid
+    pr = profs * 60
+    out = {}
+    try:
+        for t in (128, 64):
+            ctx.set_option(sg.OPT_EIG_THREADS, t)
+            b = ctx.batch(sp, pr)
+            b.run(sg.MODE_PLAIN)
+            spec = b.spectra()
+            w, err, it, st, _ = b.results()
+            b.run(sg.MODE_COARSE)
+            wc, _, _, stc, _ = b.results()
+            b.close()
+            out[t] = (spec, w, st, wc, stc)
+    finally:
+        ctx.set_option(sg.OPT_EIG_THREADS, 128)
+    s128, w128, st128, wc128, stc128 = out[128]
+    s64, w64, st64, wc64, stc64 = out[64]
+    assert np.array_equal(st128, st64) and np.array_equal(stc128, stc64)
+    assert np.max(np.abs(w64 - w128) / np.abs(w128)) < 1e-12
+    assert np.max(np.abs(wc64 - wc128) / np.abs(wc128)) < 1e-12
+    for a, b in zip(s128[:3], s64[:3]):
+        for w in a[(np.abs(a) > 0) & (np.abs(a) < 2.0)]:
+            assert np.min(np.abs(b - w)) <= 1e-10 * max(1.0, abs(w)), w

@@ -73,6 +73,7 @@ struct stab_ctx {
   int lu_tma = 1;          // STAB_OPT_POLISH_LU_TMA
   int eig_resident = 0;    // STAB_OPT_EIG_RESIDENT
   int eig_threads = 128;   // STAB_OPT_EIG_THREADS
+  int eig_mid = 0;         // STAB_OPT_EIG_MID
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -1055,7 +1056,7 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
                             b->status.as<int32_t>(), b->counter.as<int32_t>(), b->order.as<int32_t>(),
                             b->flops.as<double>(), grid, s,
                             c->arith[seed ? STAB_STAGE_SEED_EIG : STAB_STAGE_PLAIN_EIG] == STAB_ARITH_DOUBLE_WORD,
-                            seed && c->seed_qr_shared, c->eig_threads);
+                            seed && c->seed_qr_shared, c->eig_mid ? 256 : c->eig_threads);
   }));
   CK(c, timed(c, "k_post_spectrum", [&] {
     size_t sm = sizeof(zc) * b->mmax;
@@ -2138,6 +2139,11 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   }
   if (option == STAB_OPT_POLISH_LU_TMA) {
     c->lu_tma = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_EIG_MID) {
+    c->eig_mid = value ? 1 : 0;
     c->epoch += 1;
     return STAB_OK;
   }

@@ -68,6 +68,16 @@ __global__ void __launch_bounds__(HQ_T, 4) k_eig_plain(EIG_PLAIN_ARGS) {
                     s_inst);
 }
 
+// mid-size batches (at most two instances per SM): 256-thread CTAs, two per SM
+template <class C>
+__global__ void __launch_bounds__(2 * HQ_T, 2) k_eig_plain_mid(EIG_PLAIN_ARGS) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ HqrSmem<C> s;
+  __shared__ int s_inst;
+  eig_plain_body<C>(count, msz, A, a_off, Hp, h_off, eig, eig_off, status, work_counter, order, flops_out, smraw, s,
+                    s_inst);
+}
+
 // the batch kernel with 64-thread CTAs, eight per SM (more instances in flight)
 template <class C>
 __global__ void __launch_bounds__(HQ_T / 2, 8) k_eig_plain_half(EIG_PLAIN_ARGS) {
@@ -140,6 +150,14 @@ static cudaError_t launch_eig_t(int count, int mmax, const int32_t* msz, zc* A, 
     if (e != cudaSuccess) return e;
     k_eig_plain_wide<C><<<count, HQ_WIDE, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status,
                                                    work_counter, order, flops);
+    return cudaGetLastError();
+  }
+  if (threads == 2 * HQ_T && count <= 2 * sms) {
+    // one 256-thread CTA per instance, all resident at once
+    e = cudaFuncSetAttribute(k_eig_plain_mid<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_eig_plain_mid<C><<<count, 2 * HQ_T, sm, s>>>(count, msz, A, a_off, H, h_off, eig, eig_off, status,
+                                                  work_counter, order, flops);
     return cudaGetLastError();
   }
   if (threads == HQ_T / 2) {

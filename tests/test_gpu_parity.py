@@ -416,18 +416,21 @@ def test_bad_curves_are_rejected(ctx):
     assert eig.size == 160
 
 
-def test_eigensolver_64_thread_ctas_agree(ctx):
-    """STAB_OPT_EIG_THREADS = 64 (eight 64-thread CTAs per SM) gives the same
-    spectra as the default 128-thread CTAs to rounding, FP64 and double-word,
-    and the same coarse-seeded results."""
+@pytest.mark.parametrize("option,value,default", [(sg.OPT_EIG_THREADS, 64, 128), (sg.OPT_EIG_MID, 1, 0)])
+def test_eigensolver_cta_sizes_agree(ctx, option, value, default):
+    """STAB_OPT_EIG_THREADS = 64 (eight 64-thread CTAs per SM) and
+    STAB_OPT_EIG_MID (one 256-thread CTA per instance for batches of at most
+    two per SM; 180 instances here) give the same spectra as the default
+    128-thread persistent grid to rounding, FP64 and double-word, and the
+    same coarse-seeded results."""
     cases = [H.synth_case(1, N, 0.5 + 0.1 * k, 1000.0 + 100 * k, a=0.2)[0] for k, N in enumerate((24, 32, 40))]
     profs = [H.synth_case(1, c["ny"], c["Ma"], c["Re"], a=0.2)[1] for c in cases]
     sp = [H.stab_params(c) for c in cases] * 60          # enough instances for the persistent batch grid
     pr = profs * 60
     out = {}
     try:
-        for t in (128, 64):
-            ctx.set_option(sg.OPT_EIG_THREADS, t)
+        for t in (default, value):
+            ctx.set_option(option, t)
             b = ctx.batch(sp, pr)
             b.run(sg.MODE_PLAIN)
             spec = b.spectra()
@@ -437,9 +440,9 @@ def test_eigensolver_64_thread_ctas_agree(ctx):
             b.close()
             out[t] = (spec, w, st, wc, stc)
     finally:
-        ctx.set_option(sg.OPT_EIG_THREADS, 128)
-    s128, w128, st128, wc128, stc128 = out[128]
-    s64, w64, st64, wc64, stc64 = out[64]
+        ctx.set_option(option, default)
+    s128, w128, st128, wc128, stc128 = out[default]
+    s64, w64, st64, wc64, stc64 = out[value]
     assert np.array_equal(st128, st64) and np.array_equal(stc128, stc64)
     assert np.max(np.abs(w64 - w128) / np.abs(w128)) < 1e-12
     assert np.max(np.abs(wc64 - wc128) / np.abs(wc128)) < 1e-12

@@ -563,9 +563,10 @@ def main():
         # 64-thread eigensolver CTAs, eight per SM
         variants["eig_64_thread_ctas_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_THREADS, 64),
                                                        lambda: ctx.set_option(sg.OPT_EIG_THREADS, 128))
-        # 256-thread CTAs for the small N = 48 level batch
-        variants["eig_mid_256_thread_ctas_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_MID, 1),
-                                                            lambda: ctx.set_option(sg.OPT_EIG_MID, 0))
+        # the small N = 48 level batch on the 128-thread persistent grid
+        # instead of the default 256-thread CTAs
+        variants["eig_mid_off_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_MID, 0),
+                                                lambda: ctx.set_option(sg.OPT_EIG_MID, 1))
         # seed spectra at another N: a batch of its own (the seed size applies
         # to batches created afterwards), timed and checked like the default
         for sny in (28,):

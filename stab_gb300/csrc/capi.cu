@@ -73,7 +73,7 @@ struct stab_ctx {
   int lu_tma = 1;          // STAB_OPT_POLISH_LU_TMA
   int eig_resident = 0;    // STAB_OPT_EIG_RESIDENT
   int eig_threads = 128;   // STAB_OPT_EIG_THREADS
-  int eig_mid = 0;         // STAB_OPT_EIG_MID
+  int eig_mid = 1;         // STAB_OPT_EIG_MID
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 

@@ -416,13 +416,13 @@ def test_bad_curves_are_rejected(ctx):
     assert eig.size == 160
 
 
-@pytest.mark.parametrize("option,value,default", [(sg.OPT_EIG_THREADS, 64, 128), (sg.OPT_EIG_MID, 1, 0)])
+@pytest.mark.parametrize("option,value,default", [(sg.OPT_EIG_THREADS, 64, 128), (sg.OPT_EIG_MID, 0, 1)])
 def test_eigensolver_cta_sizes_agree(ctx, option, value, default):
     """STAB_OPT_EIG_THREADS = 64 (eight 64-thread CTAs per SM) and
-    STAB_OPT_EIG_MID (one 256-thread CTA per instance for batches of at most
-    two per SM; 180 instances here) give the same spectra as the default
-    128-thread persistent grid to rounding, FP64 and double-word, and the
-    same coarse-seeded results."""
+    STAB_OPT_EIG_MID (on by default: one 256-thread CTA per instance for
+    batches of at most two per SM; 180 instances here) against the
+    128-thread persistent grid: the same spectra to rounding, FP64 and
+    double-word, and the same coarse-seeded results."""
     cases = [H.synth_case(1, N, 0.5 + 0.1 * k, 1000.0 + 100 * k, a=0.2)[0] for k, N in enumerate((24, 32, 40))]
     profs = [H.synth_case(1, c["ny"], c["Ma"], c["Re"], a=0.2)[1] for c in cases]
     sp = [H.stab_params(c) for c in cases] * 60          # enough instances for the persistent batch grid

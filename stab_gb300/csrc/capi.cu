@@ -1539,7 +1539,14 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
   // instances where it failed or contracted slowly
   CK(c, b->best_src.ensure(sizeof(int32_t) * n, s));
   CK(c, cudaMemsetAsync(b->best_src.p, 0xff, sizeof(int32_t) * n, s));
-  const int rounds = 2 * kShiftCandidates + (extra ? 2 : 0);
+  // At the first candidate level without the surrogate's round, only the
+  // top candidate (its complex64 round and complex128 retry) can make an
+  // instance final: a pair from candidates 1-3 is not trusted there
+  // (k_take_best) and the instance goes to the N = 48 level whatever it
+  // holds, so those rounds are skipped.  The N = 48 level runs them all: its
+  // best pair is kept as STAB_ST_UNVERIFIED.
+  const bool first_level = (b->coarse_ny < kMediumNy) && !extra;
+  const int rounds = first_level ? 2 : 2 * kShiftCandidates + (extra ? 2 : 0);
   for (int r = 0; r < rounds; ++r) {
     const int j = r / 2;
     const bool fp64 = (r & 1) != 0;

@@ -178,9 +178,10 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
 /*   STAB_OPT_POLISH_LU_TMA  1 (default): the tensor-core LU moves each
  *     128 x 64 tile of the trailing matrix between global and shared memory
  *     with tensor (TMA) loads and stores, overlapped with the operand
- *     staging and the MMAs (batches whose orders are all even; odd orders
- *     take the other form); 0: the epilogue reads and writes the tile from
- *     the registers.  Same arithmetic either way. */
+ *     staging and the MMAs (batches larger than two instances per SM whose
+ *     orders are all even; the others take the other form, two CTAs per
+ *     SM); 0: the epilogue reads and writes the tile from the registers.
+ *     Same arithmetic either way. */
 #define STAB_OPT_POLISH_LU_TMA 2
 /*   STAB_OPT_EIG_RESIDENT  k >= 1: the batch eigensolver (seed and plain
  *     spectra of batches larger than half the SM count) keeps at most k

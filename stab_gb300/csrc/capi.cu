@@ -1127,7 +1127,9 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
     }
     if (c64 && c->arith[STAB_STAGE_POLISH_LU] == STAB_ARITH_TF32_SPLIT && lu_tc_fits(b->nmax)) {
       const CUtensorMap* tm = nullptr;
-      if (c->lu_tma && lu_tc_fits(b->nmax, true)) {
+      // TMA tiles hold one CTA per SM; a batch that two CTAs per SM take in
+      // one wave (the N = 48 level) runs the form without them
+      if (c->lu_tma && lu_tc_fits(b->nmax, true) && b->count > 2 * c->sms) {
         if (b->tmaps_state == 0) {
           std::vector<CUtensorMap> maps;
           if (lu_tc_tensor_maps(b->count, b->hn.data(), b->h_n2.data(), b->M32.as<cc>(), maps)) {

@@ -46,6 +46,7 @@ __global__ void k_post_spectrum(int count, const InstDesc* __restrict__ desc, co
   extern __shared__ zc ps[];
   __shared__ double bestv[32];
   __shared__ int besti[32];
+  __shared__ double s_amax;
   const int k = blockIdx.x;
   if (k >= count) return;
   const InstDesc d = desc[k];
@@ -54,12 +55,25 @@ __global__ void k_post_spectrum(int count, const InstDesc* __restrict__ desc, co
   zc* out = eig_sorted + eig_off[k];
   zc* val = ps;  // m
   const bool spatial = (d.itype == 2);
+  double lmax = 0.0;   // largest finite |lambda| of a spatial spectrum
   for (int q = threadIdx.x; q < m; q += blockDim.x) {
     zc l = raw[q];
-    if (spatial) l = (l.x != 0.0 || l.y != 0.0) ? zdiv(zmk(1.0, 0.0), l) : zmk(0.0, 0.0);
+    if (spatial) {
+      const double al = zabs(l);
+      if (isfinite(al)) lmax = fmax(lmax, al);
+      l = (l.x != 0.0 || l.y != 0.0) ? zdiv(zmk(1.0, 0.0), l) : zmk(0.0, 0.0);
+    }
     val[q] = l;
   }
+  for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
+  if ((threadIdx.x & 31) == 0) bestv[threadIdx.x >> 5] = lmax;
   __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) lmax = fmax(lmax, bestv[w]);
+    s_amax = (spatial && lmax > 0.0) ? 1e6 / lmax : INFINITY;
+  }
+  __syncthreads();
+  const double amax = s_amax;
   // stable ascending sort on Im: rank = #{j: key_j < key_q} + #{j < q: key_j == key_q}
   for (int q = threadIdx.x; q < m; q += blockDim.x) {
     const double kq = val[q].y;
@@ -82,7 +96,7 @@ __global__ void k_post_spectrum(int count, const InstDesc* __restrict__ desc, co
     for (int q = threadIdx.x; q < m; q += blockDim.x) {
       const zc x = out[q];
       double key;
-      if (!least_key(d, x, key)) continue;
+      if (!least_key(d, x, key, amax)) continue;
       bool dup = false;
       for (int pp = 0; pp < pass; ++pp) dup |= zabs(zsub(x, out[s_pick[pp]])) <= 1e-6 * zabs(out[s_pick[pp]]);
       if (dup) continue;

@@ -107,6 +107,12 @@ def select_least(eig: np.ndarray, d: dict) -> int:
     cmax = 10.0 * (1.0 + 1.0 / M)
     a, b, w = complex(*d["alpha"]), complex(*d["beta"]), complex(*d["omega"])
     kabs = max(abs(np.sqrt(a * a + b * b)), 1e-3)
+    # spatial spectra: lambda = 1/alpha below 1e-6 max |lambda| is a zero
+    # eigenvalue of the companion matrix at rounding level (large alpha of
+    # arbitrary phase) and is not a candidate
+    eig = np.asarray(eig)
+    fin = eig[np.isfinite(eig) & (eig != 0)]
+    amax = 1e6 * float(np.min(np.abs(fin))) if fin.size else math.inf
     best, bi = -math.inf, -1
     for q, x in enumerate(eig):
         if not np.isfinite(x):
@@ -117,7 +123,7 @@ def select_least(eig: np.ndarray, d: dict) -> int:
                 continue
             key = x.imag
         else:
-            if ax == 0 or not x.real > 0 or abs(x.imag) > x.real or abs(w / x) > cmax:
+            if ax == 0 or not x.real > 0 or abs(x.imag) > x.real or abs(w / x) > cmax or ax > amax:
                 continue
             key = -x.imag
         if key > best:

@@ -168,15 +168,12 @@ def test_fd_spatial_full_spectrum_and_polish(ctx, kw):
     g = 2.2804739411185E-001 - 6.5163146952733E-003j
     j, jo = so.getevec_select(eig, g), so.getevec_select(es.eig, g)
     assert abs(eig[j] - es.eig[jo]) / abs(es.eig[jo]) < EIG_REL
-    if not kw:
-        # with wallt = 2 and top = 1 the companion matrix has exactly singular
-        # directions whose eigenvalues come out at rounding level (alpha ~
-        # 1e14) with arbitrary phase, and the least-stable filter admits some
-        # in either solver: no well-posed least-stable mode to compare there
-        lo = H.select_least(es.eig, d)
-        assert li >= 0 and lo >= 0
-        assert abs(eig[li] - es.eig[lo]) / abs(es.eig[lo]) < EIG_REL
-        assert np.max(np.abs(H.phase_normalize(vec) - H.phase_normalize(es.evec[:, lo]))) < VEC_ABS
+    # the companion's zero eigenvalues come out at rounding level (alpha ~
+    # 1e14, arbitrary phase); the selection rule leaves them out
+    lo = H.select_least(es.eig, d)
+    assert li >= 0 and lo >= 0
+    assert abs(eig[li] - es.eig[lo]) / abs(es.eig[lo]) < EIG_REL
+    assert np.max(np.abs(H.phase_normalize(vec) - H.phase_normalize(es.evec[:, lo]))) < VEC_ABS
     w, err, iters, status, vecs = ctx.solve_batch([H.stab_params(d)], [prof], sg.MODE_SEEDED,
                                                   seeds=[es.eig[jo] * (1 + 1e-7)], want_vectors=True)
     assert status[0] == sg.ST_OK, (status, err, iters)

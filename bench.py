@@ -246,6 +246,73 @@ def serving_leg(ctx, args):
     return out
 
 
+def spatial_workload(count: int, seed: int):
+    """Batched spatial sweep around the configuration-1 case: crossflow
+    profiles W = 0.08 y exp(1 - y/1.5)/1.5 with U = erf(y/2) and the
+    Crocco-Busemann T, N in {64, 96} (companion orders 640 and 960),
+    omega ~ U[0.03, 0.07], beta ~ U[0.05, 0.15], log Re ~ U[log 1000, log 3000],
+    M ~ U[0.5, 1.0]."""
+    from oracle import stab_oracle as so
+    rng = np.random.Generator(np.random.PCG64(seed))
+    N = rng.choice([64, 96], size=count)
+    om = rng.uniform(0.03, 0.07, count)
+    be = rng.uniform(0.05, 0.15, count)
+    Re = 10.0 ** rng.uniform(3.0, math.log10(3000.0), count)
+    M = rng.uniform(0.5, 1.0, count)
+    prof = np.empty((count, 2000, 6))
+    for k in range(count):
+        y, vt = so.synthetic_profile(float(M[k]), 50.0, crossflow=True)
+        prof[k, :, 0] = y
+        prof[k, :, 1:] = vt
+    params = [dict(itype=2, ny=int(N[k]), Ma=float(M[k]), Re=float(Re[k]), Pr=0.72, mattyp=1, T0=T0_SUTH,
+                   yi=1.0 / 23.0, ymax=50.0, alpha=[0.0, 0.0], beta=[float(be[k]), 0.0],
+                   omega=[float(om[k]), 0.0], top=0, wallt=0) for k in range(count)]
+    return params, prof
+
+
+def spatial_leg(ctx, stream, count):
+    """The batched spatial sweep: one plain FP64 pass (the reference
+    result), then the coarse-seeded pass timed after a warm-up pass; modes/s
+    of both and the count matching the plain result to 1e-10 with a trusted
+    status."""
+    import torch
+    import stab_gb300 as sg
+    params, prof = spatial_workload(count, 20261206)
+    sp = [to_stab(d) for d in params]
+    b = ctx.batch(sp, [prof[k] for k in range(count)])
+    try:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        b.run(sg.MODE_PLAIN)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = ev0.elapsed_time(ev1)
+        ref, _, _, ref_st, _ = b.results()
+        b.run(sg.MODE_COARSE)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        b.run(sg.MODE_COARSE)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        w, err, iters, st, _ = b.results()
+    finally:
+        b.close()
+    rel = np.abs(w - ref) / np.maximum(np.abs(ref), 1e-300)
+    trusted = np.isin(st, [sg.ST_OK, sg.ST_FELLBACK]) & (ref_st == sg.ST_OK)
+    ok = trusted & (rel <= TOL)
+    return {"workload": f"{count} spatial crossflow instances, N in {{64, 96}} (companion orders 640, 960), "
+                        "omega~U[.03,.07], beta~U[.05,.15], Re~logU[1000,3000], M~U[.5,1], seed 20261206",
+            "coarse_seeded": {"value": float(np.sum(ok)) / (ms / 1000.0), "unit": "modes/s", "ms_per_step": ms,
+                              "converged": int(np.sum(ok)), "of": count,
+                              "trusted_but_wrong": int(np.sum(trusted & ~(rel <= TOL))),
+                              "status_histogram": {int(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}},
+            "plain_fp64": {"value": float(np.sum(ref_st == sg.ST_OK)) / (plain_ms / 1000.0), "unit": "modes/s",
+                           "ms_per_step": plain_ms},
+            "speedup_seeded_over_plain": (float(np.sum(ok)) / ms) / max(float(np.sum(ref_st == sg.ST_OK)) / plain_ms,
+                                                                        1e-300)}
+
+
 def to_stab(d):
     import stab_gb300 as sg
     return sg.StabParams.make(itype=d["itype"], ny=d["ny"], Ma=d["Ma"], Re=d["Re"], Pr=d["Pr"],
@@ -410,6 +477,7 @@ def main():
     ap.add_argument("--cpu-sample-threaded", type=int, default=16,
                     help="instances of the one-process multi-threaded CPU mode")
     ap.add_argument("--plain-reps", type=int, default=3, help="timed passes of the plain FP64 path")
+    ap.add_argument("--spatial", type=int, default=256, help="instances of the batched spatial sweep leg (0: skip)")
     ap.add_argument("--variants", type=int, default=1, help="1: also time the pass with each stage's other "
                     "implementation (polish LU on CUDA cores, seed QR in shared memory)")
     ap.add_argument("--ref-sample", type=int, default=48)
@@ -596,6 +664,7 @@ def main():
             finally:
                 ctx.set_seed_size(args.seed_ny)
 
+    spatial = spatial_leg(ctx, stream, args.spatial) if (args.spatial and rank == 0) else None
     sur = surrogate_leg(ctx, stream, args) if (args.surrogate and rank == 0) else None
     single = single_instance_leg(ctx, stream, cpu=args.cpu_sample > 0) if rank == 0 else None
     serving = serving_leg(ctx, args) if (rank == 0 and args.serve_seconds > 0) else None
@@ -711,6 +780,7 @@ def main():
         "gpu_launches": int(launches_per_step * args.steps),
         "round_ms": stages,
         "variants": variants,
+        "spatial_sweep": spatial,
         "eig_phase_share": {k: round(v / max(1, sum(phases.values())), 4) for k, v in phases.items()},
         "autotune_lu_panel": {str(n): {"c64": v["c64"][0], "c128": v["c128"][0]} for n, v in tune.items()},
         "cuda_graph": "device part of each timed pass replayed from a captured CUDA graph",

@@ -631,6 +631,9 @@ def main():
         # 64-thread eigensolver CTAs, eight per SM
         variants["eig_64_thread_ctas_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_THREADS, 64),
                                                        lambda: ctx.set_option(sg.OPT_EIG_THREADS, 128))
+        # the top candidate's polish started from the seed level's eigenvector
+        variants["seed_vectors_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_SEED_VECTORS, 1),
+                                                 lambda: ctx.set_option(sg.OPT_SEED_VECTORS, 0))
         # the small N = 48 level batch on the 128-thread persistent grid
         # instead of the default 256-thread CTAs
         variants["eig_mid_off_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_MID, 0),

@@ -74,6 +74,7 @@ struct stab_ctx {
   int eig_resident = 0;    // STAB_OPT_EIG_RESIDENT
   int eig_threads = 128;   // STAB_OPT_EIG_THREADS
   int eig_mid = 1;         // STAB_OPT_EIG_MID
+  int seed_vectors = 0;    // STAB_OPT_SEED_VECTORS
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -360,6 +361,9 @@ struct stab_batch {
   int ncheb = 0;
   bool use_start = false;
   DevBuf startc;
+  DevBuf seedc;               // coarse-level eigenvectors as Chebyshev coefficients (count x 5 x seedc_n)
+  int seedc_n = 0;
+  bool has_fd = false;        // a finite-difference instance (no Chebyshev grid)
   DevBuf seed_raw, best_src;                  // STAB_MODE_SURROGATE: the extra candidate, winner per instance
   DevBuf tmaps;                               // tensor maps of the complex64 matrices (TMA tiles of the LU)
   int tmaps_state = 0;                        // 0 not built, 1 built, -1 not possible (odd order)
@@ -382,7 +386,7 @@ struct stab_batch {
                      &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
                      &bad, &flops, &rsc, &csc, &cand, &accepted, &skip64, &lus32, &lus64, &have, &best_key, &best_theta, &best_err,
                      &best_iters, &best_out, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
-                     &done, &err, &iters, &status, &counter, &startc, &seed_raw, &best_src, &tmaps};
+                     &done, &err, &iters, &status, &counter, &startc, &seedc, &seed_raw, &best_src, &tmaps};
     for (DevBuf* d : all) {
       if (d->p) cudaFreeAsync(d->p, d->st);
       d->p = nullptr;
@@ -636,6 +640,7 @@ static int batch_finish(stab_ctx* c, stab_batch* b) {
     blk_off += (int64_t)BLK_STRIDE * d.ny;
     vec_off += (int64_t)VEC_SLOTS * d.n;
     if (d.itype == 1) b->tcount++;
+    if (d.fd) b->has_fd = true;
   }
   for (int ny : tab_ny) {
     int r = ensure_dtab(c, ny);
@@ -1093,8 +1098,13 @@ cc* polish_pool<cc>(stab_batch* b) { return b->M32.as<cc>(); }
 template <>
 zc* polish_pool<zc>(stab_batch* b) { return b->Z64.as<zc>(); }
 
+// stage 0: the whole polish; 1: only the factorisation at the shift and the
+// two inverse-iteration steps (x in vector slot 0, normalised at pcol);
+// 2: start from the coarse level's eigenvector (Chebyshev coefficients in
+// b->seedc, b->seedc_n of them per field) instead of those steps, so the
+// factorisation at the shift is skipped.
 template <typename T>
-static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
+static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip, int stage) {
   const bool c64 = std::is_same<T, cc>::value;
   const char* n_dense = c64 ? "k_dense_c" : "k_dense_z";
   const char* n_lu = c64 ? "k_lu_c" : "k_lu_z";
@@ -1113,8 +1123,10 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
   if (rc) return rc;
   if (!c64) CK(c, b->Z64.ensure(sizeof(zc) * b->sum_n2, s));
   T* MP = polish_pool<T>(b);
-  rc = dense<T>(b, all, MP, b->off_n2.as<int64_t>(), 1, 1.0, n_dense, skip);
-  if (rc) return rc;
+  if (stage != 2) {
+    rc = dense<T>(b, all, MP, b->off_n2.as<int64_t>(), 1, 1.0, n_dense, skip);
+    if (rc) return rc;
+  }
   const float* rs = c64 ? b->rsc.as<float>() : nullptr;
   const float* cs = c64 ? b->csc.as<float>() : nullptr;
   auto lu32 = [&]() {
@@ -1166,19 +1178,28 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip) {
       return launch_qmv(b->count, b->nmax, D, DT, b->blk.as<zc>(), b->theta.as<zc>(), deriv, V, xs, ys, sk, s);
     });
   };
-  CK(c, lu32());
-  if (b->use_start) {
+  if (stage == 2) {
     CK(c, timed(c, "k_cheb_start", [&] {
-      return launch_cheb_start(b->count, b->nmax, D, b->startc.as<zc>(), b->ncheb, V, 0, skip, s);
+      return launch_cheb_start(b->count, b->nmax, D, b->seedc.as<zc>(), b->seedc_n, V, 0, skip, s);
     }));
+    CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 0, b->pcol.as<int32_t>(), skip, s); }));
   } else {
-    CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
-  }
-  for (int it = 0; it < 2; ++it) {   // inverse iteration at the shift
-    CK(c, qmv(1, 0, 1, skip));
-    CK(c, solve32(1, skip));
-    CK(c, timed(c, "k_normalize", [&] { return launch_normalize(b->count, D, V, 1, b->pcol.as<int32_t>(), skip, s); }));
-    CK(c, timed(c, "k_vec_copy", [&] { return launch_vec_copy(b->count, b->nmax, D, V, 1, 0, skip, s); }));
+    CK(c, lu32());
+    if (b->use_start) {
+      CK(c, timed(c, "k_cheb_start", [&] {
+        return launch_cheb_start(b->count, b->nmax, D, b->startc.as<zc>(), b->ncheb, V, 0, skip, s);
+      }));
+    } else {
+      CK(c, timed(c, "k_vec_init", [&] { return launch_vec_init(b->count, b->nmax, D, V, 0, s, skip); }));
+    }
+    for (int it = 0; it < 2; ++it) {   // inverse iteration at the shift
+      CK(c, qmv(1, 0, 1, skip));
+      CK(c, solve32(1, skip));
+      CK(c, timed(c, "k_normalize",
+                  [&] { return launch_normalize(b->count, D, V, 1, b->pcol.as<int32_t>(), skip, s); }));
+      CK(c, timed(c, "k_vec_copy", [&] { return launch_vec_copy(b->count, b->nmax, D, V, 1, 0, skip, s); }));
+    }
+    if (stage == 1) return 0;
   }
   // bordered Jacobian at (sigma, x): Q(sigma) with column p <- Q'(sigma) x
   CK(c, qmv(1, 0, 2, skip));
@@ -1289,7 +1310,7 @@ static int run_polish64_ii(stab_batch* b, bool want_vec, const int32_t* skip) {
 }
 
 static int run_polish(stab_batch* b, bool want_vec, const int32_t* skip = nullptr) {
-  return run_polish_t<cc>(b, want_vec, skip);
+  return run_polish_t<cc>(b, want_vec, skip, 0);
 }
 
 // host-side: status from `done` and NaN checks; theta -> eigenvalue
@@ -1549,6 +1570,27 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
   // best pair is kept as STAB_ST_UNVERIFIED.
   const bool first_level = (b->coarse_ny < kMediumNy) && !extra;
   const int rounds = first_level ? 2 : 2 * kShiftCandidates + (extra ? 2 : 0);
+  // STAB_OPT_SEED_VECTORS: the top candidate's round starts from the coarse
+  // level's eigenvector (inverse iteration on the N = 32 operator at the
+  // candidate, interpolated through its Chebyshev coefficients) instead of
+  // a factorisation of the full operator at the shift and two inverse-
+  // iteration steps (Chebyshev grids only)
+  const bool seedvec = first_level && c->seed_vectors && b->coarse && !b->has_fd;
+  if (seedvec) {
+    stab_batch* cb = b->coarse;
+    CK(c, timed(c, "k_take_candidate", [&] {
+      k_take_candidate<<<(cb->count + 255) / 256, 256, 0, s>>>(cb->count, cb->cand.as<zc>(), kShiftCandidates, 0,
+                                                             cb->sigma.as<zc>());
+      return cudaGetLastError();
+    }));
+    int rc = run_polish_t<cc>(cb, false, nullptr, 1);
+    if (rc) return rc;
+    b->seedc_n = b->coarse_ny;
+    CK(c, b->seedc.ensure(sizeof(zc) * (size_t)n * 5 * b->seedc_n, s));
+    CK(c, timed(c, "k_cheb_coeffs", [&] {
+      return launch_cheb_coeffs(n, cb->desc.as<InstDesc>(), cb->vec.as<zc>(), b->seedc.as<zc>(), b->seedc_n, s);
+    }));
+  }
   for (int r = 0; r < rounds; ++r) {
     const int j = r / 2;
     const bool fp64 = (r & 1) != 0;
@@ -1569,7 +1611,8 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
       rb = get_ev(c);
       cudaEventRecord(ra, s);
     }
-    int rc = fp64 ? run_polish64_ii(b, true, b->skip64.as<int32_t>()) : run_polish_t<cc>(b, true, fin);
+    int rc = fp64 ? run_polish64_ii(b, true, b->skip64.as<int32_t>())
+                  : run_polish_t<cc>(b, true, fin, (r == 0 && seedvec) ? 2 : 0);
     b->use_start = false;
     if (c->profiling) {
       cudaEventRecord(rb, s);
@@ -2148,6 +2191,11 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   }
   if (option == STAB_OPT_POLISH_LU_TMA) {
     c->lu_tma = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_SEED_VECTORS) {
+    c->seed_vectors = value ? 1 : 0;
     c->epoch += 1;
     return STAB_OK;
   }

@@ -133,6 +133,38 @@ __global__ void k_cheb_start(int count, const InstDesc* __restrict__ desc, const
   vec[d.off_vec + (int64_t)slot * d.n + q] = s;
 }
 
+// Chebyshev coefficients of vector slot 0 of a batch whose instances all
+// have ny = M (the coarse level's eigenvectors): per instance and field
+// c_q = 2/(M-1) w_q sum_i w_i x(i) cos(pi q i/(M-1)), w_0 = w_{M-1} = 1/2,
+// so that sum_q c_q cos(q theta) interpolates x at the Gauss-Lobatto points
+// and k_cheb_start evaluates it at the nodes of another N.
+__global__ void k_cheb_coeffs(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ vec,
+                              zc* __restrict__ coef, int M) {
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  const InstDesc d = desc[k];
+  const zc* x = vec + d.off_vec;
+  const double pi = 3.14159265358979323846;
+  for (int t = threadIdx.x; t < 5 * M; t += blockDim.x) {
+    const int e = t / M, q = t % M;
+    double sr = 0.0, si = 0.0;
+    for (int i = 0; i < M; ++i) {
+      const double w = ((i == 0 || i == M - 1) ? 0.5 : 1.0) * cos(pi * (double)q * (double)i / (double)(M - 1));
+      const zc v = x[5 * i + e];
+      sr = fma(w, v.x, sr);
+      si = fma(w, v.y, si);
+    }
+    const double f = (2.0 / (double)(M - 1)) * ((q == 0 || q == M - 1) ? 0.5 : 1.0);
+    coef[((int64_t)k * 5 + e) * M + q] = zmk(f * sr, f * si);
+  }
+}
+
+cudaError_t launch_cheb_coeffs(int count, const InstDesc* desc, const zc* vec, zc* coef, int M, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_cheb_coeffs<<<count, 128, 0, s>>>(count, desc, vec, coef, M);
+  return cudaGetLastError();
+}
+
 // x <- x / x_p with p = first index of max |x|; writes p to piv_out when non-null
 __global__ void k_normalize(int count, const InstDesc* __restrict__ desc, zc* __restrict__ vec, int slot,
                             int32_t* __restrict__ piv_out, const int32_t* __restrict__ skip) {

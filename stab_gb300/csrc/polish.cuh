@@ -22,6 +22,8 @@ cudaError_t launch_newton_update(int count, const InstDesc* desc, zc* vec, int x
 cudaError_t launch_start_shift(int count, const zc* sigma, zc* theta, const int32_t* skip, cudaStream_t s);
 cudaError_t launch_reset_polish(int count, int32_t* done, int32_t* iters, const int32_t* skip, cudaStream_t s,
                                 int32_t* lus = nullptr, int nlu = 0);
+// Chebyshev coefficients of vector slot 0 (instances with ny = M): count x 5 x M
+cudaError_t launch_cheb_coeffs(int count, const InstDesc* desc, const zc* vec, zc* coef, int M, cudaStream_t s);
 cudaError_t launch_cheb_start(int count, int nmax, const InstDesc* desc, const zc* coef, int ncheb, zc* vec,
                               int slot, const int32_t* skip, cudaStream_t s);
 cudaError_t launch_ii_update(int count, const InstDesc* desc, zc* vec, int xslot, int yslot, int32_t* pcol,

@@ -597,7 +597,16 @@ def main():
     launches_per_step = sum(v[0] for v in stats.values())
 
     # the same pass with a stage switched to its other implementation (CUDA
-    # events, two passes each after one untimed pass), for the design notes
+    # events, two passes each after one untimed pass), for the design notes;
+    # each variant's results are scored like the default pass's
+    def score(b):
+        e_s, _, _, st_s, v_s = b.results(want_vectors=True)
+        rel_s = np.abs(e_s - ref_eig) / np.maximum(np.abs(ref_eig), 1e-300)
+        trusted_s = np.isin(st_s, [sg.ST_OK, sg.ST_FELLBACK]) & (ref_st == sg.ST_OK)
+        ok_s = trusted_s & (rel_s <= TOL) & (np.array([vec_diff(a, r) for a, r in zip(v_s, ref_vec)]) <= VEC_TOL)
+        return {"converged": int(np.sum(ok_s)), "trusted_but_wrong": int(np.sum(trusted_s & ~(rel_s <= TOL))),
+                "status_histogram": {int(k): int(v) for k, v in zip(*np.unique(st_s, return_counts=True))}}
+
     def variant_ms(setter, reset):
         setter()
         try:
@@ -609,7 +618,7 @@ def main():
                 batch.run(sg.MODE_COARSE)
             v1.record(stream)
             torch.cuda.synchronize()
-            return v0.elapsed_time(v1) / 2
+            return dict(ms=v0.elapsed_time(v1) / 2, **score(batch))
         finally:
             reset()
             batch.run(sg.MODE_COARSE)   # re-capture the default graph
@@ -617,26 +626,33 @@ def main():
     if args.variants:
         variants = {
             "default_ms": ms_local,
-            "polish_lu_cuda_cores_ms": variant_ms(lambda: ctx.set_arithmetic(sg.STAGE_POLISH_LU, sg.ARITH_FP32),
+            "polish_lu_cuda_cores": variant_ms(lambda: ctx.set_arithmetic(sg.STAGE_POLISH_LU, sg.ARITH_FP32),
                                                   ctx.reset_arithmetic),
-            "polish_lu_tensor_no_tma_ms": variant_ms(lambda: ctx.set_option(sg.OPT_POLISH_LU_TMA, 0),
+            "polish_lu_tensor_no_tma": variant_ms(lambda: ctx.set_option(sg.OPT_POLISH_LU_TMA, 0),
                                                      lambda: ctx.set_option(sg.OPT_POLISH_LU_TMA, 1)),
-            "seed_qr_shared_memory_ms": variant_ms(lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 1),
+            "seed_qr_shared_memory": variant_ms(lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 1),
                                                    lambda: ctx.set_option(sg.OPT_SEED_QR_SHARED, 0)),
         }
         # the batch eigensolver with 3 instances in flight per SM instead of
         # the occupancy's four (1 and 2 measured slower still)
-        variants["eig_resident_3_per_sm_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_RESIDENT, 3),
+        variants["eig_resident_3_per_sm"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_RESIDENT, 3),
                                                           lambda: ctx.set_option(sg.OPT_EIG_RESIDENT, 0))
         # 64-thread eigensolver CTAs, eight per SM
-        variants["eig_64_thread_ctas_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_THREADS, 64),
+        variants["eig_64_thread_ctas"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_THREADS, 64),
                                                        lambda: ctx.set_option(sg.OPT_EIG_THREADS, 128))
-        # the top candidate's polish started from the seed level's eigenvector
-        variants["seed_vectors_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_SEED_VECTORS, 1),
-                                                 lambda: ctx.set_option(sg.OPT_SEED_VECTORS, 0))
+        # the top candidate's polish started from a factorisation at the
+        # shift and two inverse-iteration steps instead of the seed level's
+        # eigenvector
+        variants["no_seed_vectors"] = variant_ms(lambda: ctx.set_option(sg.OPT_SEED_VECTORS, 0),
+                                                 lambda: ctx.set_option(sg.OPT_SEED_VECTORS, 1))
+        # the N = 48 level's four candidates in rounds one after another
+        # instead of side by side
+        variants["sequential_candidates"] = variant_ms(
+            lambda: ctx.set_option(sg.OPT_PARALLEL_CANDIDATES, 0),
+            lambda: ctx.set_option(sg.OPT_PARALLEL_CANDIDATES, 1))
         # the small N = 48 level batch on the 128-thread persistent grid
         # instead of the default 256-thread CTAs
-        variants["eig_mid_off_ms"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_MID, 0),
+        variants["eig_mid_off"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_MID, 0),
                                                 lambda: ctx.set_option(sg.OPT_EIG_MID, 1))
         # seed spectra at another N: a batch of its own (the seed size applies
         # to batches created afterwards), timed and checked like the default
@@ -654,15 +670,7 @@ def main():
                     bs.run(sg.MODE_COARSE)
                 v1.record(stream)
                 torch.cuda.synchronize()
-                e_s, _, _, st_s, v_s = bs.results(want_vectors=True)
-                rel_s = np.abs(e_s - ref_eig) / np.maximum(np.abs(ref_eig), 1e-300)
-                trusted_s = np.isin(st_s, [sg.ST_OK, sg.ST_FELLBACK]) & (ref_st == sg.ST_OK)
-                ok_s = trusted_s & (rel_s <= TOL) & (np.array([vec_diff(a, r) for a, r in zip(v_s, ref_vec)])
-                                                     <= VEC_TOL)
-                variants["seed_ny_%d" % sny] = {
-                    "ms": v0.elapsed_time(v1) / 2, "converged": int(np.sum(ok_s)),
-                    "trusted_but_wrong": int(np.sum(trusted_s & ~(rel_s <= TOL))),
-                    "status_histogram": {int(k): int(v) for k, v in zip(*np.unique(st_s, return_counts=True))}}
+                variants["seed_ny_%d" % sny] = dict(ms=v0.elapsed_time(v1) / 2, **score(bs))
                 bs.close()
             finally:
                 ctx.set_seed_size(args.seed_ny)

@@ -201,13 +201,19 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     instance instead of the 128-thread persistent grid; 0: the persistent
  *     grid.  Same algorithm; block sums in another order. */
 #define STAB_OPT_EIG_MID 5
-/*   STAB_OPT_SEED_VECTORS  1: STAB_MODE_COARSE starts the top candidate's
- *     polish from the seed level's eigenvector (inverse iteration on the
- *     N = 32 operator, interpolated through its Chebyshev coefficients)
- *     instead of factoring the full operator at the shift for two inverse-
- *     iteration steps (Chebyshev grids; batches with a finite-difference
- *     instance keep the steps); 0 (default): the steps. */
+/*   STAB_OPT_SEED_VECTORS  1 (default): STAB_MODE_COARSE starts the top
+ *     candidate's polish from the seed level's eigenvector (inverse iteration
+ *     on the N = 32 operator, interpolated through its Chebyshev
+ *     coefficients) instead of factoring the full operator at the shift for
+ *     two inverse-iteration steps (Chebyshev grids; batches with a finite-
+ *     difference instance keep the steps); 0: the steps. */
 #define STAB_OPT_SEED_VECTORS 6
+/*   STAB_OPT_PARALLEL_CANDIDATES  1 (default): the N = 48 level of
+ *     STAB_MODE_COARSE polishes its instances' four shift candidates side by
+ *     side (one sub-batch copy per candidate) instead of in four rounds one
+ *     after another; the kept pair and status follow the sequential rule;
+ *     0: sequential rounds. */
+#define STAB_OPT_PARALLEL_CANDIDATES 7
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,

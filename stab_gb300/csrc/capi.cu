@@ -74,7 +74,8 @@ struct stab_ctx {
   int eig_resident = 0;    // STAB_OPT_EIG_RESIDENT
   int eig_threads = 128;   // STAB_OPT_EIG_THREADS
   int eig_mid = 1;         // STAB_OPT_EIG_MID
-  int seed_vectors = 0;    // STAB_OPT_SEED_VECTORS
+  int seed_vectors = 1;    // STAB_OPT_SEED_VECTORS
+  int par_cand = 1;        // STAB_OPT_PARALLEL_CANDIDATES
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -374,6 +375,7 @@ struct stab_batch {
   std::vector<int32_t> fb_status;
   std::vector<std::vector<zc>> fb_vec;
   stab_batch* coarse = nullptr;               // N = 32 batch of STAB_MODE_COARSE, built on first use
+  stab_batch* copies = nullptr;               // one instance per shift candidate (the N = 48 level's rounds)
   // the device work of a STAB_MODE_COARSE pass (prep, N = 32 eigensolve,
   // candidate rounds) captured once as a CUDA graph and replayed
   cudaGraphExec_t coarse_graph = nullptr;
@@ -399,12 +401,17 @@ struct stab_batch {
     }
     delete coarse;
     coarse = nullptr;
+    delete copies;
+    copies = nullptr;
     if (coarse_graph) cudaGraphExecDestroy(coarse_graph);
     coarse_graph = nullptr;
   }
 };
 
-stab_batch::~stab_batch() { delete coarse; }
+stab_batch::~stab_batch() {
+  delete coarse;
+  delete copies;
+}
 
 // The station-independent scalars of circh (circh.f90:2-188, with xcloc and
 // ycloc, :201-229): the wall of a circle of radius s at arc position 0.
@@ -1542,7 +1549,10 @@ static int coarse_seeds(stab_batch* b) {
 // the N = 32 spectrum resolved) makes the instance final; otherwise the next
 // candidates are polished too.  Instances with no converged pair go to the
 // FP64 fallback.
-static int polish_candidate_rounds(stab_batch* b, bool extra) {
+// With `single` every instance is one candidate copy of a parent instance
+// (polish_candidates_parallel): only its top candidate's two rounds run, and
+// copies without a candidate are skipped.
+static int polish_candidate_rounds(stab_batch* b, bool extra, bool single = false) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
   const int n = b->count;
@@ -1558,6 +1568,12 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
   CK(c, cudaMemsetAsync(b->lus32.p, 0, sizeof(int32_t) * n, s));
   CK(c, cudaMemsetAsync(b->lus64.p, 0, sizeof(int32_t) * n, s));
   CK(c, cudaMemsetAsync(b->have.p, 0, sizeof(int32_t) * n, s));
+  if (single) {
+    CK(c, timed(c, "k_mark_missing", [&] {
+      k_mark_missing<<<(n + 255) / 256, 256, 0, s>>>(n, b->cand.as<zc>(), kShiftCandidates, fin);
+      return cudaGetLastError();
+    }));
+  }
   // per candidate: a complex64 round, then a complex128 retry for the
   // instances where it failed or contracted slowly
   CK(c, b->best_src.ensure(sizeof(int32_t) * n, s));
@@ -1568,8 +1584,8 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
   // (k_take_best) and the instance goes to the N = 48 level whatever it
   // holds, so those rounds are skipped.  The N = 48 level runs them all: its
   // best pair is kept as STAB_ST_UNVERIFIED.
-  const bool first_level = (b->coarse_ny < kMediumNy) && !extra;
-  const int rounds = first_level ? 2 : 2 * kShiftCandidates + (extra ? 2 : 0);
+  const bool first_level = (b->coarse_ny < kMediumNy) && !extra && !single;
+  const int rounds = (first_level || single) ? 2 : 2 * kShiftCandidates + (extra ? 2 : 0);
   // STAB_OPT_SEED_VECTORS: the top candidate's round starts from the coarse
   // level's eigenvector (inverse iteration on the N = 32 operator at the
   // candidate, interpolated through its Chebyshev coefficients) instead of
@@ -1639,6 +1655,51 @@ static int polish_candidate_rounds(stab_batch* b, bool extra) {
                                   b->err.as<double>(), b->iters.as<int32_t>(), b->outvec.as<zc>(), fin,
                                   b->best_src.as<int32_t>(), kShiftCandidates, kDoneUnverified,
                                   b->coarse_ny >= kMediumNy ? 1 : 0);
+    return cudaGetLastError();
+  }));
+  CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+// The candidate rounds of a small batch (the N = 48 level: a few hundred
+// instances, which leave most of the GPU idle in each round) run side by
+// side: a sub-batch holds one copy of each instance per shift candidate,
+// every copy takes its candidate's two rounds (complex64, then the
+// double-word retry where that failed or contracted slowly), and
+// k_fold_copies folds the copies in candidate order with the rules of the
+// sequential rounds (the same kept pair and status; candidates after a
+// quick-accepted one are computed but not folded).
+static int polish_candidates_parallel(stab_batch* b) {
+  stab_ctx* c = b->ctx;
+  cudaStream_t s = c->stream;
+  const int n = b->count, K = kShiftCandidates;
+  if (!b->copies) {
+    std::vector<int> ks((size_t)n * K);
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < K; ++j) ks[(size_t)k * K + j] = k;
+    stab_batch* cb = nullptr;
+    int rc = batch_build_child(b, ks, 0, &cb);
+    if (rc) return rc;
+    b->copies = cb;
+  }
+  stab_batch* x = b->copies;
+  int rc = run_prep(x);
+  if (rc) return rc;
+  // copy c = k * K + j of instance k: its top candidate is b's candidate j
+  CK(c, timed(c, "k_spread_candidates", [&] {
+    k_spread_candidates<<<(n * K + 255) / 256, 256, 0, s>>>(n * K, b->cand.as<zc>(), K, x->cand.as<zc>());
+    return cudaGetLastError();
+  }));
+  rc = polish_candidate_rounds(x, false, true);
+  if (rc) return rc;
+  x->ran = true;
+  x->last_mode = STAB_MODE_COARSE;
+  CK(c, timed(c, "k_fold_copies", [&] {
+    k_fold_copies<<<n, 128, 0, s>>>(n, K, b->desc.as<InstDesc>(), x->done.as<int32_t>(), x->best_key.as<double>(),
+                                    x->theta.as<zc>(), x->err.as<double>(), x->iters.as<int32_t>(),
+                                    x->outvec.as<zc>(), x->off_mof.as<int64_t>(), b->theta.as<zc>(),
+                                    b->done.as<int32_t>(), b->err.as<double>(), b->iters.as<int32_t>(),
+                                    b->outvec.as<zc>(), b->off_mof.as<int64_t>(), kDoneUnverified);
     return cudaGetLastError();
   }));
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
@@ -1816,6 +1877,7 @@ static int coarse_sequence(stab_batch* b, bool extra) {
   if (rc) return rc;
   rc = coarse_seeds(b);
   if (rc) return rc;
+  if (!extra && b->coarse_ny >= kMediumNy && b->ctx->par_cand) return polish_candidates_parallel(b);
   return polish_candidate_rounds(b, extra);
 }
 
@@ -2199,6 +2261,11 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
     c->epoch += 1;
     return STAB_OK;
   }
+  if (option == STAB_OPT_PARALLEL_CANDIDATES) {
+    c->par_cand = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
   if (option == STAB_OPT_EIG_MID) {
     c->eig_mid = value ? 1 : 0;
     c->epoch += 1;
@@ -2347,6 +2414,13 @@ int stab_batch_work(stab_batch* b, double* work_out) {
   work_out[1] = ((b->last_mode == STAB_MODE_COARSE && b->coarse) ? eig_flops(b->coarse) : 0.0) + b->fb_work[1];
   work_out[2] = lu_c + b->fb_work[2];
   work_out[3] = lu_z + b->fb_work[3];
+  if (b->copies && b->copies->ran && !plain) {   // the candidate copies' factorisations
+    double wx[4] = {0.0, 0.0, 0.0, 0.0};
+    int rc = stab_batch_work(b->copies, wx);
+    if (rc) return rc;
+    work_out[2] += wx[2];
+    work_out[3] += wx[3];
+  }
   return STAB_OK;
 }
 

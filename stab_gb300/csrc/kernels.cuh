@@ -69,6 +69,15 @@ __global__ void k_take_best(int count, const InstDesc* desc, const int32_t* have
                             const int64_t* out_off, zc* theta, int32_t* done, double* err, int32_t* iters, zc* out,
                             const int32_t* final_, const int32_t* best_src, int seed_src, int unverified,
                             int keep_unverified);
+// candidate copies of a small batch (k_spread_candidates, k_mark_missing,
+// k_fold_copies)
+__global__ void k_spread_candidates(int ncopy, const zc* cand, int ncand, zc* copy_cand);
+__global__ void k_mark_missing(int count, const zc* cand, int ncand, int32_t* final_);
+__global__ void k_fold_copies(int count, int ncand, const InstDesc* desc, const int32_t* copy_done,
+                              const double* copy_key, const zc* copy_theta, const double* copy_err,
+                              const int32_t* copy_iters, const zc* copy_out, const int64_t* copy_out_off, zc* theta,
+                              int32_t* done, double* err, int32_t* iters, zc* out, const int64_t* out_off,
+                              int unverified);
 __global__ void k_temporal_vec(int count, const InstDesc* desc, const zc* vec, int slot, zc* out,
                                const int64_t* out_off, const int32_t* skip);
 

@@ -237,6 +237,76 @@ __global__ void k_take_best(int count, const InstDesc* __restrict__ desc, const 
   for (int q = threadIdx.x; q < d.m; q += blockDim.x) out[o + q] = best_out[o + q];
 }
 
+// Candidate copies (one instance per shift candidate, so that the candidates
+// of a small batch are polished side by side rather than one round after
+// another): copy c = k * ncand + j of instance k takes candidate j as its
+// own top candidate; a missing candidate (NaN) marks the copy final with no
+// pair (final = 2), so its rounds skip it.
+__global__ void k_spread_candidates(int ncopy, const zc* __restrict__ cand, int ncand, zc* __restrict__ copy_cand) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncopy) return;
+  copy_cand[(int64_t)c * ncand] = cand[c];
+  for (int j = 1; j < ncand; ++j) copy_cand[(int64_t)c * ncand + j] = zmk(nan(""), nan(""));
+}
+
+__global__ void k_mark_missing(int count, const zc* __restrict__ cand, int ncand, int32_t* __restrict__ final_) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= count) return;
+  const zc v = cand[(int64_t)c * ncand];
+  if (!(isfinite(v.x) && isfinite(v.y))) final_[c] = 2;
+}
+
+// Fold the copies of each instance in candidate order, as the rounds of one
+// instance fold its candidates: the less stable converged pair wins (ties to
+// the earlier copy), and the first copy whose pair was quick-accepted ends
+// the fold.  The instance is trusted (done = 1) when that copy is the top
+// candidate's; any other kept pair is `unverified`.  copy_done is the copies'
+// k_take_best output (1: quick-accepted, unverified: converged, 0: none) and
+// copy_key the selection key of each copy's pair.
+__global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__ desc,
+                              const int32_t* __restrict__ copy_done, const double* __restrict__ copy_key,
+                              const zc* __restrict__ copy_theta, const double* __restrict__ copy_err,
+                              const int32_t* __restrict__ copy_iters, const zc* __restrict__ copy_out,
+                              const int64_t* __restrict__ copy_out_off, zc* __restrict__ theta,
+                              int32_t* __restrict__ done, double* __restrict__ err, int32_t* __restrict__ iters,
+                              zc* __restrict__ out, const int64_t* __restrict__ out_off, int unverified) {
+  __shared__ int s_pick;
+  const int k = blockIdx.x;
+  if (k >= count) return;
+  if (threadIdx.x == 0) {
+    int pick = -1, dn = 0;
+    double bk = 0.0;
+    for (int j = 0; j < ncand; ++j) {
+      const int c = k * ncand + j;
+      const int d = copy_done[c];
+      if (d != 1 && d != unverified) continue;
+      if (pick < 0 || copy_key[c] > bk) {
+        pick = c;
+        bk = copy_key[c];
+      }
+      if (d == 1) {
+        dn = (j == 0) ? 1 : unverified;
+        break;
+      }
+    }
+    if (pick >= 0 && dn == 0) dn = unverified;
+    done[k] = dn;
+    if (pick >= 0) {
+      theta[k] = copy_theta[pick];
+      err[k] = copy_err[pick];
+      iters[k] = copy_iters[pick];
+    }
+    s_pick = pick;
+  }
+  __syncthreads();
+  const int pick = s_pick;
+  if (pick < 0) return;
+  const int m = desc[k].m;
+  const zc* src = copy_out + copy_out_off[pick];
+  zc* dst = out + out_off[k];
+  for (int q = threadIdx.x; q < m; q += blockDim.x) dst[q] = src[q];
+}
+
 __global__ void k_temporal_vec(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ vec, int slot,
                                zc* __restrict__ out, const int64_t* __restrict__ out_off,
                                const int32_t* __restrict__ skip) {

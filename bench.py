@@ -650,6 +650,13 @@ def main():
         variants["sequential_candidates"] = variant_ms(
             lambda: ctx.set_option(sg.OPT_PARALLEL_CANDIDATES, 0),
             lambda: ctx.set_option(sg.OPT_PARALLEL_CANDIDATES, 1))
+        # no double-word retry at the first candidate level (its failed and
+        # slow instances go to the second level directly)
+        variants["no_first_retry"] = variant_ms(lambda: ctx.set_option(sg.OPT_FIRST_RETRY, 0),
+                                                lambda: ctx.set_option(sg.OPT_FIRST_RETRY, 1))
+        # the second candidate level at N = 40 instead of 48
+        variants["medium_ny_40"] = variant_ms(lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 40),
+                                              lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 48))
         # the small N = 48 level batch on the 128-thread persistent grid
         # instead of the default 256-thread CTAs
         variants["eig_mid_off"] = variant_ms(lambda: ctx.set_option(sg.OPT_EIG_MID, 0),

@@ -214,6 +214,16 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     after another; the kept pair and status follow the sequential rule;
  *     0: sequential rounds. */
 #define STAB_OPT_PARALLEL_CANDIDATES 7
+/*   STAB_OPT_MEDIUM_NY  N of the second candidate level of STAB_MODE_COARSE
+ *     (the seed spectra of the instances whose first-level top candidate
+ *     was not resolved): above the seed size, at most 64; default 48. */
+#define STAB_OPT_MEDIUM_NY 8
+/*   STAB_OPT_FIRST_RETRY  1 (default): at the first candidate level of
+ *     STAB_MODE_COARSE, instances whose complex64 polish of the top candidate
+ *     failed or contracted slowly take the double-word inverse-iteration
+ *     retry before the second level; 0: they go to the second level
+ *     directly. */
+#define STAB_OPT_FIRST_RETRY 9
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,

@@ -76,6 +76,8 @@ struct stab_ctx {
   int eig_mid = 1;         // STAB_OPT_EIG_MID
   int seed_vectors = 1;    // STAB_OPT_SEED_VECTORS
   int par_cand = 1;        // STAB_OPT_PARALLEL_CANDIDATES
+  int medium_ny = 48;      // STAB_OPT_MEDIUM_NY: N of the second candidate level
+  int first_retry = 1;     // STAB_OPT_FIRST_RETRY
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -1245,7 +1247,8 @@ static int run_polish_t(stab_batch* b, bool want_vec, const int32_t* skip, int s
 // ratio |sigma - lambda_1| / |sigma - lambda_2| per step, which separates
 // mode clusters that complex64 factors cannot resolve.
 static const int kInverseSteps = 8;
-// N of the second candidate level of the fallback
+// N of the second candidate level of the fallback (the default of
+// STAB_OPT_MEDIUM_NY); seed sizes stay below it
 static const int kMediumNy = 48;
 static const double kInverseTol = 1e-13;
 
@@ -1584,8 +1587,8 @@ static int polish_candidate_rounds(stab_batch* b, bool extra, bool single = fals
   // (k_take_best) and the instance goes to the N = 48 level whatever it
   // holds, so those rounds are skipped.  The N = 48 level runs them all: its
   // best pair is kept as STAB_ST_UNVERIFIED.
-  const bool first_level = (b->coarse_ny < kMediumNy) && !extra && !single;
-  const int rounds = (first_level || single) ? 2 : 2 * kShiftCandidates + (extra ? 2 : 0);
+  const bool first_level = (b->coarse_ny < c->medium_ny) && !extra && !single;
+  const int rounds = first_level ? (c->first_retry ? 2 : 1) : single ? 2 : 2 * kShiftCandidates + (extra ? 2 : 0);
   // STAB_OPT_SEED_VECTORS: the top candidate's round starts from the coarse
   // level's eigenvector (inverse iteration on the N = 32 operator at the
   // candidate, interpolated through its Chebyshev coefficients) instead of
@@ -1654,7 +1657,7 @@ static int polish_candidate_rounds(stab_batch* b, bool extra, bool single = fals
                                   b->off_mof.as<int64_t>(), b->theta.as<zc>(), b->done.as<int32_t>(),
                                   b->err.as<double>(), b->iters.as<int32_t>(), b->outvec.as<zc>(), fin,
                                   b->best_src.as<int32_t>(), kShiftCandidates, kDoneUnverified,
-                                  b->coarse_ny >= kMediumNy ? 1 : 0);
+                                  b->coarse_ny >= c->medium_ny ? 1 : 0);
     return cudaGetLastError();
   }));
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
@@ -1765,12 +1768,12 @@ static int run_fallback(stab_batch* b, bool track = false) {
   int rc = batch_build_child(b, b->fell_back, 0, &fb);
   if (rc) return rc;
   std::unique_ptr<stab_batch> guard(fb);
-  if (!track && b->coarse_ny < kMediumNy) {
+  if (!track && b->coarse_ny < c->medium_ny) {
     // A second candidate level first: seeds from the spectrum at N = 48,
     // which resolves what N = 32 did not, at a fraction of the full
     // eigensolve's cost for the large instances; its own failures take the
     // plain path.  Results keep the fallback status.
-    fb->coarse_ny = kMediumNy;
+    fb->coarse_ny = c->medium_ny;
     rc = stab_batch_run(fb, STAB_MODE_COARSE);
     const int nf = fb->count;
     std::vector<double> eig(2 * (size_t)nf), er(nf), w(4, 0.0);
@@ -1877,7 +1880,7 @@ static int coarse_sequence(stab_batch* b, bool extra) {
   if (rc) return rc;
   rc = coarse_seeds(b);
   if (rc) return rc;
-  if (!extra && b->coarse_ny >= kMediumNy && b->ctx->par_cand) return polish_candidates_parallel(b);
+  if (!extra && b->coarse_ny >= b->ctx->medium_ny && b->ctx->par_cand) return polish_candidates_parallel(b);
   return polish_candidate_rounds(b, extra);
 }
 
@@ -2266,6 +2269,18 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
     c->epoch += 1;
     return STAB_OK;
   }
+  if (option == STAB_OPT_FIRST_RETRY) {
+    c->first_retry = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_MEDIUM_NY) {
+    if (value <= c->seed_ny || value > 64)
+      return set_err(c, STAB_ERR_ARG, "the second level's N must be above the seed size and at most 64");
+    c->medium_ny = value;
+    c->epoch += 1;
+    return STAB_OK;
+  }
   if (option == STAB_OPT_EIG_MID) {
     c->eig_mid = value ? 1 : 0;
     c->epoch += 1;
@@ -2288,7 +2303,8 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
 
 int stab_set_seed_size(stab_ctx* c, int32_t ny) {
   if (!c) return STAB_ERR_ARG;
-  if (ny < 16 || ny >= kMediumNy) return set_err(c, STAB_ERR_ARG, "seed size must be in [16, 48)");
+  if (ny < 16 || ny >= c->medium_ny)
+    return set_err(c, STAB_ERR_ARG, "seed size must be at least 16 and below the second level's N (48)");
   c->seed_ny = ny;
   return STAB_OK;
 }

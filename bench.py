@@ -270,6 +270,19 @@ def spatial_workload(count: int, seed: int):
     return params, prof
 
 
+def spatial_score(w, st, ref, ref_st, ms):
+    """modes/s and status counts of a coarse-seeded spatial pass against the plain result"""
+    import stab_gb300 as sg
+    rel = np.abs(w - ref) / np.maximum(np.abs(ref), 1e-300)
+    trusted = np.isin(st, [sg.ST_OK, sg.ST_FELLBACK]) & (ref_st == sg.ST_OK)
+    ok = trusted & (rel <= TOL)
+    unver = (st == sg.ST_UNVERIFIED) & (ref_st == sg.ST_OK)
+    return {"value": float(np.sum(ok)) / (ms / 1000.0), "unit": "modes/s", "ms_per_step": ms,
+            "converged": int(np.sum(ok)), "trusted_but_wrong": int(np.sum(trusted & ~(rel <= TOL))),
+            "unverified": int(np.sum(unver)), "unverified_matching": int(np.sum(unver & (rel <= TOL))),
+            "status_histogram": {int(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}}
+
+
 def spatial_leg(ctx, stream, count):
     """The batched spatial sweep: one plain FP64 pass (the reference
     result), then the coarse-seeded pass timed after a warm-up pass; modes/s
@@ -296,17 +309,36 @@ def spatial_leg(ctx, stream, count):
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
         w, err, iters, st, _ = b.results()
+        counts = b.counts()
+        # the same pass without second-level trust by agreement of the seed levels
+        ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 0)
+        try:
+            b.run(sg.MODE_COARSE)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            b.run(sg.MODE_COARSE)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms_lc = ev0.elapsed_time(ev1)
+            w_lc, _, _, st_lc, _ = b.results()
+        finally:
+            ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 1)
     finally:
         b.close()
     rel = np.abs(w - ref) / np.maximum(np.abs(ref), 1e-300)
     trusted = np.isin(st, [sg.ST_OK, sg.ST_FELLBACK]) & (ref_st == sg.ST_OK)
     ok = trusted & (rel <= TOL)
+    unver = (st == sg.ST_UNVERIFIED) & (ref_st == sg.ST_OK)
     return {"workload": f"{count} spatial crossflow instances, N in {{64, 96}} (companion orders 640, 960), "
                         "omega~U[.03,.07], beta~U[.05,.15], Re~logU[1000,3000], M~U[.5,1], seed 20261206",
             "coarse_seeded": {"value": float(np.sum(ok)) / (ms / 1000.0), "unit": "modes/s", "ms_per_step": ms,
                               "converged": int(np.sum(ok)), "of": count,
                               "trusted_but_wrong": int(np.sum(trusted & ~(rel <= TOL))),
+                              "unverified": int(np.sum(unver)),
+                              "unverified_matching": int(np.sum(unver & (rel <= TOL))),
+                              "stages": counts,
                               "status_histogram": {int(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}},
+            "no_level_consistency": spatial_score(w_lc, st_lc, ref, ref_st, ms_lc),
             "plain_fp64": {"value": float(np.sum(ref_st == sg.ST_OK)) / (plain_ms / 1000.0), "unit": "modes/s",
                            "ms_per_step": plain_ms},
             "speedup_seeded_over_plain": (float(np.sum(ok)) / ms) / max(float(np.sum(ref_st == sg.ST_OK)) / plain_ms,
@@ -654,6 +686,10 @@ def main():
         # slow instances go to the second level directly)
         variants["no_first_retry"] = variant_ms(lambda: ctx.set_option(sg.OPT_FIRST_RETRY, 0),
                                                 lambda: ctx.set_option(sg.OPT_FIRST_RETRY, 1))
+        # second-level trust only by the N = 48 top candidate's own quick
+        # accept (without the agreement of the two seed levels)
+        variants["no_level_consistency"] = variant_ms(lambda: ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 0),
+                                                      lambda: ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 1))
         # the second candidate level at N = 40 instead of 48
         variants["medium_ny_40"] = variant_ms(lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 40),
                                               lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 48))
@@ -781,6 +817,9 @@ def main():
                       "eigenvalue_only": int(np.sum(ok_val)),
                       "status_histogram": st_hist, "stages": counts_last,
                       "trusted_but_wrong": int(wrong_trusted.size),
+                      "unverified": int(np.sum((status == sg.ST_UNVERIFIED) & (ref_st == sg.ST_OK))),
+                      "unverified_matching": int(np.sum((status == sg.ST_UNVERIFIED) & (ref_st == sg.ST_OK)
+                                                        & (rel <= TOL))),
                       "trusted_but_wrong_examples": [
                           {"index": int(q), "got": [float(eig[q].real), float(eig[q].imag)],
                            "plain": [float(ref_eig[q].real), float(ref_eig[q].imag)], "status": int(status[q])}

@@ -224,6 +224,15 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     retry before the second level; 0: they go to the second level
  *     directly. */
 #define STAB_OPT_FIRST_RETRY 9
+/*   STAB_OPT_LEVEL_CONSISTENCY  1 (default): at the second candidate level of
+ *     STAB_MODE_COARSE (with STAB_OPT_PARALLEL_CANDIDATES), an instance whose
+ *     N = 48 top candidate did not polish to within 1e-7 of itself is still
+ *     trusted (STAB_ST_FELLBACK) when the top candidates of both seed levels
+ *     polished to the same pair (within 1e-10), that pair is the least
+ *     stable of the level's converged candidates, and the seed values
+ *     converge to it (N = 48 error at most a quarter of the N = 32 error and
+ *     below 1e-3 relative); 0: such instances are STAB_ST_UNVERIFIED. */
+#define STAB_OPT_LEVEL_CONSISTENCY 10
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,

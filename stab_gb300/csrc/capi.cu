@@ -78,6 +78,7 @@ struct stab_ctx {
   int par_cand = 1;        // STAB_OPT_PARALLEL_CANDIDATES
   int medium_ny = 48;      // STAB_OPT_MEDIUM_NY: N of the second candidate level
   int first_retry = 1;     // STAB_OPT_FIRST_RETRY
+  int level_trust = 1;     // STAB_OPT_LEVEL_CONSISTENCY
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -378,6 +379,10 @@ struct stab_batch {
   std::vector<std::vector<zc>> fb_vec;
   stab_batch* coarse = nullptr;               // N = 32 batch of STAB_MODE_COARSE, built on first use
   stab_batch* copies = nullptr;               // one instance per shift candidate (the N = 48 level's rounds)
+  // second-level batches: the first level's top candidate, its polished
+  // pair and whether that converged, per instance (STAB_OPT_LEVEL_CONSISTENCY)
+  DevBuf lev1_idx, lev1_lam, lev1_th, lev1_ok;
+  bool has_lev1 = false;
   // the device work of a STAB_MODE_COARSE pass (prep, N = 32 eigensolve,
   // candidate rounds) captured once as a CUDA graph and replayed
   cudaGraphExec_t coarse_graph = nullptr;
@@ -390,7 +395,8 @@ struct stab_batch {
                      &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
                      &bad, &flops, &rsc, &csc, &cand, &accepted, &skip64, &lus32, &lus64, &have, &best_key, &best_theta, &best_err,
                      &best_iters, &best_out, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
-                     &done, &err, &iters, &status, &counter, &startc, &seedc, &seed_raw, &best_src, &tmaps};
+                     &done, &err, &iters, &status, &counter, &startc, &seedc, &seed_raw, &best_src, &tmaps,
+                     &lev1_idx, &lev1_lam, &lev1_th, &lev1_ok};
     for (DevBuf* d : all) {
       if (d->p) cudaFreeAsync(d->p, d->st);
       d->p = nullptr;
@@ -1672,6 +1678,10 @@ static int polish_candidate_rounds(stab_batch* b, bool extra, bool single = fals
 // k_fold_copies folds the copies in candidate order with the rules of the
 // sequential rounds (the same kept pair and status; candidates after a
 // quick-accepted one are computed but not folded).
+// second-level trust (STAB_OPT_LEVEL_CONSISTENCY): the N = 48 top
+// candidate's error against the polished pair is at most this fraction of
+// the N = 32 top candidate's
+static const double kLevelConvergence = 0.25;
 static int polish_candidates_parallel(stab_batch* b) {
   stab_ctx* c = b->ctx;
   cudaStream_t s = c->stream;
@@ -1702,7 +1712,9 @@ static int polish_candidates_parallel(stab_batch* b) {
                                     x->theta.as<zc>(), x->err.as<double>(), x->iters.as<int32_t>(),
                                     x->outvec.as<zc>(), x->off_mof.as<int64_t>(), b->theta.as<zc>(),
                                     b->done.as<int32_t>(), b->err.as<double>(), b->iters.as<int32_t>(),
-                                    b->outvec.as<zc>(), b->off_mof.as<int64_t>(), kDoneUnverified);
+                                    b->outvec.as<zc>(), b->off_mof.as<int64_t>(), kDoneUnverified,
+                                    b->has_lev1 ? b->lev1_lam.as<zc>() : nullptr, b->lev1_th.as<zc>(),
+                                    b->lev1_ok.as<int32_t>(), b->cand.as<zc>(), kLevelConvergence);
     return cudaGetLastError();
   }));
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
@@ -1774,6 +1786,23 @@ static int run_fallback(stab_batch* b, bool track = false) {
     // eigensolve's cost for the large instances; its own failures take the
     // plain path.  Results keep the fallback status.
     fb->coarse_ny = c->medium_ny;
+    if (c->level_trust && (b->last_mode == STAB_MODE_COARSE || b->last_mode == STAB_MODE_SURROGATE) &&
+        b->best_theta.p && b->have.p && b->best_src.p) {
+      const int nf = fb->count;
+      std::vector<int32_t> idx(b->fell_back.begin(), b->fell_back.end());
+      CK(c, upload(fb->lev1_idx, idx, c->stream));
+      CK(c, fb->lev1_lam.ensure(sizeof(zc) * nf, c->stream));
+      CK(c, fb->lev1_th.ensure(sizeof(zc) * nf, c->stream));
+      CK(c, fb->lev1_ok.ensure(sizeof(int32_t) * nf, c->stream));
+      CK(c, timed(c, "k_gather_level", [&] {
+        k_gather_level<<<(nf + 255) / 256, 256, 0, c->stream>>>(
+            nf, fb->lev1_idx.as<int32_t>(), b->cand.as<zc>(), kShiftCandidates, b->best_theta.as<zc>(),
+            b->have.as<int32_t>(), b->best_src.as<int32_t>(), fb->lev1_lam.as<zc>(), fb->lev1_th.as<zc>(),
+            fb->lev1_ok.as<int32_t>());
+        return cudaGetLastError();
+      }));
+      fb->has_lev1 = true;
+    }
     rc = stab_batch_run(fb, STAB_MODE_COARSE);
     const int nf = fb->count;
     std::vector<double> eig(2 * (size_t)nf), er(nf), w(4, 0.0);
@@ -2266,6 +2295,11 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   }
   if (option == STAB_OPT_PARALLEL_CANDIDATES) {
     c->par_cand = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_LEVEL_CONSISTENCY) {
+    c->level_trust = value ? 1 : 0;
     c->epoch += 1;
     return STAB_OK;
   }

@@ -249,6 +249,22 @@ __global__ void k_spread_candidates(int ncopy, const zc* __restrict__ cand, int 
   for (int j = 1; j < ncand; ++j) copy_cand[(int64_t)c * ncand + j] = zmk(nan(""), nan(""));
 }
 
+// The first candidate level's view of the instances that reach the second:
+// lam1 = top candidate of its seed spectrum, th1 = that candidate's polished
+// pair and ok1 = it converged (have, and the kept pair came from the top
+// candidate); idx maps second-level instances to first-level ones.
+__global__ void k_gather_level(int count, const int32_t* __restrict__ idx, const zc* __restrict__ cand, int ncand,
+                               const zc* __restrict__ best_theta, const int32_t* __restrict__ have,
+                               const int32_t* __restrict__ best_src, zc* __restrict__ lam1, zc* __restrict__ th1,
+                               int32_t* __restrict__ ok1) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= count) return;
+  const int k = idx[q];
+  lam1[q] = cand[(int64_t)k * ncand];
+  th1[q] = best_theta[k];
+  ok1[q] = (have[k] && best_src[k] == 0) ? 1 : 0;
+}
+
 __global__ void k_mark_missing(int count, const zc* __restrict__ cand, int ncand, int32_t* __restrict__ final_) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= count) return;
@@ -263,13 +279,23 @@ __global__ void k_mark_missing(int count, const zc* __restrict__ cand, int ncand
 // candidate's; any other kept pair is `unverified`.  copy_done is the copies'
 // k_take_best output (1: quick-accepted, unverified: converged, 0: none) and
 // copy_key the selection key of each copy's pair.
+//
+// With lev1 (the first level's top candidate lam1 and its polished pair th1,
+// ok1 = converged), an instance whose kept pair is `unverified` is trusted
+// when both levels identify the same mode: the top candidates of both seed
+// spectra polished to the same pair (within 1e-10), that pair is the least
+// stable of every converged copy, and the seed values converge to it
+// (|lam2 - th| <= conv |lam1 - th|, with lam2 this level's top candidate,
+// and |lam2 - th| <= 1e-3 |th|).
 __global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__ desc,
                               const int32_t* __restrict__ copy_done, const double* __restrict__ copy_key,
                               const zc* __restrict__ copy_theta, const double* __restrict__ copy_err,
                               const int32_t* __restrict__ copy_iters, const zc* __restrict__ copy_out,
                               const int64_t* __restrict__ copy_out_off, zc* __restrict__ theta,
                               int32_t* __restrict__ done, double* __restrict__ err, int32_t* __restrict__ iters,
-                              zc* __restrict__ out, const int64_t* __restrict__ out_off, int unverified) {
+                              zc* __restrict__ out, const int64_t* __restrict__ out_off, int unverified,
+                              const zc* __restrict__ lam1, const zc* __restrict__ th1, const int32_t* __restrict__ ok1,
+                              const zc* __restrict__ cand, double conv) {
   __shared__ int s_pick;
   const int k = blockIdx.x;
   if (k >= count) return;
@@ -290,6 +316,23 @@ __global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__
       }
     }
     if (pick >= 0 && dn == 0) dn = unverified;
+    if (dn == unverified && lam1 && ok1[k]) {
+      const int c0 = k * ncand;
+      bool top = (copy_done[c0] == 1 || copy_done[c0] == unverified);
+      for (int j = 1; j < ncand && top; ++j) {
+        const int c = c0 + j;
+        if ((copy_done[c] == 1 || copy_done[c] == unverified) && copy_key[c] > copy_key[c0]) top = false;
+      }
+      if (top) {
+        const zc th = copy_theta[c0];
+        const double at = zabs(th);
+        const double e2 = zabs(zsub(cand[c0], th)), e1 = zabs(zsub(lam1[k], th));
+        if (zabs(zsub(th1[k], th)) <= 1e-10 * at && e2 <= conv * e1 && e2 <= 1e-3 * at) {
+          pick = c0;
+          dn = 1;
+        }
+      }
+    }
     done[k] = dn;
     if (pick >= 0) {
       theta[k] = copy_theta[pick];

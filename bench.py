@@ -310,19 +310,25 @@ def spatial_leg(ctx, stream, count):
         ms = ev0.elapsed_time(ev1)
         w, err, iters, st, _ = b.results()
         counts = b.counts()
-        # the same pass without second-level trust by agreement of the seed levels
-        ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 0)
-        try:
-            b.run(sg.MODE_COARSE)
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            b.run(sg.MODE_COARSE)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            ms_lc = ev0.elapsed_time(ev1)
-            w_lc, _, _, st_lc, _ = b.results()
-        finally:
-            ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 1)
+        # the same pass with another setting: without second-level trust by
+        # agreement of the seed levels, and with the second level at N = 48
+        def other(setter, reset):
+            setter()
+            try:
+                b.run(sg.MODE_COARSE)
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                b.run(sg.MODE_COARSE)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                w_o, _, _, st_o, _ = b.results()
+                return spatial_score(w_o, st_o, ref, ref_st, ev0.elapsed_time(ev1))
+            finally:
+                reset()
+        no_lc = other(lambda: ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 0),
+                      lambda: ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 1))
+        lev48 = other(lambda: ctx.set_option(sg.OPT_MEDIUM_NY_SPATIAL, 48),
+                      lambda: ctx.set_option(sg.OPT_MEDIUM_NY_SPATIAL, 24))
     finally:
         b.close()
     rel = np.abs(w - ref) / np.maximum(np.abs(ref), 1e-300)
@@ -338,7 +344,8 @@ def spatial_leg(ctx, stream, count):
                               "unverified_matching": int(np.sum(unver & (rel <= TOL))),
                               "stages": counts,
                               "status_histogram": {int(k): int(v) for k, v in zip(*np.unique(st, return_counts=True))}},
-            "no_level_consistency": spatial_score(w_lc, st_lc, ref, ref_st, ms_lc),
+            "no_level_consistency": no_lc,
+            "second_level_n48": lev48,
             "plain_fp64": {"value": float(np.sum(ref_st == sg.ST_OK)) / (plain_ms / 1000.0), "unit": "modes/s",
                            "ms_per_step": plain_ms},
             "speedup_seeded_over_plain": (float(np.sum(ok)) / ms) / max(float(np.sum(ref_st == sg.ST_OK)) / plain_ms,

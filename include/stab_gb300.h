@@ -230,9 +230,18 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     trusted (STAB_ST_FELLBACK) when the top candidates of both seed levels
  *     polished to the same pair (within 1e-10), that pair is the least
  *     stable of the level's converged candidates, and the seed values
- *     converge to it (N = 48 error at most a quarter of the N = 32 error and
- *     below 1e-3 relative); 0: such instances are STAB_ST_UNVERIFIED. */
+ *     converge to it (the finer level's error at most a quarter of the
+ *     coarser one's and below 1e-3 relative); 0: such instances are
+ *     STAB_ST_UNVERIFIED. */
 #define STAB_OPT_LEVEL_CONSISTENCY 10
+/*   STAB_OPT_MEDIUM_NY_SPATIAL  N of the second candidate level for the
+ *     spatial instances (itypes 2 and 4), in [16, 64]: default 24.  Their
+ *     least-stable alpha converges algebraically in N (about 1e-3 relative
+ *     at N = 24, 1e-5 at N = 32 for crossflow profiles), so the agreement of
+ *     a coarser second level with the first (STAB_OPT_LEVEL_CONSISTENCY:
+ *     the finer level closer by a factor of four) certifies it at an eighth
+ *     of the cost of an N = 48 companion spectrum. */
+#define STAB_OPT_MEDIUM_NY_SPATIAL 11
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,

@@ -79,6 +79,7 @@ struct stab_ctx {
   int medium_ny = 48;      // STAB_OPT_MEDIUM_NY: N of the second candidate level
   int first_retry = 1;     // STAB_OPT_FIRST_RETRY
   int level_trust = 1;     // STAB_OPT_LEVEL_CONSISTENCY
+  int medium_ny_sp = 24;   // STAB_OPT_MEDIUM_NY_SPATIAL: N of the spatial instances' second level
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -374,6 +375,8 @@ struct stab_batch {
   int graph_mode = -1;                        // mode of the captured graph
   int graph_epoch = -1;                       // context settings the graph was captured under
   int coarse_ny = 32;                         // N of the seed spectrum of STAB_MODE_COARSE
+  int coarse_ny_sp = 32;                      // the same for the spatial instances
+  int level = 1;                              // candidate level: 1 first (seed size), 2 the second
   std::vector<zc> fb_val;
   std::vector<int32_t> fb_status;
   std::vector<std::vector<zc>> fb_vec;
@@ -383,6 +386,7 @@ struct stab_batch {
   // pair and whether that converged, per instance (STAB_OPT_LEVEL_CONSISTENCY)
   DevBuf lev1_idx, lev1_lam, lev1_th, lev1_ok;
   bool has_lev1 = false;
+  int lev1_n = 32;                            // N of the first level's seed spectra
   // the device work of a STAB_MODE_COARSE pass (prep, N = 32 eigensolve,
   // candidate rounds) captured once as a CUDA graph and replayed
   cudaGraphExec_t coarse_graph = nullptr;
@@ -753,6 +757,7 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
   b->ctx = c;
   b->count = count;
   b->coarse_ny = c->seed_ny;
+  b->coarse_ny_sp = c->seed_ny;
   std::vector<int> idx(count);
   for (int i = 0; i < count; ++i) idx[i] = i;
   // temporal (itype 1 and 3) before spatial (2 and 4)
@@ -853,13 +858,19 @@ static int batch_build(stab_ctx* c, int32_t count, const stab_params* p, const i
 // and their spline tables, so its prep skips k_spline: the parent must have
 // run its prep in the same pass, and must outlive the child.  Internal order
 // is the parent's order restricted to ks (still temporal first), perm[q] = q.
-static int batch_build_child(stab_batch* parent, const std::vector<int>& ks, int force_ny, stab_batch** out) {
+// force_ny > 0: every temporal instance takes that N (force_ny_sp the
+// spatial ones; 0 keeps the parent's N).
+static int batch_build_child(stab_batch* parent, const std::vector<int>& ks, int force_ny, stab_batch** out,
+                             int force_ny_sp = -1) {
+  if (force_ny_sp < 0) force_ny_sp = force_ny;
   stab_ctx* c = parent->ctx;
   if (ks.empty()) return set_err(c, STAB_ERR_ARG, "empty sub-batch");
   std::unique_ptr<stab_batch> b(new stab_batch());
   b->ctx = c;
   b->count = (int)ks.size();
   b->coarse_ny = parent->coarse_ny;
+  b->coarse_ny_sp = parent->coarse_ny_sp;
+  b->level = parent->level;
   b->shared_prof = true;
   b->nprof = parent->nprof;
   b->prof_p = parent->prof_p;
@@ -869,7 +880,8 @@ static int batch_build_child(stab_batch* parent, const std::vector<int>& ks, int
   for (int q = 0; q < b->count; ++q) {
     const int k = ks[q];
     stab_params pq = parent->Pin[k];
-    if (force_ny > 0) pq.ny = force_ny;
+    const int fny = is_spatial(pq.itype) ? force_ny_sp : force_ny;
+    if (fny > 0) pq.ny = fny;
     const InstDesc& pd0 = parent->hd[k];
     ProfDesc pd{};
     pd.off_prof = pd0.off_prof;
@@ -1531,7 +1543,7 @@ static int coarse_seeds(stab_batch* b) {
     std::vector<int> all(b->count);
     for (int k = 0; k < b->count; ++k) all[k] = k;
     stab_batch* cb = nullptr;
-    int rc = batch_build_child(b, all, b->coarse_ny, &cb);
+    int rc = batch_build_child(b, all, b->coarse_ny, &cb, b->coarse_ny_sp);
     if (rc) return rc;
     b->coarse = cb;
   }
@@ -1593,7 +1605,7 @@ static int polish_candidate_rounds(stab_batch* b, bool extra, bool single = fals
   // (k_take_best) and the instance goes to the N = 48 level whatever it
   // holds, so those rounds are skipped.  The N = 48 level runs them all: its
   // best pair is kept as STAB_ST_UNVERIFIED.
-  const bool first_level = (b->coarse_ny < c->medium_ny) && !extra && !single;
+  const bool first_level = (b->level == 1) && !extra && !single;
   const int rounds = first_level ? (c->first_retry ? 2 : 1) : single ? 2 : 2 * kShiftCandidates + (extra ? 2 : 0);
   // STAB_OPT_SEED_VECTORS: the top candidate's round starts from the coarse
   // level's eigenvector (inverse iteration on the N = 32 operator at the
@@ -1663,7 +1675,7 @@ static int polish_candidate_rounds(stab_batch* b, bool extra, bool single = fals
                                   b->off_mof.as<int64_t>(), b->theta.as<zc>(), b->done.as<int32_t>(),
                                   b->err.as<double>(), b->iters.as<int32_t>(), b->outvec.as<zc>(), fin,
                                   b->best_src.as<int32_t>(), kShiftCandidates, kDoneUnverified,
-                                  b->coarse_ny >= c->medium_ny ? 1 : 0);
+                                  b->level >= 2 ? 1 : 0);
     return cudaGetLastError();
   }));
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
@@ -1714,7 +1726,8 @@ static int polish_candidates_parallel(stab_batch* b) {
                                     b->done.as<int32_t>(), b->err.as<double>(), b->iters.as<int32_t>(),
                                     b->outvec.as<zc>(), b->off_mof.as<int64_t>(), kDoneUnverified,
                                     b->has_lev1 ? b->lev1_lam.as<zc>() : nullptr, b->lev1_th.as<zc>(),
-                                    b->lev1_ok.as<int32_t>(), b->cand.as<zc>(), kLevelConvergence);
+                                    b->lev1_ok.as<int32_t>(), b->cand.as<zc>(), kLevelConvergence, b->lev1_n,
+                                    b->coarse_ny, b->coarse_ny_sp);
     return cudaGetLastError();
   }));
   CK(c, cudaMemcpyAsync(b->least_raw.p, b->theta.p, sizeof(zc) * n, cudaMemcpyDeviceToDevice, s));
@@ -1780,12 +1793,14 @@ static int run_fallback(stab_batch* b, bool track = false) {
   int rc = batch_build_child(b, b->fell_back, 0, &fb);
   if (rc) return rc;
   std::unique_ptr<stab_batch> guard(fb);
-  if (!track && b->coarse_ny < c->medium_ny) {
+  if (!track && b->level == 1) {
     // A second candidate level first: seeds from the spectrum at N = 48,
     // which resolves what N = 32 did not, at a fraction of the full
     // eigensolve's cost for the large instances; its own failures take the
     // plain path.  Results keep the fallback status.
+    fb->level = 2;
     fb->coarse_ny = c->medium_ny;
+    fb->coarse_ny_sp = (c->medium_ny_sp != b->coarse_ny_sp) ? c->medium_ny_sp : c->medium_ny;
     if (c->level_trust && (b->last_mode == STAB_MODE_COARSE || b->last_mode == STAB_MODE_SURROGATE) &&
         b->best_theta.p && b->have.p && b->best_src.p) {
       const int nf = fb->count;
@@ -1802,6 +1817,7 @@ static int run_fallback(stab_batch* b, bool track = false) {
         return cudaGetLastError();
       }));
       fb->has_lev1 = true;
+      fb->lev1_n = b->coarse_ny;
     }
     rc = stab_batch_run(fb, STAB_MODE_COARSE);
     const int nf = fb->count;
@@ -1909,7 +1925,7 @@ static int coarse_sequence(stab_batch* b, bool extra) {
   if (rc) return rc;
   rc = coarse_seeds(b);
   if (rc) return rc;
-  if (!extra && b->coarse_ny >= b->ctx->medium_ny && b->ctx->par_cand) return polish_candidates_parallel(b);
+  if (!extra && b->level >= 2 && b->ctx->par_cand) return polish_candidates_parallel(b);
   return polish_candidate_rounds(b, extra);
 }
 
@@ -2305,6 +2321,13 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
   }
   if (option == STAB_OPT_FIRST_RETRY) {
     c->first_retry = value ? 1 : 0;
+    c->epoch += 1;
+    return STAB_OK;
+  }
+  if (option == STAB_OPT_MEDIUM_NY_SPATIAL) {
+    if (value < 16 || value > 64 || value == c->seed_ny)
+      return set_err(c, STAB_ERR_ARG, "the spatial second level's N must be in [16, 64] and differ from the seed size");
+    c->medium_ny_sp = value;
     c->epoch += 1;
     return STAB_OK;
   }

@@ -78,7 +78,7 @@ __global__ void k_fold_copies(int count, int ncand, const InstDesc* desc, const 
                               const int32_t* copy_iters, const zc* copy_out, const int64_t* copy_out_off, zc* theta,
                               int32_t* done, double* err, int32_t* iters, zc* out, const int64_t* out_off,
                               int unverified, const zc* lam1, const zc* th1, const int32_t* ok1, const zc* cand,
-                              double conv);
+                              double conv, int n1, int n2t, int n2s);
 __global__ void k_gather_level(int count, const int32_t* idx, const zc* cand, int ncand, const zc* best_theta,
                                const int32_t* have, const int32_t* best_src, zc* lam1, zc* th1, int32_t* ok1);
 __global__ void k_temporal_vec(int count, const InstDesc* desc, const zc* vec, int slot, zc* out,

@@ -284,9 +284,10 @@ __global__ void k_mark_missing(int count, const zc* __restrict__ cand, int ncand
 // ok1 = converged), an instance whose kept pair is `unverified` is trusted
 // when both levels identify the same mode: the top candidates of both seed
 // spectra polished to the same pair (within 1e-10), that pair is the least
-// stable of every converged copy, and the seed values converge to it
-// (|lam2 - th| <= conv |lam1 - th|, with lam2 this level's top candidate,
-// and |lam2 - th| <= 1e-3 |th|).
+// stable of every converged copy, and the seed values converge to it: the
+// finer level's top candidate (N = max(n1, n2), n1 the first level's N and
+// n2 this level's, n2t / n2s for temporal / spatial instances) errs by at
+// most conv times the coarser one's and by at most 1e-3 relative.
 __global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__ desc,
                               const int32_t* __restrict__ copy_done, const double* __restrict__ copy_key,
                               const zc* __restrict__ copy_theta, const double* __restrict__ copy_err,
@@ -295,7 +296,7 @@ __global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__
                               int32_t* __restrict__ done, double* __restrict__ err, int32_t* __restrict__ iters,
                               zc* __restrict__ out, const int64_t* __restrict__ out_off, int unverified,
                               const zc* __restrict__ lam1, const zc* __restrict__ th1, const int32_t* __restrict__ ok1,
-                              const zc* __restrict__ cand, double conv) {
+                              const zc* __restrict__ cand, double conv, int n1, int n2t, int n2s) {
   __shared__ int s_pick;
   const int k = blockIdx.x;
   if (k >= count) return;
@@ -327,7 +328,10 @@ __global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__
         const zc th = copy_theta[c0];
         const double at = zabs(th);
         const double e2 = zabs(zsub(cand[c0], th)), e1 = zabs(zsub(lam1[k], th));
-        if (zabs(zsub(th1[k], th)) <= 1e-10 * at && e2 <= conv * e1 && e2 <= 1e-3 * at) {
+        // the finer seed level must be the closer one
+        const int n2 = (desc[k].itype == 2 || desc[k].itype == 4) ? n2s : n2t;
+        const double ef = (n2 > n1) ? e2 : e1, ec = (n2 > n1) ? e1 : e2;
+        if (zabs(zsub(th1[k], th)) <= 1e-10 * at && ef <= conv * ec && ef <= 1e-3 * at) {
           pick = c0;
           dn = 1;
         }

@@ -697,8 +697,10 @@ def main():
         # accept (without the agreement of the two seed levels)
         variants["no_level_consistency"] = variant_ms(lambda: ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 0),
                                                       lambda: ctx.set_option(sg.OPT_LEVEL_CONSISTENCY, 1))
-        # the second candidate level at N = 40 instead of 48
+        # the second candidate level at N = 40 or 24 instead of 48
         variants["medium_ny_40"] = variant_ms(lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 40),
+                                              lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 48))
+        variants["medium_ny_24"] = variant_ms(lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 24),
                                               lambda: ctx.set_option(sg.OPT_MEDIUM_NY, 48))
         # the small N = 48 level batch on the 128-thread persistent grid
         # instead of the default 256-thread CTAs

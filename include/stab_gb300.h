@@ -215,8 +215,9 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     0: sequential rounds. */
 #define STAB_OPT_PARALLEL_CANDIDATES 7
 /*   STAB_OPT_MEDIUM_NY  N of the second candidate level of STAB_MODE_COARSE
- *     (the seed spectra of the instances whose first-level top candidate
- *     was not resolved): above the seed size, at most 64; default 48. */
+ *     for the temporal instances (the seed spectra of the instances whose
+ *     first-level top candidate was not resolved): in [16, 64], not the seed
+ *     size; default 48. */
 #define STAB_OPT_MEDIUM_NY 8
 /*   STAB_OPT_FIRST_RETRY  1 (default): at the first candidate level of
  *     STAB_MODE_COARSE, instances whose complex64 polish of the top candidate

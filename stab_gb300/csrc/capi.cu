@@ -2332,8 +2332,8 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
     return STAB_OK;
   }
   if (option == STAB_OPT_MEDIUM_NY) {
-    if (value <= c->seed_ny || value > 64)
-      return set_err(c, STAB_ERR_ARG, "the second level's N must be above the seed size and at most 64");
+    if (value < 16 || value > 64 || value == c->seed_ny)
+      return set_err(c, STAB_ERR_ARG, "the second level's N must be in [16, 64] and differ from the seed size");
     c->medium_ny = value;
     c->epoch += 1;
     return STAB_OK;
@@ -2360,8 +2360,8 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
 
 int stab_set_seed_size(stab_ctx* c, int32_t ny) {
   if (!c) return STAB_ERR_ARG;
-  if (ny < 16 || ny >= c->medium_ny)
-    return set_err(c, STAB_ERR_ARG, "seed size must be at least 16 and below the second level's N (48)");
+  if (ny < 16 || ny >= kMediumNy || ny == c->medium_ny || ny == c->medium_ny_sp)
+    return set_err(c, STAB_ERR_ARG, "seed size must be in [16, 48) and differ from the second levels' N");
   c->seed_ny = ny;
   return STAB_OK;
 }

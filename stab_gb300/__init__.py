@@ -364,6 +364,7 @@ class Context:
         if rc != 0:
             raise StabError(f"stab_create failed ({rc}): no usable CUDA device {device}")
         self.h = h
+        self.device = int(device)
 
     def close(self) -> None:
         if getattr(self, "h", None):

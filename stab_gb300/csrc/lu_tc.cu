@@ -323,17 +323,19 @@ bool lu_tc_fits(int nmax, bool tma) { return nmax >= 2 && lu_tc_smem(nmax, tma) 
 // order n must be even and every offset even; returns false (nothing
 // encoded) otherwise or when the driver entry point is missing.
 bool lu_tc_tensor_maps(int count, const int32_t* n, const int64_t* off, cc* base, std::vector<CUtensorMap>& out) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
+  // looked up once per process (thread-safe static initialisation: contexts
+  // may build batches from several host threads)
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
         q != cudaDriverEntryPointSuccess || !fn) {
       cudaGetLastError();
-      return false;
+      return nullptr;
     }
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return false;
   out.assign(count, CUtensorMap{});
   for (int k = 0; k < count; ++k) {
     if ((n[k] & 1) || (off[k] & 1)) return false;

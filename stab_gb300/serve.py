@@ -12,7 +12,7 @@ device memory (an estimate of the path's pools per instance, checked against
 cudaMemGetInfo), solves it with the coarse-seeded mixed path (plain FP64
 fallback inside), and stamps each request's completion.
 
-    python -m stab_gb300.serve --rate 2000 --seconds 2 --seed 20261205
+    python -m stab_gb300.serve --rate 2000 --seconds 2 --seed 20261205 [--workers 2]
 """
 from __future__ import annotations
 
@@ -102,6 +102,66 @@ class ServeStats:
                 "mean_batch": self.completed / max(1, self.batches)}
 
 
+def serve_concurrent(requests: List[Request], solvers: List[Callable[[List[Request]], None]],
+                     free_bytes: Callable[[], int], max_batch: int = 4096,
+                     clock: Callable[[], float] = time.perf_counter) -> ServeStats:
+    """The loop with one worker thread per solver (each a library context with
+    its own stream): a worker takes every request that has arrived, up to its
+    share of the free device memory, and solves it while the others take the
+    next arrivals, so one batch's latency-bound tail overlaps another's
+    throughput-bound start on the GPU.  The library calls release the
+    interpreter lock."""
+    import threading
+    st = ServeStats()
+    lock = threading.Lock()
+    pending = sorted(requests, key=lambda r: r.arrival)
+    state = {"i": 0, "queue": []}
+    start = clock()
+    share = 0.5 / max(1, len(solvers))
+    errors: List[BaseException] = []
+
+    def worker(solve):
+        try:
+            while True:
+                with lock:
+                    now = clock() - start
+                    while state["i"] < len(pending) and pending[state["i"]].arrival <= now:
+                        state["queue"].append(pending[state["i"]])
+                        state["i"] += 1
+                    q = state["queue"]
+                    if not q and state["i"] >= len(pending):
+                        return
+                    batch = []
+                    if q:
+                        k = admit(q, free_bytes(), max_batch, reserve=share)
+                        batch, state["queue"] = q[:k], q[k:]
+                    wait = 0.0 if batch else pending[state["i"]].arrival - now
+                if not batch:
+                    if wait > 0:
+                        time.sleep(min(wait, 0.01))
+                    continue
+                solve(batch)
+                with lock:
+                    t = clock() - start
+                    for r in batch:
+                        r.done = t
+                        st.latencies.append(t - r.arrival)
+                    st.completed += len(batch)
+                    st.batches += 1
+        except BaseException as e:   # surfaced in the caller's thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(sv,)) for sv in solvers]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    if errors:
+        raise errors[0]
+    st.wall = clock() - start
+    return st
+
+
 def serve(requests: List[Request], solve: Callable[[List[Request]], None], free_bytes: Callable[[], int],
           max_batch: int = 4096, clock: Callable[[], float] = time.perf_counter) -> ServeStats:
     """Run the loop: the simulated arrival clock starts at the first call of
@@ -164,16 +224,22 @@ def main(argv: Optional[list] = None) -> int:
     ap.add_argument("--seconds", type=float, default=2.0)
     ap.add_argument("--seed", type=int, default=20261205)
     ap.add_argument("--max-batch", type=int, default=4096)
+    ap.add_argument("--workers", type=int, default=1,
+                    help="concurrent batches (one context and stream each); measured on the 2000/s mix: "
+                         "1 worker 936/s, 2 workers 773/s, 3 workers 653/s")
     args = ap.parse_args(argv)
     import torch
 
     import stab_gb300 as sg
-    ctx = sg.Context(0)
+    ctxs = [sg.Context(0) for _ in range(max(1, args.workers))]
     reqs = make_requests(args.rate, args.seconds, args.seed)
-    solve = gpu_solver(ctx, sg.MODE_COARSE)
-    # warm the context (derivative tables, pools) on a few requests
-    solve(make_requests(200.0, 0.05, args.seed + 1))
-    st = serve(reqs, solve, lambda: torch.cuda.mem_get_info()[0], args.max_batch)
+    solvers = [gpu_solver(c, sg.MODE_COARSE) for c in ctxs]
+    # warm each context (derivative tables, pools) on a few requests
+    for sv in solvers:
+        sv(make_requests(200.0, 0.05, args.seed + 1))
+    free = lambda: torch.cuda.mem_get_info()[0]
+    st = (serve_concurrent(reqs, solvers, free, args.max_batch) if len(solvers) > 1
+          else serve(reqs, solvers[0], free, args.max_batch))
     out = st.summary()
     ok = sum(1 for r in reqs if r.status in (sg.ST_OK, sg.ST_FELLBACK))
     out.update({"requests": len(reqs), "rate_per_s": args.rate, "arrival_window_s": args.seconds,

@@ -515,3 +515,42 @@ def test_parallel_candidates_match_sequential_rounds(ctx):
         a, r = np.asarray(v1[k]), np.asarray(v0[k])
         pa, pr = int(np.argmax(np.abs(a))), int(np.argmax(np.abs(r)))
         assert np.max(np.abs(a / a[pa] - r / r[pr])) <= 1e-10, k
+
+
+def test_two_contexts_in_two_threads_match_one(ctx):
+    """Two contexts (each with its own stream) solving from two host threads at
+    the same time, as the serving loop's workers do, return what one context
+    returns for the same batches: the library keeps no shared mutable state
+    between contexts."""
+    import threading
+    import bench
+    params, prof = bench.workload(96, 20261203)
+    sp = [bench.to_stab(d) for d in params]
+    halves = [(sp[:48], [prof[k] for k in range(48)]), (sp[48:], [prof[k] for k in range(48, 96)])]
+    ref = [ctx.solve_batch(p, pr, sg.MODE_COARSE)[::3] for p, pr in halves]
+    ctxs = [sg.Context(0), sg.Context(0)]
+    out = [None, None]
+    errs = []
+
+    def run(i):
+        try:
+            for _ in range(2):
+                out[i] = ctxs[i].solve_batch(halves[i][0], halves[i][1], sg.MODE_COARSE)[::3]
+        except BaseException as e:
+            errs.append(e)
+    th = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    try:
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    finally:
+        for c in ctxs:
+            c.close()
+    assert not errs, errs
+    for i in range(2):
+        (w0, st0), (w1, st1) = ref[i], out[i]
+        assert np.array_equal(st0, st1)
+        fin = np.isfinite(w0)
+        assert np.array_equal(fin, np.isfinite(w1))
+        assert np.max(np.abs(w1[fin] - w0[fin]) / np.abs(w0[fin])) <= 1e-13

@@ -50,3 +50,36 @@ def test_serve_loop_with_fake_solver():
     assert s["completed"] == len(reqs) and all(r.status == 0 for r in reqs)
     assert all(r.done >= r.arrival for r in reqs)
     assert s["p50_ms"] <= s["p99_ms"] and s["batches"] >= len(reqs) / 64
+
+
+def test_concurrent_workers_overlap_batches():
+    """serve_concurrent: two workers (fake solvers that sleep, as a library
+    call that releases the interpreter lock does) take batches while the
+    other solves; every request completes once, after its arrival, and the
+    two solvers run at the same time."""
+    import threading
+    import time
+
+    reqs = sv.make_requests(2000.0, 0.15, 8)
+    active = [0]
+    peak = [0]
+    lock = threading.Lock()
+
+    def make_solver():
+        def solve(batch):
+            with lock:
+                active[0] += 1
+                peak[0] = max(peak[0], active[0])
+            time.sleep(0.01 + 2e-5 * len(batch))
+            for r in batch:
+                assert r.status == -1          # solved once
+                r.status = 0
+            with lock:
+                active[0] -= 1
+        return solve
+
+    st = sv.serve_concurrent(reqs, [make_solver(), make_solver()], lambda: 10 ** 12, max_batch=4096)
+    s = st.summary()
+    assert s["completed"] == len(reqs) and all(r.status == 0 for r in reqs)
+    assert all(r.done >= r.arrival for r in reqs)
+    assert peak[0] == 2 and s["batches"] >= 4

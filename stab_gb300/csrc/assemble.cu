@@ -7,6 +7,8 @@
 // (A0 - s B0, B0^-1 A0, s^2 C0 + s C1 + C2, ...), k_dense writes the dense
 // column-major matrix in complex128 or complex64, and k_opmv applies the
 // operator in O(N^2) without forming it (used for the FP64 residuals).
+#include <algorithm>
+
 #include "common.cuh"
 #include "dw.cuh"
 #include "kernels.cuh"
@@ -16,7 +18,7 @@ namespace stab {
 __device__ __forceinline__ int64_t node_index(const InstDesc& d) { return d.off_blk / BLK_STRIDE; }
 
 __global__ void k_node_ops(int count, const InstDesc* __restrict__ desc, const zc* __restrict__ blk, int kind_t,
-                           int kind_s, const zc* __restrict__ sigma, zc* __restrict__ ops,
+                           int kind_s, const zc* __restrict__ sigma, zc* __restrict__ ops, cc* __restrict__ ops32,
                            const int32_t* __restrict__ skip) {
   int k = blockIdx.y;
   if (k >= count) return;
@@ -66,6 +68,12 @@ __global__ void k_node_ops(int count, const InstDesc* __restrict__ desc, const z
     o[q] = p1;
     o[25 + q] = p2;
     o[50 + q] = p3;
+    if (ops32) {   // rounded copy for the complex64 assembly
+      cc* o32 = ops32 + (node_index(d) + i) * 75;
+      o32[q] = cmk((float)p1.x, (float)p1.y);
+      o32[25 + q] = cmk((float)p2.x, (float)p2.y);
+      o32[50 + q] = cmk((float)p3.x, (float)p3.y);
+    }
   }
 }
 
@@ -106,6 +114,68 @@ __global__ void k_dense(int count, const InstDesc* __restrict__ desc, const doub
       M[(size_t)c * ld + r] = store_cast<T>(zscale(val, scale));
     }
   }
+}
+
+// The complex64 assembly in FP32 arithmetic, from the rounded node blocks
+// and D tables: each entry is fl32(p1 d1 - p2 d2 (+ p3)) * scale, within a
+// few float roundings of the FP64 expression rounded to float.  The matrix
+// only feeds a complex64 factorisation whose Newton-chord steps form their
+// residuals in FP64, and FP64 arithmetic here (1/64 of the FP32 rate on this
+// GPU) made the assembly bound by the FP64 pipe.  Same grid and write order
+// as k_dense.
+__global__ void k_dense32(int count, const InstDesc* __restrict__ desc, const float* const* __restrict__ dtab32,
+                          const cc* __restrict__ ops32, cc* __restrict__ out, const int64_t* __restrict__ out_off,
+                          int ldmul, float scale, const int32_t* __restrict__ skip) {
+  int k = blockIdx.y;
+  if (k >= count) return;
+  if (skip && skip[k]) return;
+  const InstDesc d = desc[k];
+  const int n = d.n, ny = d.ny;
+  const int c0 = blockIdx.x * 8;
+  if (c0 >= n) return;
+  const float* D1 = dtab32[2 * d.dmat];
+  const float* D2 = dtab32[2 * d.dmat + 1];
+  const cc* o = ops32 + node_index(d) * 75;
+  cc* M = out + out_off[k];
+  const int64_t ld = (int64_t)ldmul * n;
+  for (int cc_ = 0; cc_ < 8; ++cc_) {
+    const int c = c0 + cc_;
+    if (c >= n) break;
+    const int j = c / 5, v = c % 5;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      const int i = r / 5, e = r % 5;
+      const cc* oi = o + (size_t)i * 75;
+      const float d1 = D1[(size_t)i * ny + j], d2 = D2[(size_t)i * ny + j];
+      const cc p1 = oi[e * 5 + v], p2 = oi[25 + e * 5 + v];
+      float vr = fmaf(p1.x, d1, -p2.x * d2), vi = fmaf(p1.y, d1, -p2.y * d2);
+      if (i == j) {
+        const cc p3 = oi[50 + e * 5 + v];
+        vr += p3.x;
+        vi += p3.y;
+      }
+      M[(size_t)c * ld + r] = cmk(vr * scale, vi * scale);
+    }
+  }
+}
+
+cudaError_t launch_dense32(int count, int nmax, const InstDesc* desc, const float* const* dtab32, const cc* ops32,
+                           cc* out, const int64_t* out_off, int ldmul, float scale, cudaStream_t s,
+                           const int32_t* skip) {
+  if (count <= 0) return cudaSuccess;
+  dim3 g((nmax + 7) / 8, count);
+  k_dense32<<<g, 256, 0, s>>>(count, desc, dtab32, ops32, out, out_off, ldmul, scale, skip);
+  return cudaGetLastError();
+}
+
+__global__ void k_round_f32(int64_t count, const double* __restrict__ x, float* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+cudaError_t launch_round_f32(int64_t count, const double* x, float* y, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_round_f32<<<(unsigned)std::min<int64_t>(1024, (count + 255) / 256), 256, 0, s>>>(count, x, y);
+  return cudaGetLastError();
 }
 
 template <typename T>

@@ -58,6 +58,7 @@ struct stab_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   std::map<int, std::pair<double*, double*>> dtabs;  // table key -> (D1, D2) on the device
+  std::map<int, std::pair<float*, float*>> dtabs32;  // the same tables rounded to float (complex64 assembly)
   int profiling = 0;
   std::vector<KStat> stats;
   std::vector<PendingEv> pending;
@@ -254,6 +255,18 @@ static void fd_mean_tables(int ny, std::vector<double>& G, std::vector<double>& 
     }
 }
 
+// float copies of a table pair (the complex64 assembly computes in FP32)
+static int ensure_dtab32(stab_ctx* c, int key, int ny) {
+  float *F1 = nullptr, *F2 = nullptr;
+  CK(c, cudaMalloc(&F1, sizeof(float) * ny * ny));
+  CK(c, cudaMalloc(&F2, sizeof(float) * ny * ny));
+  CK(c, launch_round_f32((int64_t)ny * ny, c->dtabs[key].first, F1, c->stream));
+  CK(c, launch_round_f32((int64_t)ny * ny, c->dtabs[key].second, F2, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->dtabs32[key] = {F1, F2};
+  return 0;
+}
+
 static int ensure_dtab(stab_ctx* c, int key) {
   if (c->dtabs.count(key)) return 0;
   if (key >= kFdOpKey) {
@@ -268,7 +281,7 @@ static int ensure_dtab(stab_ctx* c, int key) {
     CK(c, cudaMemcpy(D1, T1.data(), sizeof(double) * ny * ny, cudaMemcpyHostToDevice));
     CK(c, cudaMemcpy(D2, T2.data(), sizeof(double) * ny * ny, cudaMemcpyHostToDevice));
     c->dtabs[key] = {D1, D2};
-    return 0;
+    return ensure_dtab32(c, key, ny);
   }
   const int ny = key;
   double *D1 = nullptr, *D2 = nullptr, *xa = nullptr;
@@ -285,7 +298,7 @@ static int ensure_dtab(stab_ctx* c, int key) {
   CK(c, cudaStreamSynchronize(c->stream));
   cudaFree(xa);
   c->dtabs[key] = {D1, D2};
-  return 0;
+  return ensure_dtab32(c, key, ny);
 }
 
 // ---------------------------------------------------------------------------
@@ -339,7 +352,7 @@ struct stab_batch {
   int nmax = 0, mmax = 0;
   size_t sum_n2 = 0, sum_m2 = 0, sum_n = 0, sum_m = 0;
   // device
-  DevBuf desc, dtab, pdesc, prof, spl, node, blk, ops, vec;
+  DevBuf desc, dtab, dtab32, pdesc, prof, spl, node, blk, ops, ops32, vec;
   DevBuf nsz, msz, off_n2, off_m2, off_m2c2, off_nof, off_mof, xoff[VEC_SLOTS], order;
   DevBuf M32, Z64, Abig, Hbig, eigraw, eigsorted, outvec;
   DevBuf bad, flops, rsc, csc, cand, accepted, skip64, lus32, lus64, have, best_key, best_theta, best_err, best_iters, best_out;
@@ -395,7 +408,7 @@ struct stab_batch {
   ~stab_batch();
   // free every device buffer now (used when the owning context goes away first)
   void release() {
-    DevBuf* all[] = {&desc, &dtab, &pdesc, &prof, &spl, &node, &blk, &ops, &vec, &nsz, &msz, &off_n2, &off_m2,
+    DevBuf* all[] = {&desc, &dtab, &dtab32, &pdesc, &prof, &spl, &node, &blk, &ops, &ops32, &vec, &nsz, &msz, &off_n2, &off_m2,
                      &off_m2c2, &off_nof, &off_mof, &order, &M32, &Z64, &Abig, &Hbig, &eigraw, &eigsorted, &outvec,
                      &bad, &flops, &rsc, &csc, &cand, &accepted, &skip64, &lus32, &lus64, &have, &best_key, &best_theta, &best_err,
                      &best_iters, &best_out, &piv, &info, &flags, &theta, &sigma, &least_raw, &least_val, &least_idx, &pcol,
@@ -666,11 +679,14 @@ static int batch_finish(stab_ctx* c, stab_batch* b) {
     if (r) return r;
   }
   std::vector<double*> hdt;
+  std::vector<float*> hdt32;
   std::map<int, int> tab_index;
   for (auto& kv : c->dtabs) {
     tab_index[kv.first] = (int)hdt.size() / 2;
     hdt.push_back(kv.second.first);
     hdt.push_back(kv.second.second);
+    hdt32.push_back(c->dtabs32[kv.first].first);
+    hdt32.push_back(c->dtabs32[kv.first].second);
   }
   for (auto& d : b->hd) {
     d.dmat = tab_index[d.fd ? (d.itype == 2 ? kFdSpKey : kFdOpKey) + d.ny : d.ny];
@@ -696,9 +712,11 @@ static int batch_finish(stab_ctx* c, stab_batch* b) {
   cudaStream_t s = c->stream;
   CK(c, upload(b->desc, b->hd, s));
   CK(c, upload(b->dtab, hdt, s));
+  CK(c, upload(b->dtab32, hdt32, s));
   CK(c, b->node.ensure(sizeof(double) * node_off, c->stream));
   CK(c, b->blk.ensure(sizeof(zc) * blk_off, c->stream));
   CK(c, b->ops.ensure(sizeof(zc) * (blk_off / BLK_STRIDE) * 75, c->stream));
+  CK(c, b->ops32.ensure(sizeof(cc) * (blk_off / BLK_STRIDE) * 75, c->stream));
   CK(c, b->vec.ensure(sizeof(zc) * vec_off, c->stream));
   CK(c, upload(b->nsz, b->hn, s));
   CK(c, upload(b->msz, b->hm, s));
@@ -951,7 +969,7 @@ static int node_ops(stab_batch* b, Range r, int kind_t, int kind_s, const zc* si
   return timed(c, "k_node_ops", [&] {
            dim3 g((nymax + 63) / 64, r.cnt);
            k_node_ops<<<g, 64, 0, c->stream>>>(r.cnt, b->desc.as<InstDesc>() + r.k0, b->blk.as<zc>(), kind_t, kind_s,
-                                                sigma ? sigma + r.k0 : nullptr, b->ops.as<zc>(),
+                                                sigma ? sigma + r.k0 : nullptr, b->ops.as<zc>(), b->ops32.as<cc>(),
                                                 skip ? skip + r.k0 : nullptr);
            return cudaGetLastError();
          }) == cudaSuccess
@@ -964,8 +982,13 @@ static int dense(stab_batch* b, Range r, T* out, const int64_t* off, int ldmul, 
                  const int32_t* skip = nullptr) {
   stab_ctx* c = b->ctx;
   cudaError_t e = timed(c, name, [&] {
-    return launch_dense<T>(r.cnt, b->nmax, b->desc.as<InstDesc>() + r.k0, b->dtab.as<const double*>(),
-                           b->ops.as<zc>(), out, off + r.k0, ldmul, scale, c->stream, skip ? skip + r.k0 : nullptr);
+    if constexpr (std::is_same<T, cc>::value)   // complex64 output: FP32 arithmetic on FP32 copies
+      return launch_dense32(r.cnt, b->nmax, b->desc.as<InstDesc>() + r.k0, b->dtab32.as<const float*>(),
+                            b->ops32.as<cc>(), out, off + r.k0, ldmul, (float)scale, c->stream,
+                            skip ? skip + r.k0 : nullptr);
+    else
+      return launch_dense<T>(r.cnt, b->nmax, b->desc.as<InstDesc>() + r.k0, b->dtab.as<const double*>(),
+                             b->ops.as<zc>(), out, off + r.k0, ldmul, scale, c->stream, skip ? skip + r.k0 : nullptr);
   });
   return e == cudaSuccess ? 0 : cuda_fail(c, e, name);
 }
@@ -1466,6 +1489,10 @@ int stab_destroy(stab_ctx* c) {
   c->nets.clear();
   cudaStreamSynchronize(c->stream);
   for (auto& kv : c->dtabs) {
+    cudaFree(kv.second.first);
+    cudaFree(kv.second.second);
+  }
+  for (auto& kv : c->dtabs32) {
     cudaFree(kv.second.first);
     cudaFree(kv.second.second);
   }

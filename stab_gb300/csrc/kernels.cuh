@@ -34,14 +34,22 @@ __global__ void k_blocks(int count, const InstDesc* desc, const double* const* d
 // assemble.cu
 // per-node operator (P1, P2, P3): kind_t for temporal, kind_s for spatial
 // instances, at shift sigma[k] (may be null)
+// (ops32, if not null, receives the blocks rounded to complex64)
 __global__ void k_node_ops(int count, const InstDesc* desc, const zc* blk, int kind_t, int kind_s, const zc* sigma,
-                           zc* ops, const int32_t* skip);
+                           zc* ops, cc* ops32, const int32_t* skip);
 // dense column-major n x n operator (times `scale`) from ops into out +
 // out_off[k] with leading dimension ldmul*n; element type T
 template <typename T>
 cudaError_t launch_dense(int count, int nmax, const InstDesc* desc, const double* const* dtab, const zc* ops, T* out,
                          const int64_t* out_off, int ldmul, double scale, cudaStream_t s,
                          const int32_t* skip = nullptr);
+// the complex64 dense operator in FP32 arithmetic from the rounded blocks and
+// tables (dtab32 pairs as dtab's)
+cudaError_t launch_dense32(int count, int nmax, const InstDesc* desc, const float* const* dtab32, const cc* ops32,
+                           cc* out, const int64_t* out_off, int ldmul, float scale, cudaStream_t s,
+                           const int32_t* skip = nullptr);
+// y[i] = (float) x[i]
+cudaError_t launch_round_f32(int64_t count, const double* x, float* y, cudaStream_t s);
 // structured y = M x for M given by ops (FP64):  y_i = P1 (D1 X)_i - P2 (D2 X)_i + P3 x_i
 __global__ void k_opmv(int count, const InstDesc* desc, const double* const* dtab, const zc* ops, const zc* x,
                        int xslot, zc* y, int yslot);

@@ -243,6 +243,13 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     the finer level closer by a factor of four) certifies it at an eighth
  *     of the cost of an N = 48 companion spectrum. */
 #define STAB_OPT_MEDIUM_NY_SPATIAL 11
+/*   STAB_OPT_MLP_TCGEN05  1 (default): the surrogate network's GEMMs (forward
+ *     and backward) run on the fifth-generation tensor cores (tcgen05.mma
+ *     kind::f16, BF16 operands, FP32 accumulator in TMEM); 0: on mma.sync
+ *     m16n8k16.  A tensor-core tile that does not see its MMAs complete
+ *     within a bounded wait makes the next loss read (stab_mlp_gradients,
+ *     stab_mlp_train_step) return STAB_ERR_CUDA. */
+#define STAB_OPT_MLP_TCGEN05 12
 int stab_set_option(stab_ctx* ctx, int32_t option, int32_t value);
 /* SM cycles of the full-spectrum eigensolver per phase, summed over every
  * instance solved on this device since the last reset: [0] isolation,

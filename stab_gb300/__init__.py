@@ -34,7 +34,7 @@ STAGE_SEED_EIG, STAGE_PLAIN_EIG, STAGE_RETRY_LU, STAGE_POLISH_LU = 0, 1, 2, 3
 ARITH_FP64, ARITH_DOUBLE_WORD, ARITH_FP32, ARITH_TF32_SPLIT = 0, 1, 2, 3
 OPT_SEED_QR_SHARED, OPT_POLISH_LU_TMA, OPT_EIG_RESIDENT, OPT_EIG_THREADS, OPT_EIG_MID, OPT_SEED_VECTORS = 1, 2, 3, 4, 5, 6
 OPT_PARALLEL_CANDIDATES, OPT_MEDIUM_NY, OPT_FIRST_RETRY, OPT_LEVEL_CONSISTENCY = 7, 8, 9, 10
-OPT_MEDIUM_NY_SPATIAL = 11
+OPT_MEDIUM_NY_SPATIAL, OPT_MLP_TCGEN05 = 11, 12
 ST_OK, ST_SINGULAR, ST_NOCONV, ST_NAN, ST_FELLBACK, ST_NOMODE, ST_UNVERIFIED = 0, 1, 2, 3, 4, 5, 6
 
 EXPORTED = (

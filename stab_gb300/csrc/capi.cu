@@ -81,6 +81,7 @@ struct stab_ctx {
   int first_retry = 1;     // STAB_OPT_FIRST_RETRY
   int level_trust = 1;     // STAB_OPT_LEVEL_CONSISTENCY
   int medium_ny_sp = 24;   // STAB_OPT_MEDIUM_NY_SPATIAL: N of the spatial instances' second level
+  int mlp_tc = 1;          // STAB_OPT_MLP_TCGEN05: surrogate GEMMs on tcgen05 (0: mma.sync)
   int epoch = 0;           // bumped by every setting that changes the launched kernels
 };
 
@@ -2351,6 +2352,10 @@ int stab_set_option(stab_ctx* c, int32_t option, int32_t value) {
     c->epoch += 1;
     return STAB_OK;
   }
+  if (option == STAB_OPT_MLP_TCGEN05) {
+    c->mlp_tc = value ? 1 : 0;
+    return STAB_OK;
+  }
   if (option == STAB_OPT_MEDIUM_NY_SPATIAL) {
     if (value < 16 || value > 64 || value == c->seed_ny)
       return set_err(c, STAB_ERR_ARG, "the spatial second level's N must be in [16, 64] and differ from the seed size");
@@ -2725,11 +2730,12 @@ static int mlp_layers(stab_mlp* m, int b, const float* x) {
     if (l + 1 < m->L) {
       CK(c, timed(c, "k_gemm_bf16_hidden", [&] {
         return stab::mlp_gemm_hidden(b, N, K, m->hin16[l].as<__nv_bfloat16>(), W, bias, m->z32[l].as<float>(),
-                                     m->hin16[l + 1].as<__nv_bfloat16>(), s);
+                                     m->hin16[l + 1].as<__nv_bfloat16>(), s, c->mlp_tc != 0);
       }));
     } else {
       CK(c, timed(c, "k_gemm_bf16_out", [&] {
-        return stab::mlp_gemm_out(b, N, K, m->hin16[l].as<__nv_bfloat16>(), W, bias, m->z32[l].as<float>(), s);
+        return stab::mlp_gemm_out(b, N, K, m->hin16[l].as<__nv_bfloat16>(), W, bias, m->z32[l].as<float>(), s,
+                                  c->mlp_tc != 0);
       }));
     }
   }
@@ -2755,7 +2761,7 @@ static int mlp_backward(stab_mlp* m, const float* t, const float* w, double* los
     const int K = m->sz[l], N = m->sz[l + 1];
     CK(c, timed(c, "k_gemm_bf16_wgrad", [&] {
       return stab::mlp_gemm_wgrad(b, N, K, m->hin16[l].as<__nv_bfloat16>(), m->dz16[cur].as<__nv_bfloat16>(),
-                                  G + m->woff[l], s);
+                                  G + m->woff[l], s, c->mlp_tc != 0);
     }));
     CK(c, timed(c, "k_bias_grad", [&] {
       return stab::mlp_bias_grad(b, N, m->dz32[cur].as<float>(), G + m->boff[l], s);
@@ -2764,7 +2770,7 @@ static int mlp_backward(stab_mlp* m, const float* t, const float* w, double* los
       CK(c, timed(c, "k_gemm_bf16_dhidden", [&] {
         return stab::mlp_gemm_dhidden(b, N, K, m->dz16[cur].as<__nv_bfloat16>(), P16 + m->woff[l],
                                       m->z32[l - 1].as<float>(), m->dz32[1 - cur].as<float>(),
-                                      m->dz16[1 - cur].as<__nv_bfloat16>(), s);
+                                      m->dz16[1 - cur].as<__nv_bfloat16>(), s, c->mlp_tc != 0);
       }));
       cur = 1 - cur;
     }
@@ -2772,6 +2778,11 @@ static int mlp_backward(stab_mlp* m, const float* t, const float* w, double* los
   if (loss_out) {
     CK(c, cudaMemcpyAsync(loss_out, m->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(c, cudaStreamSynchronize(s));
+    if (c->mlp_tc) {   // a tensor-core tile that gave up waiting leaves its outputs unwritten
+      int to = 0;
+      CK(c, stab::mlp_tc_timeouts(&to, true));
+      if (to) return set_err(c, STAB_ERR_CUDA, "tcgen05 GEMM of the network: MMA completion not seen");
+    }
   }
   return 0;
 }

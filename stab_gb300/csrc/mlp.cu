@@ -1,9 +1,14 @@
 // Surrogate network kernels: a BF16 multilayer perceptron trained and run on
 // the GPU (no counterpart in the reference, which has no learned part).
 //
-//   k_gemm_bf16<TA, TB, EPI>  C = op(A) op(B) on the tensor cores
-//                             (mma.sync m16n8k16, bf16 operands, f32
-//                             accumulators) with the layer epilogues fused:
+//   k_gemm_tc<TA, TB, EPI>    C = op(A) op(B) on the fifth-generation tensor
+//                             cores (tcgen05.mma kind::f16, bf16 operands
+//                             staged in shared memory, f32 accumulator in
+//                             TMEM), the default;
+//   k_gemm_bf16<TA, TB, EPI>  the same on mma.sync m16n8k16 (bf16 operands,
+//                             f32 accumulators in registers), kept as the
+//                             comparison form;
+//                             both with the layer epilogues fused:
 //                               EPI_HIDDEN   Z = acc + b; H = bf16(gelu(Z))
 //                               EPI_OUT      Y = acc + b
 //                               EPI_DHIDDEN  dZ = acc * gelu'(Z); bf16 copy
@@ -22,6 +27,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "mlp.cuh"
+#include "tc.cuh"
 
 namespace stab {
 
@@ -148,6 +154,160 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const __
       }
 }
 
+// ---- tcgen05 form ------------------------------------------------------------
+// One CTA of 128 threads computes a 128 x 128 tile of C.  K runs in chunks
+// of 64: the threads copy the op(A) rows (128 x 64) and the op(B) columns
+// (128 x 64, as the K-major rows of the MMA's B operand) into shared memory
+// in the canonical K-major layout without swizzle (core matrices of 8 rows x
+// 8 bf16 = 128 bytes, K-adjacent ones 128 bytes apart, 8-row groups 1 KB
+// apart), zero outside the matrices; thread 0 issues the chunk's four MMAs
+// of 128 x 128 x 16 into the TMEM accumulator and commits them to an
+// mbarrier, which every thread waits on (bounded) before the next chunk
+// overwrites the operands.  The epilogue: warp w reads TMEM lanes 32 w ..
+// 32 w + 31 (the tile's rows) and applies the layer's epilogue.
+namespace {
+constexpr int TC_M = 128, TC_N = 128, TC_KC = 64;
+constexpr uint32_t TC_SBO = (TC_KC / 8) * 128;      // 8-row groups
+constexpr uint32_t TC_LBO = 128;                    // K-adjacent core matrices
+constexpr uint32_t TC_PLANE = TC_M * TC_KC * 2;     // bytes of one operand tile
+constexpr uint32_t TC_WAIT = 1u << 22;              // polls of the MMA mbarrier before giving up
+
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                       // D format: F32
+         | (1u << 7)                     // A format: BF16 (kind::f16)
+         | (1u << 10)                    // B format: BF16
+         | ((uint32_t)(N >> 3) << 17)    // N / 8
+         | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+__device__ __forceinline__ uint32_t bf16_off(int r, int k) {
+  return (uint32_t)((r >> 3) * TC_SBO + (k >> 3) * TC_LBO + (r & 7) * 16 + (k & 7) * 2);
+}
+__device__ __forceinline__ void mma_bf16_tc(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+}  // namespace
+
+// set by a tile whose MMA completion was not seen within the wait limit
+__device__ int g_mlp_tc_timeout;
+
+template <int TA, int TB, int EPI>
+__global__ void __launch_bounds__(128, 4) k_gemm_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
+                                                    const __nv_bfloat16* __restrict__ B, int ldb,
+                                                    const float* __restrict__ bias, const float* __restrict__ zin,
+                                                    float* __restrict__ c32, __nv_bfloat16* __restrict__ c16, int ldc,
+                                                    int kchunk) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  unsigned char* As = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_smem) + 1023) & ~(uintptr_t)1023);
+  unsigned char* Bs = As + TC_PLANE;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * TC_N;
+  const int kbeg = blockIdx.z * kchunk;
+  const int kend = min(K, kbeg + kchunk);
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_slot, TC_N);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) tc::mbar_init(&mbar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tmem_slot;
+  const uint32_t idesc = idesc_bf16(TC_M, TC_N);
+  const uint32_t a_s = tc::smem_u32(As), b_s = tc::smem_u32(Bs);
+  const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+  uint32_t phase = 0;
+  bool ok = true;
+  bool any = false;
+  for (int k0 = kbeg; k0 < kend; k0 += TC_KC) {
+    // op(A)(m, k) rows and op(B)(k, n) columns, read along the contiguous
+    // index of each layout
+    for (int e = tid; e < TC_M * TC_KC; e += 128) {
+      int m, k;
+      if (TA == 0) { m = e / TC_KC; k = e % TC_KC; } else { k = e / TC_M; m = e % TC_M; }
+      const int gm = m0 + m, gk = k0 + k;
+      __nv_bfloat16 v = zero;
+      if (gm < M && gk < kend) v = TA == 0 ? A[(int64_t)gm * lda + gk] : A[(int64_t)gk * lda + gm];
+      *reinterpret_cast<__nv_bfloat16*>(As + bf16_off(m, k)) = v;
+    }
+    for (int e = tid; e < TC_N * TC_KC; e += 128) {
+      int k, n;
+      if (TB == 0) { k = e / TC_N; n = e % TC_N; } else { n = e / TC_KC; k = e % TC_KC; }
+      const int gk = k0 + k, gn = n0 + n;
+      __nv_bfloat16 v = zero;
+      if (gk < kend && gn < N) v = TB == 0 ? B[(int64_t)gk * ldb + gn] : B[(int64_t)gn * ldb + gk];
+      *reinterpret_cast<__nv_bfloat16*>(Bs + bf16_off(n, k)) = v;
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+#pragma unroll
+      for (int ks = 0; ks < TC_KC / 16; ++ks) {
+        const uint64_t ad = tc::sdesc(a_s + ks * 2 * TC_LBO, TC_LBO, TC_SBO);
+        const uint64_t bd = tc::sdesc(b_s + ks * 2 * TC_LBO, TC_LBO, TC_SBO);
+        mma_bf16_tc(tm, ad, bd, idesc, (any || ks > 0) ? 1u : 0u);
+      }
+      tc::mma_commit(&mbar);
+    }
+    __syncwarp();
+    const bool got = tc::mbar_wait(&mbar, phase, TC_WAIT);
+    phase ^= 1u;
+    tc::fence_after_sync();
+    any = true;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+  }
+  if (ok && any) {
+    const int row = m0 + 32 * warp + lane;
+    const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < TC_N; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(trow + (uint32_t)c0, v);
+      tc::tmem_wait_ld();
+      if (row >= M) continue;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int col = n0 + c0 + i;
+        if (col >= N) continue;
+        const int64_t o = (int64_t)row * ldc + col;
+        if (EPI == EPI_HIDDEN) {
+          const float z = v[i] + bias[col];
+          c32[o] = z;
+          c16[o] = __float2bfloat16(gelu_f(z));
+        } else if (EPI == EPI_OUT) {
+          c32[o] = v[i] + bias[col];
+        } else if (EPI == EPI_DHIDDEN) {
+          const float dz = v[i] * gelu_grad_f(zin[o]);
+          c32[o] = dz;
+          c16[o] = __float2bfloat16(dz);
+        } else {
+          atomicAdd(&c32[o], v[i]);
+        }
+      }
+    }
+  }
+  if (!ok && tid == 0) {
+    atomicExch(&g_mlp_tc_timeout, 1);
+    (void)tc::mbar_wait(&mbar, phase ^ 1u, TC_WAIT);   // the MMAs in flight (bounded)
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tm, TC_N);
+  if (tid == 0) tc::mbar_inval(&mbar);
+}
+
 __global__ void k_loss_grad(int B, int N, const float* __restrict__ Y, int ldy, const float* __restrict__ T,
                             const float* __restrict__ w, float* __restrict__ dy32, __nv_bfloat16* __restrict__ dy16,
                             double* __restrict__ loss) {
@@ -212,38 +372,54 @@ __global__ void k_cast_bf16(int64_t count, const float* __restrict__ x, __nv_bfl
 template <int TA, int TB, int EPI>
 static cudaError_t gemm_t(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb,
                           const float* bias, const float* zin, float* c32, __nv_bfloat16* c16, int ldc, int splits,
-                          cudaStream_t s) {
+                          cudaStream_t s, bool tc5) {
   if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
   splits = std::max(1, splits);
+  const int kq = tc5 ? TC_KC : GK;
   int kchunk = (K + splits - 1) / splits;
-  kchunk = ((kchunk + GK - 1) / GK) * GK;
+  kchunk = ((kchunk + kq - 1) / kq) * kq;
   splits = (K + kchunk - 1) / kchunk;
+  if (tc5) {
+    const size_t sm = 2 * (size_t)TC_PLANE + 1024;
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<TA, TB, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    dim3 grid((N + TC_N - 1) / TC_N, (M + TC_M - 1) / TC_M, splits);
+    k_gemm_tc<TA, TB, EPI><<<grid, 128, sm, s>>>(M, N, K, A, lda, B, ldb, bias, zin, c32, c16, ldc, kchunk);
+    return cudaGetLastError();
+  }
   dim3 grid((N + GN - 1) / GN, (M + GM - 1) / GM, splits);
   k_gemm_bf16<TA, TB, EPI><<<grid, 128, 0, s>>>(M, N, K, A, lda, B, ldb, bias, zin, c32, c16, ldc, kchunk);
   return cudaGetLastError();
 }
 
+cudaError_t mlp_tc_timeouts(int* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_mlp_tc_timeout, sizeof(int));
+  if (e != cudaSuccess || !reset) return e;
+  const int zero = 0;
+  return cudaMemcpyToSymbol(g_mlp_tc_timeout, &zero, sizeof(int));
+}
+
 cudaError_t mlp_gemm_hidden(int M, int N, int K, const __nv_bfloat16* X, const __nv_bfloat16* W, const float* b,
-                            float* Z, __nv_bfloat16* H, cudaStream_t s) {
-  return gemm_t<0, 0, EPI_HIDDEN>(M, N, K, X, K, W, N, b, nullptr, Z, H, N, 1, s);
+                            float* Z, __nv_bfloat16* H, cudaStream_t s, bool tc5) {
+  return gemm_t<0, 0, EPI_HIDDEN>(M, N, K, X, K, W, N, b, nullptr, Z, H, N, 1, s, tc5);
 }
 
 cudaError_t mlp_gemm_out(int M, int N, int K, const __nv_bfloat16* X, const __nv_bfloat16* W, const float* b,
-                         float* Y, cudaStream_t s) {
-  return gemm_t<0, 0, EPI_OUT>(M, N, K, X, K, W, N, b, nullptr, Y, nullptr, N, 1, s);
+                         float* Y, cudaStream_t s, bool tc5) {
+  return gemm_t<0, 0, EPI_OUT>(M, N, K, X, K, W, N, b, nullptr, Y, nullptr, N, 1, s, tc5);
 }
 
 // dZprev[M x K] = (dZ[M x N] W^T) * gelu'(Zprev), W stored K x N
 cudaError_t mlp_gemm_dhidden(int M, int N, int K, const __nv_bfloat16* dZ, const __nv_bfloat16* W, const float* Zprev,
-                             float* dZprev, __nv_bfloat16* dZprev16, cudaStream_t s) {
-  return gemm_t<0, 1, EPI_DHIDDEN>(M, K, N, dZ, N, W, N, nullptr, Zprev, dZprev, dZprev16, K, 1, s);
+                             float* dZprev, __nv_bfloat16* dZprev16, cudaStream_t s, bool tc5) {
+  return gemm_t<0, 1, EPI_DHIDDEN>(M, K, N, dZ, N, W, N, nullptr, Zprev, dZprev, dZprev16, K, 1, s, tc5);
 }
 
 // G[K x N] += X[B x K]^T dZ[B x N] (G zeroed by the caller)
 cudaError_t mlp_gemm_wgrad(int Bsz, int N, int K, const __nv_bfloat16* X, const __nv_bfloat16* dZ, float* G,
-                           cudaStream_t s) {
+                           cudaStream_t s, bool tc5) {
   const int splits = std::min(64, std::max(1, Bsz / 256));
-  return gemm_t<1, 0, EPI_WGRAD>(K, N, Bsz, X, K, dZ, N, nullptr, nullptr, G, nullptr, N, splits, s);
+  return gemm_t<1, 0, EPI_WGRAD>(K, N, Bsz, X, K, dZ, N, nullptr, nullptr, G, nullptr, N, splits, s, tc5);
 }
 
 cudaError_t mlp_loss_grad(int B, int N, const float* Y, int ldy, const float* T, const float* w, float* dy32,

@@ -96,3 +96,38 @@ def test_training_lowers_the_loss(ctx):
     last = net.gradients(2048, x.data_ptr(), t.data_ptr(), wd.data_ptr())
     assert last < 0.05 * first
     net.close()
+
+
+@pytest.mark.parametrize("B", [37, 300])
+def test_tcgen05_and_mma_sync_forms_agree(ctx, B):
+    """The network's GEMMs on tcgen05 (STAB_OPT_MLP_TCGEN05, default) and on
+    mma.sync multiply the same bf16 operands and accumulate in float32 in
+    another order: outputs agree within 2e-4 and gradients within 1e-3
+    relative (a bf16 rounding of a hidden activation that flips between them
+    moves one element by one bf16 step), and the tcgen05 outputs match the
+    oracle within 1e-3."""
+    flat = _init(SIZES, 5)
+    X, T, w = _data(B, 6)
+    dev = "cuda:0"
+    x, t, wd = (torch.from_numpy(a).to(dev) for a in (X, T, w))
+    out = {}
+    try:
+        for tc5 in (1, 0):
+            ctx.set_option(sg.OPT_MLP_TCGEN05, tc5)
+            net = sg.Network(ctx, SIZES, 1024)
+            net.set_params(flat)
+            y = torch.empty((B, SIZES[-1]), dtype=torch.float32, device=dev)
+            net.forward(B, x.data_ptr(), y.data_ptr())
+            ctx.sync()
+            loss = net.gradients(B, x.data_ptr(), t.data_ptr(), wd.data_ptr())
+            _, g = net.get_params(grads=True)
+            out[tc5] = (y.cpu().numpy(), loss, g.copy(), net.split(flat))
+            net.close()
+    finally:
+        ctx.set_option(sg.OPT_MLP_TCGEN05, 1)
+    (y1, l1, g1, params), (y0, l0, g0, _) = out[1], out[0]
+    assert _rel(y1, y0) < 2e-4, _rel(y1, y0)
+    assert abs(l1 - l0) <= 2e-4 * abs(l0), (l1, l0)
+    assert _rel(g1, g0) < 1e-3, _rel(g1, g0)
+    Yo, _ = mo.forward(params, X)
+    assert _rel(y1, Yo) < 1e-3

@@ -46,3 +46,22 @@ def test_tensor_core_lu_backward_error(ctx, n, tma):
     assert np.isfinite(bt)
     assert bt < 1e-5, (bt, bs, pd)
     assert bt <= 4.0 * bs + 1e-7, (bt, bs, pd)
+
+
+@pytest.mark.parametrize("n", [320, 640])
+def test_tensor_core_lu_tma_form_identical_to_register_form(ctx, n):
+    """The TMA form of the tensor-core LU moves each A22 tile through shared
+    memory by tensor loads and stores; every tile takes the same MMAs in the
+    same order and the same epilogue additions as the register form, so both
+    factor the same matrices to the same bits: equal backward errors and
+    pivots."""
+    out = {}
+    try:
+        for tma in (1, 0):
+            ctx.set_option(sg.OPT_POLISH_LU_TMA, tma)
+            out[tma] = ctx.lu_tc_check(n, 4)
+    finally:
+        ctx.set_option(sg.OPT_POLISH_LU_TMA, 1)
+    (bt1, bs1, pd1), (bt0, bs0, pd0) = out[1], out[0]
+    assert bt1 == bt0, (bt1, bt0)
+    assert pd1 == pd0 and bs1 == bs0

@@ -260,7 +260,10 @@ static void fd_mean_tables(int ny, std::vector<double>& G, std::vector<double>& 
 static int ensure_dtab32(stab_ctx* c, int key, int ny) {
   float *F1 = nullptr, *F2 = nullptr;
   CK(c, cudaMalloc(&F1, sizeof(float) * ny * ny));
-  CK(c, cudaMalloc(&F2, sizeof(float) * ny * ny));
+  if (cudaMalloc(&F2, sizeof(float) * ny * ny) != cudaSuccess) {
+    cudaFree(F1);
+    return cuda_fail(c, cudaGetLastError(), "cudaMalloc of a float D table");
+  }
   CK(c, launch_round_f32((int64_t)ny * ny, c->dtabs[key].first, F1, c->stream));
   CK(c, launch_round_f32((int64_t)ny * ny, c->dtabs[key].second, F2, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
@@ -269,7 +272,12 @@ static int ensure_dtab32(stab_ctx* c, int key, int ny) {
 }
 
 static int ensure_dtab(stab_ctx* c, int key) {
-  if (c->dtabs.count(key)) return 0;
+  if (c->dtabs.count(key)) {
+    if (c->dtabs32.count(key)) return 0;
+    // the float copies failed earlier (allocation): build them now
+    const int ny = key >= kFdOpKey ? (key & (kFdOpKey - 1)) : key;
+    return ensure_dtab32(c, key, ny);
+  }
   if (key >= kFdOpKey) {
     const int ny = key & (kFdOpKey - 1);
     std::vector<double> T1, T2;

@@ -226,24 +226,68 @@ __global__ void __launch_bounds__(128, 4) k_gemm_tc(int M, int N, int K, const _
   uint32_t phase = 0;
   bool ok = true;
   bool any = false;
+  // 16-byte loads (8 bf16) where the matrix and its leading dimension allow
+  const bool a_vec = ((reinterpret_cast<uintptr_t>(A) & 15) == 0) && (lda % 8 == 0);
+  const bool b_vec = ((reinterpret_cast<uintptr_t>(B) & 15) == 0) && (ldb % 8 == 0);
   for (int k0 = kbeg; k0 < kend; k0 += TC_KC) {
     // op(A)(m, k) rows and op(B)(k, n) columns, read along the contiguous
-    // index of each layout
-    for (int e = tid; e < TC_M * TC_KC; e += 128) {
+    // index of each layout, 8 values per thread and step: an 8-run along k
+    // is one 16-byte row of a core matrix; an 8-run along m (n) goes to 8
+    // rows.  Runs that leave the matrix, or matrices without 16-byte rows,
+    // take element loads with zero fill.
+    for (int e = tid; e < TC_M * TC_KC / 8; e += 128) {
       int m, k;
-      if (TA == 0) { m = e / TC_KC; k = e % TC_KC; } else { k = e / TC_M; m = e % TC_M; }
+      if (TA == 0) { m = e / (TC_KC / 8); k = (e % (TC_KC / 8)) * 8; } else { k = e / (TC_M / 8); m = (e % (TC_M / 8)) * 8; }
       const int gm = m0 + m, gk = k0 + k;
-      __nv_bfloat16 v = zero;
-      if (gm < M && gk < kend) v = TA == 0 ? A[(int64_t)gm * lda + gk] : A[(int64_t)gk * lda + gm];
-      *reinterpret_cast<__nv_bfloat16*>(As + bf16_off(m, k)) = v;
+      if (TA == 0) {
+        if (a_vec && gm < M && gk + 8 <= kend) {
+          *reinterpret_cast<uint4*>(As + bf16_off(m, k)) = *reinterpret_cast<const uint4*>(A + (int64_t)gm * lda + gk);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            *reinterpret_cast<__nv_bfloat16*>(As + bf16_off(m, k + i)) =
+                (gm < M && gk + i < kend) ? A[(int64_t)gm * lda + gk + i] : zero;
+        }
+      } else {
+        if (a_vec && gk < kend && gm + 8 <= M) {
+          const uint4 v = *reinterpret_cast<const uint4*>(A + (int64_t)gk * lda + gm);
+          const __nv_bfloat16* pv = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) *reinterpret_cast<__nv_bfloat16*>(As + bf16_off(m + i, k)) = pv[i];
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            *reinterpret_cast<__nv_bfloat16*>(As + bf16_off(m + i, k)) =
+                (gm + i < M && gk < kend) ? A[(int64_t)gk * lda + gm + i] : zero;
+        }
+      }
     }
-    for (int e = tid; e < TC_N * TC_KC; e += 128) {
+    for (int e = tid; e < TC_N * TC_KC / 8; e += 128) {
       int k, n;
-      if (TB == 0) { k = e / TC_N; n = e % TC_N; } else { n = e / TC_KC; k = e % TC_KC; }
+      if (TB == 0) { k = e / (TC_N / 8); n = (e % (TC_N / 8)) * 8; } else { n = e / (TC_KC / 8); k = (e % (TC_KC / 8)) * 8; }
       const int gk = k0 + k, gn = n0 + n;
-      __nv_bfloat16 v = zero;
-      if (gk < kend && gn < N) v = TB == 0 ? B[(int64_t)gk * ldb + gn] : B[(int64_t)gn * ldb + gk];
-      *reinterpret_cast<__nv_bfloat16*>(Bs + bf16_off(n, k)) = v;
+      if (TB == 1) {
+        if (b_vec && gn < N && gk + 8 <= kend) {
+          *reinterpret_cast<uint4*>(Bs + bf16_off(n, k)) = *reinterpret_cast<const uint4*>(B + (int64_t)gn * ldb + gk);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            *reinterpret_cast<__nv_bfloat16*>(Bs + bf16_off(n, k + i)) =
+                (gn < N && gk + i < kend) ? B[(int64_t)gn * ldb + gk + i] : zero;
+        }
+      } else {
+        if (b_vec && gk < kend && gn + 8 <= N) {
+          const uint4 v = *reinterpret_cast<const uint4*>(B + (int64_t)gk * ldb + gn);
+          const __nv_bfloat16* pv = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) *reinterpret_cast<__nv_bfloat16*>(Bs + bf16_off(n + i, k)) = pv[i];
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            *reinterpret_cast<__nv_bfloat16*>(Bs + bf16_off(n + i, k)) =
+                (gn + i < N && gk < kend) ? B[(int64_t)gk * ldb + gn + i] : zero;
+        }
+      }
     }
     tc::fence_async_smem();
     __syncthreads();

@@ -131,3 +131,31 @@ def test_tcgen05_and_mma_sync_forms_agree(ctx, B):
     assert _rel(g1, g0) < 1e-3, _rel(g1, g0)
     Yo, _ = mo.forward(params, X)
     assert _rel(y1, Yo) < 1e-3
+
+
+def test_inference_batch_8192_both_forms(ctx):
+    """Inference at the surrogate's full batch (8192 rows, the 6 -> 4 x 256 ->
+    162 network): the tcgen05 and mma.sync forms agree within 2e-4 and the
+    tcgen05 output matches the oracle within 1e-3 on the first 256 rows."""
+    B = 8192
+    flat = _init(SIZES, 7)
+    X, _, _ = _data(B, 8)
+    dev = "cuda:0"
+    x = torch.from_numpy(X).to(dev)
+    out = {}
+    try:
+        for tc5 in (1, 0):
+            ctx.set_option(sg.OPT_MLP_TCGEN05, tc5)
+            net = sg.Network(ctx, SIZES, B)
+            net.set_params(flat)
+            y = torch.empty((B, SIZES[-1]), dtype=torch.float32, device=dev)
+            net.forward(B, x.data_ptr(), y.data_ptr())
+            ctx.sync()
+            out[tc5] = (y.cpu().numpy(), net.split(flat))
+            net.close()
+    finally:
+        ctx.set_option(sg.OPT_MLP_TCGEN05, 1)
+    (y1, params), (y0, _) = out[1], out[0]
+    assert _rel(y1, y0) < 2e-4, _rel(y1, y0)
+    Yo, _ = mo.forward(params, X[:256])
+    assert _rel(y1[:256], Yo) < 1e-3

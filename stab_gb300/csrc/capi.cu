@@ -1076,17 +1076,32 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
     rc = dense<zc>(b, tr, b->Abig.as<zc>(), b->off_m2.as<int64_t>(), 1, 1.0, "k_dense_z");
     if (rc) return rc;
   }
+  // seed spectra in double-word arithmetic also form their spatial companion
+  // matrices in it (ZGETRF/ZGETRS of spatial.f90:978-1002 on the FP32 pipe;
+  // the companion matrix only feeds the double-word eigensolve); spectra
+  // that are answers keep FP64
+  const bool seed_dw = seed && c->arith[STAB_STAGE_SEED_EIG] == STAB_ARITH_DOUBLE_WORD;
   if (sr.cnt > 0) {
     const InstDesc* D = b->desc.as<InstDesc>() + sr.k0;
     rc = node_ops(b, sr, OP_S_C0, OP_S_C0, nullptr);
     if (rc) return rc;
-    rc = dense<zc>(b, sr, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z");
-    if (rc) return rc;
-    CK(c, timed(c, "k_lu_z", [&] {
-      return launch_lu<zc>(sr.cnt, D, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<zc>(),
-                           b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + sr.k0,
-                           b->info.as<int32_t>() + sr.k0, s, nullptr, tuned_nb(c, true, b->nmax));
-    }));
+    if (seed_dw) {
+      rc = dense<dz>(b, sr, b->Z64.as<dz>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_dz");
+      if (rc) return rc;
+      CK(c, timed(c, "k_lu_dz_seed", [&] {
+        return launch_lu<dz>(sr.cnt, D, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<dz>(),
+                             b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + sr.k0,
+                             b->info.as<int32_t>() + sr.k0, s, nullptr, tuned_nb(c, true, b->nmax));
+      }));
+    } else {
+      rc = dense<zc>(b, sr, b->Z64.as<zc>(), b->off_n2.as<int64_t>(), 1, 1.0, "k_dense_z");
+      if (rc) return rc;
+      CK(c, timed(c, "k_lu_z", [&] {
+        return launch_lu<zc>(sr.cnt, D, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<zc>(),
+                             b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(), b->off_nof.as<int64_t>() + sr.k0,
+                             b->info.as<int32_t>() + sr.k0, s, nullptr, tuned_nb(c, true, b->nmax));
+      }));
+    }
     rc = node_ops(b, sr, OP_S_C1, OP_S_C1, nullptr);
     if (rc) return rc;
     rc = dense<zc>(b, sr, b->Abig.as<zc>(), b->off_m2.as<int64_t>(), 2, -1.0, "k_dense_z");
@@ -1095,11 +1110,15 @@ static int run_plain(stab_batch* b, bool want_vec, const char* eig_name = "k_eig
     if (rc) return rc;
     rc = dense<zc>(b, sr, b->Abig.as<zc>(), b->off_m2c2.as<int64_t>(), 2, -1.0, "k_dense_z");
     if (rc) return rc;
-    CK(c, timed(c, "k_getrs_z", [&] {
-      return launch_getrs<zc>(sr.cnt, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<zc>(),
-                              b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(),
-                              b->off_nof.as<int64_t>() + sr.k0, b->Abig.as<zc>(), b->off_m2.as<int64_t>() + sr.k0, 0,
-                              2, 2, nullptr, s);
+    CK(c, timed(c, seed_dw ? "k_getrs_dz_seed" : "k_getrs_z", [&] {
+      return seed_dw ? launch_getrs<dz>(sr.cnt, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<dz>(),
+                                        b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(),
+                                        b->off_nof.as<int64_t>() + sr.k0, b->Abig.as<zc>(),
+                                        b->off_m2.as<int64_t>() + sr.k0, 0, 2, 2, nullptr, s)
+                     : launch_getrs<zc>(sr.cnt, b->nsz.as<int32_t>() + sr.k0, b->nmax, b->Z64.as<zc>(),
+                                        b->off_n2.as<int64_t>() + sr.k0, b->piv.as<int32_t>(),
+                                        b->off_nof.as<int64_t>() + sr.k0, b->Abig.as<zc>(),
+                                        b->off_m2.as<int64_t>() + sr.k0, 0, 2, 2, nullptr, s);
     }));
     CK(c, timed(c, "k_companion_fill", [&] {
       dim3 g(2 * (b->nmax), sr.cnt);

@@ -208,7 +208,7 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     two inverse-iteration steps (Chebyshev grids; batches with a finite-
  *     difference instance keep the steps); 0: the steps. */
 #define STAB_OPT_SEED_VECTORS 6
-/*   STAB_OPT_PARALLEL_CANDIDATES  1 (default): the N = 48 level of
+/*   STAB_OPT_PARALLEL_CANDIDATES  1 (default): the second candidate level of
  *     STAB_MODE_COARSE polishes its instances' four shift candidates side by
  *     side (one sub-batch copy per candidate) instead of in four rounds one
  *     after another; the kept pair and status follow the sequential rule;
@@ -227,7 +227,7 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
 #define STAB_OPT_FIRST_RETRY 9
 /*   STAB_OPT_LEVEL_CONSISTENCY  1 (default): at the second candidate level of
  *     STAB_MODE_COARSE (with STAB_OPT_PARALLEL_CANDIDATES), an instance whose
- *     N = 48 top candidate did not polish to within 1e-7 of itself is still
+ *     second-level top candidate did not polish to within 1e-7 of itself is still
  *     trusted (STAB_ST_FELLBACK) when the top candidates of both seed levels
  *     polished to the same pair (within 1e-10), that pair is the least
  *     stable of the level's converged candidates, and the seed values

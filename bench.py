@@ -832,7 +832,7 @@ def main():
                       "trusted_but_wrong_examples": [
                           {"index": int(q), "got": [float(eig[q].real), float(eig[q].imag)],
                            "plain": [float(ref_eig[q].real), float(ref_eig[q].imag)], "status": int(status[q])}
-                          for q in wrong_trusted[:5]],
+                          for q in wrong_trusted[:16]],
                       "max_rel_err": float(np.nanmax(rel[ok])) if np.any(ok) else None,
                       "max_vec_err": float(np.nanmax(vdiff[ok])) if np.any(ok) else None},
         "plain_fp64": {"value": total / (plain_ms / 1000.0), "unit": UNIT, "ms_per_step": plain_ms,

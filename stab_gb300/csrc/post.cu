@@ -21,6 +21,7 @@
 // The least-stable selection rule is stated in select.cuh.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "fold.cuh"
 #include "select.cuh"
 
 namespace stab {
@@ -272,22 +273,10 @@ __global__ void k_mark_missing(int count, const zc* __restrict__ cand, int ncand
   if (!(isfinite(v.x) && isfinite(v.y))) final_[c] = 2;
 }
 
-// Fold the copies of each instance in candidate order, as the rounds of one
-// instance fold its candidates: the less stable converged pair wins (ties to
-// the earlier copy), and the first copy whose pair was quick-accepted ends
-// the fold.  The instance is trusted (done = 1) when that copy is the top
-// candidate's; any other kept pair is `unverified`.  copy_done is the copies'
-// k_take_best output (1: quick-accepted, unverified: converged, 0: none) and
-// copy_key the selection key of each copy's pair.
-//
-// With lev1 (the first level's top candidate lam1 and its polished pair th1,
-// ok1 = converged), an instance whose kept pair is `unverified` is trusted
-// when both levels identify the same mode: the top candidates of both seed
-// spectra polished to the same pair (within 1e-10), that pair is the least
-// stable of every converged copy, and the seed values converge to it: the
-// finer level's top candidate (N = max(n1, n2), n1 the first level's N and
-// n2 this level's, n2t / n2s for temporal / spatial instances) errs by at
-// most conv times the coarser one's and by at most 1e-3 relative.
+// Fold the copies of each instance (k = blockIdx.x): thread 0 takes the
+// decision of fold_copies_pick (fold.cuh: the sequential rounds' rule and
+// the agreement of the two seed levels), then the block copies the kept
+// pair's eigenvector.
 __global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__ desc,
                               const int32_t* __restrict__ copy_done, const double* __restrict__ copy_key,
                               const zc* __restrict__ copy_theta, const double* __restrict__ copy_err,
@@ -301,42 +290,9 @@ __global__ void k_fold_copies(int count, int ncand, const InstDesc* __restrict__
   const int k = blockIdx.x;
   if (k >= count) return;
   if (threadIdx.x == 0) {
-    int pick = -1, dn = 0;
-    double bk = 0.0;
-    for (int j = 0; j < ncand; ++j) {
-      const int c = k * ncand + j;
-      const int d = copy_done[c];
-      if (d != 1 && d != unverified) continue;
-      if (pick < 0 || copy_key[c] > bk) {
-        pick = c;
-        bk = copy_key[c];
-      }
-      if (d == 1) {
-        dn = (j == 0) ? 1 : unverified;
-        break;
-      }
-    }
-    if (pick >= 0 && dn == 0) dn = unverified;
-    if (dn == unverified && lam1 && ok1[k]) {
-      const int c0 = k * ncand;
-      bool top = (copy_done[c0] == 1 || copy_done[c0] == unverified);
-      for (int j = 1; j < ncand && top; ++j) {
-        const int c = c0 + j;
-        if ((copy_done[c] == 1 || copy_done[c] == unverified) && copy_key[c] > copy_key[c0]) top = false;
-      }
-      if (top) {
-        const zc th = copy_theta[c0];
-        const double at = zabs(th);
-        const double e2 = zabs(zsub(cand[c0], th)), e1 = zabs(zsub(lam1[k], th));
-        // the finer seed level must be the closer one
-        const int n2 = (desc[k].itype == 2 || desc[k].itype == 4) ? n2s : n2t;
-        const double ef = (n2 > n1) ? e2 : e1, ec = (n2 > n1) ? e1 : e2;
-        if (zabs(zsub(th1[k], th)) <= 1e-10 * at && ef <= conv * ec && ef <= 1e-3 * at) {
-          pick = c0;
-          dn = 1;
-        }
-      }
-    }
+    const FoldPick f = fold_copies_pick(k, ncand, desc[k].itype, copy_done, copy_key, copy_theta, unverified, lam1,
+                                        th1, ok1, cand, conv, n1, n2t, n2s);
+    const int pick = f.pick, dn = f.dn;
     done[k] = dn;
     if (pick >= 0) {
       theta[k] = copy_theta[pick];

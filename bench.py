@@ -11,10 +11,13 @@ ymax = 50 and half the points below y = 2.
 
 One step = one pass of the seeded mixed-precision path over the whole batch
 (STAB_MODE_COARSE: a full spectrum at N = 32 in double-word arithmetic for
-the candidate shifts, complex64 LU shift-invert with FP64 residuals at full
-N, a double-word LU retry where that contracts slowly; instances whose seed
-spectrum did not resolve the mode take seeds at N = 48 and then the plain
-FP64 path).  A mode counts as converged when it agrees with the plain FP64
+the candidate shifts; the top candidate polished at full N from its N = 32
+eigenvector by complex64 LU shift-invert with FP64 residuals, with a
+double-word LU retry where that contracts slowly; instances whose seed
+spectrum did not resolve the mode take a second seed level at N = 48, its
+four candidates polished side by side and trusted when that level resolved
+the mode or both levels agree on it; the rest keep an unverified pair or
+take the plain FP64 path).  A mode counts as converged when it agrees with the plain FP64
 path (the full GPU spectrum, itself checked against the CPU oracle by the
 tests) to |d omega| / |omega| <= 1e-10 and its eigenvector to 1e-8.  The
 working set (393 MB of profiles and ~7 GB of matrices) is far larger than

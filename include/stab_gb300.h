@@ -137,7 +137,8 @@ int stab_reset_kernel_stats(stab_ctx* ctx);
 /* Arithmetic of three stages (no reference counterpart):
  *   STAB_STAGE_SEED_EIG   Hessenberg reduction and QR of the spectra that
  *                         only seed the polish (STAB_MODE_COARSE /
- *                         STAB_MODE_SURROGATE and their N = 48 level);
+ *                         STAB_MODE_SURROGATE and their second candidate
+ *                         level: N = 48 temporal, N = 24 spatial);
  *                         default STAB_ARITH_DOUBLE_WORD;
  *   STAB_STAGE_PLAIN_EIG  the same for STAB_MODE_PLAIN, stab_full_spectrum
  *                         and the FP64 fallback (ZGEEV, temporal.f90:803);
@@ -196,8 +197,8 @@ int stab_set_seed_size(stab_ctx* ctx, int32_t ny);
  *     order, so eigenvalues agree to rounding, not bit for bit. */
 #define STAB_OPT_EIG_THREADS 4
 /*   STAB_OPT_EIG_MID  1 (default, measured 2.6 % faster on the 4096-instance
- *     sweep): batches of at most two instances per SM (the N = 48 level of
- *     STAB_MODE_COARSE, small serving batches) run one 256-thread CTA per
+ *     sweep): batches of at most two instances per SM (the second candidate
+ *     level of STAB_MODE_COARSE, small serving batches) run one 256-thread CTA per
  *     instance instead of the 128-thread persistent grid; 0: the persistent
  *     grid.  Same algorithm; block sums in another order. */
 #define STAB_OPT_EIG_MID 5

@@ -485,7 +485,8 @@ def test_coarse_with_seed_vectors_matches_plain(ctx):
 
 
 def test_parallel_candidates_match_sequential_rounds(ctx):
-    """STAB_OPT_PARALLEL_CANDIDATES: the N = 48 level polishes its four shift
+    """STAB_OPT_PARALLEL_CANDIDATES: the second candidate level (N = 48 for
+    these temporal instances) polishes its four shift
     candidates side by side (one sub-batch copy per candidate) instead of in
     four rounds.  On 256 instances of the benchmark sweep (about 16 of them
     reach that level) both forms return the same statuses and eigenvalues

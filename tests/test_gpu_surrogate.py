@@ -4,11 +4,12 @@ Region: supersonic second modes (M in [1.5, 2], alpha in [0.2, 0.4],
 Re in [1500, 3000], beta in [0, 0.1]).  Here the N = 32 seed spectrum does
 not resolve the least-stable discrete mode, so the coarse-seeded method
 (STAB_MODE_COARSE, the method without the network) can verify few instances
-at its first level and sends the rest through the N = 48 seed level.  The
+at its first level and sends the rest through the second seed level (N = 48 for these temporal
+instances).  The
 network, trained here by the library's BF16 kernels on plain FP64 solves at
 N = 64, adds its prediction as one more candidate (STAB_MODE_SURROGATE);
 where that candidate's converged pair is the least stable, the instance is
-settled without the N = 48 level, with STAB_ST_UNVERIFIED.
+settled without the second level, with STAB_ST_UNVERIFIED.
 
 Checks on 512 instances: the network's fit halves its loss; the surrogate
 mode settles at least one instance from the network's seed and sends that
